@@ -1,0 +1,376 @@
+"""Benchmark: SAR back-projection on the 4096-pulse x 8192-sample, 4096^2-pixel
+scene (200 Rayleigh point targets, 20 dB clutter, 0.25 m pixels), split-precision
+FP32 arithmetic, one GB300.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--mode split|fp16store|fp32|fp64]
+  python bench.py --impl reference ...   # the CPU back-projection (FP64 oracle port) on host cores
+
+Metric: Gpix*pulse/s = Nx*Ny*Np / back-projection time, with the range-compressed
+data resident in HBM (range compression timed and reported separately).
+`e2e` is the same metric through sarbp_image() with pinned host buffers: echo
+upload, range compression, back-projection and image download every step.
+Inputs (256 MB echo, 2 GB range-compressed data, 128 MB image) exceed the
+129 MB L2, so no explicit flush is needed between steps.
+
+Multi-GPU (torchrun): every rank images its own replica of the scene (weak
+scaling; tiles/replicas need no exchange); time = max over ranks.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+# Algorithmic work of one pixel*pulse update (slant range, bin, linear
+# interpolation, phase rotation, complex accumulate): 19 FP32-pipe operations
+# and 3 MUFU operations (a square-root-class op, sin, cos).
+FP32_OPS_PER_UPDATE = 19
+MUFU_OPS_PER_UPDATE = 3
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--mode", default="split", choices=["split", "fp16store", "fp32", "fp64"])
+    ap.add_argument("--size", default="full", choices=["full", "small"],
+                    help="small: 512 pulses x 1024 samples, 512^2 (for profiling captures)")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    return ap.parse_args()
+
+
+def dist_init(n):
+    if n <= 1 or "RANK" not in os.environ:
+        return 0, 1, None
+    import torch.distributed as dist
+    backend = "nccl"
+    dist.init_process_group(backend)
+    return dist.get_rank(), dist.get_world_size(), dist
+
+
+def barrier(dist):
+    if dist is not None:
+        dist.barrier()
+
+
+def max_over_ranks(dist, v: float) -> float:
+    if dist is None:
+        return v
+    import torch
+    t = torch.tensor([v], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device_index: int):
+        self.dev = device_index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.dev), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.f.close()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        os.unlink(self.path)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def workload(size):
+    from sar_cambrianaccelerationcard_gb300 import scenes
+    if size == "small":
+        return scenes.config1()
+    return scenes.config2()
+
+
+def cpu_sample(scene, threads=None):
+    """FP64 oracle back-projection of a 128x128 tile (all pulses) of the scene,
+    on range-compressed data computed by the oracle.  Returns (updates/s,
+    cores, description, seconds)."""
+    from oracle import oracle as orc
+    if threads:
+        orc.set_threads(threads)
+    cores = orc.threads()
+    g = scene.grid
+    w = h = 128
+    x0, y0 = g.nx // 2 - w // 2, g.ny // 2 - h // 2
+    # range-compress the pulses once (untimed setup): oracle FP64 chain
+    echo = orc.echo(scene)
+    rc = orc.range_compress(scene, echo)
+    t = time.perf_counter()
+    orc.backproject(scene, rc, (x0, y0, w, h))
+    dt = time.perf_counter() - t
+    upd = w * h * scene.np_
+    desc = (f"FP64 oracle BP (restated BPA_SAR.m:177-197, linear interpolation) over a {w}x{h}-pixel tile "
+            f"x all {scene.np_} pulses of the same scene ({upd:.3g} updates), {cores} OpenMP threads")
+    return upd / dt, cores, desc, dt, rc, (x0, y0, w, h)
+
+
+def run_reference(args):
+    """CPU arm: the reference's back-projection algorithm on the host cores."""
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return 0
+    from oracle import oracle as orc
+    scene = workload(args.size)
+    echo = orc.echo(scene)
+    rc = orc.range_compress(scene, echo)
+    g = scene.grid
+    w = h = 128 if args.size == "full" else 64
+    region = (g.nx // 2 - w // 2, g.ny // 2 - h // 2, w, h)
+    for _ in range(args.warmup):
+        orc.backproject(scene, rc, region)
+    t = time.perf_counter()
+    for _ in range(args.steps):
+        orc.backproject(scene, rc, region)
+    dt = (time.perf_counter() - t) / max(1, args.steps)
+    upd = w * h * scene.np_
+    v = upd / dt / 1e9
+    cores = orc.threads()
+    line = {
+        "impl": "reference", "metric": "BP Gpix*pulse/s", "value": v, "unit": "Gpix*pulse/s",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": f"stripmap BP {scene.np_} pulses x {scene.ns} samples -> {g.nx}x{g.ny} image",
+                   "mode": "fp64-cpu", "sample_tile": [w, h]},
+        "cpu_baseline": {"value": v, "unit": "Gpix*pulse/s", "cores": cores, "kind": "port",
+                         "sample": f"{w}x{h} tile x {scene.np_} pulses per step (range compression untimed)"},
+        "e2e": {"value": v, "unit": "Gpix*pulse/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+    return 0
+
+
+def run_ours(args):
+    import torch
+    rank, world, dist = dist_init(args.gpus)
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    from sar_cambrianaccelerationcard_gb300 import metrics, sarbp, scenes
+
+    mode = sarbp.MODES[args.mode]
+    scene = workload(args.size)
+    r, g, lay = sarbp.scene_args(scene)
+    ctx = sarbp.Context(local)
+    stream = torch.cuda.Stream()
+    sptr = sarbp.ctypes.c_void_p(stream.cuda_stream)
+
+    # --- inputs: GPU-synthesised echo (device), pinned host copy for e2e
+    echo_d = torch.empty((scene.np_, scene.ns * 2), dtype=torch.float32, device="cuda")
+    apc_d = torch.from_numpy(scene.apc).cuda()
+    sarbp.synthesize(ctx, scene, out=echo_d)
+    ctx.synchronize()
+    storage = sarbp.STORE_C32H if mode == sarbp.MODE_FP16STORE else sarbp.STORE_C64
+    esize = 8 if storage == sarbp.STORE_C64 else 4
+    rc_d = torch.empty((scene.np_, lay.nbins * esize // 4), dtype=torch.float32, device="cuda")
+    scale_d = torch.ones(scene.np_, dtype=torch.float32, device="cuda")
+    img_d = torch.zeros((g.ny, g.nx * 2), dtype=torch.float32, device="cuda")
+
+    def rc_step():
+        ctx.check(ctx.lib.sarbp_range_compress(ctx.h, sarbp.ctypes.byref(r), echo_d.data_ptr(), scene.np_, scene.ns,
+                                               storage, rc_d.data_ptr(), scale_d.data_ptr(), sptr), "rc")
+
+    view = sarbp.RcView()
+    view.data, view.scale = rc_d.data_ptr(), scale_d.data_ptr() if storage == sarbp.STORE_C32H else None
+    view.storage, view.np, view.nbins = storage, scene.np_, lay.nbins
+    view.t0_bins, view.bin_rate = lay.t0_bins, lay.bin_rate
+
+    def bp_step():
+        ctx.check(ctx.lib.sarbp_backproject(ctx.h, sarbp.ctypes.byref(r), sarbp.ctypes.byref(view), apc_d.data_ptr(),
+                                            sarbp.ctypes.byref(g), mode, img_d.data_ptr(), 0, sptr), "bp")
+
+    with torch.cuda.stream(stream):
+        rc_step()
+    stream.synchronize()
+    ctx.synchronize()
+    rc_ms = ctx.timings()[0]
+
+    # --- device-resident timing of back-projection
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    for _ in range(args.warmup):
+        bp_step()
+    stream.synchronize()
+    barrier(dist)
+    torch.cuda.synchronize()
+    clocks = ClockSampler(local)
+    clocks.start()
+    n0 = ctx.launches()
+    ev0.record(stream)
+    bp_ms_each = []
+    for _ in range(args.steps):
+        bp_step()
+    ev1.record(stream)
+    stream.synchronize()
+    torch.cuda.synchronize()
+    barrier(dist)
+    launches = ctx.launches() - n0
+    clk = clocks.stop()
+    ms = ev0.elapsed_time(ev1) / args.steps
+    ms = max_over_ranks(dist, ms)
+    ctx.synchronize()
+    bp_ms_each = ctx.timings()[1]  # last launch, events on the launching stream
+    updates = scene.updates
+    value = updates * world / (ms * 1e-3) / 1e9
+
+    # --- accuracy of this run's image against the FP64 GPU comparator on a tile
+    acc = {}
+    if rank == 0 and args.mode != "fp64" and args.size == "full":
+        img_ours = img_d.cpu().numpy().view(np.complex64)
+        g64 = sarbp.grid_struct(scenes.centred_grid(scene.radar, 512, 512, 0.25))
+        sub = scene.grid
+        ox, oy = sub.nx // 2 - 256, sub.ny // 2 - 256
+        g64 = sarbp.Grid()
+        for i in range(3):
+            g64.origin[i] = sub.origin[i] + ox * sub.ux[i] + oy * sub.uy[i]
+            g64.ux[i], g64.uy[i] = sub.ux[i], sub.uy[i]
+        g64.nx = g64.ny = 512
+        ref = torch.zeros((512, 1024), dtype=torch.float32, device="cuda")
+        ctx.check(ctx.lib.sarbp_backproject(ctx.h, sarbp.ctypes.byref(r), sarbp.ctypes.byref(view), apc_d.data_ptr(),
+                                            sarbp.ctypes.byref(g64), sarbp.MODE_FP64, ref.data_ptr(), 0, sptr), "fp64")
+        stream.synchronize()
+        ctx.synchronize()
+        fp64_ms = ctx.timings()[1]
+        refi = ref.cpu().numpy().view(np.complex64)
+        acc["rel_l2_db_vs_fp64_gpu_512tile"] = metrics.rel_l2_db(img_ours[oy:oy + 512, ox:ox + 512], refi)
+        acc["fp64_gpu_gpix_pulse_s"] = 512 * 512 * scene.np_ / (fp64_ms * 1e-3) / 1e9
+
+    # --- end to end through sarbp_image with pinned host buffers
+    e2e = None
+    if not args.no_e2e:
+        echo_h = torch.empty((scene.np_, scene.ns * 2), dtype=torch.float32, pin_memory=True)
+        echo_h.copy_(echo_d.cpu())
+        img_h = torch.empty((g.ny, g.nx * 2), dtype=torch.float32, pin_memory=True)
+        apc_h = np.ascontiguousarray(scene.apc)
+
+        def e2e_step():
+            ctx.check(ctx.lib.sarbp_image(ctx.h, sarbp.ctypes.byref(r), echo_h.data_ptr(), scene.np_, scene.ns,
+                                          apc_h.ctypes.data, sarbp.ctypes.byref(g), mode, img_h.data_ptr(), sptr),
+                      "e2e")
+
+        for _ in range(max(1, args.warmup)):
+            e2e_step()
+        barrier(dist)
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        ksteps = max(1, min(args.steps, 5))
+        for _ in range(ksteps):
+            e2e_step()
+        torch.cuda.synchronize()
+        barrier(dist)
+        e2e_s = max_over_ranks(dist, (time.perf_counter() - t) / ksteps)
+        e2e = {"value": updates * world / e2e_s / 1e9, "unit": "Gpix*pulse/s",
+               "h2d_bytes_per_step": scene.np_ * scene.ns * 8 + scene.np_ * 24,
+               "d2h_bytes_per_step": g.nx * g.ny * 8, "ms_per_step": e2e_s * 1e3}
+
+    # --- roofline: issue-rate ceiling from live microbenchmarks
+    fp32_rate, mufu_rate, sms = ctx.probe_issue_rates()
+    peak = min(fp32_rate / FP32_OPS_PER_UPDATE, mufu_rate / MUFU_OPS_PER_UPDATE) / 1e9
+    bp_rate = updates / (bp_ms_each * 1e-3) / 1e9 if bp_ms_each else None
+    roofline = {
+        "bound": "issue (FP32+MUFU)", "achieved": bp_rate, "peak": peak, "unit": "Gpix*pulse/s",
+        "frac": (bp_rate / peak) if bp_rate else None, "traffic": None,
+        "peak_source": (f"measured live: FP32 FMA {fp32_rate / 1e12:.1f} T lanes/s, MUFU {mufu_rate / 1e12:.2f} T "
+                        f"lanes/s on {sms} SMs; peak = min(FP32/{FP32_OPS_PER_UPDATE}, MUFU/{MUFU_OPS_PER_UPDATE})"),
+        "kernel": "bp_kernel<SPLIT>",
+    }
+    peaks_path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    hbm = None
+    if os.path.exists(peaks_path):
+        hbm = json.load(open(peaks_path)).get("hbm_gbs")
+    rc_bytes = scene.np_ * scene.ns * 8 + scene.np_ * lay.nbins * esize
+    roofline_rc = {"bound": "hbm", "achieved": rc_bytes / (rc_ms * 1e-3) / 1e9 if rc_ms else None, "peak": hbm,
+                   "unit": "GB/s", "frac": (rc_bytes / (rc_ms * 1e-3) / 1e9 / hbm) if (rc_ms and hbm) else None,
+                   "traffic": None, "kernel": "rc_forward + rc_inverse", "ms": rc_ms}
+
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        v, cores, desc, secs, _, _ = cpu_sample(scene)
+        cpu = {"value": v / 1e9, "unit": "Gpix*pulse/s", "cores": cores, "kind": "port", "sample": desc,
+               "seconds": secs}
+
+    if rank == 0:
+        line = {
+            "metric": "BP Gpix*pulse/s", "value": value, "unit": "Gpix*pulse/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32" if args.mode != "fp64" else "f64",
+            "data": "synthetic (GPU echo synthesiser, seeded)",
+            "config": {"workload": (f"stripmap BP {scene.np_} pulses x {scene.ns} samples -> {g.nx}x{g.ny} image "
+                                    f"at 0.25 m, {len(scene.targets)} targets, 20 dB clutter"),
+                       "mode": args.mode, "upsample": scene.radar.upsample, "interp": "linear",
+                       "l2": "inputs larger than L2 (2 GB range-compressed data, 128 MB image)"},
+            "rc_ms": rc_ms,
+            "accuracy": acc,
+            "e2e": e2e,
+            "roofline": roofline,
+            "roofline_rc": roofline_rc,
+            "cpu_baseline": cpu,
+            "gpu_launches": launches,
+            "clocks": clk,
+        }
+        print(json.dumps(line))
+    ctx.close()
+    if dist is not None:
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,237 @@
+/*
+ * sarbp.h -- C ABI of the GB300-native SAR back-projection imager (libsarbp.so).
+ *
+ * Drop-in boundary for the reference's back-projection path
+ * (wenj-yan/SAR_CambrianAccelerationCard):
+ *   launchBackProjection(cufftComplex* Srnm, cufftComplex* Image, const SARParams, int Na, int Nr)
+ *     declared code/SAR_BP/CUDA/BPA_CUDA.cpp:8-9, defined BPA_CUDA_kernels.cu:91-98,
+ *     called by SAR_Processor::applyBPAlgorithm (BPA_CUDA.cpp:83-90);
+ *   launchGenerateEcho(...)  BPA_CUDA.cpp:4-6, BPA_CUDA_kernels.cu:79-89;
+ * and of the algorithm those stand for, code/SAR_BP/matlab/BPA_SAR.m
+ *   (echo :80-89, range compression :93-100, 8x upsampling :106-111,
+ *    back-projection :177-197).
+ *
+ * Unlike the reference, every entry point
+ *   - takes the antenna phase-centre (APC) track and the pixel grid explicitly
+ *     (the reference derives them from SARParams only);
+ *   - returns a status code instead of calling exit() (CHECK_CUDA, BPA_CUDA.h:11-17);
+ *   - works on caller-owned buffers; pointers may be host or device memory
+ *     (detected per call).  With host pointers the call is synchronous; with
+ *     device pointers it is asynchronous on `stream` (a cudaStream_t, or NULL
+ *     for the context's own stream).
+ * A context is not thread-safe; use one per host thread.
+ *
+ * Complex data are interleaved float pairs (layout-compatible with
+ * cufftComplex / float2).  Arrays are row-major: echo [np][ns], range-compressed
+ * data [np][nbins], APC [np][3] doubles, image [ny][nx].
+ */
+#ifndef SARBP_H
+#define SARBP_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SARBP_ABI_VERSION 1
+
+typedef enum sarbp_status {
+    SARBP_OK = 0,
+    SARBP_ERR_INVALID_ARGUMENT = 1, /* null pointer, bad size, bad enum */
+    SARBP_ERR_UNSUPPORTED = 2,      /* valid but outside what this build handles */
+    SARBP_ERR_OUT_OF_MEMORY = 3,    /* device or pinned-host allocation failed */
+    SARBP_ERR_CUDA = 4,             /* a CUDA runtime call failed; see sarbp_last_error */
+    SARBP_ERR_NO_DEVICE = 5,        /* no usable sm_103 device */
+    SARBP_ERR_TIMEOUT = 6,          /* a bounded device-side wait ran out */
+    SARBP_ERR_DEVICE_CHECK = 7,     /* a kernel's own consistency check tripped */
+    SARBP_ERR_NOT_READY = 8,        /* serving: job still running */
+    SARBP_ERR_CANCELLED = 9,        /* serving: job cancelled */
+    SARBP_ERR_BUDGET = 10,          /* serving: job larger than the HBM budget */
+    SARBP_ERR_INTERNAL = 11
+} sarbp_status;
+
+/* Back-projection arithmetic. */
+typedef enum sarbp_mode {
+    SARBP_MODE_FP64 = 0,     /* plain FP64 per pixel and pulse (the comparator) */
+    SARBP_MODE_FP32 = 1,     /* plain FP32: absolute ranges and phases in FP32 */
+    SARBP_MODE_SPLIT = 2,    /* FP64 per-(tile, pulse) reference range and phase wrap,
+                                FP32 per-pixel differential range, compensated phase */
+    SARBP_MODE_FP16STORE = 3 /* SPLIT arithmetic on FP16-stored range-compressed data */
+} sarbp_mode;
+
+/* Storage of range-compressed data. */
+typedef enum sarbp_storage {
+    SARBP_STORE_C64 = 0, /* complex float32 (8 bytes per bin) */
+    SARBP_STORE_C32H = 1 /* complex float16 (4 bytes per bin) times a per-pulse float scale */
+} sarbp_storage;
+
+typedef struct sarbp_complex64 {
+    float re, im;
+} sarbp_complex64;
+
+/* Radar constants (replaces SARParams, BPA_CUDA.h:28-50, for this path). */
+typedef struct sarbp_radar {
+    double c;        /* propagation speed, m/s */
+    double fc;       /* carrier frequency, Hz */
+    double fs;       /* fast-time sampling rate, Hz */
+    double kr;       /* chirp rate, Hz/s */
+    double tp;       /* pulse duration, s */
+    double tc;       /* time within the pulse where the chirp frequency is 0 (tp/2: centred) */
+    double t_rec0;   /* two-way delay of echo sample 0, s */
+    int32_t upsample;/* range upsampling factor L: power of two in [1, 16] */
+    int32_t reserved;/* must be 0 */
+} sarbp_radar;
+
+/* Pixel (x, y) sits at origin + x*ux + y*uy; image is [ny][nx]. */
+typedef struct sarbp_grid {
+    double origin[3];
+    double ux[3];
+    double uy[3];
+    int32_t nx, ny;
+} sarbp_grid;
+
+/* Derived range-compression layout for `ns` echo samples. */
+typedef struct sarbp_rc_layout {
+    int32_t nc;       /* chirp samples round(tp*fs) */
+    int32_t nfft;     /* nextpow2(ns + nc - 1) */
+    int32_t shift;    /* output lag shift nc/2 */
+    int32_t nbins;    /* upsample * ns bins per pulse */
+    double t0_bins;   /* two-way delay of bin 0: t_rec0 - shift/fs */
+    double bin_rate;  /* upsample * fs, bins per second of delay */
+} sarbp_rc_layout;
+
+/* View of range-compressed data (device or host memory). */
+typedef struct sarbp_rc_view {
+    const void *data;     /* [np][nbins] complex64 or complex16 */
+    const float *scale;   /* [np] per-pulse scale for SARBP_STORE_C32H, else NULL */
+    int32_t storage;      /* sarbp_storage */
+    int32_t np;
+    int32_t nbins;
+    int32_t reserved;
+    double t0_bins;
+    double bin_rate;
+} sarbp_rc_view;
+
+/* Point target for the echo synthesiser. */
+typedef struct sarbp_target {
+    double x, y, z, amp;
+} sarbp_target;
+
+typedef struct sarbp_ctx sarbp_ctx;
+
+/* ---------------------------------------------------------------- basics -- */
+
+int sarbp_abi_version(void);
+const char *sarbp_status_string(sarbp_status s);
+
+/* Create a context on CUDA device `device` (needs compute capability 10.3).
+ * Replaces SAR_Processor's constructor-time allocation (BPA_CUDA.cpp:11-13,51-56). */
+sarbp_status sarbp_create(sarbp_ctx **out, int device);
+/* Frees every device buffer the context holds (BPA_CUDA.cpp:15-22). */
+sarbp_status sarbp_destroy(sarbp_ctx *ctx);
+/* Detail message of the last failing call on this context ("" if none). */
+const char *sarbp_last_error(const sarbp_ctx *ctx);
+/* Waits for all work issued through the context and reports device-side checks. */
+sarbp_status sarbp_synchronize(sarbp_ctx *ctx);
+/* Releases cached device buffers (they are re-grown on demand). */
+sarbp_status sarbp_trim(sarbp_ctx *ctx);
+/* Bytes of device memory the context currently holds. */
+size_t sarbp_device_bytes(const sarbp_ctx *ctx);
+
+sarbp_status sarbp_rc_layout_get(const sarbp_radar *radar, int32_t ns, sarbp_rc_layout *out);
+
+/* --------------------------------------------------------- imaging path -- */
+
+/* Range compression + upsampling (BPA_SAR.m:93-111; the reference CUDA program
+ * declares a cuFFT plan for this, BPA_CUDA.h:65, but never runs it).
+ * echo [np][ns] complex64 -> rc_out [np][nbins] (storage), rc_scale_out [np]
+ * (required for SARBP_STORE_C32H, ignored otherwise).  nbins = upsample*ns. */
+sarbp_status sarbp_range_compress(sarbp_ctx *ctx, const sarbp_radar *radar,
+                                  const sarbp_complex64 *echo, int32_t np, int32_t ns,
+                                  int32_t storage, void *rc_out, float *rc_scale_out,
+                                  void *stream);
+
+/* Back-projection of range-compressed data onto the grid (BPA_SAR.m:177-197,
+ * with linear interpolation on the upsampled bins; replaces
+ * backProjectionKernel / launchBackProjection, BPA_CUDA_kernels.cu:47-77,91-98).
+ * apc [np][3]; image [ny][nx].  accumulate != 0 adds into image. */
+sarbp_status sarbp_backproject(sarbp_ctx *ctx, const sarbp_radar *radar,
+                               const sarbp_rc_view *rc, const double *apc,
+                               const sarbp_grid *grid, int32_t mode,
+                               sarbp_complex64 *image, int32_t accumulate, void *stream);
+
+/* The SAR_BP entry point: echo + APC track + radar + grid in, complex image out.
+ * Range compression (storage chosen by mode) followed by back-projection
+ * (SAR_Processor::processImage + applyBPAlgorithm, BPA_CUDA.cpp:70-90). */
+sarbp_status sarbp_image(sarbp_ctx *ctx, const sarbp_radar *radar,
+                         const sarbp_complex64 *echo, int32_t np, int32_t ns,
+                         const double *apc, const sarbp_grid *grid, int32_t mode,
+                         sarbp_complex64 *image, void *stream);
+
+/* ------------------------------------------------------ echo synthesiser -- */
+
+/* Point-target echo with FP64 phase (BPA_SAR.m:80-89; replaces
+ * generateEchoKernel, BPA_CUDA_kernels.cu:3-45), plus counter-based complex
+ * Gaussian noise at snr_db below the mean noiseless power (no noise when
+ * snr_db is NaN).  echo_out [np][ns]. */
+sarbp_status sarbp_synthesize_echo(sarbp_ctx *ctx, const sarbp_radar *radar,
+                                   const double *apc, int32_t np, int32_t ns,
+                                   const sarbp_target *targets, int32_t nt,
+                                   double snr_db, uint64_t seed,
+                                   sarbp_complex64 *echo_out, void *stream);
+
+/* ------------------------------------------------- reference-layout shim -- */
+
+/* Byte-for-byte layout of the reference's SARParams (BPA_CUDA.h:28-50):
+ * 12 floats then 3 ints, 60 bytes. */
+typedef struct sarbp_ref_params {
+    float c, fc, lambda, Kr, Tr, Br, Fr, vr, H, La, Rg0, Az0;
+    int32_t Nfast, Mslow, Ntarget;
+} sarbp_ref_params;
+
+/* launchBackProjection (BPA_CUDA_kernels.cu:91-98) with the intended
+ * BPA_SAR.m semantics on the reference's data model:
+ *   Srnm  [Mslow][Nfast] raw echo, device memory, fast time tr_i = i/Fr
+ *         (BPA_CUDA.cpp:44-48), uncentred chirp Kr over Tr;
+ *   APC_m = (vr*ta_m, 0, H), ta = linspace(-La/(2vr), La/(2vr), Mslow)
+ *         (BPA_CUDA.cpp:35-42);
+ *   Image [Na][Nr] device memory, pixel (i, j) on the ground at
+ *         (Az0 + (i - Na/2) m, Rg0 + (j - Nr/2) m, 0) (the 1 m pixel of
+ *         BPA_CUDA_kernels.cu:56-57, centred on the scene centre);
+ *   range compression + 8x upsampling + SPLIT back-projection.
+ * Synchronous (the reference synchronises, :97-98).  Uses a process-wide
+ * context on the current device. */
+sarbp_status sarbp_launch_back_projection(sarbp_complex64 *Srnm, sarbp_complex64 *Image,
+                                          const sarbp_ref_params *params, int32_t Na, int32_t Nr);
+
+/* launchGenerateEcho (BPA_CUDA_kernels.cu:79-89): same formula and gates as
+ * generateEchoKernel (:18-42), evaluated in FP64.  Ptarget [Ntarget][3] =
+ * (Az, Rg, sigma), ta [Mslow], tr [Nfast], Srnm [Mslow][Nfast]: device memory. */
+sarbp_status sarbp_launch_generate_echo(sarbp_complex64 *Srnm, const float *Ptarget,
+                                        const float *ta, const float *tr,
+                                        const sarbp_ref_params *params,
+                                        int32_t Mslow, int32_t Nfast);
+
+/* ------------------------------------------------------------ measurement -- */
+
+/* Issue-rate microbenchmarks on the context's device: FP32 FMA lanes/s and
+ * MUFU (sin/cos) lanes/s, plus the SM clock (Hz) seen during the run.  The
+ * back-projection roofline is built from these (the kernel is FP32/MUFU issue
+ * bound, not HBM or tensor bound). */
+sarbp_status sarbp_probe_issue_rates(sarbp_ctx *ctx, double *fp32_lanes_per_s,
+                                     double *mufu_lanes_per_s, int32_t *sm_count);
+
+/* Time of the last kernel launches issued by the context, measured with CUDA
+ * events on the launching stream: range compression and back-projection, ms.
+ * Valid after a synchronous call or sarbp_synchronize. */
+sarbp_status sarbp_last_timings(sarbp_ctx *ctx, float *rc_ms, float *bp_ms);
+
+/* Number of this library's kernels launched through the context so far. */
+int64_t sarbp_kernel_launches(const sarbp_ctx *ctx);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* SARBP_H */

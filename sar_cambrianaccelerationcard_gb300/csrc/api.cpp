@@ -1,0 +1,868 @@
+// api.cpp -- C ABI of libsarbp: context, planning, host<->device staging.
+//
+// Replaces the host orchestration of the reference's BP program
+// (code/SAR_BP/CUDA/BPA_CUDA.cpp:11-100, SAR_Processor) with a context that
+// owns cached device buffers, validates every argument, returns status codes
+// instead of exit() (CHECK_CUDA, BPA_CUDA.h:11-17), and plans the kernels:
+// range-compression tables, pulse batching of the spectrum scratch, the
+// back-projection staging window and pulse segmentation.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <complex>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "sarbp_internal.h"
+
+using sarbp::BpPlan;
+using sarbp::RcPlan;
+
+namespace {
+
+constexpr double kPi = 3.14159265358979323846;
+constexpr size_t kSpecScratchBudget = size_t(256) << 20;  // bytes of spectrum scratch per batch
+
+struct DevBuf {
+    void *ptr = nullptr;
+    size_t bytes = 0;
+    cudaError_t ensure(size_t need) {
+        if (need <= bytes && ptr) return cudaSuccess;
+        if (ptr) cudaFree(ptr);
+        ptr = nullptr;
+        bytes = 0;
+        if (need == 0) return cudaSuccess;
+        cudaError_t e = cudaMalloc(&ptr, need);
+        if (e == cudaSuccess) bytes = need;
+        else cudaGetLastError();
+        return e;
+    }
+    void release() {
+        if (ptr) cudaFree(ptr);
+        ptr = nullptr;
+        bytes = 0;
+    }
+    template <class T>
+    T *as() const { return static_cast<T *>(ptr); }
+};
+
+struct RcTables {
+    bool valid = false;
+    int nfft = 0, L = 0, nc = 0, shift = 0;
+    double kr = 0, fs = 0, tc = 0, tp = 0;
+    DevBuf filt, tw, ramp;
+};
+
+}  // namespace
+
+struct sarbp_ctx {
+    int device = 0;
+    int sms = 0;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+    std::string err;
+    DevBuf echo, spec, rc, scale, apc, image, partial, errword, power, targets;
+    RcTables tables;
+    int64_t launches = 0;
+    float rc_ms = 0.f, bp_ms = 0.f;
+    bool timed_rc = false, timed_bp = false;
+};
+
+namespace {
+
+sarbp_status fail(sarbp_ctx *ctx, sarbp_status st, const char *fmt, ...) {
+    if (ctx) {
+        char buf[512];
+        va_list ap;
+        va_start(ap, fmt);
+        vsnprintf(buf, sizeof buf, fmt, ap);
+        va_end(ap);
+        ctx->err = buf;
+    }
+    return st;
+}
+
+sarbp_status cuda_fail(sarbp_ctx *ctx, cudaError_t e, const char *what) {
+    cudaGetLastError();
+    if (e == cudaErrorMemoryAllocation)
+        return fail(ctx, SARBP_ERR_OUT_OF_MEMORY, "%s: %s", what, cudaGetErrorString(e));
+    return fail(ctx, SARBP_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
+}
+
+#define SARBP_CUDA(ctx, call, what)                            \
+    do {                                                       \
+        cudaError_t e_ = (call);                               \
+        if (e_ != cudaSuccess) return cuda_fail(ctx, e_, what); \
+    } while (0)
+
+bool is_device_ptr(const void *p) {
+    if (!p) return false;
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+}
+
+bool is_pow2(long long n) { return n > 0 && (n & (n - 1)) == 0; }
+
+long long next_pow2(long long n) {
+    long long p = 1;
+    while (p < n) p <<= 1;
+    return p;
+}
+
+sarbp_status check_radar(sarbp_ctx *ctx, const sarbp_radar *r) {
+    if (!r) return fail(ctx, SARBP_ERR_INVALID_ARGUMENT, "radar is null");
+    if (!(r->c > 0) || !(r->fc > 0) || !(r->fs > 0) || !(r->tp > 0) || !std::isfinite(r->kr) ||
+        !std::isfinite(r->tc) || !std::isfinite(r->t_rec0))
+        return fail(ctx, SARBP_ERR_INVALID_ARGUMENT, "radar constants must be finite, c/fc/fs/tp > 0");
+    if (!is_pow2(r->upsample) || r->upsample > 16)
+        return fail(ctx, SARBP_ERR_INVALID_ARGUMENT, "upsample must be a power of two in [1, 16]");
+    if (r->reserved != 0) return fail(ctx, SARBP_ERR_INVALID_ARGUMENT, "radar.reserved must be 0");
+    return SARBP_OK;
+}
+
+sarbp_status layout(sarbp_ctx *ctx, const sarbp_radar *r, int32_t ns, sarbp_rc_layout *out) {
+    sarbp_status st = check_radar(ctx, r);
+    if (st != SARBP_OK) return st;
+    if (ns <= 0) return fail(ctx, SARBP_ERR_INVALID_ARGUMENT, "ns must be > 0");
+    const double ncd = std::floor(r->tp * r->fs + 0.5);
+    if (!(ncd >= 1 && ncd < (1 << 24))) return fail(ctx, SARBP_ERR_INVALID_ARGUMENT, "tp*fs out of range");
+    const int nc = (int)ncd;
+    const long long nfft = next_pow2((long long)ns + nc - 1);
+    if ((long long)r->upsample * ns > (1LL << 30) || nfft > (1LL << 30))
+        return fail(ctx, SARBP_ERR_INVALID_ARGUMENT, "ns too large");
+    out->nc = nc;
+    out->nfft = (int32_t)nfft;
+    out->shift = nc / 2;
+    out->nbins = r->upsample * ns;
+    out->t0_bins = r->t_rec0 - (double)out->shift / r->fs;
+    out->bin_rate = (double)r->upsample * r->fs;
+    return SARBP_OK;
+}
+
+// iterative radix-2 FFT on the host (double), unnormalised, sign -1 forward
+void host_fft(std::vector<std::complex<double>> &x, int sign) {
+    const size_t n = x.size();
+    for (size_t i = 1, j = 0; i < n; ++i) {
+        size_t bit = n >> 1;
+        for (; j & bit; bit >>= 1) j ^= bit;
+        j ^= bit;
+        if (i < j) std::swap(x[i], x[j]);
+    }
+    for (size_t len = 2; len <= n; len <<= 1) {
+        for (size_t i = 0; i < n; i += len) {
+            for (size_t k = 0; k < len / 2; ++k) {
+                const double a = sign * 2.0 * kPi * (double)k / (double)len;
+                const std::complex<double> w(std::cos(a), std::sin(a));
+                const std::complex<double> u = x[i + k], v = x[i + k + len / 2] * w;
+                x[i + k] = u + v;
+                x[i + k + len / 2] = u - v;
+            }
+        }
+    }
+}
+
+sarbp_status ensure_tables(sarbp_ctx *ctx, const sarbp_radar *r, const sarbp_rc_layout &lay) {
+    RcTables &t = ctx->tables;
+    if (t.valid && t.nfft == lay.nfft && t.L == r->upsample && t.nc == lay.nc && t.shift == lay.shift &&
+        t.kr == r->kr && t.fs == r->fs && t.tc == r->tc && t.tp == r->tp)
+        return SARBP_OK;
+    t.valid = false;
+    const int N = lay.nfft, L = r->upsample;
+    // matched-filter spectrum G[k] = conj(H[k]) e^{-j2pi k shift/N} / N
+    std::vector<std::complex<double>> h(N);
+    for (int i = 0; i < lay.nc; ++i) {
+        const double u = (double)i / r->fs;
+        if (u >= 0.0 && u < r->tp) {
+            const double ph = kPi * r->kr * (u - r->tc) * (u - r->tc);
+            h[i] = std::complex<double>(std::cos(ph), std::sin(ph));
+        }
+    }
+    host_fft(h, -1);
+    std::vector<float2> g(N), tw(N), ramp((size_t)L * N);
+    for (int k = 0; k < N; ++k) {
+        const long long m = ((long long)k * lay.shift) % N;
+        const double a = -2.0 * kPi * (double)m / (double)N;
+        const std::complex<double> v = std::conj(h[k]) * std::complex<double>(std::cos(a), std::sin(a)) / (double)N;
+        g[k] = make_float2((float)v.real(), (float)v.imag());
+        const double b = -2.0 * kPi * (double)k / (double)N;
+        tw[k] = make_float2((float)std::cos(b), (float)std::sin(b));
+    }
+    for (size_t m = 0; m < (size_t)L * N; ++m) {
+        const double a = 2.0 * kPi * (double)m / ((double)L * N);
+        ramp[m] = make_float2((float)std::cos(a), (float)std::sin(a));
+    }
+    SARBP_CUDA(ctx, t.filt.ensure(sizeof(float2) * N), "alloc filter");
+    SARBP_CUDA(ctx, t.tw.ensure(sizeof(float2) * N), "alloc twiddles");
+    SARBP_CUDA(ctx, t.ramp.ensure(sizeof(float2) * ramp.size()), "alloc ramp");
+    SARBP_CUDA(ctx, cudaMemcpy(t.filt.ptr, g.data(), sizeof(float2) * N, cudaMemcpyHostToDevice), "upload filter");
+    SARBP_CUDA(ctx, cudaMemcpy(t.tw.ptr, tw.data(), sizeof(float2) * N, cudaMemcpyHostToDevice), "upload twiddles");
+    SARBP_CUDA(ctx, cudaMemcpy(t.ramp.ptr, ramp.data(), sizeof(float2) * ramp.size(), cudaMemcpyHostToDevice),
+               "upload ramp");
+    t.valid = true;
+    t.nfft = N;
+    t.L = L;
+    t.nc = lay.nc;
+    t.shift = lay.shift;
+    t.kr = r->kr;
+    t.fs = r->fs;
+    t.tc = r->tc;
+    t.tp = r->tp;
+    return SARBP_OK;
+}
+
+cudaStream_t pick_stream(sarbp_ctx *ctx, void *stream) {
+    return stream ? static_cast<cudaStream_t>(stream) : ctx->stream;
+}
+
+sarbp_status check_errword(sarbp_ctx *ctx) {
+    unsigned w = 0;
+    SARBP_CUDA(ctx, cudaMemcpy(&w, ctx->errword.ptr, sizeof w, cudaMemcpyDeviceToHost), "read device check word");
+    if (w == 0) return SARBP_OK;
+    SARBP_CUDA(ctx, cudaMemset(ctx->errword.ptr, 0, sizeof(unsigned)), "reset device check word");
+    if (w & sarbp::kErrWaitTimeout) return fail(ctx, SARBP_ERR_TIMEOUT, "a bounded device wait ran out (0x%x)", w);
+    if (w & sarbp::kErrWindow)
+        return fail(ctx, SARBP_ERR_DEVICE_CHECK, "a tile needed more range bins than the staging window (0x%x)", w);
+    return fail(ctx, SARBP_ERR_DEVICE_CHECK, "device check word 0x%x", w);
+}
+
+// finish a call: synchronise when host memory is involved, read timings and checks
+sarbp_status finish(sarbp_ctx *ctx, cudaStream_t s, bool sync) {
+    if (!sync) return SARBP_OK;
+    SARBP_CUDA(ctx, cudaStreamSynchronize(s), "stream synchronize");
+    if (ctx->timed_rc) cudaEventElapsedTime(&ctx->rc_ms, ctx->ev[0], ctx->ev[1]);
+    if (ctx->timed_bp) cudaEventElapsedTime(&ctx->bp_ms, ctx->ev[2], ctx->ev[3]);
+    return check_errword(ctx);
+}
+
+// Range compression of a device-resident echo into a device rc buffer.
+sarbp_status rc_device(sarbp_ctx *ctx, const sarbp_radar *r, const sarbp_rc_layout &lay, const float2 *echo,
+                       int np, int ns, int storage, void *rc_out, float *scale_out, cudaStream_t s) {
+    if (!sarbp::rc_size_supported(lay.nfft))
+        return fail(ctx, SARBP_ERR_UNSUPPORTED, "range FFT size %d not supported (max 16384: ns + tp*fs - 1 <= 16384)",
+                    lay.nfft);
+    sarbp_status st = ensure_tables(ctx, r, lay);
+    if (st != SARBP_OK) return st;
+    const size_t row = sizeof(float2) * (size_t)lay.nfft;
+    const int batch = (int)std::max<size_t>(1, std::min<size_t>((size_t)np, kSpecScratchBudget / row));
+    SARBP_CUDA(ctx, ctx->spec.ensure(row * (size_t)batch), "alloc spectrum scratch");
+    float *scale = scale_out;
+    if (storage == SARBP_STORE_C32H && !scale) return fail(ctx, SARBP_ERR_INVALID_ARGUMENT, "fp16 storage needs a scale array");
+    const size_t esize = storage == SARBP_STORE_C64 ? 8 : 4;
+    cudaEventRecord(ctx->ev[0], s);
+    for (int p0 = 0; p0 < np; p0 += batch) {
+        RcPlan plan;
+        plan.np = std::min(batch, np - p0);
+        plan.ns = ns;
+        plan.nfft = lay.nfft;
+        plan.L = r->upsample;
+        plan.nbins = lay.nbins;
+        plan.storage = storage;
+        SARBP_CUDA(ctx, sarbp::launch_rc_forward(plan, echo + (size_t)p0 * ns, ctx->tables.filt.as<float2>(),
+                                                 ctx->tables.tw.as<float2>(), ctx->spec.as<float2>(),
+                                                 scale ? scale + p0 : nullptr, s),
+                   "range compression (forward)");
+        SARBP_CUDA(ctx, sarbp::launch_rc_inverse(plan, ctx->spec.as<float2>(), ctx->tables.tw.as<float2>(),
+                                                 ctx->tables.ramp.as<float2>(), scale ? scale + p0 : nullptr,
+                                                 static_cast<char *>(rc_out) + (size_t)p0 * lay.nbins * esize, s),
+                   "range compression (inverse)");
+        ctx->launches += 2;
+    }
+    cudaEventRecord(ctx->ev[1], s);
+    ctx->timed_rc = true;
+    return SARBP_OK;
+}
+
+sarbp_status check_grid(sarbp_ctx *ctx, const sarbp_grid *g) {
+    if (!g) return fail(ctx, SARBP_ERR_INVALID_ARGUMENT, "grid is null");
+    if (g->nx < 0 || g->ny < 0) return fail(ctx, SARBP_ERR_INVALID_ARGUMENT, "grid size must be >= 0");
+    if ((long long)g->nx * g->ny > (1LL << 31)) return fail(ctx, SARBP_ERR_INVALID_ARGUMENT, "grid too large");
+    for (int i = 0; i < 3; ++i)
+        if (!std::isfinite(g->origin[i]) || !std::isfinite(g->ux[i]) || !std::isfinite(g->uy[i]))
+            return fail(ctx, SARBP_ERR_INVALID_ARGUMENT, "grid vectors must be finite");
+    return SARBP_OK;
+}
+
+double dot3(const double *a, const double *b) { return a[0] * b[0] + a[1] * b[1] + a[2] * b[2]; }
+
+// Back-projection of device-resident rc + apc into a device image.
+sarbp_status bp_device(sarbp_ctx *ctx, const sarbp_radar *r, const sarbp_rc_view &rc, const double *apc_dev,
+                       const double *apc_host, const sarbp_grid *g, int mode, float2 *image, int accumulate,
+                       cudaStream_t s) {
+    const int np = rc.np;
+    if (g->nx == 0 || g->ny == 0) return SARBP_OK;
+    if (np == 0) {
+        if (!accumulate)
+            SARBP_CUDA(ctx, cudaMemsetAsync(image, 0, sizeof(float2) * (size_t)g->nx * g->ny, s), "clear image");
+        return SARBP_OK;
+    }
+    if (rc.nbins % 4 != 0) return fail(ctx, SARBP_ERR_UNSUPPORTED, "nbins must be a multiple of 4");
+    if (((uintptr_t)rc.data & 15) != 0) return fail(ctx, SARBP_ERR_INVALID_ARGUMENT, "rc data must be 16-byte aligned");
+    int tx, ty;
+    sarbp::bp_tile_dims(mode, &tx, &ty);
+    BpPlan p;
+    std::memset(&p, 0, sizeof p);
+    p.rc = rc.data;
+    p.scale = rc.scale;
+    p.storage = rc.storage;
+    p.np = np;
+    p.nbins = rc.nbins;
+    p.mode = mode;
+    p.apc = apc_dev;
+    for (int i = 0; i < 3; ++i) {
+        p.g.origin[i] = g->origin[i];
+        p.g.ux[i] = g->ux[i];
+        p.g.uy[i] = g->uy[i];
+    }
+    p.g.g11 = dot3(g->ux, g->ux);
+    p.g.g12 = dot3(g->ux, g->uy);
+    p.g.g22 = dot3(g->uy, g->uy);
+    p.g.nx = g->nx;
+    p.g.ny = g->ny;
+    p.fc = r->fc;
+    p.c = r->c;
+    p.t0_bins = rc.t0_bins;
+    p.bin_rate = rc.bin_rate;
+    p.image = image;
+    p.accumulate = accumulate;
+    p.err = ctx->errword.as<unsigned>();
+
+    // Staging window: bins a tile can touch for one pulse, bounded over all pulses
+    // from the grid's extreme line-of-sight directions (sampled on a 9x9 lattice).
+    const double hx = 0.5 * (tx - 1), hy = 0.5 * (ty - 1);
+    const double lux = std::sqrt(p.g.g11), luy = std::sqrt(p.g.g22);
+    const double qq_max = hx * hx * p.g.g11 + 2 * hx * hy * std::fabs(p.g.g12) + hy * hy * p.g.g22;
+    double cx = 0, sy = 0, rmin = 1e300, rmax = 0;
+    for (int i = 0; i < np; ++i) {
+        const double *a = apc_host + 3 * (size_t)i;
+        for (int u = 0; u <= 8; ++u) {
+            for (int v = 0; v <= 8; ++v) {
+                const double fx = (g->nx - 1) * u / 8.0, fy = (g->ny - 1) * v / 8.0;
+                double w[3];
+                for (int k = 0; k < 3; ++k) w[k] = g->origin[k] + fx * g->ux[k] + fy * g->uy[k] - a[k];
+                const double R = std::sqrt(dot3(w, w));
+                rmin = std::min(rmin, R);
+                rmax = std::max(rmax, R);
+                if (R > 0) {
+                    if (lux > 0) cx = std::max(cx, std::fabs(dot3(g->ux, w)) / (R * lux));
+                    if (luy > 0) sy = std::max(sy, std::fabs(dot3(g->uy, w)) / (R * luy));
+                }
+            }
+        }
+    }
+    const double tile_diag = std::sqrt(qq_max);
+    const double rmin_tile = rmin - tile_diag;
+    if (mode == SARBP_MODE_SPLIT || mode == SARBP_MODE_FP16STORE || mode == SARBP_MODE_FP32 || mode == SARBP_MODE_FP64) {
+        if (!(rmin_tile > 20.0 * tile_diag))
+            return fail(ctx, SARBP_ERR_UNSUPPORTED, "an antenna position is within 20 tile diagonals of the grid");
+    }
+    cx = std::min(1.0, cx * 1.05 + 0.01);
+    sy = std::min(1.0, sy * 1.05 + 0.01);
+    const double bpm = 2.0 / r->c * rc.bin_rate;
+    const double half = bpm * (lux * hx * cx + luy * hy * sy + qq_max / (2 * rmin_tile)) * 1.01 + 2.0;
+    int win = (int)std::ceil(2 * half) + 8;
+    win = (win + 3) & ~3;
+    if (win > 1024) return fail(ctx, SARBP_ERR_UNSUPPORTED, "tile spans too many range bins (%d)", win);
+    p.win = win;
+    // series terms: dR error ~ R (5/128) e^4 for 3 terms, e = |n|/R^2 <= (2 diag R + diag^2)/R^2
+    const double e = (2 * tile_diag * rmax + qq_max) / (rmin_tile * rmin_tile);
+    p.nterms = (rmax * 0.0390625 * e * e * e * e < 1e-8) ? 3 : 4;
+    if (rmax * 0.02734375 * std::pow(e, 5) > 1e-7)
+        return fail(ctx, SARBP_ERR_UNSUPPORTED, "tiles too large for the differential-range series");
+
+    // pulse segments: fill at least ~2 waves of CTAs
+    const int tiles = ((g->nx + tx - 1) / tx) * ((g->ny + ty - 1) / ty);
+    const int chunk = sarbp::bp_pulses_per_chunk(mode);
+    int cta_per_sm = 2;
+    const size_t smem = sarbp::bp_smem_bytes(mode, win);
+    if (smem > 0) cta_per_sm = std::max<int>(1, std::min<int>(3, (int)((227u << 10) / (smem + 1024))));
+    const int want = 2 * ctx->sms * cta_per_sm;
+    int segments = 1;
+    while (tiles * segments < want && np / (segments * 2) >= 4 * chunk) segments *= 2;
+    p.segments = segments;
+    if (segments > 1) {
+        SARBP_CUDA(ctx, ctx->partial.ensure(sizeof(float2) * (size_t)segments * g->nx * g->ny), "alloc partial images");
+        p.partial = ctx->partial.as<float2>();
+    }
+    int launches = 0;
+    cudaEventRecord(ctx->ev[2], s);
+    SARBP_CUDA(ctx, sarbp::launch_bp(p, s, &launches), "back-projection launch");
+    cudaEventRecord(ctx->ev[3], s);
+    ctx->timed_bp = true;
+    ctx->launches += launches;
+    return SARBP_OK;
+}
+
+std::mutex g_shim_mu;
+sarbp_ctx *g_shim_ctx = nullptr;
+int g_shim_dev = -1;
+
+}  // namespace
+
+extern "C" {
+
+int sarbp_abi_version(void) { return SARBP_ABI_VERSION; }
+
+const char *sarbp_status_string(sarbp_status s) {
+    switch (s) {
+        case SARBP_OK: return "ok";
+        case SARBP_ERR_INVALID_ARGUMENT: return "invalid argument";
+        case SARBP_ERR_UNSUPPORTED: return "unsupported";
+        case SARBP_ERR_OUT_OF_MEMORY: return "out of memory";
+        case SARBP_ERR_CUDA: return "CUDA error";
+        case SARBP_ERR_NO_DEVICE: return "no usable device";
+        case SARBP_ERR_TIMEOUT: return "device wait timed out";
+        case SARBP_ERR_DEVICE_CHECK: return "device-side check failed";
+        case SARBP_ERR_NOT_READY: return "not ready";
+        case SARBP_ERR_CANCELLED: return "cancelled";
+        case SARBP_ERR_BUDGET: return "over memory budget";
+        case SARBP_ERR_INTERNAL: return "internal error";
+    }
+    return "unknown status";
+}
+
+sarbp_status sarbp_create(sarbp_ctx **out, int device) {
+    if (!out) return SARBP_ERR_INVALID_ARGUMENT;
+    *out = nullptr;
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess || n <= 0) {
+        cudaGetLastError();
+        return SARBP_ERR_NO_DEVICE;
+    }
+    if (device < 0 || device >= n) return SARBP_ERR_INVALID_ARGUMENT;
+    cudaDeviceProp prop;
+    if (cudaGetDeviceProperties(&prop, device) != cudaSuccess) return SARBP_ERR_NO_DEVICE;
+    if (prop.major * 10 + prop.minor != 103) return SARBP_ERR_NO_DEVICE;
+    if (cudaSetDevice(device) != cudaSuccess) return SARBP_ERR_NO_DEVICE;
+    sarbp_ctx *ctx = new sarbp_ctx();
+    ctx->device = device;
+    ctx->sms = prop.multiProcessorCount;
+    bool ok = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) == cudaSuccess;
+    for (int i = 0; i < 4 && ok; ++i) ok = cudaEventCreate(&ctx->ev[i]) == cudaSuccess;
+    ok = ok && ctx->errword.ensure(sizeof(unsigned)) == cudaSuccess && ctx->power.ensure(sizeof(double)) == cudaSuccess;
+    ok = ok && cudaMemset(ctx->errword.ptr, 0, sizeof(unsigned)) == cudaSuccess;
+    if (!ok) {
+        cudaGetLastError();
+        sarbp_destroy(ctx);
+        return SARBP_ERR_CUDA;
+    }
+    *out = ctx;
+    return SARBP_OK;
+}
+
+sarbp_status sarbp_destroy(sarbp_ctx *ctx) {
+    if (!ctx) return SARBP_ERR_INVALID_ARGUMENT;
+    cudaSetDevice(ctx->device);
+    if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    for (DevBuf *b : {&ctx->echo, &ctx->spec, &ctx->rc, &ctx->scale, &ctx->apc, &ctx->image, &ctx->partial,
+                      &ctx->errword, &ctx->power, &ctx->targets, &ctx->tables.filt, &ctx->tables.tw,
+                      &ctx->tables.ramp})
+        b->release();
+    for (cudaEvent_t &e : ctx->ev)
+        if (e) cudaEventDestroy(e);
+    if (ctx->stream) cudaStreamDestroy(ctx->stream);
+    delete ctx;
+    return SARBP_OK;
+}
+
+const char *sarbp_last_error(const sarbp_ctx *ctx) { return ctx ? ctx->err.c_str() : "null context"; }
+
+sarbp_status sarbp_synchronize(sarbp_ctx *ctx) {
+    if (!ctx) return SARBP_ERR_INVALID_ARGUMENT;
+    cudaSetDevice(ctx->device);
+    SARBP_CUDA(ctx, cudaDeviceSynchronize(), "device synchronize");
+    if (ctx->timed_rc) cudaEventElapsedTime(&ctx->rc_ms, ctx->ev[0], ctx->ev[1]);
+    if (ctx->timed_bp) cudaEventElapsedTime(&ctx->bp_ms, ctx->ev[2], ctx->ev[3]);
+    return check_errword(ctx);
+}
+
+sarbp_status sarbp_trim(sarbp_ctx *ctx) {
+    if (!ctx) return SARBP_ERR_INVALID_ARGUMENT;
+    cudaSetDevice(ctx->device);
+    cudaStreamSynchronize(ctx->stream);
+    for (DevBuf *b : {&ctx->echo, &ctx->spec, &ctx->rc, &ctx->scale, &ctx->apc, &ctx->image, &ctx->partial,
+                      &ctx->targets})
+        b->release();
+    return SARBP_OK;
+}
+
+size_t sarbp_device_bytes(const sarbp_ctx *ctx) {
+    if (!ctx) return 0;
+    size_t t = 0;
+    for (const DevBuf *b : {&ctx->echo, &ctx->spec, &ctx->rc, &ctx->scale, &ctx->apc, &ctx->image, &ctx->partial,
+                            &ctx->errword, &ctx->power, &ctx->targets, &ctx->tables.filt, &ctx->tables.tw,
+                            &ctx->tables.ramp})
+        t += b->bytes;
+    return t;
+}
+
+sarbp_status sarbp_rc_layout_get(const sarbp_radar *radar, int32_t ns, sarbp_rc_layout *out) {
+    if (!out) return SARBP_ERR_INVALID_ARGUMENT;
+    return layout(nullptr, radar, ns, out);
+}
+
+sarbp_status sarbp_range_compress(sarbp_ctx *ctx, const sarbp_radar *radar, const sarbp_complex64 *echo,
+                                  int32_t np, int32_t ns, int32_t storage, void *rc_out, float *rc_scale_out,
+                                  void *stream) {
+    if (!ctx) return SARBP_ERR_INVALID_ARGUMENT;
+    ctx->err.clear();
+    cudaSetDevice(ctx->device);
+    sarbp_rc_layout lay;
+    sarbp_status st = layout(ctx, radar, ns, &lay);
+    if (st != SARBP_OK) return st;
+    if (np < 0) return fail(ctx, SARBP_ERR_INVALID_ARGUMENT, "np must be >= 0");
+    if (storage != SARBP_STORE_C64 && storage != SARBP_STORE_C32H)
+        return fail(ctx, SARBP_ERR_INVALID_ARGUMENT, "unknown storage %d", storage);
+    if (np == 0) return SARBP_OK;
+    if (!echo || !rc_out) return fail(ctx, SARBP_ERR_INVALID_ARGUMENT, "echo and rc_out must be non-null");
+    if (storage == SARBP_STORE_C32H && !rc_scale_out)
+        return fail(ctx, SARBP_ERR_INVALID_ARGUMENT, "fp16 storage needs rc_scale_out");
+    cudaStream_t s = pick_stream(ctx, stream);
+    const size_t esize = storage == SARBP_STORE_C64 ? 8 : 4;
+    const bool dev_in = is_device_ptr(echo), dev_out = is_device_ptr(rc_out);
+    const bool dev_sc = storage == SARBP_STORE_C64 || is_device_ptr(rc_scale_out);
+    const float2 *d_echo = reinterpret_cast<const float2 *>(echo);
+    if (!dev_in) {
+        SARBP_CUDA(ctx, ctx->echo.ensure(sizeof(float2) * (size_t)np * ns), "alloc echo");
+        SARBP_CUDA(ctx, cudaMemcpyAsync(ctx->echo.ptr, echo, sizeof(float2) * (size_t)np * ns, cudaMemcpyHostToDevice, s),
+                   "upload echo");
+        d_echo = ctx->echo.as<float2>();
+    }
+    void *d_rc = rc_out;
+    if (!dev_out) {
+        SARBP_CUDA(ctx, ctx->rc.ensure(esize * (size_t)np * lay.nbins), "alloc rc");
+        d_rc = ctx->rc.ptr;
+    }
+    float *d_scale = rc_scale_out;
+    if (storage == SARBP_STORE_C32H && !dev_sc) {
+        SARBP_CUDA(ctx, ctx->scale.ensure(sizeof(float) * np), "alloc scale");
+        d_scale = ctx->scale.as<float>();
+    }
+    ctx->timed_bp = false;
+    st = rc_device(ctx, radar, lay, d_echo, np, ns, storage, d_rc, storage == SARBP_STORE_C32H ? d_scale : nullptr, s);
+    if (st != SARBP_OK) return st;
+    if (!dev_out)
+        SARBP_CUDA(ctx, cudaMemcpyAsync(rc_out, d_rc, esize * (size_t)np * lay.nbins, cudaMemcpyDeviceToHost, s),
+                   "download rc");
+    if (storage == SARBP_STORE_C32H && !dev_sc)
+        SARBP_CUDA(ctx, cudaMemcpyAsync(rc_scale_out, d_scale, sizeof(float) * np, cudaMemcpyDeviceToHost, s),
+                   "download scale");
+    return finish(ctx, s, !dev_in || !dev_out || !dev_sc);
+}
+
+sarbp_status sarbp_backproject(sarbp_ctx *ctx, const sarbp_radar *radar, const sarbp_rc_view *rc,
+                               const double *apc, const sarbp_grid *grid, int32_t mode, sarbp_complex64 *image,
+                               int32_t accumulate, void *stream) {
+    if (!ctx) return SARBP_ERR_INVALID_ARGUMENT;
+    ctx->err.clear();
+    cudaSetDevice(ctx->device);
+    sarbp_status st = check_radar(ctx, radar);
+    if (st != SARBP_OK) return st;
+    if (!rc) return fail(ctx, SARBP_ERR_INVALID_ARGUMENT, "rc view is null");
+    st = check_grid(ctx, grid);
+    if (st != SARBP_OK) return st;
+    if (mode < SARBP_MODE_FP64 || mode > SARBP_MODE_FP16STORE)
+        return fail(ctx, SARBP_ERR_INVALID_ARGUMENT, "unknown mode %d", mode);
+    if (rc->np < 0 || rc->nbins < 0) return fail(ctx, SARBP_ERR_INVALID_ARGUMENT, "negative rc size");
+    if (rc->storage != SARBP_STORE_C64 && rc->storage != SARBP_STORE_C32H)
+        return fail(ctx, SARBP_ERR_INVALID_ARGUMENT, "unknown storage %d", rc->storage);
+    if (mode == SARBP_MODE_FP16STORE && rc->storage != SARBP_STORE_C32H)
+        return fail(ctx, SARBP_ERR_INVALID_ARGUMENT, "FP16STORE mode needs SARBP_STORE_C32H data");
+    if (!(rc->bin_rate > 0) || !std::isfinite(rc->t0_bins))
+        return fail(ctx, SARBP_ERR_INVALID_ARGUMENT, "rc bin_rate must be > 0 and t0_bins finite");
+    const size_t npix = (size_t)grid->nx * grid->ny;
+    if (npix == 0) return SARBP_OK;
+    if (!image) return fail(ctx, SARBP_ERR_INVALID_ARGUMENT, "image is null");
+    if (rc->np > 0 && (!rc->data || !apc)) return fail(ctx, SARBP_ERR_INVALID_ARGUMENT, "rc data and apc must be non-null");
+    if (rc->np > 0 && rc->nbins < 2) return fail(ctx, SARBP_ERR_INVALID_ARGUMENT, "nbins must be >= 2");
+    if (rc->storage == SARBP_STORE_C32H && rc->np > 0 && !rc->scale)
+        return fail(ctx, SARBP_ERR_INVALID_ARGUMENT, "fp16 storage needs a scale array");
+    cudaStream_t s = pick_stream(ctx, stream);
+    const size_t esize = rc->storage == SARBP_STORE_C64 ? 8 : 4;
+    const int np = rc->np;
+    bool any_host = false;
+    // APC: always needed on the host for planning, and on the device for the kernel
+    std::vector<double> apc_h;
+    const double *apc_host = apc, *apc_dev = apc;
+    if (np > 0) {
+        if (is_device_ptr(apc)) {
+            apc_h.resize((size_t)3 * np);
+            SARBP_CUDA(ctx, cudaMemcpyAsync(apc_h.data(), apc, sizeof(double) * 3 * np, cudaMemcpyDeviceToHost, s),
+                       "read apc");
+            SARBP_CUDA(ctx, cudaStreamSynchronize(s), "read apc");
+            apc_host = apc_h.data();
+        } else {
+            SARBP_CUDA(ctx, ctx->apc.ensure(sizeof(double) * 3 * np), "alloc apc");
+            SARBP_CUDA(ctx, cudaMemcpyAsync(ctx->apc.ptr, apc, sizeof(double) * 3 * np, cudaMemcpyHostToDevice, s),
+                       "upload apc");
+            apc_dev = ctx->apc.as<double>();
+            any_host = true;
+        }
+        for (size_t i = 0; i < (size_t)3 * np; ++i)
+            if (!std::isfinite(apc_host[i])) return fail(ctx, SARBP_ERR_INVALID_ARGUMENT, "apc must be finite");
+    }
+    sarbp_rc_view v = *rc;
+    if (np > 0 && !is_device_ptr(rc->data)) {
+        SARBP_CUDA(ctx, ctx->rc.ensure(esize * (size_t)np * rc->nbins), "alloc rc");
+        SARBP_CUDA(ctx, cudaMemcpyAsync(ctx->rc.ptr, rc->data, esize * (size_t)np * rc->nbins, cudaMemcpyHostToDevice, s),
+                   "upload rc");
+        v.data = ctx->rc.ptr;
+        any_host = true;
+    }
+    if (np > 0 && rc->storage == SARBP_STORE_C32H && !is_device_ptr(rc->scale)) {
+        SARBP_CUDA(ctx, ctx->scale.ensure(sizeof(float) * np), "alloc scale");
+        SARBP_CUDA(ctx, cudaMemcpyAsync(ctx->scale.ptr, rc->scale, sizeof(float) * np, cudaMemcpyHostToDevice, s),
+                   "upload scale");
+        v.scale = ctx->scale.as<float>();
+        any_host = true;
+    }
+    float2 *d_img = reinterpret_cast<float2 *>(image);
+    const bool dev_img = is_device_ptr(image);
+    if (!dev_img) {
+        SARBP_CUDA(ctx, ctx->image.ensure(sizeof(float2) * npix), "alloc image");
+        d_img = ctx->image.as<float2>();
+        if (accumulate)
+            SARBP_CUDA(ctx, cudaMemcpyAsync(d_img, image, sizeof(float2) * npix, cudaMemcpyHostToDevice, s), "upload image");
+        any_host = true;
+    }
+    ctx->timed_rc = false;
+    st = bp_device(ctx, radar, v, apc_dev, apc_host, grid, mode, d_img, accumulate, s);
+    if (st != SARBP_OK) return st;
+    if (!dev_img)
+        SARBP_CUDA(ctx, cudaMemcpyAsync(image, d_img, sizeof(float2) * npix, cudaMemcpyDeviceToHost, s), "download image");
+    return finish(ctx, s, any_host);
+}
+
+sarbp_status sarbp_image(sarbp_ctx *ctx, const sarbp_radar *radar, const sarbp_complex64 *echo, int32_t np,
+                         int32_t ns, const double *apc, const sarbp_grid *grid, int32_t mode, sarbp_complex64 *image,
+                         void *stream) {
+    if (!ctx) return SARBP_ERR_INVALID_ARGUMENT;
+    ctx->err.clear();
+    cudaSetDevice(ctx->device);
+    sarbp_rc_layout lay;
+    sarbp_status st = layout(ctx, radar, ns, &lay);
+    if (st != SARBP_OK) return st;
+    st = check_grid(ctx, grid);
+    if (st != SARBP_OK) return st;
+    if (mode < SARBP_MODE_FP64 || mode > SARBP_MODE_FP16STORE)
+        return fail(ctx, SARBP_ERR_INVALID_ARGUMENT, "unknown mode %d", mode);
+    if (np < 0) return fail(ctx, SARBP_ERR_INVALID_ARGUMENT, "np must be >= 0");
+    const size_t npix = (size_t)grid->nx * grid->ny;
+    if (npix == 0) return SARBP_OK;
+    if (!image) return fail(ctx, SARBP_ERR_INVALID_ARGUMENT, "image is null");
+    if (np > 0 && (!echo || !apc)) return fail(ctx, SARBP_ERR_INVALID_ARGUMENT, "echo and apc must be non-null");
+    cudaStream_t s = pick_stream(ctx, stream);
+    const int storage = mode == SARBP_MODE_FP16STORE ? SARBP_STORE_C32H : SARBP_STORE_C64;
+    const size_t esize = storage == SARBP_STORE_C64 ? 8 : 4;
+    bool any_host = false;
+    const float2 *d_echo = reinterpret_cast<const float2 *>(echo);
+    if (np > 0 && !is_device_ptr(echo)) {
+        SARBP_CUDA(ctx, ctx->echo.ensure(sizeof(float2) * (size_t)np * ns), "alloc echo");
+        SARBP_CUDA(ctx, cudaMemcpyAsync(ctx->echo.ptr, echo, sizeof(float2) * (size_t)np * ns, cudaMemcpyHostToDevice, s),
+                   "upload echo");
+        d_echo = ctx->echo.as<float2>();
+        any_host = true;
+    }
+    std::vector<double> apc_h;
+    const double *apc_host = apc, *apc_dev = apc;
+    if (np > 0) {
+        if (is_device_ptr(apc)) {
+            apc_h.resize((size_t)3 * np);
+            SARBP_CUDA(ctx, cudaMemcpy(apc_h.data(), apc, sizeof(double) * 3 * np, cudaMemcpyDeviceToHost), "read apc");
+            apc_host = apc_h.data();
+        } else {
+            SARBP_CUDA(ctx, ctx->apc.ensure(sizeof(double) * 3 * np), "alloc apc");
+            SARBP_CUDA(ctx, cudaMemcpyAsync(ctx->apc.ptr, apc, sizeof(double) * 3 * np, cudaMemcpyHostToDevice, s),
+                       "upload apc");
+            apc_dev = ctx->apc.as<double>();
+            any_host = true;
+        }
+        for (size_t i = 0; i < (size_t)3 * np; ++i)
+            if (!std::isfinite(apc_host[i])) return fail(ctx, SARBP_ERR_INVALID_ARGUMENT, "apc must be finite");
+    }
+    float2 *d_img = reinterpret_cast<float2 *>(image);
+    const bool dev_img = is_device_ptr(image);
+    if (!dev_img) {
+        SARBP_CUDA(ctx, ctx->image.ensure(sizeof(float2) * npix), "alloc image");
+        d_img = ctx->image.as<float2>();
+        any_host = true;
+    }
+    ctx->timed_rc = ctx->timed_bp = false;
+    sarbp_rc_view v;
+    std::memset(&v, 0, sizeof v);
+    v.storage = storage;
+    v.np = np;
+    v.nbins = lay.nbins;
+    v.t0_bins = lay.t0_bins;
+    v.bin_rate = lay.bin_rate;
+    if (np > 0) {
+        SARBP_CUDA(ctx, ctx->rc.ensure(esize * (size_t)np * lay.nbins), "alloc rc");
+        if (storage == SARBP_STORE_C32H) SARBP_CUDA(ctx, ctx->scale.ensure(sizeof(float) * np), "alloc scale");
+        st = rc_device(ctx, radar, lay, d_echo, np, ns, storage, ctx->rc.ptr,
+                       storage == SARBP_STORE_C32H ? ctx->scale.as<float>() : nullptr, s);
+        if (st != SARBP_OK) return st;
+        v.data = ctx->rc.ptr;
+        v.scale = storage == SARBP_STORE_C32H ? ctx->scale.as<float>() : nullptr;
+    }
+    st = bp_device(ctx, radar, v, apc_dev, apc_host, grid, mode, d_img, 0, s);
+    if (st != SARBP_OK) return st;
+    if (!dev_img)
+        SARBP_CUDA(ctx, cudaMemcpyAsync(image, d_img, sizeof(float2) * npix, cudaMemcpyDeviceToHost, s), "download image");
+    return finish(ctx, s, any_host);
+}
+
+sarbp_status sarbp_synthesize_echo(sarbp_ctx *ctx, const sarbp_radar *radar, const double *apc, int32_t np,
+                                   int32_t ns, const sarbp_target *targets, int32_t nt, double snr_db, uint64_t seed,
+                                   sarbp_complex64 *echo_out, void *stream) {
+    if (!ctx) return SARBP_ERR_INVALID_ARGUMENT;
+    ctx->err.clear();
+    cudaSetDevice(ctx->device);
+    sarbp_status st = check_radar(ctx, radar);
+    if (st != SARBP_OK) return st;
+    if (np < 0 || ns <= 0 || nt < 0 || nt > 4096)
+        return fail(ctx, SARBP_ERR_INVALID_ARGUMENT, "need np >= 0, ns > 0, 0 <= nt <= 4096");
+    if (np == 0) return SARBP_OK;
+    if (!apc || !echo_out || (nt > 0 && !targets)) return fail(ctx, SARBP_ERR_INVALID_ARGUMENT, "null pointer");
+    cudaStream_t s = pick_stream(ctx, stream);
+    bool any_host = false;
+    const double *d_apc = apc;
+    if (!is_device_ptr(apc)) {
+        SARBP_CUDA(ctx, ctx->apc.ensure(sizeof(double) * 3 * np), "alloc apc");
+        SARBP_CUDA(ctx, cudaMemcpyAsync(ctx->apc.ptr, apc, sizeof(double) * 3 * np, cudaMemcpyHostToDevice, s), "upload apc");
+        d_apc = ctx->apc.as<double>();
+        any_host = true;
+    }
+    const sarbp_target *d_tg = targets;
+    if (nt > 0 && !is_device_ptr(targets)) {
+        SARBP_CUDA(ctx, ctx->targets.ensure(sizeof(sarbp_target) * nt), "alloc targets");
+        SARBP_CUDA(ctx, cudaMemcpyAsync(ctx->targets.ptr, targets, sizeof(sarbp_target) * nt, cudaMemcpyHostToDevice, s),
+                   "upload targets");
+        d_tg = ctx->targets.as<sarbp_target>();
+        any_host = true;
+    }
+    float2 *d_echo = reinterpret_cast<float2 *>(echo_out);
+    const bool dev_out = is_device_ptr(echo_out);
+    if (!dev_out) {
+        SARBP_CUDA(ctx, ctx->echo.ensure(sizeof(float2) * (size_t)np * ns), "alloc echo");
+        d_echo = ctx->echo.as<float2>();
+        any_host = true;
+    }
+    const bool noise = !std::isnan(snr_db);
+    SARBP_CUDA(ctx, cudaMemsetAsync(ctx->power.ptr, 0, sizeof(double), s), "clear power");
+    SARBP_CUDA(ctx, sarbp::launch_echo_synth(d_apc, np, ns, d_tg, nt, radar->t_rec0, radar->fs, radar->kr, radar->tp,
+                                             radar->tc, radar->fc, radar->c, d_echo, ctx->power.as<double>(), s),
+               "echo synthesis");
+    ctx->launches += 1;
+    if (noise) {
+        SARBP_CUDA(ctx, sarbp::launch_echo_noise(d_echo, (int64_t)np * ns, ctx->power.as<double>(), snr_db, seed, s),
+                   "echo noise");
+        ctx->launches += 1;
+    }
+    if (!dev_out)
+        SARBP_CUDA(ctx, cudaMemcpyAsync(echo_out, d_echo, sizeof(float2) * (size_t)np * ns, cudaMemcpyDeviceToHost, s),
+                   "download echo");
+    ctx->timed_rc = ctx->timed_bp = false;
+    return finish(ctx, s, any_host);
+}
+
+// ------------------------------------------------------- reference shims --
+
+static sarbp_status shim_ctx(sarbp_ctx **out) {
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) {
+        cudaGetLastError();
+        return SARBP_ERR_NO_DEVICE;
+    }
+    std::lock_guard<std::mutex> lk(g_shim_mu);
+    if (!g_shim_ctx || g_shim_dev != dev) {
+        if (g_shim_ctx) sarbp_destroy(g_shim_ctx);
+        g_shim_ctx = nullptr;
+        sarbp_status st = sarbp_create(&g_shim_ctx, dev);
+        if (st != SARBP_OK) return st;
+        g_shim_dev = dev;
+    }
+    *out = g_shim_ctx;
+    return SARBP_OK;
+}
+
+sarbp_status sarbp_launch_back_projection(sarbp_complex64 *Srnm, sarbp_complex64 *Image,
+                                          const sarbp_ref_params *params, int32_t Na, int32_t Nr) {
+    if (!Srnm || !Image || !params || Na < 0 || Nr < 0) return SARBP_ERR_INVALID_ARGUMENT;
+    const sarbp_ref_params &q = *params;
+    if (q.Mslow <= 0 || q.Nfast <= 0 || !(q.vr != 0.f) || !(q.Fr > 0.f)) return SARBP_ERR_INVALID_ARGUMENT;
+    sarbp_ctx *ctx = nullptr;
+    sarbp_status st = shim_ctx(&ctx);
+    if (st != SARBP_OK) return st;
+    sarbp_radar r;
+    std::memset(&r, 0, sizeof r);
+    r.c = q.c;
+    r.fc = q.fc;
+    r.fs = q.Fr;
+    r.kr = q.Kr;
+    r.tp = q.Tr;
+    r.tc = 0.0;      // uncentred chirp, as generateEchoKernel emits (BPA_CUDA_kernels.cu:28)
+    r.t_rec0 = 0.0;  // tr_i = i / Fr (BPA_CUDA.cpp:44-48)
+    r.upsample = 8;
+    std::vector<double> apc((size_t)3 * q.Mslow);
+    const double ta0 = -(double)q.La / (2.0 * q.vr), ta1 = (double)q.La / (2.0 * q.vr);
+    const double step = q.Mslow > 1 ? (ta1 - ta0) / (q.Mslow - 1) : 0.0;
+    for (int m = 0; m < q.Mslow; ++m) {
+        apc[3 * m] = q.vr * (ta0 + m * step);
+        apc[3 * m + 1] = 0.0;
+        apc[3 * m + 2] = q.H;
+    }
+    sarbp_grid g;
+    std::memset(&g, 0, sizeof g);
+    g.origin[0] = (double)q.Az0 - (double)(Na / 2);
+    g.origin[1] = (double)q.Rg0 - (double)(Nr / 2);
+    g.uy[0] = 1.0;
+    g.ux[1] = 1.0;
+    g.nx = Nr;
+    g.ny = Na;
+    st = sarbp_image(ctx, &r, Srnm, q.Mslow, q.Nfast, apc.data(), &g, SARBP_MODE_SPLIT, Image, nullptr);
+    if (st != SARBP_OK) return st;
+    return sarbp_synchronize(ctx);
+}
+
+sarbp_status sarbp_launch_generate_echo(sarbp_complex64 *Srnm, const float *Ptarget, const float *ta, const float *tr,
+                                        const sarbp_ref_params *params, int32_t Mslow, int32_t Nfast) {
+    if (!Srnm || !ta || !tr || !params || Mslow < 0 || Nfast < 0) return SARBP_ERR_INVALID_ARGUMENT;
+    if (params->Ntarget > 0 && !Ptarget) return SARBP_ERR_INVALID_ARGUMENT;
+    sarbp_ctx *ctx = nullptr;
+    sarbp_status st = shim_ctx(&ctx);
+    if (st != SARBP_OK) return st;
+    SARBP_CUDA(ctx, sarbp::launch_ref_echo(reinterpret_cast<float2 *>(Srnm), Ptarget, ta, tr, *params, Mslow, Nfast,
+                                           ctx->stream),
+               "reference echo");
+    ctx->launches += 1;
+    SARBP_CUDA(ctx, cudaStreamSynchronize(ctx->stream), "reference echo sync");
+    return SARBP_OK;
+}
+
+sarbp_status sarbp_probe_issue_rates(sarbp_ctx *ctx, double *fp32_lanes_per_s, double *mufu_lanes_per_s,
+                                     int32_t *sm_count) {
+    if (!ctx) return SARBP_ERR_INVALID_ARGUMENT;
+    cudaSetDevice(ctx->device);
+    SARBP_CUDA(ctx, sarbp::run_issue_probe(ctx->sms, fp32_lanes_per_s, mufu_lanes_per_s, ctx->stream), "issue probe");
+    if (sm_count) *sm_count = ctx->sms;
+    return SARBP_OK;
+}
+
+sarbp_status sarbp_last_timings(sarbp_ctx *ctx, float *rc_ms, float *bp_ms) {
+    if (!ctx) return SARBP_ERR_INVALID_ARGUMENT;
+    if (rc_ms) *rc_ms = ctx->timed_rc ? ctx->rc_ms : 0.f;
+    if (bp_ms) *bp_ms = ctx->timed_bp ? ctx->bp_ms : 0.f;
+    return SARBP_OK;
+}
+
+int64_t sarbp_kernel_launches(const sarbp_ctx *ctx) { return ctx ? ctx->launches : 0; }
+
+}  // extern "C"

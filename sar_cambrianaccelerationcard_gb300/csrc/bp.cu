@@ -1,0 +1,514 @@
+// bp.cu -- back-projection on sm_103a.
+//
+// Algorithm: code/SAR_BP/matlab/BPA_SAR.m:177-197 (per pixel and pulse: slant
+// range, range bin, sample, phase compensation exp(+j 4 pi fc R / c), coherent
+// sum), with linear interpolation on the upsampled bins instead of the script's
+// nearest bin.  Kernel shape replaces backProjectionKernel
+// (code/SAR_BP/CUDA/BPA_CUDA_kernels.cu:47-77: one thread per pixel, global
+// loads, sqrtf + sincosf per pulse).
+//
+// Design (one CTA per TILE_X x TILE_Y pixel tile, optionally per pulse segment):
+//  * Pulses are processed in chunks of CHUNK.  For each chunk one warp computes,
+//    per pulse and in FP64, the tile-centre reference: range R_T, the wrapped
+//    carrier phase, the bin of the tile centre and the window of bins the tile
+//    can touch; it then issues one TMA bulk copy (cp.async.bulk, local HBM ->
+//    shared memory, completion on an mbarrier) per pulse for that window.  Two
+//    raw buffers alternate so the copies of chunk c+1 overlap the arithmetic of
+//    chunk c.
+//  * A conversion pass turns each raw window (complex64, or complex16 times the
+//    per-pulse scale) into interpolation-ready pairs (mid, diff) with
+//    mid_i = (s_i + s_{i+1})/2, diff_i = s_{i+1} - s_i, so one 16-byte shared load
+//    and two FMAs interpolate.
+//  * SPLIT arithmetic per pixel and pulse: with q the pixel offset from the tile
+//    centre, n = 2 q.w + |q|^2 (w = tile centre - APC) and the differential
+//    range dR = sqrt(R_T^2 + n) - R_T = n (c1 + n (c2 + n (c3 + n c4))) (series
+//    of sqrt(1+e), |e| = |n|/R_T^2 < 1e-2 enforced by the planner) -- all on the
+//    FMA pipe; the phase fma(dR, k_hi, phi_T) + dR k_lo (compensated product);
+//    the only MUFU work is one sin/cos pair.
+//  * Pulse geometry is computed once per (tile, pulse) and broadcast to all
+//    warps from shared memory.
+//  * FP32 and FP64 modes use the same staging with plain absolute-range
+//    arithmetic (the comparators).
+#include "sarbp_internal.h"
+
+#include <math_constants.h>
+
+namespace sarbp {
+namespace {
+
+constexpr int kThreads = 256;
+constexpr int kTileX = 32;  // pixels along x (columns)
+constexpr int kTileY = 64;  // pixels along y (rows)
+constexpr int kPix = kTileX * kTileY / kThreads;  // 8 pixels per thread
+constexpr int kChunk = 16;  // pulses per staged chunk
+constexpr float kMagic = 12582912.0f;  // 1.5 * 2^23: adding it rounds to an integer
+constexpr unsigned kMagicBitsShift4 = 0x4B400000u << 4;
+
+struct __align__(16) Prm {
+    float4 k0;     // SPLIT: A, B, c1, c2       FP32: apc x, y, z, bin offset
+    float4 k1;     // SPLIT: c3, c4, bin', phT
+    double ax, ay, az;  // FP64: APC position
+    float mp;      // kMagic + pulse slot * win
+    int ws;        // first bin of the window
+    int lo, hi;    // copied part of the window [lo, hi) relative to ws
+    float scale;   // FP16 storage scale
+    int pad0;
+};
+
+__device__ __forceinline__ unsigned smem_addr(const void *p) {
+    return static_cast<unsigned>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ void mbar_init(unsigned bar, unsigned count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx_arrive(unsigned bar, unsigned bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes)
+                 : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(unsigned bar, unsigned parity) {
+    unsigned ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(bar), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+
+__device__ __forceinline__ uint64_t globaltimer_ns() {
+    uint64_t t;
+    asm volatile("mov.u64 %0, %globaltimer;" : "=l"(t));
+    return t;
+}
+
+// Bounded wait: gives up after ~limit_ns and reports false.
+__device__ __forceinline__ bool mbar_wait_bounded(unsigned bar, unsigned parity, uint64_t limit_ns) {
+    if (mbar_try_wait(bar, parity)) return true;
+    const uint64_t t0 = globaltimer_ns();
+    for (;;) {
+#pragma unroll 1
+        for (int i = 0; i < 256; ++i)
+            if (mbar_try_wait(bar, parity)) return true;
+        if (globaltimer_ns() - t0 > limit_ns) return false;
+    }
+}
+
+__device__ __forceinline__ void tma_bulk_g2s(unsigned dst, const void *src, unsigned bytes,
+                                             unsigned bar) {
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+            dst),
+        "l"(src), "r"(bytes), "r"(bar)
+        : "memory");
+}
+
+__device__ __forceinline__ float4 lds128(unsigned addr) {
+    float4 v;
+    asm volatile("ld.shared.v4.f32 {%0, %1, %2, %3}, [%4];"
+                 : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w)
+                 : "r"(addr));
+    return v;
+}
+
+struct Smem {
+    float4 *staged;      // [kChunk][win]
+    unsigned char *raw;  // [2][kChunk][win] * 8 bytes
+    Prm *prm;            // [2][kChunk]
+    uint64_t *bar;       // [2]
+};
+
+__device__ __forceinline__ Smem carve(unsigned char *base, int win) {
+    Smem s;
+    s.staged = reinterpret_cast<float4 *>(base);
+    s.raw = base + (size_t)kChunk * win * 16;
+    s.prm = reinterpret_cast<Prm *>(s.raw + (size_t)2 * kChunk * win * 8);
+    s.bar = reinterpret_cast<uint64_t *>(s.prm + 2 * kChunk);
+    return s;
+}
+
+// Per-(tile, pulse) geometry, window, and TMA issue for one chunk (warp 0).
+template <int MODE, int STORE>
+__device__ __forceinline__ void produce_chunk(const BpPlan &P, const Smem &S, int buf, int p0, int count,
+                                             double pcx, double pcy, double pcz, float qq_max) {
+    const int lane = threadIdx.x & 31;
+    const int win = P.win;
+    const int esize = STORE == SARBP_STORE_C64 ? 8 : 4;
+    unsigned bytes = 0;
+    const char *src = nullptr;
+    unsigned dst = 0;
+    if (lane < count) {
+        const int p = p0 + lane;
+        const double ax = __ldg(&P.apc[3 * p]), ay = __ldg(&P.apc[3 * p + 1]),
+                     az = __ldg(&P.apc[3 * p + 2]);
+        const double wx = pcx - ax, wy = pcy - ay, wz = pcz - az;
+        const double R = sqrt(wx * wx + wy * wy + wz * wz);
+        const double A = 2.0 * (P.g.ux[0] * wx + P.g.ux[1] * wy + P.g.ux[2] * wz);
+        const double B = 2.0 * (P.g.uy[0] * wx + P.g.uy[1] * wy + P.g.uy[2] * wz);
+        const double bpm = 2.0 / P.c * P.bin_rate;  // bins per metre of range
+        const double bT = (2.0 * R / P.c - P.t0_bins) * P.bin_rate;
+        // |dR| <= (|A| hx + |B| hy + |q|^2_max) / (2 R) within the tile
+        const double hx = 0.5 * (kTileX - 1), hy = 0.5 * (kTileY - 1);
+        const double half = bpm * (fabs(A) * hx + fabs(B) * hy + (double)qq_max) / (2.0 * R) * 1.01 + 2.0;
+        long long ws = (long long)floor(bT - half);
+        ws &= ~3LL;
+        const long long need_end = (long long)ceil(bT + half) + 2;
+        if (need_end - ws > win) atomicOr(P.err, kErrWindow);
+        long long lo = ws < 0 ? 0 : ws;
+        long long hi = ws + win > P.nbins ? P.nbins : ws + win;
+        if (hi < lo) hi = lo;
+        Prm &q = S.prm[buf * kChunk + lane];
+        q.ws = (int)ws;
+        q.lo = (int)(lo - ws);
+        q.hi = (int)(hi - ws);
+        q.mp = kMagic + (float)(lane * win);
+        q.scale = STORE == SARBP_STORE_C32H ? __ldg(&P.scale[p]) : 1.f;
+        if (MODE == SARBP_MODE_SPLIT || MODE == SARBP_MODE_FP16STORE) {
+            const double iR = 1.0 / R;
+            const double c1 = 0.5 * iR;
+            const double c2 = -0.125 * iR * iR * iR;
+            const double c3 = 0.0625 * iR * iR * iR * iR * iR;
+            const double c4 = -0.0390625 * iR * iR * iR * iR * iR * iR * iR;
+            const double cyc = 2.0 * P.fc / P.c * R;
+            const double phT = 2.0 * CUDART_PI * (cyc - rint(cyc));
+            q.k0 = make_float4((float)A, (float)B, (float)c1, (float)c2);
+            q.k1 = make_float4((float)c3, (float)c4, (float)(bT - (double)ws - 0.5), (float)phT);
+        } else if (MODE == SARBP_MODE_FP32) {
+            q.k0 = make_float4((float)ax, (float)ay, (float)az,
+                               (float)(-P.t0_bins * P.bin_rate - (double)ws - 0.5));
+        } else {
+            q.ax = ax;
+            q.ay = ay;
+            q.az = az;
+        }
+        if (hi > lo) {
+            bytes = (unsigned)((hi - lo) * esize);
+            src = reinterpret_cast<const char *>(P.rc) + ((size_t)p * P.nbins + (size_t)lo) * esize;
+            dst = smem_addr(S.raw + ((size_t)buf * kChunk + (size_t)lane) * win * 8 + (size_t)(lo - ws) * esize);
+        }
+    }
+    unsigned total = bytes;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) total += __shfl_xor_sync(0xffffffffu, total, o);
+    const unsigned bar = smem_addr(&S.bar[buf]);
+    if (lane == 0) mbar_expect_tx_arrive(bar, total);
+    __syncwarp();
+    if (bytes) tma_bulk_g2s(dst, src, bytes, bar);
+}
+
+// raw window -> (mid, diff) pairs; bins outside [lo, hi) read as zero.
+template <int STORE>
+__device__ __forceinline__ void convert_chunk(const Smem &S, int buf, int count, int win) {
+    for (int pl = 0; pl < count; ++pl) {
+        const Prm &q = S.prm[buf * kChunk + pl];
+        const int lo = q.lo, hi = q.hi;
+        const float sc = q.scale;
+        const unsigned char *rw = S.raw + ((size_t)buf * kChunk + pl) * win * 8;
+        for (int i = threadIdx.x; i < win; i += kThreads) {
+            float2 a = make_float2(0.f, 0.f), b = make_float2(0.f, 0.f);
+            if (STORE == SARBP_STORE_C64) {
+                const float2 *r = reinterpret_cast<const float2 *>(rw);
+                if (i >= lo && i < hi) a = r[i];
+                if (i + 1 >= lo && i + 1 < hi) b = r[i + 1];
+            } else {
+                const __half2 *r = reinterpret_cast<const __half2 *>(rw);
+                if (i >= lo && i < hi) a = __half22float2(r[i]);
+                if (i + 1 >= lo && i + 1 < hi) b = __half22float2(r[i + 1]);
+                a.x *= sc; a.y *= sc; b.x *= sc; b.y *= sc;
+            }
+            S.staged[pl * win + i] =
+                make_float4(0.5f * (a.x + b.x), 0.5f * (a.y + b.y), b.x - a.x, b.y - a.y);
+        }
+    }
+}
+
+template <int MODE, int STORE, int NTERMS>
+__global__ void __launch_bounds__(kThreads, 2)
+    bp_kernel(const __grid_constant__ BpPlan P, int tiles_y, int pulses_per_seg, float qq_max) {
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    const int win = P.win;
+    const Smem S = carve(smem_raw, win);
+
+    const int tile = blockIdx.x;
+    const int ty = tile % tiles_y;  // tiles sharing a range strip run together (L2 reuse)
+    const int tx = tile / tiles_y;
+    const int seg = blockIdx.y;
+    const int p_begin = seg * pulses_per_seg;
+    const int p_end = min(P.np, p_begin + pulses_per_seg);
+    const int nchunks = p_end > p_begin ? (p_end - p_begin + kChunk - 1) / kChunk : 0;
+
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int lx = lane >> 2, ly = lane & 3;
+    const int xl = (warp & 3) * 8 + lx;
+    const float xc = (float)xl - 0.5f * (kTileX - 1);
+    float yc[kPix], qq[kPix];
+    const float g11 = (float)P.g.g11, g12 = (float)P.g.g12, g22 = (float)P.g.g22;
+#pragma unroll
+    for (int j = 0; j < kPix; ++j) {
+        const int yl = ((warp >> 2) + 2 * j) * 4 + ly;
+        yc[j] = (float)yl - 0.5f * (kTileY - 1);
+        qq[j] = xc * xc * g11 + 2.f * xc * yc[j] * g12 + yc[j] * yc[j] * g22;
+    }
+    const double pcx_i = tx * kTileX + 0.5 * (kTileX - 1), pcy_i = ty * kTileY + 0.5 * (kTileY - 1);
+    const double pcx = P.g.origin[0] + pcx_i * P.g.ux[0] + pcy_i * P.g.uy[0];
+    const double pcy = P.g.origin[1] + pcx_i * P.g.ux[1] + pcy_i * P.g.uy[1];
+    const double pcz = P.g.origin[2] + pcx_i * P.g.ux[2] + pcy_i * P.g.uy[2];
+
+    if (threadIdx.x == 0) {
+        mbar_init(smem_addr(&S.bar[0]), 1);
+        mbar_init(smem_addr(&S.bar[1]), 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    }
+    __syncthreads();
+
+    float acc_r[kPix], acc_i[kPix];
+    double dacc_r[MODE == SARBP_MODE_FP64 ? kPix : 1], dacc_i[MODE == SARBP_MODE_FP64 ? kPix : 1];
+#pragma unroll
+    for (int j = 0; j < kPix; ++j) { acc_r[j] = 0.f; acc_i[j] = 0.f; }
+#pragma unroll
+    for (int j = 0; j < (MODE == SARBP_MODE_FP64 ? kPix : 1); ++j) { dacc_r[j] = 0.0; dacc_i[j] = 0.0; }
+
+    // per-mode constants
+    const float bpm = (float)(2.0 / P.c * P.bin_rate);
+    const double kph_d = 4.0 * CUDART_PI * P.fc / P.c;
+    const float kph_hi = (float)kph_d;
+    const float kph_lo = (float)(kph_d - (double)kph_hi);
+    const float wmax = (float)(win - 2);
+    const unsigned sbase = smem_addr(S.staged) - kMagicBitsShift4;
+
+    // absolute pixel positions for the plain modes
+    float fpy[kPix], fpz[kPix], fpxx[kPix];
+    if (MODE == SARBP_MODE_FP32) {
+#pragma unroll
+        for (int j = 0; j < kPix; ++j) {
+            const double xi = tx * kTileX + xl, yi = ty * kTileY + ((warp >> 2) + 2 * j) * 4 + ly;
+            fpxx[j] = (float)(P.g.origin[0] + xi * P.g.ux[0] + yi * P.g.uy[0]);
+            fpy[j] = (float)(P.g.origin[1] + xi * P.g.ux[1] + yi * P.g.uy[1]);
+            fpz[j] = (float)(P.g.origin[2] + xi * P.g.ux[2] + yi * P.g.uy[2]);
+        }
+    }
+
+    if (warp == 0 && nchunks > 0)
+        produce_chunk<MODE, STORE>(P, S, 0, p_begin, min(kChunk, p_end - p_begin), pcx, pcy, pcz, qq_max);
+
+    bool failed = false;
+#pragma unroll 1
+    for (int c = 0; c < nchunks; ++c) {
+        const int buf = c & 1;
+        const int pc0 = p_begin + c * kChunk;
+        const int count = min(kChunk, p_end - pc0);
+        if (warp == 0 && c + 1 < nchunks) {
+            const int pn = pc0 + kChunk;
+            produce_chunk<MODE, STORE>(P, S, buf ^ 1, pn, min(kChunk, p_end - pn), pcx, pcy, pcz, qq_max);
+        }
+        const bool ok = mbar_wait_bounded(smem_addr(&S.bar[buf]), (c >> 1) & 1, 2000000000ull);
+        if (__syncthreads_or(!ok)) { failed = true; break; }
+        convert_chunk<STORE>(S, buf, count, win);
+        __syncthreads();
+
+        if (MODE == SARBP_MODE_SPLIT || MODE == SARBP_MODE_FP16STORE) {
+#pragma unroll 1
+            for (int pl = 0; pl < count; ++pl) {
+                const Prm &q = S.prm[buf * kChunk + pl];
+                const float4 k0 = q.k0, k1 = q.k1;
+                const float mp = q.mp;
+                const float xA = xc * k0.x;
+#pragma unroll
+                for (int j = 0; j < kPix; ++j) {
+                    const float n = fmaf(yc[j], k0.y, xA + qq[j]);
+                    float poly = NTERMS == 4 ? fmaf(n, fmaf(n, k1.y, k1.x), k0.w) : fmaf(n, k1.x, k0.w);
+                    poly = fmaf(n, poly, k0.z);
+                    const float dR = n * poly;
+                    float b = fmaf(dR, bpm, k1.z);
+                    b = fminf(fmaxf(b, 0.f), wmax);
+                    const float t = b + mp;
+                    const float f = b - (t - mp);
+                    const float4 v = lds128((__float_as_uint(t) << 4) + sbase);
+                    const float sr = fmaf(f, v.z, v.x);
+                    const float si = fmaf(f, v.w, v.y);
+                    float ph = fmaf(dR, kph_hi, k1.w);
+                    ph = fmaf(dR, kph_lo, ph);
+                    float sn, cs;
+                    __sincosf(ph, &sn, &cs);
+                    acc_r[j] = fmaf(sr, cs, fmaf(-si, sn, acc_r[j]));
+                    acc_i[j] = fmaf(sr, sn, fmaf(si, cs, acc_i[j]));
+                }
+            }
+        } else if (MODE == SARBP_MODE_FP32) {
+#pragma unroll 1
+            for (int pl = 0; pl < count; ++pl) {
+                const Prm &q = S.prm[buf * kChunk + pl];
+                const float4 k0 = q.k0;
+                const float mp = q.mp;
+                const float kph = (float)kph_d;
+#pragma unroll
+                for (int j = 0; j < kPix; ++j) {
+                    const float dx = k0.x - fpxx[j], dy = k0.y - fpy[j], dz = k0.z - fpz[j];
+                    const float R = sqrtf(fmaf(dx, dx, fmaf(dy, dy, dz * dz)));
+                    float b = fmaf(R, bpm, k0.w);
+                    b = fminf(fmaxf(b, 0.f), wmax);
+                    const float t = b + mp;
+                    const float f = b - (t - mp);
+                    const float4 v = lds128((__float_as_uint(t) << 4) + sbase);
+                    const float sr = fmaf(f, v.z, v.x);
+                    const float si = fmaf(f, v.w, v.y);
+                    float sn, cs;
+                    sincosf(kph * R, &sn, &cs);
+                    acc_r[j] = fmaf(sr, cs, fmaf(-si, sn, acc_r[j]));
+                    acc_i[j] = fmaf(sr, sn, fmaf(si, cs, acc_i[j]));
+                }
+            }
+        } else {  // FP64
+            const double cyc_per_m = 2.0 * P.fc / P.c;
+#pragma unroll 1
+            for (int pl = 0; pl < count; ++pl) {
+                const Prm &q = S.prm[buf * kChunk + pl];
+                const double ax = q.ax, ay = q.ay, az = q.az;
+                const double boff = -P.t0_bins * P.bin_rate - (double)q.ws;
+                const float4 *st = S.staged + pl * win;
+#pragma unroll
+                for (int j = 0; j < kPix; ++j) {
+                    const double xi = tx * kTileX + xl, yi = ty * kTileY + ((warp >> 2) + 2 * j) * 4 + ly;
+                    const double px = P.g.origin[0] + xi * P.g.ux[0] + yi * P.g.uy[0];
+                    const double py = P.g.origin[1] + xi * P.g.ux[1] + yi * P.g.uy[1];
+                    const double pz = P.g.origin[2] + xi * P.g.ux[2] + yi * P.g.uy[2];
+                    const double dx = ax - px, dy = ay - py, dz = az - pz;
+                    const double R = sqrt(dx * dx + dy * dy + dz * dz);
+                    double b = fma(R, 2.0 / P.c * P.bin_rate, boff) - 0.5;
+                    b = fmin(fmax(b, 0.0), (double)(win - 2));
+                    const double r0 = rint(b);
+                    const double f = b - r0;
+                    const float4 v = st[(int)r0];
+                    const double sr = fma(f, (double)v.z, (double)v.x);
+                    const double si = fma(f, (double)v.w, (double)v.y);
+                    const double cyc = cyc_per_m * R;
+                    double sn, cs;
+                    sincospi(2.0 * (cyc - rint(cyc)), &sn, &cs);
+                    dacc_r[j] = fma(sr, cs, fma(-si, sn, dacc_r[j]));
+                    dacc_i[j] = fma(sr, sn, fma(si, cs, dacc_i[j]));
+                }
+            }
+        }
+        __syncthreads();
+    }
+
+    if (failed) {
+        if (threadIdx.x == 0) atomicOr(P.err, kErrWaitTimeout);
+        // let any copy still in flight land before the CTA's shared memory is released
+        if (threadIdx.x == 0) {
+            mbar_wait_bounded(smem_addr(&S.bar[0]), 0, 1000000000ull);
+            mbar_wait_bounded(smem_addr(&S.bar[1]), 0, 1000000000ull);
+        }
+        __syncthreads();
+        return;
+    }
+
+    // write the tile
+    float2 *dst = P.segments > 1 ? P.partial + (size_t)seg * P.g.nx * P.g.ny : P.image;
+    const bool acc_mode = P.segments == 1 && P.accumulate;
+    const int x = tx * kTileX + xl;
+#pragma unroll
+    for (int j = 0; j < kPix; ++j) {
+        const int y = ty * kTileY + ((warp >> 2) + 2 * j) * 4 + ly;
+        if (x < P.g.nx && y < P.g.ny) {
+            float2 v = MODE == SARBP_MODE_FP64 ? make_float2((float)dacc_r[j], (float)dacc_i[j])
+                                               : make_float2(acc_r[j], acc_i[j]);
+            const size_t idx = (size_t)y * P.g.nx + x;
+            if (acc_mode) {
+                const float2 o = dst[idx];
+                v.x += o.x;
+                v.y += o.y;
+            }
+            dst[idx] = v;
+        }
+    }
+}
+
+// image (=|+=) sum over segments of the partial images, fixed order.
+__global__ void reduce_segments_kernel(const float2 *__restrict__ partial, int segments, size_t count,
+                                       float2 *__restrict__ image, int accumulate) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < count;
+         i += (size_t)gridDim.x * blockDim.x) {
+        float2 s = accumulate ? image[i] : make_float2(0.f, 0.f);
+        for (int k = 0; k < segments; ++k) {
+            const float2 v = __ldg(&partial[(size_t)k * count + i]);
+            s.x += v.x;
+            s.y += v.y;
+        }
+        image[i] = s;
+    }
+}
+
+template <int MODE, int STORE, int NTERMS>
+cudaError_t launch_variant(const BpPlan &p, cudaStream_t s, int tiles, int tiles_y, int pps,
+                           float qq_max) {
+    auto k = bp_kernel<MODE, STORE, NTERMS>;
+    const size_t smem = bp_smem_bytes(MODE, p.win);
+    cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    dim3 grid(tiles, p.segments);
+    k<<<grid, kThreads, smem, s>>>(p, tiles_y, pps, qq_max);
+    return cudaGetLastError();
+}
+
+}  // namespace
+
+void bp_tile_dims(int, int *tile_x, int *tile_y) {
+    *tile_x = kTileX;
+    *tile_y = kTileY;
+}
+
+int bp_pulses_per_chunk(int) { return kChunk; }
+
+size_t bp_smem_bytes(int, int win) {
+    return (size_t)kChunk * win * 16 + (size_t)2 * kChunk * win * 8 + 2 * kChunk * sizeof(Prm) + 16;
+}
+
+cudaError_t launch_bp(const BpPlan &p, cudaStream_t s, int *launches) {
+    if (p.np <= 0 || p.g.nx <= 0 || p.g.ny <= 0) return cudaSuccess;
+    const int tiles_x = (p.g.nx + kTileX - 1) / kTileX;
+    const int tiles_y = (p.g.ny + kTileY - 1) / kTileY;
+    const int tiles = tiles_x * tiles_y;
+    int pps = (p.np + p.segments - 1) / p.segments;
+    pps = (pps + kChunk - 1) / kChunk * kChunk;
+    // |q|^2 bound over a tile (pixel offsets from the tile centre)
+    const double hx = 0.5 * (kTileX - 1), hy = 0.5 * (kTileY - 1);
+    const float qq_max = (float)(hx * hx * p.g.g11 + 2.0 * hx * hy * fabs(p.g.g12) + hy * hy * p.g.g22);
+    cudaError_t e;
+    const bool fp16 = p.storage == SARBP_STORE_C32H;
+    switch (p.mode) {
+        case SARBP_MODE_FP64:
+            e = fp16 ? launch_variant<SARBP_MODE_FP64, SARBP_STORE_C32H, 4>(p, s, tiles, tiles_y, pps, qq_max)
+                     : launch_variant<SARBP_MODE_FP64, SARBP_STORE_C64, 4>(p, s, tiles, tiles_y, pps, qq_max);
+            break;
+        case SARBP_MODE_FP32:
+            e = fp16 ? launch_variant<SARBP_MODE_FP32, SARBP_STORE_C32H, 4>(p, s, tiles, tiles_y, pps, qq_max)
+                     : launch_variant<SARBP_MODE_FP32, SARBP_STORE_C64, 4>(p, s, tiles, tiles_y, pps, qq_max);
+            break;
+        default:
+            if (p.nterms == 3)
+                e = fp16 ? launch_variant<SARBP_MODE_SPLIT, SARBP_STORE_C32H, 3>(p, s, tiles, tiles_y, pps, qq_max)
+                         : launch_variant<SARBP_MODE_SPLIT, SARBP_STORE_C64, 3>(p, s, tiles, tiles_y, pps, qq_max);
+            else
+                e = fp16 ? launch_variant<SARBP_MODE_SPLIT, SARBP_STORE_C32H, 4>(p, s, tiles, tiles_y, pps, qq_max)
+                         : launch_variant<SARBP_MODE_SPLIT, SARBP_STORE_C64, 4>(p, s, tiles, tiles_y, pps, qq_max);
+            break;
+    }
+    if (e != cudaSuccess) return e;
+    if (launches) ++*launches;
+    if (p.segments > 1) {
+        const size_t count = (size_t)p.g.nx * p.g.ny;
+        const int blocks = (int)std::min<size_t>((count + 255) / 256, 152 * 8);
+        reduce_segments_kernel<<<blocks, 256, 0, s>>>(p.partial, p.segments, count, p.image, p.accumulate);
+        e = cudaGetLastError();
+        if (launches) ++*launches;
+    }
+    return e;
+}
+
+}  // namespace sarbp

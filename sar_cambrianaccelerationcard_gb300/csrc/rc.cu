@@ -1,0 +1,312 @@
+// rc.cu -- range compression and range upsampling on sm_103a.
+//
+// Implements code/SAR_BP/matlab/BPA_SAR.m:93-111 (matched filter
+// ifft(fft(s).*conj(fft(h))) followed by 8x upsampling through mid-spectrum
+// zero insertion) as two kernels:
+//
+//   rc_forward  (one CTA per pulse): zero-padded echo row -> shared memory ->
+//               forward FFT -> multiply by the filter spectrum
+//               G[k] = conj(H[k]) e^{-j2pi k D/N} / N -> spectrum scratch.
+//               Also emits the per-pulse bound sum_k |Y[k]| (>= max |output|)
+//               from which the FP16 storage scale is derived.
+//   rc_inverse  (one CTA per pulse and upsampling phase r): the L*N-point
+//               inverse of the zero-inserted spectrum evaluated at bins
+//               b = L*i + r equals the N-point inverse of Y[k]*e^{+j2pi kappa r/(LN)}
+//               (kappa = signed frequency), so each CTA runs one N-point
+//               inverse FFT and writes every L-th output bin.
+//
+// The FFT is a Stockham autosort transform with radix-8 stages (one radix-4
+// or radix-2 stage when log2 N is not a multiple of 3), in place in shared
+// memory with a barrier between each stage's loads and stores.  Twiddles come
+// from a table computed in double precision on the host.
+#include "sarbp_internal.h"
+
+namespace sarbp {
+namespace {
+
+__device__ __forceinline__ float2 cmul(float2 a, float2 b) {
+    return make_float2(fmaf(a.x, b.x, -a.y * b.y), fmaf(a.x, b.y, a.y * b.x));
+}
+__device__ __forceinline__ float2 cadd(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
+__device__ __forceinline__ float2 csub(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
+// multiply by -j (forward kernel) or +j (inverse kernel)
+template <bool INV>
+__device__ __forceinline__ float2 mulj(float2 a) {
+    return INV ? make_float2(-a.y, a.x) : make_float2(a.y, -a.x);
+}
+
+// one float2 of padding per 32 entries breaks the power-of-two store strides
+__device__ __forceinline__ int pad(int i) { return i + (i >> 5); }
+__host__ __device__ constexpr int padded(int n) { return n + (n >> 5); }
+
+template <int R, bool INV>
+struct Dft;
+
+template <bool INV>
+struct Dft<2, INV> {
+    __device__ __forceinline__ static void run(float2 *v) {
+        float2 a = v[0], b = v[1];
+        v[0] = cadd(a, b);
+        v[1] = csub(a, b);
+    }
+};
+
+template <bool INV>
+struct Dft<4, INV> {
+    __device__ __forceinline__ static void run(float2 *v) {
+        float2 t0 = cadd(v[0], v[2]), t1 = csub(v[0], v[2]);
+        float2 t2 = cadd(v[1], v[3]), t3 = mulj<INV>(csub(v[1], v[3]));
+        v[0] = cadd(t0, t2);
+        v[2] = csub(t0, t2);
+        v[1] = cadd(t1, t3);
+        v[3] = csub(t1, t3);
+    }
+};
+
+template <bool INV>
+struct Dft<8, INV> {
+    __device__ __forceinline__ static void run(float2 *v) {
+        float2 e[4] = {v[0], v[2], v[4], v[6]};
+        float2 o[4] = {v[1], v[3], v[5], v[7]};
+        Dft<4, INV>::run(e);
+        Dft<4, INV>::run(o);
+        const float h = 0.70710678118654752440f;
+        // W8^1, W8^2, W8^3 for the chosen direction
+        float2 o1 = INV ? make_float2(h * (o[1].x - o[1].y), h * (o[1].x + o[1].y))
+                        : make_float2(h * (o[1].x + o[1].y), h * (o[1].y - o[1].x));
+        float2 o2 = mulj<INV>(o[2]);
+        float2 o3 = INV ? make_float2(-h * (o[3].x + o[3].y), h * (o[3].x - o[3].y))
+                        : make_float2(h * (o[3].y - o[3].x), -h * (o[3].x + o[3].y));
+        v[0] = cadd(e[0], o[0]);
+        v[4] = csub(e[0], o[0]);
+        v[1] = cadd(e[1], o1);
+        v[5] = csub(e[1], o1);
+        v[2] = cadd(e[2], o2);
+        v[6] = csub(e[2], o2);
+        v[3] = cadd(e[3], o3);
+        v[7] = csub(e[3], o3);
+    }
+};
+
+// One Stockham stage: butterfly j reads s[j + r*N/R], applies twiddles
+// W_N^{k r N/(Ns R)} (k = j mod Ns), runs a radix-R DFT and writes
+// s[(j - k) R + k + r Ns].
+template <int N, int R, int T, bool INV>
+__device__ __forceinline__ void stage(float2 *s, const float2 *__restrict__ tw, int Ns) {
+    constexpr int NB = N / R;
+    constexpr int PER = (NB + T - 1) / T;
+    float2 v[PER][R];
+#pragma unroll
+    for (int b = 0; b < PER; ++b) {
+        const int j = threadIdx.x + b * T;
+        if (PER * T == NB || j < NB) {
+#pragma unroll
+            for (int r = 0; r < R; ++r) v[b][r] = s[pad(j + r * NB)];
+        }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int b = 0; b < PER; ++b) {
+        const int j = threadIdx.x + b * T;
+        if (PER * T == NB || j < NB) {
+            const int k = j & (Ns - 1);
+            if (Ns > 1) {
+                const int step = N / (Ns * R);
+#pragma unroll
+                for (int r = 1; r < R; ++r) {
+                    float2 w = __ldg(&tw[k * r * step]);
+                    if (INV) w.y = -w.y;
+                    v[b][r] = cmul(v[b][r], w);
+                }
+            }
+            Dft<R, INV>::run(v[b]);
+            const int base = (j - k) * R + k;
+#pragma unroll
+            for (int r = 0; r < R; ++r) s[pad(base + r * Ns)] = v[b][r];
+        }
+    }
+    __syncthreads();
+}
+
+template <int N>
+struct Log2 {
+    static constexpr int value = 1 + Log2<N / 2>::value;
+};
+template <>
+struct Log2<1> {
+    static constexpr int value = 0;
+};
+
+// Unnormalised in-place FFT of N points held (padded) in shared memory.
+// Caller must have synchronised after filling s; returns synchronised.
+template <int N, int T, bool INV>
+__device__ void fft_smem(float2 *s, const float2 *__restrict__ tw) {
+    constexpr int LOG = Log2<N>::value;
+    constexpr int N8 = LOG / 3;
+    constexpr int REM = LOG % 3;
+    int Ns = 1;
+#pragma unroll 1
+    for (int i = 0; i < N8; ++i) {
+        stage<N, 8, T, INV>(s, tw, Ns);
+        Ns *= 8;
+    }
+    if (REM == 2) stage<N, 4, T, INV>(s, tw, Ns);
+    if (REM == 1) stage<N, 2, T, INV>(s, tw, Ns);
+}
+
+template <int T>
+__device__ __forceinline__ float block_sum(float v, float *red) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+    if (l == 0) red[w] = v;
+    __syncthreads();
+    float t = 0.f;
+    if (threadIdx.x < 32) {
+        t = (l < T / 32) ? red[l] : 0.f;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+    }
+    return t;  // valid in thread 0
+}
+
+template <int N, int T>
+__global__ void __launch_bounds__(T) rc_forward_kernel(int ns, const float2 *__restrict__ echo,
+                                                       const float2 *__restrict__ filt,
+                                                       const float2 *__restrict__ tw,
+                                                       float2 *__restrict__ spec,
+                                                       float *__restrict__ scale) {
+    extern __shared__ float2 sm[];
+    __shared__ float red[32];
+    const int p = blockIdx.x;
+    const float2 *row = echo + (size_t)p * ns;
+    for (int i = threadIdx.x; i < N; i += T) sm[pad(i)] = i < ns ? __ldg(&row[i]) : make_float2(0.f, 0.f);
+    __syncthreads();
+    fft_smem<N, T, false>(sm, tw);
+    float2 *out = spec + (size_t)p * N;
+    float acc = 0.f;
+    for (int k = threadIdx.x; k < N; k += T) {
+        float2 y = cmul(sm[pad(k)], __ldg(&filt[k]));
+        out[k] = y;
+        acc += sqrtf(fmaf(y.x, y.x, y.y * y.y));
+    }
+    const float bound = block_sum<T>(acc, red);
+    if (threadIdx.x == 0 && scale) {
+        // power-of-two scale so that stored FP16 magnitudes stay <= 2^14
+        float sc = 1.f;
+        if (bound > 0.f && isfinite(bound)) sc = exp2f(ceilf(log2f(bound) - 14.f));
+        scale[p] = sc;
+    }
+}
+
+template <int N, int T, int STORE>
+__global__ void __launch_bounds__(T) rc_inverse_kernel(int ns, int L, int nbins,
+                                                       const float2 *__restrict__ spec,
+                                                       const float2 *__restrict__ tw,
+                                                       const float2 *__restrict__ ramp,
+                                                       const float *__restrict__ scale,
+                                                       void *__restrict__ out) {
+    extern __shared__ float2 sm[];
+    const int p = blockIdx.x / L;
+    const int r = blockIdx.x - p * L;
+    const float2 *in = spec + (size_t)p * N;
+    const int LN = L * N;
+    for (int k = threadIdx.x; k < N; k += T) {
+        float2 y = __ldg(&in[k]);
+        if (r != 0) {
+            const int kap = k < N / 2 ? k : k - N;  // MATLAB split floor((N+1)/2) for even N
+            int m = (kap * r) % LN;
+            if (m < 0) m += LN;
+            y = cmul(y, __ldg(&ramp[m]));
+        }
+        sm[pad(k)] = y;
+    }
+    __syncthreads();
+    fft_smem<N, T, true>(sm, tw);
+    if (STORE == SARBP_STORE_C64) {
+        float2 *o = reinterpret_cast<float2 *>(out) + (size_t)p * nbins + r;
+        for (int i = threadIdx.x; i < ns; i += T) o[(size_t)L * i] = sm[pad(i)];
+    } else {
+        const float inv = 1.f / __ldg(&scale[p]);  // exact: scale is a power of two
+        __half2 *o = reinterpret_cast<__half2 *>(out) + (size_t)p * nbins + r;
+        for (int i = threadIdx.x; i < ns; i += T) {
+            float2 v = sm[pad(i)];
+            o[(size_t)L * i] = __floats2half2_rn(v.x * inv, v.y * inv);
+        }
+    }
+}
+
+template <int N>
+constexpr int threads_for() {
+    return N >= 4096 ? 512 : (N >= 512 ? N / 8 : 64);
+}
+
+template <int N>
+cudaError_t fwd_n(const RcPlan &p, const float2 *echo, const float2 *filt, const float2 *tw,
+                  float2 *spec, float *scale, cudaStream_t s) {
+    constexpr int T = threads_for<N>();
+    const size_t smem = sizeof(float2) * padded(N);
+    auto k = rc_forward_kernel<N, T>;
+    cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    k<<<p.np, T, smem, s>>>(p.ns, echo, filt, tw, spec, scale);
+    return cudaGetLastError();
+}
+
+template <int N>
+cudaError_t inv_n(const RcPlan &p, const float2 *spec, const float2 *tw, const float2 *ramp,
+                  const float *scale, void *out, cudaStream_t s) {
+    constexpr int T = threads_for<N>();
+    const size_t smem = sizeof(float2) * padded(N);
+    cudaError_t e;
+    if (p.storage == SARBP_STORE_C64) {
+        auto k = rc_inverse_kernel<N, T, SARBP_STORE_C64>;
+        e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+        k<<<p.np * p.L, T, smem, s>>>(p.ns, p.L, p.nbins, spec, tw, ramp, scale, out);
+    } else {
+        auto k = rc_inverse_kernel<N, T, SARBP_STORE_C32H>;
+        e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+        k<<<p.np * p.L, T, smem, s>>>(p.ns, p.L, p.nbins, spec, tw, ramp, scale, out);
+    }
+    return cudaGetLastError();
+}
+
+}  // namespace
+
+bool rc_size_supported(int nfft) {
+    return nfft >= 64 && nfft <= 16384 && (nfft & (nfft - 1)) == 0;
+}
+
+#define SARBP_RC_SWITCH(N_, CALL)      \
+    switch (N_) {                      \
+        case 64: return CALL(64);      \
+        case 128: return CALL(128);    \
+        case 256: return CALL(256);    \
+        case 512: return CALL(512);    \
+        case 1024: return CALL(1024);  \
+        case 2048: return CALL(2048);  \
+        case 4096: return CALL(4096);  \
+        case 8192: return CALL(8192);  \
+        case 16384: return CALL(16384); \
+        default: return cudaErrorInvalidValue; \
+    }
+
+cudaError_t launch_rc_forward(const RcPlan &p, const float2 *echo, const float2 *filt,
+                              const float2 *tw, float2 *spec, float *scale, cudaStream_t s) {
+    if (p.np <= 0) return cudaSuccess;
+#define SARBP_FWD(N) fwd_n<N>(p, echo, filt, tw, spec, scale, s)
+    SARBP_RC_SWITCH(p.nfft, SARBP_FWD)
+#undef SARBP_FWD
+}
+
+cudaError_t launch_rc_inverse(const RcPlan &p, const float2 *spec, const float2 *tw,
+                              const float2 *ramp, const float *scale, void *out, cudaStream_t s) {
+    if (p.np <= 0) return cudaSuccess;
+#define SARBP_INV(N) inv_n<N>(p, spec, tw, ramp, scale, out, s)
+    SARBP_RC_SWITCH(p.nfft, SARBP_INV)
+#undef SARBP_INV
+}
+
+}  // namespace sarbp

@@ -1,0 +1,85 @@
+// sarbp_internal.h -- shared declarations of libsarbp's CUDA translation units.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cuda_fp16.h>
+#include <stdint.h>
+
+#include "sarbp.h"
+
+namespace sarbp {
+
+// Device-side error bits, OR-ed into a context-owned word and read by the host
+// after synchronisation.
+enum : unsigned {
+    kErrWaitTimeout = 1u << 0,   // an mbarrier wait ran out of iterations
+    kErrIndexClamp = 1u << 1,    // (checked builds) an interpolation index was clamped
+    kErrBadLaunch = 1u << 2,     // a kernel saw inconsistent launch parameters
+    kErrWindow = 1u << 3,        // a (tile, pulse) needed more bins than the staging window
+};
+
+// ---------------------------------------------------------------- range compression
+struct RcPlan {
+    int np;          // pulses in this launch
+    int ns;          // echo samples per pulse
+    int nfft;        // FFT size (power of two)
+    int L;           // upsampling factor
+    int nbins;       // L * ns
+    int storage;     // sarbp_storage
+};
+
+// Host-side launchers (rc.cu).  spec: scratch [np][nfft] complex; filt: [nfft];
+// tw: FFT twiddles [nfft] (e^{-j2pi k/nfft}); ramp: [L*nfft] (e^{+j2pi m/(L nfft)}).
+cudaError_t launch_rc_forward(const RcPlan &p, const float2 *echo, const float2 *filt,
+                              const float2 *tw, float2 *spec, float *scale, cudaStream_t s);
+cudaError_t launch_rc_inverse(const RcPlan &p, const float2 *spec, const float2 *tw,
+                              const float2 *ramp, const float *scale, void *out, cudaStream_t s);
+bool rc_size_supported(int nfft);
+
+// ---------------------------------------------------------------- back-projection
+struct BpGeom {
+    double origin[3], ux[3], uy[3];
+    double g11, g12, g22;   // ux.ux, ux.uy, uy.uy
+    int nx, ny;
+};
+
+struct BpPlan {
+    const void *rc;          // [np][nbins] c64 or c32h
+    const float *scale;      // [np] or null
+    int storage;
+    int np;                  // pulses
+    int nbins;
+    int mode;                // sarbp_mode
+    const double *apc;       // [np][3] device
+    BpGeom g;
+    double fc, c, t0_bins, bin_rate;
+    float2 *image;           // [ny][nx] final image
+    float2 *partial;         // [segments][ny][nx] scratch when segments > 1
+    int segments;            // pulse segments (1: write image directly)
+    int accumulate;
+    int win;                 // staged bins per (tile, pulse), multiple of 4
+    int nterms;              // polynomial terms for the differential range (3 or 4)
+    unsigned *err;           // device error word
+};
+
+cudaError_t launch_bp(const BpPlan &p, cudaStream_t s, int *launches);
+// Tile geometry the planner needs to size the staging window.
+void bp_tile_dims(int mode, int *tile_x, int *tile_y);
+size_t bp_smem_bytes(int mode, int win);
+int bp_pulses_per_chunk(int mode);
+
+// ---------------------------------------------------------------- echo synthesis
+cudaError_t launch_echo_synth(const double *apc, int np, int ns, const sarbp_target *tg, int nt,
+                              double t_rec0, double fs, double kr, double tp, double tc,
+                              double fc, double c, float2 *echo, double *power_acc,
+                              cudaStream_t s);
+cudaError_t launch_echo_noise(float2 *echo, int64_t count, const double *power_acc,
+                              double snr_db, uint64_t seed, cudaStream_t s);
+cudaError_t launch_ref_echo(float2 *Srnm, const float *Ptarget, const float *ta, const float *tr,
+                            const sarbp_ref_params &p, int Mslow, int Nfast, cudaStream_t s);
+
+// ---------------------------------------------------------------- probes
+cudaError_t run_issue_probe(int sms, double *fp32_lanes_per_s, double *mufu_lanes_per_s,
+                            cudaStream_t s);
+
+}  // namespace sarbp

@@ -1,0 +1,324 @@
+"""ctypes binding of libsarbp.so (include/sarbp.h) and a small Pythonic layer.
+
+The library is the product: every call here goes through the C ABI into the
+CUDA kernels.  There is no CPU fallback; importing works without a GPU, but
+creating a :class:`Context` fails loudly unless an sm_103 device and the built
+library are present.
+
+Arrays may be numpy arrays (host memory: the call is synchronous) or any
+object exposing ``data_ptr()`` (e.g. torch CUDA tensors: the call is
+asynchronous on the given stream).
+"""
+from __future__ import annotations
+
+import ctypes
+import math
+import os
+
+import numpy as np
+
+from . import scenes
+
+_PKG = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_PKG, "libsarbp.so")
+
+OK = 0
+ERR_INVALID_ARGUMENT = 1
+ERR_UNSUPPORTED = 2
+ERR_OUT_OF_MEMORY = 3
+ERR_CUDA = 4
+ERR_NO_DEVICE = 5
+ERR_TIMEOUT = 6
+ERR_DEVICE_CHECK = 7
+ERR_NOT_READY = 8
+ERR_CANCELLED = 9
+ERR_BUDGET = 10
+ERR_INTERNAL = 11
+
+MODE_FP64 = 0
+MODE_FP32 = 1
+MODE_SPLIT = 2
+MODE_FP16STORE = 3
+MODES = {"fp64": MODE_FP64, "fp32": MODE_FP32, "split": MODE_SPLIT, "fp16store": MODE_FP16STORE}
+
+STORE_C64 = 0
+STORE_C32H = 1
+
+
+class Radar(ctypes.Structure):
+    _fields_ = [("c", ctypes.c_double), ("fc", ctypes.c_double), ("fs", ctypes.c_double),
+                ("kr", ctypes.c_double), ("tp", ctypes.c_double), ("tc", ctypes.c_double),
+                ("t_rec0", ctypes.c_double), ("upsample", ctypes.c_int32), ("reserved", ctypes.c_int32)]
+
+
+class Grid(ctypes.Structure):
+    _fields_ = [("origin", ctypes.c_double * 3), ("ux", ctypes.c_double * 3), ("uy", ctypes.c_double * 3),
+                ("nx", ctypes.c_int32), ("ny", ctypes.c_int32)]
+
+
+class RcLayout(ctypes.Structure):
+    _fields_ = [("nc", ctypes.c_int32), ("nfft", ctypes.c_int32), ("shift", ctypes.c_int32),
+                ("nbins", ctypes.c_int32), ("t0_bins", ctypes.c_double), ("bin_rate", ctypes.c_double)]
+
+
+class RcView(ctypes.Structure):
+    _fields_ = [("data", ctypes.c_void_p), ("scale", ctypes.c_void_p), ("storage", ctypes.c_int32),
+                ("np", ctypes.c_int32), ("nbins", ctypes.c_int32), ("reserved", ctypes.c_int32),
+                ("t0_bins", ctypes.c_double), ("bin_rate", ctypes.c_double)]
+
+
+class Target(ctypes.Structure):
+    _fields_ = [("x", ctypes.c_double), ("y", ctypes.c_double), ("z", ctypes.c_double), ("amp", ctypes.c_double)]
+
+
+class RefParams(ctypes.Structure):
+    """Byte layout of the reference's SARParams (code/SAR_BP/CUDA/BPA_CUDA.h:28-50)."""
+    _fields_ = [(n, ctypes.c_float) for n in ("c", "fc", "lam", "Kr", "Tr", "Br", "Fr", "vr", "H", "La",
+                                              "Rg0", "Az0")] + \
+               [("Nfast", ctypes.c_int32), ("Mslow", ctypes.c_int32), ("Ntarget", ctypes.c_int32)]
+
+    @classmethod
+    def defaults(cls) -> "RefParams":
+        """The reference's default-constructed SARParams (BPA_CUDA.h:29-49)."""
+        p = cls()
+        p.c, p.fc = 3e8, 5.3e9
+        p.lam = np.float32(p.c) / np.float32(p.fc)
+        p.Kr, p.Tr, p.Br, p.Fr = 4e12, 2.5e-6, 1e8, 1.2e8
+        p.vr, p.H, p.La, p.Rg0, p.Az0 = 150.0, 5000.0, 4.0, 10000.0, 0.0
+        p.Nfast = int(np.float32(p.Tr) * np.float32(p.Fr))
+        p.Mslow = 1024
+        p.Ntarget = 5
+        return p
+
+
+SIGNATURES = {
+    "sarbp_abi_version": ([], ctypes.c_int),
+    "sarbp_status_string": ([ctypes.c_int], ctypes.c_char_p),
+    "sarbp_create": ([ctypes.POINTER(ctypes.c_void_p), ctypes.c_int], ctypes.c_int),
+    "sarbp_destroy": ([ctypes.c_void_p], ctypes.c_int),
+    "sarbp_last_error": ([ctypes.c_void_p], ctypes.c_char_p),
+    "sarbp_synchronize": ([ctypes.c_void_p], ctypes.c_int),
+    "sarbp_trim": ([ctypes.c_void_p], ctypes.c_int),
+    "sarbp_device_bytes": ([ctypes.c_void_p], ctypes.c_size_t),
+    "sarbp_rc_layout_get": ([ctypes.POINTER(Radar), ctypes.c_int32, ctypes.POINTER(RcLayout)], ctypes.c_int),
+    "sarbp_range_compress": ([ctypes.c_void_p, ctypes.POINTER(Radar), ctypes.c_void_p, ctypes.c_int32,
+                              ctypes.c_int32, ctypes.c_int32, ctypes.c_void_p, ctypes.c_void_p,
+                              ctypes.c_void_p], ctypes.c_int),
+    "sarbp_backproject": ([ctypes.c_void_p, ctypes.POINTER(Radar), ctypes.POINTER(RcView), ctypes.c_void_p,
+                           ctypes.POINTER(Grid), ctypes.c_int32, ctypes.c_void_p, ctypes.c_int32,
+                           ctypes.c_void_p], ctypes.c_int),
+    "sarbp_image": ([ctypes.c_void_p, ctypes.POINTER(Radar), ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32,
+                     ctypes.c_void_p, ctypes.POINTER(Grid), ctypes.c_int32, ctypes.c_void_p, ctypes.c_void_p],
+                    ctypes.c_int),
+    "sarbp_synthesize_echo": ([ctypes.c_void_p, ctypes.POINTER(Radar), ctypes.c_void_p, ctypes.c_int32,
+                               ctypes.c_int32, ctypes.c_void_p, ctypes.c_int32, ctypes.c_double, ctypes.c_uint64,
+                               ctypes.c_void_p, ctypes.c_void_p], ctypes.c_int),
+    "sarbp_launch_back_projection": ([ctypes.c_void_p, ctypes.c_void_p, ctypes.POINTER(RefParams),
+                                      ctypes.c_int32, ctypes.c_int32], ctypes.c_int),
+    "sarbp_launch_generate_echo": ([ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                    ctypes.POINTER(RefParams), ctypes.c_int32, ctypes.c_int32], ctypes.c_int),
+    "sarbp_probe_issue_rates": ([ctypes.c_void_p, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double),
+                                 ctypes.POINTER(ctypes.c_int32)], ctypes.c_int),
+    "sarbp_last_timings": ([ctypes.c_void_p, ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_float)],
+                           ctypes.c_int),
+    "sarbp_kernel_launches": ([ctypes.c_void_p], ctypes.c_int64),
+}
+
+_lib = None
+
+
+def load(path: str = LIB_PATH):
+    """Load libsarbp.so; raises if it has not been built."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(path):
+            raise RuntimeError(f"{path} is missing: build it with "
+                               "`python -c 'import __graft_entry__ as g; g.build()'`")
+        L = ctypes.CDLL(path)
+        for name, (args, res) in SIGNATURES.items():
+            f = getattr(L, name)
+            f.argtypes = args
+            f.restype = res
+        _lib = L
+    return _lib
+
+
+class SarbpError(RuntimeError):
+    def __init__(self, status: int, msg: str):
+        super().__init__(f"{msg} (status {status})")
+        self.status = status
+
+
+def _ptr(a):
+    """Raw address of a numpy array or of a tensor exposing data_ptr()."""
+    if a is None:
+        return None
+    if isinstance(a, np.ndarray):
+        if not a.flags.c_contiguous:
+            raise ValueError("arrays must be C-contiguous")
+        return a.ctypes.data
+    if hasattr(a, "data_ptr"):
+        return int(a.data_ptr())
+    if isinstance(a, int):
+        return a
+    raise TypeError(f"unsupported buffer type {type(a)}")
+
+
+def radar_struct(radar: scenes.Radar, t_rec0: float, tc: float | None = None) -> Radar:
+    r = Radar()
+    r.c, r.fc, r.fs, r.kr, r.tp = radar.c, radar.fc, radar.fs, radar.kr, radar.tp
+    r.tc = radar.tp / 2.0 if tc is None else tc
+    r.t_rec0 = t_rec0
+    r.upsample = radar.upsample
+    r.reserved = 0
+    return r
+
+
+def grid_struct(g: scenes.Grid) -> Grid:
+    s = Grid()
+    for i in range(3):
+        s.origin[i], s.ux[i], s.uy[i] = float(g.origin[i]), float(g.ux[i]), float(g.uy[i])
+    s.nx, s.ny = int(g.nx), int(g.ny)
+    return s
+
+
+def targets_struct(tg: np.ndarray):
+    arr = (Target * max(1, len(tg)))()
+    for i, t in enumerate(tg):
+        arr[i].x, arr[i].y, arr[i].z, arr[i].amp = (float(v) for v in t[:4])
+    return arr
+
+
+class Context:
+    """One libsarbp context on one device (not thread-safe)."""
+
+    def __init__(self, device: int = 0):
+        self.lib = load()
+        h = ctypes.c_void_p()
+        st = self.lib.sarbp_create(ctypes.byref(h), device)
+        if st != OK:
+            raise SarbpError(st, f"sarbp_create(device={device}) failed: "
+                                 f"{self.lib.sarbp_status_string(st).decode()}")
+        self.h = h
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.sarbp_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def check(self, st: int, what: str):
+        if st != OK:
+            detail = self.lib.sarbp_last_error(self.h).decode()
+            raise SarbpError(st, f"{what}: {self.lib.sarbp_status_string(st).decode()}: {detail}")
+
+    # ---------------------------------------------------------------- calls
+    def layout(self, radar: Radar, ns: int) -> RcLayout:
+        lay = RcLayout()
+        self.check(self.lib.sarbp_rc_layout_get(ctypes.byref(radar), ns, ctypes.byref(lay)), "rc_layout")
+        return lay
+
+    def range_compress(self, radar: Radar, echo, storage: int = STORE_C64, out=None, scale=None, stream=None):
+        np_, ns = echo.shape
+        lay = self.layout(radar, ns)
+        if out is None:
+            out = np.zeros((np_, lay.nbins), dtype=np.complex64 if storage == STORE_C64 else np.float16)
+            if storage == STORE_C32H:
+                out = np.zeros((np_, lay.nbins, 2), dtype=np.float16)
+        if storage == STORE_C32H and scale is None:
+            scale = np.zeros(np_, dtype=np.float32)
+        self.check(self.lib.sarbp_range_compress(self.h, ctypes.byref(radar), _ptr(echo), np_, ns, storage,
+                                                 _ptr(out), _ptr(scale), stream), "range_compress")
+        return (out, scale) if storage == STORE_C32H else out
+
+    def backproject(self, radar: Radar, rc, apc, grid: Grid, mode: int, t0_bins: float, bin_rate: float,
+                    scale=None, image=None, accumulate: bool = False, stream=None):
+        v = RcView()
+        if isinstance(rc, np.ndarray) and rc.dtype == np.float16:
+            v.storage = STORE_C32H
+            v.np, v.nbins = rc.shape[0], rc.shape[1]
+        else:
+            v.storage = STORE_C64 if scale is None else STORE_C32H
+            v.np, v.nbins = int(rc.shape[0]), int(rc.shape[1])
+        v.data = _ptr(rc)
+        v.scale = _ptr(scale)
+        v.t0_bins, v.bin_rate = t0_bins, bin_rate
+        if image is None:
+            image = np.zeros((grid.ny, grid.nx), dtype=np.complex64)
+        self.check(self.lib.sarbp_backproject(self.h, ctypes.byref(radar), ctypes.byref(v), _ptr(apc),
+                                              ctypes.byref(grid), mode, _ptr(image), int(accumulate), stream),
+                   "backproject")
+        return image
+
+    def image(self, radar: Radar, echo, apc, grid: Grid, mode: int, image=None, stream=None):
+        np_, ns = echo.shape
+        if image is None:
+            image = np.zeros((grid.ny, grid.nx), dtype=np.complex64)
+        self.check(self.lib.sarbp_image(self.h, ctypes.byref(radar), _ptr(echo), np_, ns, _ptr(apc),
+                                        ctypes.byref(grid), mode, _ptr(image), stream), "image")
+        return image
+
+    def synthesize_echo(self, radar: Radar, apc, ns: int, targets: np.ndarray, snr_db=None, seed: int = 0,
+                        out=None, stream=None):
+        apc_a = apc
+        np_ = int(apc.shape[0])
+        tg = targets_struct(targets)
+        if out is None:
+            out = np.zeros((np_, ns), dtype=np.complex64)
+        snr = float("nan") if snr_db is None else float(snr_db)
+        self.check(self.lib.sarbp_synthesize_echo(self.h, ctypes.byref(radar), _ptr(apc_a), np_, ns,
+                                                  ctypes.cast(tg, ctypes.c_void_p), len(targets), snr,
+                                                  ctypes.c_uint64(seed & (2**64 - 1)), _ptr(out), stream),
+                   "synthesize_echo")
+        return out
+
+    def synchronize(self):
+        self.check(self.lib.sarbp_synchronize(self.h), "synchronize")
+
+    def timings(self):
+        a, b = ctypes.c_float(), ctypes.c_float()
+        self.check(self.lib.sarbp_last_timings(self.h, ctypes.byref(a), ctypes.byref(b)), "timings")
+        return a.value, b.value
+
+    def launches(self) -> int:
+        return int(self.lib.sarbp_kernel_launches(self.h))
+
+    def probe_issue_rates(self):
+        f, m, n = ctypes.c_double(), ctypes.c_double(), ctypes.c_int32()
+        self.check(self.lib.sarbp_probe_issue_rates(self.h, ctypes.byref(f), ctypes.byref(m), ctypes.byref(n)),
+                   "probe")
+        return f.value, m.value, n.value
+
+
+# --------------------------------------------------------- scene helpers --
+
+def scene_args(scene: scenes.Scene):
+    """(radar struct, grid struct, layout) for a synthetic scene."""
+    r = radar_struct(scene.radar, scene.t_rec0)
+    return r, grid_struct(scene.grid), scene.layout
+
+
+def synthesize(ctx: Context, scene: scenes.Scene, out=None, stream=None):
+    r = radar_struct(scene.radar, scene.t_rec0)
+    return ctx.synthesize_echo(r, scene.apc, scene.ns, scene.targets, scene.snr_db, scene.seed, out=out,
+                               stream=stream)
+
+
+def image_scene(ctx: Context, scene: scenes.Scene, echo, mode: int, image=None, stream=None):
+    r, g, _ = scene_args(scene)
+    return ctx.image(r, echo, scene.apc, g, mode, image=image, stream=stream)
+
+
+def nan_to_none(x):
+    return None if x is None or (isinstance(x, float) and math.isnan(x)) else x
