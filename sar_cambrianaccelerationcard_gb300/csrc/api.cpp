@@ -367,10 +367,12 @@ sarbp_status bp_device(sarbp_ctx *ctx, const sarbp_radar *r, const sarbp_rc_view
     cx = std::min(1.0, cx * 1.05 + 0.01);
     sy = std::min(1.0, sy * 1.05 + 0.01);
     const double bpm = 2.0 / r->c * rc.bin_rate;
-    const double half = bpm * (lux * hx * cx + luy * hy * sy + qq_max / (2 * rmin_tile)) * 1.01 + 2.0;
+    const double half = bpm * (lux * hx * cx + luy * hy * sy + qq_max / (2 * rmin_tile)) * 1.03 + 2.0;
+    if (!(half < 4096.0)) return fail(ctx, SARBP_ERR_UNSUPPORTED, "tile spans too many range bins");
     int win = (int)std::ceil(2 * half) + 8;
     win = (win + 3) & ~3;
-    if (win > 1024) return fail(ctx, SARBP_ERR_UNSUPPORTED, "tile spans too many range bins (%d)", win);
+    if (sarbp::bp_smem_bytes(mode, win) > (size_t)(227u << 10))
+        return fail(ctx, SARBP_ERR_UNSUPPORTED, "tile spans too many range bins (%d) for shared memory", win);
     p.win = win;
     // series terms: dR error ~ R (5/128) e^4 for 3 terms, e = |n|/R^2 <= (2 diag R + diag^2)/R^2
     const double e = (2 * tile_diag * rmax + qq_max) / (rmin_tile * rmin_tile);

@@ -153,8 +153,9 @@ __device__ __forceinline__ void produce_chunk(const BpPlan &P, const Smem &S, in
         const double bT = (2.0 * R / P.c - P.t0_bins) * P.bin_rate;
         // |dR| <= (|A| hx + |B| hy + |q|^2_max) / (2 R) within the tile
         const double hx = 0.5 * (kTileX - 1), hy = 0.5 * (kTileY - 1);
-        const double half = bpm * (fabs(A) * hx + fabs(B) * hy + (double)qq_max) / (2.0 * R) * 1.01 + 2.0;
-        long long ws = (long long)floor(bT - half);
+        // 1.03 covers the curvature term |q|/(2R) <= 1/40 the planner guarantees
+        const double half = bpm * (fabs(A) * hx + fabs(B) * hy + (double)qq_max) / (2.0 * R) * 1.03 + 2.0;
+        long long ws = (long long)floor(fmin(fmax(bT - half, -1.0e9), 1.0e9));
         ws &= ~3LL;
         const long long need_end = (long long)ceil(bT + half) + 2;
         if (need_end - ws > win) atomicOr(P.err, kErrWindow);
