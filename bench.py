@@ -46,10 +46,11 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--mode", default="split", choices=["split", "fp16store", "fp32", "fp64"])
-    ap.add_argument("--size", default="full", choices=["full", "small"],
-                    help="small: 512 pulses x 1024 samples, 512^2 (for profiling captures)")
+    ap.add_argument("--size", default="full", choices=["full", "medium", "small"],
+                    help="medium: 1024 pulses x 8192 samples, 2048^2 (profiling captures); small: config 1")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-probe", action="store_true", help="skip the issue-rate probe (profiling runs)")
     return ap.parse_args()
 
 
@@ -131,6 +132,8 @@ def workload(size):
     from sar_cambrianaccelerationcard_gb300 import scenes
     if size == "small":
         return scenes.config1()
+    if size == "medium":
+        return scenes.config2(np_=1024, n_img=2048)
     return scenes.config2()
 
 
@@ -314,7 +317,7 @@ def run_ours(args):
                "d2h_bytes_per_step": g.nx * g.ny * 8, "ms_per_step": e2e_s * 1e3}
 
     # --- roofline: issue-rate ceiling from live microbenchmarks
-    fp32_rate, mufu_rate, sms = ctx.probe_issue_rates()
+    fp32_rate, mufu_rate, sms = (1.0, 1.0, 0) if args.no_probe else ctx.probe_issue_rates()
     peak = min(fp32_rate / FP32_OPS_PER_UPDATE, mufu_rate / MUFU_OPS_PER_UPDATE) / 1e9
     bp_rate = updates / (bp_ms_each * 1e-3) / 1e9 if bp_ms_each else None
     roofline = {
