@@ -13,6 +13,7 @@
 #include <complex>
 #include <cstdarg>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <mutex>
 #include <string>
@@ -69,6 +70,7 @@ struct sarbp_ctx {
     DevBuf echo, spec, rc, scale, apc, image, partial, errword, power, targets;
     RcTables tables;
     int64_t launches = 0;
+    int checked = 0;  // SARBP_BOUNDS_CHECK=1 at creation: clamped, self-reporting BP kernels
     float rc_ms = 0.f, bp_ms = 0.f;
     bool timed_rc = false, timed_bp = false;
 };
@@ -229,6 +231,8 @@ sarbp_status check_errword(sarbp_ctx *ctx) {
     if (w == 0) return SARBP_OK;
     SARBP_CUDA(ctx, cudaMemset(ctx->errword.ptr, 0, sizeof(unsigned)), "reset device check word");
     if (w & sarbp::kErrWaitTimeout) return fail(ctx, SARBP_ERR_TIMEOUT, "a bounded device wait ran out (0x%x)", w);
+    if (w & sarbp::kErrIndexClamp)
+        return fail(ctx, SARBP_ERR_DEVICE_CHECK, "an interpolation index left its staging window (0x%x)", w);
     if (w & sarbp::kErrWindow)
         return fail(ctx, SARBP_ERR_DEVICE_CHECK, "a tile needed more range bins than the staging window (0x%x)", w);
     return fail(ctx, SARBP_ERR_DEVICE_CHECK, "device check word 0x%x", w);
@@ -334,6 +338,7 @@ sarbp_status bp_device(sarbp_ctx *ctx, const sarbp_radar *r, const sarbp_rc_view
     p.image = image;
     p.accumulate = accumulate;
     p.err = ctx->errword.as<unsigned>();
+    p.checked = ctx->checked;
 
     // Staging window: bins a tile can touch for one pulse, bounded over all pulses
     // from the grid's extreme line-of-sight directions (sampled on a 9x9 lattice).
@@ -376,7 +381,8 @@ sarbp_status bp_device(sarbp_ctx *ctx, const sarbp_radar *r, const sarbp_rc_view
     p.win = win;
     // series terms: dR error ~ R (5/128) e^4 for 3 terms, e = |n|/R^2 <= (2 diag R + diag^2)/R^2
     const double e = (2 * tile_diag * rmax + qq_max) / (rmin_tile * rmin_tile);
-    p.nterms = (rmax * 0.0390625 * e * e * e * e < 1e-8) ? 3 : 4;
+    // 3 terms when their truncation stays below 1e-6 m (2e-4 rad of C-band phase)
+    p.nterms = (rmax * 0.0390625 * e * e * e * e < 1e-6) ? 3 : 4;
     if (rmax * 0.02734375 * std::pow(e, 5) > 1e-7)
         return fail(ctx, SARBP_ERR_UNSUPPORTED, "tiles too large for the differential-range series");
 
@@ -447,6 +453,8 @@ sarbp_status sarbp_create(sarbp_ctx **out, int device) {
     sarbp_ctx *ctx = new sarbp_ctx();
     ctx->device = device;
     ctx->sms = prop.multiProcessorCount;
+    const char *chk = std::getenv("SARBP_BOUNDS_CHECK");
+    ctx->checked = (chk && chk[0] == '1') ? 1 : 0;
     bool ok = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) == cudaSuccess;
     for (int i = 0; i < 4 && ok; ++i) ok = cudaEventCreate(&ctx->ev[i]) == cudaSuccess;
     ok = ok && ctx->errword.ensure(sizeof(unsigned)) == cudaSuccess && ctx->power.ensure(sizeof(double)) == cudaSuccess;

@@ -8,27 +8,31 @@
 // loads, sqrtf + sincosf per pulse).
 //
 // Design (one CTA per TILE_X x TILE_Y pixel tile, optionally per pulse segment):
-//  * Pulses are processed in chunks of CHUNK.  For each chunk one warp computes,
-//    per pulse and in FP64, the tile-centre reference: range R_T, the wrapped
+//  * Pulses are processed in chunks of CHUNK.  For each chunk every warp
+//    computes, for two of its pulses, the tile-centre reference: range R_T
+//    (FP32 square root refined by one FP64 Newton step), the FP64-wrapped
 //    carrier phase, the bin of the tile centre and the window of bins the tile
 //    can touch; it then issues one TMA bulk copy (cp.async.bulk, local HBM ->
-//    shared memory, completion on an mbarrier) per pulse for that window.  Two
-//    raw buffers alternate so the copies of chunk c+1 overlap the arithmetic of
-//    chunk c.
+//    shared memory, completion on an mbarrier) per pulse for that window.  A
+//    three-stage ring of raw windows lets chunk c+1 load while chunk c computes.
 //  * A conversion pass turns each raw window (complex64, or complex16 times the
 //    per-pulse scale) into interpolation-ready pairs (mid, diff) with
 //    mid_i = (s_i + s_{i+1})/2, diff_i = s_{i+1} - s_i, so one 16-byte shared load
-//    and two FMAs interpolate.
+//    and two FMAs interpolate.  Converted windows are double-buffered: one
+//    block barrier per chunk.
 //  * SPLIT arithmetic per pixel and pulse: with q the pixel offset from the tile
 //    centre, n = 2 q.w + |q|^2 (w = tile centre - APC) and the differential
 //    range dR = sqrt(R_T^2 + n) - R_T = n (c1 + n (c2 + n (c3 + n c4))) (series
-//    of sqrt(1+e), |e| = |n|/R_T^2 < 1e-2 enforced by the planner) -- all on the
-//    FMA pipe; the phase fma(dR, k_hi, phi_T) + dR k_lo (compensated product);
-//    the only MUFU work is one sin/cos pair.
-//  * Pulse geometry is computed once per (tile, pulse) and broadcast to all
-//    warps from shared memory.
+//    of sqrt(1+e); the planner bounds the truncation error) -- all on the FMA
+//    pipe; the phase fma(dR, k_hi, phi_T) + dR k_lo (compensated product); the
+//    only MUFU work is one sin/cos pair.
+//  * Staging windows are sized so every bin a pixel can need lies inside
+//    [1, win-3]; the producer checks this per (tile, pulse) and, should a pulse
+//    fail the check, neutralises it (no data, bin 1) and raises an error bit,
+//    so shared-memory indices stay in bounds without a per-update clamp.  The
+//    CHECKED variant keeps a clamp and reports whether it ever fired.
 //  * FP32 and FP64 modes use the same staging with plain absolute-range
-//    arithmetic (the comparators).
+//    arithmetic (the comparators) and always clamp.
 #include "sarbp_internal.h"
 
 #include <math_constants.h>
@@ -37,10 +41,13 @@ namespace sarbp {
 namespace {
 
 constexpr int kThreads = 256;
+constexpr int kWarps = kThreads / 32;
 constexpr int kTileX = 32;  // pixels along x (columns)
 constexpr int kTileY = 64;  // pixels along y (rows)
 constexpr int kPix = kTileX * kTileY / kThreads;  // 8 pixels per thread
 constexpr int kChunk = 16;  // pulses per staged chunk
+constexpr int kPerWarp = kChunk / kWarps;  // pulses each warp prepares
+constexpr int kStages = 3;  // raw-window ring depth
 constexpr float kMagic = 12582912.0f;  // 1.5 * 2^23: adding it rounds to an integer
 constexpr unsigned kMagicBitsShift4 = 0x4B400000u << 4;
 
@@ -48,11 +55,9 @@ struct __align__(16) Prm {
     float4 k0;     // SPLIT: A, B, c1, c2       FP32: apc x, y, z, bin offset
     float4 k1;     // SPLIT: c3, c4, bin', phT
     double ax, ay, az;  // FP64: APC position
-    float mp;      // kMagic + pulse slot * win
     int ws;        // first bin of the window
     int lo, hi;    // copied part of the window [lo, hi) relative to ws
     float scale;   // FP16 storage scale
-    int pad0;
 };
 
 __device__ __forceinline__ unsigned smem_addr(const void *p) {
@@ -116,71 +121,89 @@ __device__ __forceinline__ float4 lds128(unsigned addr) {
 }
 
 struct Smem {
-    float4 *staged;      // [kChunk][win]
-    unsigned char *raw;  // [2][kChunk][win] * 8 bytes
-    Prm *prm;            // [2][kChunk]
-    uint64_t *bar;       // [2]
+    float4 *staged;      // [2][kChunk][win]
+    unsigned char *raw;  // [kStages][kChunk][win] * 8 bytes
+    Prm *prm;            // [kStages][kChunk]
+    uint64_t *bar;       // [kStages]
 };
 
 __device__ __forceinline__ Smem carve(unsigned char *base, int win) {
     Smem s;
     s.staged = reinterpret_cast<float4 *>(base);
-    s.raw = base + (size_t)kChunk * win * 16;
-    s.prm = reinterpret_cast<Prm *>(s.raw + (size_t)2 * kChunk * win * 8);
-    s.bar = reinterpret_cast<uint64_t *>(s.prm + 2 * kChunk);
+    s.raw = base + (size_t)2 * kChunk * win * 16;
+    s.prm = reinterpret_cast<Prm *>(s.raw + (size_t)kStages * kChunk * win * 8);
+    s.bar = reinterpret_cast<uint64_t *>(s.prm + kStages * kChunk);
     return s;
 }
 
-// Per-(tile, pulse) geometry, window, and TMA issue for one chunk (warp 0).
+struct TileGeo {
+    double pcx, pcy, pcz;   // tile centre
+    float qq_max;           // max |q|^2 over the tile
+};
+
+// Per-(tile, pulse) geometry, window and TMA issue for this warp's pulses of
+// one chunk.  Every warp arrives once on the stage's barrier.
 template <int MODE, int STORE>
-__device__ __forceinline__ void produce_chunk(const BpPlan &P, const Smem &S, int buf, int p0, int count,
-                                             double pcx, double pcy, double pcz, float qq_max) {
-    const int lane = threadIdx.x & 31;
+__device__ __forceinline__ void produce(const BpPlan &P, const Smem &S, int stage, int p0, int count,
+                                        const TileGeo &T) {
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int win = P.win;
     const int esize = STORE == SARBP_STORE_C64 ? 8 : 4;
+    const int slot = warp * kPerWarp + lane;
     unsigned bytes = 0;
     const char *src = nullptr;
     unsigned dst = 0;
-    if (lane < count) {
-        const int p = p0 + lane;
-        const double ax = __ldg(&P.apc[3 * p]), ay = __ldg(&P.apc[3 * p + 1]),
-                     az = __ldg(&P.apc[3 * p + 2]);
-        const double wx = pcx - ax, wy = pcy - ay, wz = pcz - az;
-        const double R = sqrt(wx * wx + wy * wy + wz * wz);
-        const double A = 2.0 * (P.g.ux[0] * wx + P.g.ux[1] * wy + P.g.ux[2] * wz);
-        const double B = 2.0 * (P.g.uy[0] * wx + P.g.uy[1] * wy + P.g.uy[2] * wz);
-        const double bpm = 2.0 / P.c * P.bin_rate;  // bins per metre of range
-        const double bT = (2.0 * R / P.c - P.t0_bins) * P.bin_rate;
-        // |dR| <= (|A| hx + |B| hy + |q|^2_max) / (2 R) within the tile
-        const double hx = 0.5 * (kTileX - 1), hy = 0.5 * (kTileY - 1);
-        // 1.03 covers the curvature term |q|/(2R) <= 1/40 the planner guarantees
-        const double half = bpm * (fabs(A) * hx + fabs(B) * hy + (double)qq_max) / (2.0 * R) * 1.03 + 2.0;
-        long long ws = (long long)floor(fmin(fmax(bT - half, -1.0e9), 1.0e9));
+    if (lane < kPerWarp && slot < count) {
+        const int p = p0 + slot;
+        const double ax = __ldg(&P.apc[3 * p]), ay = __ldg(&P.apc[3 * p + 1]), az = __ldg(&P.apc[3 * p + 2]);
+        const double wx = T.pcx - ax, wy = T.pcy - ay, wz = T.pcz - az;
+        const double R2 = fma(wx, wx, fma(wy, wy, wz * wz));
+        // FP32 square root, one FP64 Newton step: |error| ~ 1e-14 R
+        const float r0 = sqrtf((float)R2);
+        double R = (double)r0;
+        R = fma(fma(-R, R, R2), (double)(0.5f / r0), R);
+        const float Rf = (float)R;
+        const float iR = 1.0f / Rf;
+        const float wxf = (float)wx, wyf = (float)wy, wzf = (float)wz;
+        const float A = 2.f * ((float)P.g.ux[0] * wxf + (float)P.g.ux[1] * wyf + (float)P.g.ux[2] * wzf);
+        const float B = 2.f * ((float)P.g.uy[0] * wxf + (float)P.g.uy[1] * wyf + (float)P.g.uy[2] * wzf);
+        const float bpm = (float)(2.0 / P.c * P.bin_rate);  // bins per metre of range
+        const double bT = fma(R, 2.0 / P.c * P.bin_rate, -P.t0_bins * P.bin_rate);
+        // |dR| <= (|A| hx + |B| hy + |q|^2_max) / (2 R) within the tile; 1.03 covers
+        // the curvature term |q|/(2R) <= 1/40 that the planner guarantees.
+        const float hx = 0.5f * (kTileX - 1), hy = 0.5f * (kTileY - 1);
+        const float half = bpm * (fabsf(A) * hx + fabsf(B) * hy + T.qq_max) * 0.5f * iR * 1.03f + 2.f;
+        const float bTf = (float)bT;
+        long long ws = (long long)floorf(fminf(fmaxf(bTf - half, -1.0e9f), 1.0e9f));
         ws &= ~3LL;
-        const long long need_end = (long long)ceil(bT + half) + 2;
-        if (need_end - ws > win) atomicOr(P.err, kErrWindow);
+        const long long need_end = (long long)ceilf(fminf(bTf + half, 1.0e9f)) + 2;
+        const bool sane = isfinite(R) && R > 0.0 && isfinite(half) && need_end - ws <= win;
+        if (!sane) atomicOr(P.err, kErrWindow);
         long long lo = ws < 0 ? 0 : ws;
         long long hi = ws + win > P.nbins ? P.nbins : ws + win;
-        if (hi < lo) hi = lo;
-        Prm &q = S.prm[buf * kChunk + lane];
+        if (hi < lo || !sane) hi = lo;
+        Prm &q = S.prm[stage * kChunk + slot];
         q.ws = (int)ws;
         q.lo = (int)(lo - ws);
         q.hi = (int)(hi - ws);
-        q.mp = kMagic + (float)(lane * win);
         q.scale = STORE == SARBP_STORE_C32H ? __ldg(&P.scale[p]) : 1.f;
         if (MODE == SARBP_MODE_SPLIT || MODE == SARBP_MODE_FP16STORE) {
-            const double iR = 1.0 / R;
-            const double c1 = 0.5 * iR;
-            const double c2 = -0.125 * iR * iR * iR;
-            const double c3 = 0.0625 * iR * iR * iR * iR * iR;
-            const double c4 = -0.0390625 * iR * iR * iR * iR * iR * iR * iR;
-            const double cyc = 2.0 * P.fc / P.c * R;
-            const double phT = 2.0 * CUDART_PI * (cyc - rint(cyc));
-            q.k0 = make_float4((float)A, (float)B, (float)c1, (float)c2);
-            q.k1 = make_float4((float)c3, (float)c4, (float)(bT - (double)ws - 0.5), (float)phT);
+            const float i2 = iR * iR;
+            const float c1 = 0.5f * iR;
+            const float c2 = -0.125f * iR * i2;
+            const float c3 = 0.0625f * iR * i2 * i2;
+            const float c4 = -0.0390625f * iR * i2 * i2 * i2;
+            const double cyc = R * (2.0 * P.fc / P.c);
+            const float phT = (float)(cyc - rint(cyc)) * (float)(2.0 * CUDART_PI);
+            if (sane) {
+                q.k0 = make_float4(A, B, c1, c2);
+                q.k1 = make_float4(c3, c4, (float)(bT - (double)ws - 0.5), phT);
+            } else {  // inert pulse: every pixel reads bin 1 of an all-zero window
+                q.k0 = make_float4(0.f, 0.f, 0.f, 0.f);
+                q.k1 = make_float4(0.f, 0.f, 1.f, 0.f);
+            }
         } else if (MODE == SARBP_MODE_FP32) {
-            q.k0 = make_float4((float)ax, (float)ay, (float)az,
-                               (float)(-P.t0_bins * P.bin_rate - (double)ws - 0.5));
+            q.k0 = make_float4((float)ax, (float)ay, (float)az, (float)(-P.t0_bins * P.bin_rate - (double)ws - 0.5));
         } else {
             q.ax = ax;
             q.ay = ay;
@@ -189,13 +212,13 @@ __device__ __forceinline__ void produce_chunk(const BpPlan &P, const Smem &S, in
         if (hi > lo) {
             bytes = (unsigned)((hi - lo) * esize);
             src = reinterpret_cast<const char *>(P.rc) + ((size_t)p * P.nbins + (size_t)lo) * esize;
-            dst = smem_addr(S.raw + ((size_t)buf * kChunk + (size_t)lane) * win * 8 + (size_t)(lo - ws) * esize);
+            dst = smem_addr(S.raw + ((size_t)stage * kChunk + (size_t)slot) * win * 8 + (size_t)(lo - ws) * esize);
         }
     }
     unsigned total = bytes;
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) total += __shfl_xor_sync(0xffffffffu, total, o);
-    const unsigned bar = smem_addr(&S.bar[buf]);
+    const unsigned bar = smem_addr(&S.bar[stage]);
     if (lane == 0) mbar_expect_tx_arrive(bar, total);
     __syncwarp();
     if (bytes) tma_bulk_g2s(dst, src, bytes, bar);
@@ -203,36 +226,38 @@ __device__ __forceinline__ void produce_chunk(const BpPlan &P, const Smem &S, in
 
 // raw window -> (mid, diff) pairs; bins outside [lo, hi) read as zero.
 template <int STORE>
-__device__ __forceinline__ void convert_chunk(const Smem &S, int buf, int count, int win) {
-    for (int pl = 0; pl < count; ++pl) {
-        const Prm &q = S.prm[buf * kChunk + pl];
+__device__ __forceinline__ void convert(const Smem &S, int stage, int sbuf, int count, int win, unsigned win_magic) {
+    const int total = count * win;
+    float4 *st = S.staged + (size_t)sbuf * kChunk * win;
+    for (int e = threadIdx.x; e < total; e += kThreads) {
+        const int pl = (int)__umulhi((unsigned)e, win_magic);
+        const int i = e - pl * win;
+        const Prm &q = S.prm[stage * kChunk + pl];
         const int lo = q.lo, hi = q.hi;
-        const float sc = q.scale;
-        const unsigned char *rw = S.raw + ((size_t)buf * kChunk + pl) * win * 8;
-        for (int i = threadIdx.x; i < win; i += kThreads) {
-            float2 a = make_float2(0.f, 0.f), b = make_float2(0.f, 0.f);
-            if (STORE == SARBP_STORE_C64) {
-                const float2 *r = reinterpret_cast<const float2 *>(rw);
-                if (i >= lo && i < hi) a = r[i];
-                if (i + 1 >= lo && i + 1 < hi) b = r[i + 1];
-            } else {
-                const __half2 *r = reinterpret_cast<const __half2 *>(rw);
-                if (i >= lo && i < hi) a = __half22float2(r[i]);
-                if (i + 1 >= lo && i + 1 < hi) b = __half22float2(r[i + 1]);
-                a.x *= sc; a.y *= sc; b.x *= sc; b.y *= sc;
-            }
-            S.staged[pl * win + i] =
-                make_float4(0.5f * (a.x + b.x), 0.5f * (a.y + b.y), b.x - a.x, b.y - a.y);
+        const unsigned char *rw = S.raw + ((size_t)stage * kChunk + pl) * win * 8;
+        float2 a = make_float2(0.f, 0.f), b = make_float2(0.f, 0.f);
+        if (STORE == SARBP_STORE_C64) {
+            const float2 *r = reinterpret_cast<const float2 *>(rw);
+            if (i >= lo && i < hi) a = r[i];
+            if (i + 1 >= lo && i + 1 < hi) b = r[i + 1];
+        } else {
+            const __half2 *r = reinterpret_cast<const __half2 *>(rw);
+            const float sc = q.scale;
+            if (i >= lo && i < hi) a = __half22float2(r[i]);
+            if (i + 1 >= lo && i + 1 < hi) b = __half22float2(r[i + 1]);
+            a.x *= sc; a.y *= sc; b.x *= sc; b.y *= sc;
         }
+        st[e] = make_float4(0.5f * (a.x + b.x), 0.5f * (a.y + b.y), b.x - a.x, b.y - a.y);
     }
 }
 
-template <int MODE, int STORE, int NTERMS>
+template <int MODE, int STORE, int NTERMS, bool CHECKED>
 __global__ void __launch_bounds__(kThreads, 2)
     bp_kernel(const __grid_constant__ BpPlan P, int tiles_y, int pulses_per_seg, float qq_max) {
     extern __shared__ __align__(128) unsigned char smem_raw[];
     const int win = P.win;
     const Smem S = carve(smem_raw, win);
+    const unsigned win_magic = (unsigned)((0xFFFFFFFFull + (unsigned long long)win) / (unsigned long long)win);
 
     const int tile = blockIdx.x;
     const int ty = tile % tiles_y;  // tiles sharing a range strip run together (L2 reuse)
@@ -254,14 +279,17 @@ __global__ void __launch_bounds__(kThreads, 2)
         yc[j] = (float)yl - 0.5f * (kTileY - 1);
         qq[j] = xc * xc * g11 + 2.f * xc * yc[j] * g12 + yc[j] * yc[j] * g22;
     }
-    const double pcx_i = tx * kTileX + 0.5 * (kTileX - 1), pcy_i = ty * kTileY + 0.5 * (kTileY - 1);
-    const double pcx = P.g.origin[0] + pcx_i * P.g.ux[0] + pcy_i * P.g.uy[0];
-    const double pcy = P.g.origin[1] + pcx_i * P.g.ux[1] + pcy_i * P.g.uy[1];
-    const double pcz = P.g.origin[2] + pcx_i * P.g.ux[2] + pcy_i * P.g.uy[2];
+    TileGeo T;
+    {
+        const double pcx_i = tx * kTileX + 0.5 * (kTileX - 1), pcy_i = ty * kTileY + 0.5 * (kTileY - 1);
+        T.pcx = P.g.origin[0] + pcx_i * P.g.ux[0] + pcy_i * P.g.uy[0];
+        T.pcy = P.g.origin[1] + pcx_i * P.g.ux[1] + pcy_i * P.g.uy[1];
+        T.pcz = P.g.origin[2] + pcx_i * P.g.ux[2] + pcy_i * P.g.uy[2];
+        T.qq_max = qq_max;
+    }
 
     if (threadIdx.x == 0) {
-        mbar_init(smem_addr(&S.bar[0]), 1);
-        mbar_init(smem_addr(&S.bar[1]), 1);
+        for (int s = 0; s < kStages; ++s) mbar_init(smem_addr(&S.bar[s]), kWarps);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     }
@@ -274,15 +302,12 @@ __global__ void __launch_bounds__(kThreads, 2)
 #pragma unroll
     for (int j = 0; j < (MODE == SARBP_MODE_FP64 ? kPix : 1); ++j) { dacc_r[j] = 0.0; dacc_i[j] = 0.0; }
 
-    // per-mode constants
     const float bpm = (float)(2.0 / P.c * P.bin_rate);
     const double kph_d = 4.0 * CUDART_PI * P.fc / P.c;
     const float kph_hi = (float)kph_d;
     const float kph_lo = (float)(kph_d - (double)kph_hi);
     const float wmax = (float)(win - 2);
-    const unsigned sbase = smem_addr(S.staged) - kMagicBitsShift4;
 
-    // absolute pixel positions for the plain modes
     float fpy[kPix], fpz[kPix], fpxx[kPix];
     if (MODE == SARBP_MODE_FP32) {
 #pragma unroll
@@ -294,30 +319,34 @@ __global__ void __launch_bounds__(kThreads, 2)
         }
     }
 
-    if (warp == 0 && nchunks > 0)
-        produce_chunk<MODE, STORE>(P, S, 0, p_begin, min(kChunk, p_end - p_begin), pcx, pcy, pcz, qq_max);
+    if (nchunks > 0) produce<MODE, STORE>(P, S, 0, p_begin, min(kChunk, p_end - p_begin), T);
 
     bool failed = false;
+    bool clamped = false;
 #pragma unroll 1
     for (int c = 0; c < nchunks; ++c) {
-        const int buf = c & 1;
+        const int stage = c % kStages;
+        const int sbuf = c & 1;
         const int pc0 = p_begin + c * kChunk;
         const int count = min(kChunk, p_end - pc0);
-        if (warp == 0 && c + 1 < nchunks) {
+        if (c + 1 < nchunks) {
             const int pn = pc0 + kChunk;
-            produce_chunk<MODE, STORE>(P, S, buf ^ 1, pn, min(kChunk, p_end - pn), pcx, pcy, pcz, qq_max);
+            produce<MODE, STORE>(P, S, (c + 1) % kStages, pn, min(kChunk, p_end - pn), T);
         }
-        const bool ok = mbar_wait_bounded(smem_addr(&S.bar[buf]), (c >> 1) & 1, 2000000000ull);
-        if (__syncthreads_or(!ok)) { failed = true; break; }
-        convert_chunk<STORE>(S, buf, count, win);
+        const bool ok = mbar_wait_bounded(smem_addr(&S.bar[stage]), (c / kStages) & 1, 2000000000ull);
+        if (!ok) { failed = true; }
+        if (__syncthreads_or(failed)) { failed = true; break; }
+        convert<STORE>(S, stage, sbuf, count, win, win_magic);
         __syncthreads();
 
+        const float4 *stg = S.staged + (size_t)sbuf * kChunk * win;
+        const unsigned sbase = smem_addr(stg) - kMagicBitsShift4;
         if (MODE == SARBP_MODE_SPLIT || MODE == SARBP_MODE_FP16STORE) {
 #pragma unroll 1
             for (int pl = 0; pl < count; ++pl) {
-                const Prm &q = S.prm[buf * kChunk + pl];
+                const Prm &q = S.prm[stage * kChunk + pl];
                 const float4 k0 = q.k0, k1 = q.k1;
-                const float mp = q.mp;
+                const float mp = kMagic + (float)(pl * win);
                 const float xA = xc * k0.x;
 #pragma unroll
                 for (int j = 0; j < kPix; ++j) {
@@ -326,7 +355,11 @@ __global__ void __launch_bounds__(kThreads, 2)
                     poly = fmaf(n, poly, k0.z);
                     const float dR = n * poly;
                     float b = fmaf(dR, bpm, k1.z);
-                    b = fminf(fmaxf(b, 0.f), wmax);
+                    if (CHECKED) {
+                        const float bc = fminf(fmaxf(b, 0.f), wmax);
+                        clamped |= !(bc == b);
+                        b = bc;
+                    }
                     const float t = b + mp;
                     const float f = b - (t - mp);
                     const float4 v = lds128((__float_as_uint(t) << 4) + sbase);
@@ -343,9 +376,9 @@ __global__ void __launch_bounds__(kThreads, 2)
         } else if (MODE == SARBP_MODE_FP32) {
 #pragma unroll 1
             for (int pl = 0; pl < count; ++pl) {
-                const Prm &q = S.prm[buf * kChunk + pl];
+                const Prm &q = S.prm[stage * kChunk + pl];
                 const float4 k0 = q.k0;
-                const float mp = q.mp;
+                const float mp = kMagic + (float)(pl * win);
                 const float kph = (float)kph_d;
 #pragma unroll
                 for (int j = 0; j < kPix; ++j) {
@@ -368,10 +401,10 @@ __global__ void __launch_bounds__(kThreads, 2)
             const double cyc_per_m = 2.0 * P.fc / P.c;
 #pragma unroll 1
             for (int pl = 0; pl < count; ++pl) {
-                const Prm &q = S.prm[buf * kChunk + pl];
+                const Prm &q = S.prm[stage * kChunk + pl];
                 const double ax = q.ax, ay = q.ay, az = q.az;
                 const double boff = -P.t0_bins * P.bin_rate - (double)q.ws;
-                const float4 *st = S.staged + pl * win;
+                const float4 *st = stg + pl * win;
 #pragma unroll
                 for (int j = 0; j < kPix; ++j) {
                     const double xi = tx * kTileX + xl, yi = ty * kTileY + ((warp >> 2) + 2 * j) * 4 + ly;
@@ -395,15 +428,14 @@ __global__ void __launch_bounds__(kThreads, 2)
                 }
             }
         }
-        __syncthreads();
     }
 
+    if (CHECKED && clamped) atomicOr(P.err, kErrIndexClamp);
     if (failed) {
-        if (threadIdx.x == 0) atomicOr(P.err, kErrWaitTimeout);
-        // let any copy still in flight land before the CTA's shared memory is released
         if (threadIdx.x == 0) {
-            mbar_wait_bounded(smem_addr(&S.bar[0]), 0, 1000000000ull);
-            mbar_wait_bounded(smem_addr(&S.bar[1]), 0, 1000000000ull);
+            atomicOr(P.err, kErrWaitTimeout);
+            // let copies still in flight land before the CTA's shared memory is released
+            for (int s = 0; s < kStages; ++s) mbar_wait_bounded(smem_addr(&S.bar[s]), 0, 500000000ull);
         }
         __syncthreads();
         return;
@@ -445,16 +477,24 @@ __global__ void reduce_segments_kernel(const float2 *__restrict__ partial, int s
     }
 }
 
-template <int MODE, int STORE, int NTERMS>
-cudaError_t launch_variant(const BpPlan &p, cudaStream_t s, int tiles, int tiles_y, int pps,
-                           float qq_max) {
-    auto k = bp_kernel<MODE, STORE, NTERMS>;
+template <int MODE, int STORE, int NTERMS, bool CHECKED>
+cudaError_t launch_variant(const BpPlan &p, cudaStream_t s, int tiles, int tiles_y, int pps, float qq_max) {
+    auto k = bp_kernel<MODE, STORE, NTERMS, CHECKED>;
     const size_t smem = bp_smem_bytes(MODE, p.win);
     cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     dim3 grid(tiles, p.segments);
     k<<<grid, kThreads, smem, s>>>(p, tiles_y, pps, qq_max);
     return cudaGetLastError();
+}
+
+template <int MODE, int STORE>
+cudaError_t launch_split(const BpPlan &p, cudaStream_t s, int tiles, int tiles_y, int pps, float qq_max) {
+    if (p.checked)
+        return p.nterms == 3 ? launch_variant<MODE, STORE, 3, true>(p, s, tiles, tiles_y, pps, qq_max)
+                             : launch_variant<MODE, STORE, 4, true>(p, s, tiles, tiles_y, pps, qq_max);
+    return p.nterms == 3 ? launch_variant<MODE, STORE, 3, false>(p, s, tiles, tiles_y, pps, qq_max)
+                         : launch_variant<MODE, STORE, 4, false>(p, s, tiles, tiles_y, pps, qq_max);
 }
 
 }  // namespace
@@ -467,7 +507,8 @@ void bp_tile_dims(int, int *tile_x, int *tile_y) {
 int bp_pulses_per_chunk(int) { return kChunk; }
 
 size_t bp_smem_bytes(int, int win) {
-    return (size_t)kChunk * win * 16 + (size_t)2 * kChunk * win * 8 + 2 * kChunk * sizeof(Prm) + 16;
+    return (size_t)2 * kChunk * win * 16 + (size_t)kStages * kChunk * win * 8 + kStages * kChunk * sizeof(Prm) +
+           kStages * sizeof(uint64_t);
 }
 
 cudaError_t launch_bp(const BpPlan &p, cudaStream_t s, int *launches) {
@@ -484,20 +525,16 @@ cudaError_t launch_bp(const BpPlan &p, cudaStream_t s, int *launches) {
     const bool fp16 = p.storage == SARBP_STORE_C32H;
     switch (p.mode) {
         case SARBP_MODE_FP64:
-            e = fp16 ? launch_variant<SARBP_MODE_FP64, SARBP_STORE_C32H, 4>(p, s, tiles, tiles_y, pps, qq_max)
-                     : launch_variant<SARBP_MODE_FP64, SARBP_STORE_C64, 4>(p, s, tiles, tiles_y, pps, qq_max);
+            e = fp16 ? launch_variant<SARBP_MODE_FP64, SARBP_STORE_C32H, 4, false>(p, s, tiles, tiles_y, pps, qq_max)
+                     : launch_variant<SARBP_MODE_FP64, SARBP_STORE_C64, 4, false>(p, s, tiles, tiles_y, pps, qq_max);
             break;
         case SARBP_MODE_FP32:
-            e = fp16 ? launch_variant<SARBP_MODE_FP32, SARBP_STORE_C32H, 4>(p, s, tiles, tiles_y, pps, qq_max)
-                     : launch_variant<SARBP_MODE_FP32, SARBP_STORE_C64, 4>(p, s, tiles, tiles_y, pps, qq_max);
+            e = fp16 ? launch_variant<SARBP_MODE_FP32, SARBP_STORE_C32H, 4, false>(p, s, tiles, tiles_y, pps, qq_max)
+                     : launch_variant<SARBP_MODE_FP32, SARBP_STORE_C64, 4, false>(p, s, tiles, tiles_y, pps, qq_max);
             break;
         default:
-            if (p.nterms == 3)
-                e = fp16 ? launch_variant<SARBP_MODE_SPLIT, SARBP_STORE_C32H, 3>(p, s, tiles, tiles_y, pps, qq_max)
-                         : launch_variant<SARBP_MODE_SPLIT, SARBP_STORE_C64, 3>(p, s, tiles, tiles_y, pps, qq_max);
-            else
-                e = fp16 ? launch_variant<SARBP_MODE_SPLIT, SARBP_STORE_C32H, 4>(p, s, tiles, tiles_y, pps, qq_max)
-                         : launch_variant<SARBP_MODE_SPLIT, SARBP_STORE_C64, 4>(p, s, tiles, tiles_y, pps, qq_max);
+            e = fp16 ? launch_split<SARBP_MODE_SPLIT, SARBP_STORE_C32H>(p, s, tiles, tiles_y, pps, qq_max)
+                     : launch_split<SARBP_MODE_SPLIT, SARBP_STORE_C64>(p, s, tiles, tiles_y, pps, qq_max);
             break;
     }
     if (e != cudaSuccess) return e;

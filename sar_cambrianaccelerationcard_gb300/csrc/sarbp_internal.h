@@ -59,6 +59,7 @@ struct BpPlan {
     int accumulate;
     int win;                 // staged bins per (tile, pulse), multiple of 4
     int nterms;              // polynomial terms for the differential range (3 or 4)
+    int checked;             // 1: clamp every interpolation index and report clamps
     unsigned *err;           // device error word
 };
 

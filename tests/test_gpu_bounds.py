@@ -1,0 +1,49 @@
+"""Evidence for the unclamped back-projection inner loop.
+
+The production SPLIT / FP16STORE kernels index the staged range window
+without a per-update clamp: the window is sized (and checked per tile and
+pulse by the producer) so that every bin a pixel needs lies inside it.  The
+checked build (SARBP_BOUNDS_CHECK=1 when the context is created) keeps a clamp
+on every index and reports through the context if it ever changed one.  Over
+straight, curved and ragged geometries it must report nothing and produce the
+same image bit for bit.
+"""
+import os
+
+import numpy as np
+import pytest
+
+from sar_cambrianaccelerationcard_gb300 import sarbp, scenes
+
+pytestmark = pytest.mark.gpu
+
+
+def scenes_to_check():
+    a = scenes.config1(np_=256, ns=1024)
+    b = scenes.config2(np_=512, ns=4096, n_img=512)
+    c = scenes.config2(np_=512, ns=4096, n_img=300)
+    c.apc = scenes.curved_track(c.radar, c.np_, seed=5)
+    d = scenes.config1(np_=100, ns=700)
+    d.grid = scenes.centred_grid(d.radar, 77, 130, 0.5)
+    return [a, b, c, d]
+
+
+@pytest.mark.parametrize("mode", ["split", "fp16store"])
+def test_checked_kernel_never_clamps(mode):
+    old = os.environ.get("SARBP_BOUNDS_CHECK")
+    os.environ["SARBP_BOUNDS_CHECK"] = "1"
+    try:
+        checked = sarbp.Context(0)
+    finally:
+        if old is None:
+            del os.environ["SARBP_BOUNDS_CHECK"]
+        else:
+            os.environ["SARBP_BOUNDS_CHECK"] = old
+    plain = sarbp.Context(0)
+    for s in scenes_to_check():
+        echo = sarbp.synthesize(plain, s)
+        a = sarbp.image_scene(plain, s, echo, sarbp.MODES[mode])
+        b = sarbp.image_scene(checked, s, echo, sarbp.MODES[mode])  # raises on a clamp
+        assert np.array_equal(a, b), s.name
+    checked.close()
+    plain.close()
