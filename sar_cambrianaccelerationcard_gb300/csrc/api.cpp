@@ -67,7 +67,7 @@ struct sarbp_ctx {
     cudaStream_t stream = nullptr;
     cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
     std::string err;
-    DevBuf echo, spec, rc, scale, apc, image, partial, errword, power, targets;
+    DevBuf echo, spec, rc, scale, apc, image, partial, errword, power, targets, pref;
     RcTables tables;
     int64_t launches = 0;
     int checked = 0;  // SARBP_BOUNDS_CHECK=1 at creation: clamped, self-reporting BP kernels
@@ -339,6 +339,15 @@ sarbp_status bp_device(sarbp_ctx *ctx, const sarbp_radar *r, const sarbp_rc_view
     p.accumulate = accumulate;
     p.err = ctx->errword.as<unsigned>();
     p.checked = ctx->checked;
+    auto split2 = [](double v, float *h, float *l) {
+        *h = (float)v;
+        *l = (float)(v - (double)*h);
+    };
+    split2(2.0 / r->c * rc.bin_rate, &p.kb_h, &p.kb_l);
+    split2(rc.t0_bins * rc.bin_rate, &p.tb_h, &p.tb_l);
+    split2(2.0 * r->fc / r->c, &p.kc_h, &p.kc_l);
+    SARBP_CUDA(ctx, ctx->pref.ensure(sizeof(float) * 8 * (size_t)np), "alloc pulse references");
+    p.pref = ctx->pref.as<float4>();
 
     // Staging window: bins a tile can touch for one pulse, bounded over all pulses
     // from the grid's extreme line-of-sight directions (sampled on a 9x9 lattice).
@@ -473,7 +482,7 @@ sarbp_status sarbp_destroy(sarbp_ctx *ctx) {
     cudaSetDevice(ctx->device);
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
     for (DevBuf *b : {&ctx->echo, &ctx->spec, &ctx->rc, &ctx->scale, &ctx->apc, &ctx->image, &ctx->partial,
-                      &ctx->errword, &ctx->power, &ctx->targets, &ctx->tables.filt, &ctx->tables.tw,
+                      &ctx->errword, &ctx->power, &ctx->targets, &ctx->pref, &ctx->tables.filt, &ctx->tables.tw,
                       &ctx->tables.ramp})
         b->release();
     for (cudaEvent_t &e : ctx->ev)
@@ -499,7 +508,7 @@ sarbp_status sarbp_trim(sarbp_ctx *ctx) {
     cudaSetDevice(ctx->device);
     cudaStreamSynchronize(ctx->stream);
     for (DevBuf *b : {&ctx->echo, &ctx->spec, &ctx->rc, &ctx->scale, &ctx->apc, &ctx->image, &ctx->partial,
-                      &ctx->targets})
+                      &ctx->targets, &ctx->pref})
         b->release();
     return SARBP_OK;
 }
@@ -508,7 +517,7 @@ size_t sarbp_device_bytes(const sarbp_ctx *ctx) {
     if (!ctx) return 0;
     size_t t = 0;
     for (const DevBuf *b : {&ctx->echo, &ctx->spec, &ctx->rc, &ctx->scale, &ctx->apc, &ctx->image, &ctx->partial,
-                            &ctx->errword, &ctx->power, &ctx->targets, &ctx->tables.filt, &ctx->tables.tw,
+                            &ctx->errword, &ctx->power, &ctx->targets, &ctx->pref, &ctx->tables.filt, &ctx->tables.tw,
                             &ctx->tables.ramp})
         t += b->bytes;
     return t;

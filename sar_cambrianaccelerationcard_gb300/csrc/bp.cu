@@ -139,7 +139,50 @@ __device__ __forceinline__ Smem carve(unsigned char *base, int win) {
 struct TileGeo {
     double pcx, pcy, pcz;   // tile centre
     float qq_max;           // max |q|^2 over the tile
+    float xT, yT;           // tile centre in pixel units from the grid origin (exact)
+    float qqh, qql;         // |xT ux + yT uy|^2 as a float pair
 };
+
+// Float-float ("double-float") arithmetic on the FP32 pipe: a value is h + l
+// with |l| <= ulp(h)/2, about 48 significant bits.  Error-free transforms
+// (Knuth two-sum, FMA two-product).
+struct ff {
+    float h, l;
+};
+__device__ __forceinline__ ff two_sum(float a, float b) {
+    const float s = a + b;
+    const float bb = s - a;
+    return {s, (a - (s - bb)) + (b - bb)};
+}
+__device__ __forceinline__ ff quick_two_sum(float a, float b) {
+    const float s = a + b;
+    return {s, b - (s - a)};
+}
+__device__ __forceinline__ ff ff_add(ff a, ff b) {
+    const ff s = two_sum(a.h, b.h);
+    return quick_two_sum(s.h, s.l + (a.l + b.l));
+}
+__device__ __forceinline__ ff ff_mul_f(ff a, float b) {
+    const float p = a.h * b;
+    const float e = fmaf(a.h, b, -p);
+    return quick_two_sum(p, fmaf(a.l, b, e));
+}
+
+// Per-pulse reference (FP64), relative to the grid origin O:
+//   a0 = |O - apc|^2, a1 = 2 ux.(O - apc), a2 = 2 uy.(O - apc)
+// stored as float pairs: pref[2p] = (a0h, a0l, a1h, a1l), pref[2p+1] = (a2h, a2l, 0, 0).
+// With (xT, yT) a tile centre in pixel units, R_T^2 = a0 + xT a1 + yT a2 + |q_T|^2.
+__global__ void pulse_ref_kernel(const double *__restrict__ apc, int np, BpGeom g, float4 *__restrict__ pref) {
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= np) return;
+    const double wx = g.origin[0] - apc[3 * p], wy = g.origin[1] - apc[3 * p + 1], wz = g.origin[2] - apc[3 * p + 2];
+    const double a0 = fma(wx, wx, fma(wy, wy, wz * wz));
+    const double a1 = 2.0 * (g.ux[0] * wx + g.ux[1] * wy + g.ux[2] * wz);
+    const double a2 = 2.0 * (g.uy[0] * wx + g.uy[1] * wy + g.uy[2] * wz);
+    const float a0h = (float)a0, a1h = (float)a1, a2h = (float)a2;
+    pref[2 * p] = make_float4(a0h, (float)(a0 - (double)a0h), a1h, (float)(a1 - (double)a1h));
+    pref[2 * p + 1] = make_float4(a2h, (float)(a2 - (double)a2h), 0.f, 0.f);
+}
 
 // Per-(tile, pulse) geometry, window and TMA issue for this warp's pulses of
 // one chunk.  Every warp arrives once on the stage's barrier.
@@ -155,60 +198,78 @@ __device__ __forceinline__ void produce(const BpPlan &P, const Smem &S, int stag
     unsigned dst = 0;
     if (lane < kPerWarp && slot < count) {
         const int p = p0 + slot;
-        const double ax = __ldg(&P.apc[3 * p]), ay = __ldg(&P.apc[3 * p + 1]), az = __ldg(&P.apc[3 * p + 2]);
-        const double wx = T.pcx - ax, wy = T.pcy - ay, wz = T.pcz - az;
-        const double R2 = fma(wx, wx, fma(wy, wy, wz * wz));
-        // FP32 square root, one FP64 Newton step: |error| ~ 1e-14 R
-        const float r0 = sqrtf((float)R2);
-        double R = (double)r0;
-        R = fma(fma(-R, R, R2), (double)(0.5f / r0), R);
-        const float Rf = (float)R;
-        const float iR = 1.0f / Rf;
-        const float wxf = (float)wx, wyf = (float)wy, wzf = (float)wz;
-        const float A = 2.f * ((float)P.g.ux[0] * wxf + (float)P.g.ux[1] * wyf + (float)P.g.ux[2] * wzf);
-        const float B = 2.f * ((float)P.g.uy[0] * wxf + (float)P.g.uy[1] * wyf + (float)P.g.uy[2] * wzf);
         const float bpm = (float)(2.0 / P.c * P.bin_rate);  // bins per metre of range
-        const double bT = fma(R, 2.0 / P.c * P.bin_rate, -P.t0_bins * P.bin_rate);
-        // |dR| <= (|A| hx + |B| hy + |q|^2_max) / (2 R) within the tile; 1.03 covers
-        // the curvature term |q|/(2R) <= 1/40 that the planner guarantees.
         const float hx = 0.5f * (kTileX - 1), hy = 0.5f * (kTileY - 1);
-        const float half = bpm * (fabsf(A) * hx + fabsf(B) * hy + T.qq_max) * 0.5f * iR * 1.03f + 2.f;
-        const float bTf = (float)bT;
-        long long ws = (long long)floorf(fminf(fmaxf(bTf - half, -1.0e9f), 1.0e9f));
-        ws &= ~3LL;
-        const long long need_end = (long long)ceilf(fminf(bTf + half, 1.0e9f)) + 2;
-        const bool sane = isfinite(R) && R > 0.0 && isfinite(half) && need_end - ws <= win;
-        if (!sane) atomicOr(P.err, kErrWindow);
-        long long lo = ws < 0 ? 0 : ws;
-        long long hi = ws + win > P.nbins ? P.nbins : ws + win;
-        if (hi < lo || !sane) hi = lo;
+        const int cen = win >> 1;  // staged index origin
         Prm &q = S.prm[stage * kChunk + slot];
-        q.ws = (int)ws;
-        q.lo = (int)(lo - ws);
-        q.hi = (int)(hi - ws);
-        q.scale = STORE == SARBP_STORE_C32H ? __ldg(&P.scale[p]) : 1.f;
+        long long ws;
+        bool sane;
         if (MODE == SARBP_MODE_SPLIT || MODE == SARBP_MODE_FP16STORE) {
+            // R_T^2 = a0 + xT a1 + yT a2 + |q_T|^2 in float-float
+            const float4 r0v = __ldg(&P.pref[2 * p]);
+            const float4 r1v = __ldg(&P.pref[2 * p + 1]);
+            const ff a0 = {r0v.x, r0v.y}, a1 = {r0v.z, r0v.w}, a2 = {r1v.x, r1v.y};
+            const ff S2 = ff_add(ff_add(a0, ff_mul_f(a1, T.xT)), ff_add(ff_mul_f(a2, T.yT), ff{T.qqh, T.qql}));
+            const float r = sqrtf(S2.h);
+            const float corr = (fmaf(-r, r, S2.h) + S2.l) * (0.5f / r);  // R_T = r + corr
+            // bin of the tile centre: (2 R_T / c - t0) * bin_rate
+            const float kbh = P.kb_h, kbl = P.kb_l;
+            float ph_ = r * kbh;
+            float pl_ = fmaf(r, kbh, -ph_) + fmaf(r, kbl, corr * kbh);
+            const ff bT = ff_add(quick_two_sum(ph_, pl_), ff{-P.tb_h, -P.tb_l});
+            // carrier phase 2 pi frac(R_T * 2 fc / c)
+            const float kch = P.kc_h, kcl = P.kc_l;
+            const float cy = r * kch;
+            const float cy_e = fmaf(r, kch, -cy) + fmaf(r, kcl, corr * kch);
+            const float fr = (cy - rintf(cy)) + cy_e;
+            const float phT = fr * 6.28318530717958647692f;
+            const float iR = 1.0f / r;
+            const float A = r0v.z + 2.f * (T.xT * (float)P.g.g11 + T.yT * (float)P.g.g12);
+            const float B = r1v.x + 2.f * (T.xT * (float)P.g.g12 + T.yT * (float)P.g.g22);
+            const float half = bpm * (fabsf(A) * hx + fabsf(B) * hy + T.qq_max) * 0.5f * iR * 1.03f + 2.f;
+            ws = (long long)floorf(fminf(fmaxf(bT.h - half, -1.0e9f), 1.0e9f));
+            ws &= ~3LL;
+            const long long need_end = (long long)ceilf(fminf(bT.h + half, 1.0e9f)) + 2;
+            sane = isfinite(r) && r > 0.f && isfinite(half) && isfinite(phT) && need_end - ws <= win;
             const float i2 = iR * iR;
-            const float c1 = 0.5f * iR;
-            const float c2 = -0.125f * iR * i2;
-            const float c3 = 0.0625f * iR * i2 * i2;
-            const float c4 = -0.0390625f * iR * i2 * i2 * i2;
-            const double cyc = R * (2.0 * P.fc / P.c);
-            const float phT = (float)(cyc - rint(cyc)) * (float)(2.0 * CUDART_PI);
             if (sane) {
-                q.k0 = make_float4(A, B, c1, c2);
-                q.k1 = make_float4(c3, c4, (float)(bT - (double)ws - 0.5), phT);
-            } else {  // inert pulse: every pixel reads bin 1 of an all-zero window
+                q.k0 = make_float4(A, B, 0.5f * iR, -0.125f * iR * i2);
+                q.k1 = make_float4(0.0625f * iR * i2 * i2, -0.0390625f * iR * i2 * i2 * i2,
+                                   ((bT.h - (float)ws) + bT.l) - 0.5f - (float)cen, phT);
+            } else {  // inert pulse: every pixel reads the centre bin of an all-zero window
                 q.k0 = make_float4(0.f, 0.f, 0.f, 0.f);
-                q.k1 = make_float4(0.f, 0.f, 1.f, 0.f);
+                q.k1 = make_float4(0.f, 0.f, 0.f, 0.f);
             }
-        } else if (MODE == SARBP_MODE_FP32) {
-            q.k0 = make_float4((float)ax, (float)ay, (float)az, (float)(-P.t0_bins * P.bin_rate - (double)ws - 0.5));
         } else {
+            const double ax = __ldg(&P.apc[3 * p]), ay = __ldg(&P.apc[3 * p + 1]), az = __ldg(&P.apc[3 * p + 2]);
+            const double wx = T.pcx - ax, wy = T.pcy - ay, wz = T.pcz - az;
+            const double R = sqrt(fma(wx, wx, fma(wy, wy, wz * wz)));
+            const float iR = (float)(1.0 / R);
+            const float wxf = (float)wx, wyf = (float)wy, wzf = (float)wz;
+            const float A = 2.f * ((float)P.g.ux[0] * wxf + (float)P.g.ux[1] * wyf + (float)P.g.ux[2] * wzf);
+            const float B = 2.f * ((float)P.g.uy[0] * wxf + (float)P.g.uy[1] * wyf + (float)P.g.uy[2] * wzf);
+            const double bT = fma(R, 2.0 / P.c * P.bin_rate, -P.t0_bins * P.bin_rate);
+            const float half = bpm * (fabsf(A) * hx + fabsf(B) * hy + T.qq_max) * 0.5f * iR * 1.03f + 2.f;
+            const float bTf = (float)bT;
+            ws = (long long)floorf(fminf(fmaxf(bTf - half, -1.0e9f), 1.0e9f));
+            ws &= ~3LL;
+            const long long need_end = (long long)ceilf(fminf(bTf + half, 1.0e9f)) + 2;
+            sane = isfinite(R) && R > 0.0 && isfinite(half) && need_end - ws <= win;
+            if (MODE == SARBP_MODE_FP32)
+                q.k0 = make_float4((float)ax, (float)ay, (float)az,
+                                   (float)(-P.t0_bins * P.bin_rate - (double)ws - 0.5 - (double)cen));
             q.ax = ax;
             q.ay = ay;
             q.az = az;
         }
+        if (!sane) atomicOr(P.err, kErrWindow);
+        long long lo = ws < 0 ? 0 : ws;
+        long long hi = ws + win > P.nbins ? P.nbins : ws + win;
+        if (hi < lo || !sane) hi = lo;
+        q.ws = (int)ws;
+        q.lo = (int)(lo - ws);
+        q.hi = (int)(hi - ws);
+        q.scale = STORE == SARBP_STORE_C32H ? __ldg(&P.scale[p]) : 1.f;
         if (hi > lo) {
             bytes = (unsigned)((hi - lo) * esize);
             src = reinterpret_cast<const char *>(P.rc) + ((size_t)p * P.nbins + (size_t)lo) * esize;
@@ -225,7 +286,7 @@ __device__ __forceinline__ void produce(const BpPlan &P, const Smem &S, int stag
 }
 
 // raw window -> (mid, diff) pairs; bins outside [lo, hi) read as zero.
-template <int STORE>
+template <int MODE, int STORE>
 __device__ __forceinline__ void convert(const Smem &S, int stage, int sbuf, int count, int win, unsigned win_magic) {
     const int total = count * win;
     float4 *st = S.staged + (size_t)sbuf * kChunk * win;
@@ -247,7 +308,11 @@ __device__ __forceinline__ void convert(const Smem &S, int stage, int sbuf, int 
             if (i + 1 >= lo && i + 1 < hi) b = __half22float2(r[i + 1]);
             a.x *= sc; a.y *= sc; b.x *= sc; b.y *= sc;
         }
-        st[e] = make_float4(0.5f * (a.x + b.x), 0.5f * (a.y + b.y), b.x - a.x, b.y - a.y);
+        const float dx = b.x - a.x, dy = b.y - a.y;
+        // FP32 arithmetic: pairs centred on the window middle, so that s = M + b d
+        // takes the centred position b directly; FP64 keeps (mid, diff).
+        const float o = MODE == SARBP_MODE_FP64 ? 0.f : (float)(i - (win >> 1));
+        st[e] = make_float4(fmaf(-o, dx, 0.5f * (a.x + b.x)), fmaf(-o, dy, 0.5f * (a.y + b.y)), dx, dy);
     }
 }
 
@@ -286,7 +351,17 @@ __global__ void __launch_bounds__(kThreads, 2)
         T.pcy = P.g.origin[1] + pcx_i * P.g.ux[1] + pcy_i * P.g.uy[1];
         T.pcz = P.g.origin[2] + pcx_i * P.g.ux[2] + pcy_i * P.g.uy[2];
         T.qq_max = qq_max;
+        T.xT = (float)pcx_i;
+        T.yT = (float)pcy_i;
+        T.qqh = T.qql = 0.f;
+        if (lane < kPerWarp) {  // producer lanes only: FP64 once per CTA
+            const double qq = pcx_i * pcx_i * P.g.g11 + 2.0 * pcx_i * pcy_i * P.g.g12 + pcy_i * pcy_i * P.g.g22;
+            T.qqh = (float)qq;
+            T.qql = (float)(qq - (double)T.qqh);
+        }
     }
+    const int cen = win >> 1;
+    const float cenf = (float)cen;
 
     if (threadIdx.x == 0) {
         for (int s = 0; s < kStages; ++s) mbar_init(smem_addr(&S.bar[s]), kWarps);
@@ -336,7 +411,7 @@ __global__ void __launch_bounds__(kThreads, 2)
         const bool ok = mbar_wait_bounded(smem_addr(&S.bar[stage]), (c / kStages) & 1, 2000000000ull);
         if (!ok) { failed = true; }
         if (__syncthreads_or(failed)) { failed = true; break; }
-        convert<STORE>(S, stage, sbuf, count, win, win_magic);
+        convert<MODE, STORE>(S, stage, sbuf, count, win, win_magic);
         __syncthreads();
 
         const float4 *stg = S.staged + (size_t)sbuf * kChunk * win;
@@ -346,7 +421,7 @@ __global__ void __launch_bounds__(kThreads, 2)
             for (int pl = 0; pl < count; ++pl) {
                 const Prm &q = S.prm[stage * kChunk + pl];
                 const float4 k0 = q.k0, k1 = q.k1;
-                const float mp = kMagic + (float)(pl * win);
+                const float mp = kMagic + (float)(pl * win + cen);
                 const float xA = xc * k0.x;
 #pragma unroll
                 for (int j = 0; j < kPix; ++j) {
@@ -354,17 +429,16 @@ __global__ void __launch_bounds__(kThreads, 2)
                     float poly = NTERMS == 4 ? fmaf(n, fmaf(n, k1.y, k1.x), k0.w) : fmaf(n, k1.x, k0.w);
                     poly = fmaf(n, poly, k0.z);
                     const float dR = n * poly;
-                    float b = fmaf(dR, bpm, k1.z);
+                    float b = fmaf(dR, bpm, k1.z);  // bin position relative to the window middle
                     if (CHECKED) {
-                        const float bc = fminf(fmaxf(b, 0.f), wmax);
+                        const float bc = fminf(fmaxf(b, -cenf), wmax - cenf);
                         clamped |= !(bc == b);
                         b = bc;
                     }
                     const float t = b + mp;
-                    const float f = b - (t - mp);
                     const float4 v = lds128((__float_as_uint(t) << 4) + sbase);
-                    const float sr = fmaf(f, v.z, v.x);
-                    const float si = fmaf(f, v.w, v.y);
+                    const float sr = fmaf(b, v.z, v.x);
+                    const float si = fmaf(b, v.w, v.y);
                     float ph = fmaf(dR, kph_hi, k1.w);
                     ph = fmaf(dR, kph_lo, ph);
                     float sn, cs;
@@ -378,19 +452,18 @@ __global__ void __launch_bounds__(kThreads, 2)
             for (int pl = 0; pl < count; ++pl) {
                 const Prm &q = S.prm[stage * kChunk + pl];
                 const float4 k0 = q.k0;
-                const float mp = kMagic + (float)(pl * win);
+                const float mp = kMagic + (float)(pl * win + cen);
                 const float kph = (float)kph_d;
 #pragma unroll
                 for (int j = 0; j < kPix; ++j) {
                     const float dx = k0.x - fpxx[j], dy = k0.y - fpy[j], dz = k0.z - fpz[j];
                     const float R = sqrtf(fmaf(dx, dx, fmaf(dy, dy, dz * dz)));
                     float b = fmaf(R, bpm, k0.w);
-                    b = fminf(fmaxf(b, 0.f), wmax);
+                    b = fminf(fmaxf(b, -cenf), wmax - cenf);
                     const float t = b + mp;
-                    const float f = b - (t - mp);
                     const float4 v = lds128((__float_as_uint(t) << 4) + sbase);
-                    const float sr = fmaf(f, v.z, v.x);
-                    const float si = fmaf(f, v.w, v.y);
+                    const float sr = fmaf(b, v.z, v.x);
+                    const float si = fmaf(b, v.w, v.y);
                     float sn, cs;
                     sincosf(kph * R, &sn, &cs);
                     acc_r[j] = fmaf(sr, cs, fmaf(-si, sn, acc_r[j]));
@@ -523,6 +596,12 @@ cudaError_t launch_bp(const BpPlan &p, cudaStream_t s, int *launches) {
     const float qq_max = (float)(hx * hx * p.g.g11 + 2.0 * hx * hy * fabs(p.g.g12) + hy * hy * p.g.g22);
     cudaError_t e;
     const bool fp16 = p.storage == SARBP_STORE_C32H;
+    if (p.mode == SARBP_MODE_SPLIT || p.mode == SARBP_MODE_FP16STORE) {
+        pulse_ref_kernel<<<(p.np + 127) / 128, 128, 0, s>>>(p.apc, p.np, p.g, p.pref);
+        e = cudaGetLastError();
+        if (e != cudaSuccess) return e;
+        if (launches) ++*launches;
+    }
     switch (p.mode) {
         case SARBP_MODE_FP64:
             e = fp16 ? launch_variant<SARBP_MODE_FP64, SARBP_STORE_C32H, 4, false>(p, s, tiles, tiles_y, pps, qq_max)

@@ -51,8 +51,12 @@ struct BpPlan {
     int nbins;
     int mode;                // sarbp_mode
     const double *apc;       // [np][3] device
+    float4 *pref;            // [np][2] per-pulse FP64 references as float pairs (written by launch_bp)
     BpGeom g;
     double fc, c, t0_bins, bin_rate;
+    // float pairs of 2 bin_rate / c (bins per metre of range), t0_bins * bin_rate and
+    // 2 fc / c (carrier cycles per metre of range) for the float-float tile references
+    float kb_h, kb_l, tb_h, tb_l, kc_h, kc_l;
     float2 *image;           // [ny][nx] final image
     float2 *partial;         // [segments][ny][nx] scratch when segments > 1
     int segments;            // pulse segments (1: write image directly)
