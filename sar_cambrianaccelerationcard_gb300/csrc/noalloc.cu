@@ -1,0 +1,201 @@
+// noalloc.cu -- range compression that allocates no device memory.
+//
+// Some callers cannot call cudaMalloc once they are running: a host program
+// whose own allocator has already reserved the GPU's memory at start-up, or a
+// latency-bound processing loop that must not stall on an allocation (which
+// can synchronise the whole device).  sarbp_range_compress_noalloc serves
+// them.  It runs the same range-compression kernels as sarbp_range_compress,
+// but every byte of scratch it needs -- the matched-filter spectrum, the FFT
+// twiddles, the upsampling phase ramp and a batch of per-pulse spectra --
+// lives in the fixed array below, which every GPU that loads this library
+// holds until the process exits.
+//
+// Set-up: the first call on each device, with that device current, looks up
+// the array's device address with cudaGetSymbolAddress (the array's name in
+// host code is only a host-side stand-in).  Make that first call before any
+// stream capture.  All calls share the array and it keeps the last call's
+// contents; calls whose work overlaps on the GPU (different host threads or
+// streams) race on it and must be serialised by the caller.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <complex>
+#include <cstring>
+#include <mutex>
+
+#include "sarbp_internal.h"
+
+namespace {
+
+constexpr size_t kScratchBytes = size_t(4) << 20;  // SARBP_NOALLOC_SCRATCH_BYTES
+constexpr int kMaxDevices = 64;
+constexpr int kMaxN = 16384;  // largest range FFT the kernels support
+constexpr int kMaxL = 16;
+
+static __device__ __align__(256) unsigned char g_rc_scratch[kScratchBytes];
+
+struct TableKey {
+    int nfft = 0, L = 0, nc = 0, shift = 0;
+    double kr = 0, fs = 0, tc = 0, tp = 0;
+    bool operator==(const TableKey &o) const {
+        return nfft == o.nfft && L == o.L && nc == o.nc && shift == o.shift && kr == o.kr && fs == o.fs &&
+               tc == o.tc && tp == o.tp;
+    }
+};
+
+std::mutex g_mu;
+unsigned char *g_dev_scratch[kMaxDevices] = {};
+bool g_have_tables[kMaxDevices] = {};
+TableKey g_keys[kMaxDevices];
+
+// host staging for the tables: static storage, no heap
+std::complex<double> g_h[kMaxN];
+float2 g_filt[kMaxN], g_tw[kMaxN], g_ramp[kMaxL * kMaxN];
+
+constexpr double kPi = 3.14159265358979323846;
+
+void fft_inplace(std::complex<double> *x, int n) {
+    for (int i = 1, j = 0; i < n; ++i) {
+        int bit = n >> 1;
+        for (; j & bit; bit >>= 1) j ^= bit;
+        j ^= bit;
+        if (i < j) std::swap(x[i], x[j]);
+    }
+    for (int len = 2; len <= n; len <<= 1) {
+        for (int i = 0; i < n; i += len) {
+            for (int k = 0; k < len / 2; ++k) {
+                const double a = -2.0 * kPi * (double)k / (double)len;
+                const std::complex<double> w(std::cos(a), std::sin(a));
+                const std::complex<double> u = x[i + k], v = x[i + k + len / 2] * w;
+                x[i + k] = u + v;
+                x[i + k + len / 2] = u - v;
+            }
+        }
+    }
+}
+
+// Fills g_filt, g_tw, g_ramp for the layout (same tables as the allocating path).
+void build_tables(const sarbp_radar &r, const sarbp_rc_layout &lay) {
+    const int N = lay.nfft, L = r.upsample;
+    for (int i = 0; i < N; ++i) g_h[i] = 0.0;
+    for (int i = 0; i < lay.nc && i < N; ++i) {
+        const double u = (double)i / r.fs;
+        if (u >= 0.0 && u < r.tp) {
+            const double ph = kPi * r.kr * (u - r.tc) * (u - r.tc);
+            g_h[i] = std::complex<double>(std::cos(ph), std::sin(ph));
+        }
+    }
+    fft_inplace(g_h, N);
+    for (int k = 0; k < N; ++k) {
+        const long long m = ((long long)k * lay.shift) % N;
+        const double a = -2.0 * kPi * (double)m / (double)N;
+        const std::complex<double> v = std::conj(g_h[k]) * std::complex<double>(std::cos(a), std::sin(a)) / (double)N;
+        g_filt[k] = make_float2((float)v.real(), (float)v.imag());
+        const double b = -2.0 * kPi * (double)k / (double)N;
+        g_tw[k] = make_float2((float)std::cos(b), (float)std::sin(b));
+    }
+    for (long long m = 0; m < (long long)L * N; ++m) {
+        const double a = 2.0 * kPi * (double)m / ((double)L * N);
+        g_ramp[m] = make_float2((float)std::cos(a), (float)std::sin(a));
+    }
+}
+
+bool on_device(const void *p) {
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+}
+
+}  // namespace
+
+extern "C" sarbp_status sarbp_range_compress_noalloc(const sarbp_radar *radar, const sarbp_complex64 *echo,
+                                                     int32_t np, int32_t ns, int32_t storage, void *rc_out,
+                                                     float *rc_scale_out, void *stream) {
+    sarbp_rc_layout lay;
+    sarbp_status st = sarbp_rc_layout_get(radar, ns, &lay);
+    if (st != SARBP_OK) return st;
+    if (np < 0) return SARBP_ERR_INVALID_ARGUMENT;
+    if (storage != SARBP_STORE_C64 && storage != SARBP_STORE_C32H) return SARBP_ERR_INVALID_ARGUMENT;
+    if (np == 0) return SARBP_OK;
+    if (!echo || !rc_out || (storage == SARBP_STORE_C32H && !rc_scale_out)) return SARBP_ERR_INVALID_ARGUMENT;
+    if (!sarbp::rc_size_supported(lay.nfft)) return SARBP_ERR_UNSUPPORTED;
+    // tables (filter, twiddles, ramp) plus at least one pulse spectrum must fit
+    const size_t N = (size_t)lay.nfft, L = (size_t)radar->upsample;
+    const size_t tables = sizeof(float2) * (2 * N + L * N);
+    const size_t row = sizeof(float2) * N;
+    if (tables + row > kScratchBytes || N > (size_t)kMaxN || L > (size_t)kMaxL) return SARBP_ERR_UNSUPPORTED;
+    if (!on_device(echo) || !on_device(rc_out) || (storage == SARBP_STORE_C32H && !on_device(rc_scale_out)))
+        return SARBP_ERR_INVALID_ARGUMENT;  // device memory only: a host buffer would need a staging copy
+
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) {
+        cudaGetLastError();
+        return SARBP_ERR_NO_DEVICE;
+    }
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    std::lock_guard<std::mutex> lk(g_mu);
+    if (!g_dev_scratch[dev]) {  // once per device, with that device current
+        void *p = nullptr;
+        if (cudaGetSymbolAddress(&p, g_rc_scratch) != cudaSuccess || !p) {
+            cudaGetLastError();
+            return SARBP_ERR_CUDA;
+        }
+        g_dev_scratch[dev] = static_cast<unsigned char *>(p);
+    }
+    unsigned char *base = g_dev_scratch[dev];
+    float2 *d_filt = reinterpret_cast<float2 *>(base);
+    float2 *d_tw = d_filt + N;
+    float2 *d_ramp = d_tw + N;
+    float2 *d_spec = reinterpret_cast<float2 *>(base + ((tables + 255) & ~size_t(255)));
+    const size_t spec_bytes = kScratchBytes - ((tables + 255) & ~size_t(255));
+    const int batch = (int)std::max<size_t>(1, std::min<size_t>((size_t)np, spec_bytes / row));
+
+    TableKey key;
+    key.nfft = lay.nfft;
+    key.L = radar->upsample;
+    key.nc = lay.nc;
+    key.shift = lay.shift;
+    key.kr = radar->kr;
+    key.fs = radar->fs;
+    key.tc = radar->tc;
+    key.tp = radar->tp;
+    if (!g_have_tables[dev] || !(g_keys[dev] == key)) {
+        build_tables(*radar, lay);
+        // the host staging arrays are reused by the next call: wait for the copies
+        if (cudaMemcpyAsync(d_filt, g_filt, sizeof(float2) * N, cudaMemcpyHostToDevice, s) != cudaSuccess ||
+            cudaMemcpyAsync(d_tw, g_tw, sizeof(float2) * N, cudaMemcpyHostToDevice, s) != cudaSuccess ||
+            cudaMemcpyAsync(d_ramp, g_ramp, sizeof(float2) * L * N, cudaMemcpyHostToDevice, s) != cudaSuccess ||
+            cudaStreamSynchronize(s) != cudaSuccess) {
+            cudaGetLastError();
+            g_have_tables[dev] = false;
+            return SARBP_ERR_CUDA;
+        }
+        g_keys[dev] = key;
+        g_have_tables[dev] = true;
+    }
+    // No scratch byte needs clearing: every spectrum the inverse kernel reads
+    // was written by the forward kernel of the same batch.
+    const size_t esize = storage == SARBP_STORE_C64 ? 8 : 4;
+    const float2 *e2 = reinterpret_cast<const float2 *>(echo);
+    for (int p0 = 0; p0 < np; p0 += batch) {
+        sarbp::RcPlan plan;
+        plan.np = std::min(batch, np - p0);
+        plan.ns = ns;
+        plan.nfft = lay.nfft;
+        plan.L = radar->upsample;
+        plan.nbins = lay.nbins;
+        plan.storage = storage;
+        float *sc = storage == SARBP_STORE_C32H ? rc_scale_out + p0 : nullptr;
+        if (sarbp::launch_rc_forward(plan, e2 + (size_t)p0 * ns, d_filt, d_tw, d_spec, sc, s) != cudaSuccess ||
+            sarbp::launch_rc_inverse(plan, d_spec, d_tw, d_ramp, sc,
+                                     static_cast<char *>(rc_out) + (size_t)p0 * lay.nbins * esize, s) != cudaSuccess) {
+            cudaGetLastError();
+            return SARBP_ERR_CUDA;
+        }
+    }
+    return SARBP_OK;
+}

@@ -104,6 +104,9 @@ SIGNATURES = {
     "sarbp_range_compress": ([ctypes.c_void_p, ctypes.POINTER(Radar), ctypes.c_void_p, ctypes.c_int32,
                               ctypes.c_int32, ctypes.c_int32, ctypes.c_void_p, ctypes.c_void_p,
                               ctypes.c_void_p], ctypes.c_int),
+    "sarbp_range_compress_noalloc": ([ctypes.POINTER(Radar), ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32,
+                                      ctypes.c_int32, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p],
+                                     ctypes.c_int),
     "sarbp_backproject": ([ctypes.c_void_p, ctypes.POINTER(Radar), ctypes.POINTER(RcView), ctypes.c_void_p,
                            ctypes.POINTER(Grid), ctypes.c_int32, ctypes.c_void_p, ctypes.c_int32,
                            ctypes.c_void_p], ctypes.c_int),
