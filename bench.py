@@ -69,12 +69,8 @@ def barrier(dist):
 
 
 def max_over_ranks(dist, v: float) -> float:
-    if dist is None:
-        return v
-    import torch
-    t = torch.tensor([v], dtype=torch.float64, device="cuda")
-    dist.all_reduce(t, op=dist.ReduceOp.MAX)
-    return float(t.item())
+    from sar_cambrianaccelerationcard_gb300 import replicas
+    return replicas.max_over_ranks(v, dist, device="cuda")
 
 
 class ClockSampler:
@@ -204,6 +200,7 @@ def run_ours(args):
 
     mode = sarbp.MODES[args.mode]
     scene = workload(args.size)
+    scene.seed += rank  # every rank images its own independent scene (replicas, weak scaling)
     r, g, lay = sarbp.scene_args(scene)
     ctx = sarbp.Context(local)
     stream = torch.cuda.Stream()
