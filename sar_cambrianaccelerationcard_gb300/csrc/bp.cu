@@ -52,8 +52,11 @@ constexpr float kMagic = 12582912.0f;  // 1.5 * 2^23: adding it rounds to an int
 constexpr unsigned kMagicBitsShift4 = 0x4B400000u << 4;
 
 struct __align__(16) Prm {
-    float4 k0;     // SPLIT: A, B, c1, c2       FP32: apc x, y, z, bin offset
-    float4 k1;     // SPLIT: c3, c4, bin', phT
+    // SPLIT: each constant twice, so a 16-byte load yields two packed f32x2 operands
+    float4 k0;     // SPLIT: c1, c1, c2, c2     FP32: apc x, y, z, bin offset
+    float4 k1;     // SPLIT: c3, c3, c4, c4
+    float4 k2;     // SPLIT: bin', bin', phT, phT
+    float4 k3;     // SPLIT: A, A, B, B
     double ax, ay, az;  // FP64: APC position
     int ws;        // first bin of the window
     int lo, hi;    // copied part of the window [lo, hi) relative to ws
@@ -118,6 +121,38 @@ __device__ __forceinline__ float4 lds128(unsigned addr) {
                  : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w)
                  : "r"(addr));
     return v;
+}
+
+// Packed FP32x2 arithmetic (sm_100+ f32x2 instructions): two IEEE FP32
+// operations, each rounded to nearest, per issue slot.  A pair lives in a
+// 64-bit register pair (lo, hi).
+typedef unsigned long long f2;
+__device__ __forceinline__ f2 pk2(float lo, float hi) {
+    f2 r;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(lo), "f"(hi));
+    return r;
+}
+__device__ __forceinline__ void upk2(f2 v, float &lo, float &hi) {
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(v));
+}
+__device__ __forceinline__ f2 ffma2(f2 a, f2 b, f2 c) {
+    f2 d;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
+    return d;
+}
+__device__ __forceinline__ f2 fadd2(f2 a, f2 b) {
+    f2 d;
+    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+__device__ __forceinline__ f2 fmul2(f2 a, f2 b) {
+    f2 d;
+    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+// 16-byte shared load as two packed pairs
+__device__ __forceinline__ void lds2x2(const void *p, f2 &a, f2 &b) {
+    asm volatile("ld.shared.v2.b64 {%0, %1}, [%2];" : "=l"(a), "=l"(b) : "r"(smem_addr(p)));
 }
 
 struct Smem {
@@ -233,12 +268,15 @@ __device__ __forceinline__ void produce(const BpPlan &P, const Smem &S, int stag
             sane = isfinite(r) && r > 0.f && isfinite(half) && isfinite(phT) && need_end - ws <= win;
             const float i2 = iR * iR;
             if (sane) {
-                q.k0 = make_float4(A, B, 0.5f * iR, -0.125f * iR * i2);
-                q.k1 = make_float4(0.0625f * iR * i2 * i2, -0.0390625f * iR * i2 * i2 * i2,
-                                   ((bT.h - (float)ws) + bT.l) - 0.5f - (float)cen, phT);
+                const float c1 = 0.5f * iR, c2 = -0.125f * iR * i2, c3 = 0.0625f * iR * i2 * i2;
+                const float c4 = -0.0390625f * iR * i2 * i2 * i2;
+                const float bb = ((bT.h - (float)ws) + bT.l) - 0.5f - (float)cen;
+                q.k0 = make_float4(c1, c1, c2, c2);
+                q.k1 = make_float4(c3, c3, c4, c4);
+                q.k2 = make_float4(bb, bb, phT, phT);
+                q.k3 = make_float4(A, A, B, B);
             } else {  // inert pulse: every pixel reads the centre bin of an all-zero window
-                q.k0 = make_float4(0.f, 0.f, 0.f, 0.f);
-                q.k1 = make_float4(0.f, 0.f, 0.f, 0.f);
+                q.k0 = q.k1 = q.k2 = q.k3 = make_float4(0.f, 0.f, 0.f, 0.f);
             }
         } else {
             const double ax = __ldg(&P.apc[3 * p]), ay = __ldg(&P.apc[3 * p + 1]), az = __ldg(&P.apc[3 * p + 2]);
@@ -394,6 +432,15 @@ __global__ void __launch_bounds__(kThreads, 2)
         }
     }
 
+    const f2 XC2 = pk2(xc, xc);
+    const f2 BPM2 = pk2(bpm, bpm), KH2 = pk2(kph_hi, kph_hi), KL2 = pk2(kph_lo, kph_lo);
+    f2 YC2[kPix / 2], QQ2[kPix / 2];
+#pragma unroll
+    for (int h = 0; h < kPix / 2; ++h) {
+        YC2[h] = pk2(yc[2 * h], yc[2 * h + 1]);
+        QQ2[h] = pk2(qq[2 * h], qq[2 * h + 1]);
+    }
+
     if (nchunks > 0) produce<MODE, STORE>(P, S, 0, p_begin, min(kChunk, p_end - p_begin), T);
 
     bool failed = false;
@@ -417,35 +464,55 @@ __global__ void __launch_bounds__(kThreads, 2)
         const float4 *stg = S.staged + (size_t)sbuf * kChunk * win;
         const unsigned sbase = smem_addr(stg) - kMagicBitsShift4;
         if (MODE == SARBP_MODE_SPLIT || MODE == SARBP_MODE_FP16STORE) {
+            // geometry, bin and phase for pixel pairs (2j, 2j+1) in packed FP32x2;
+            // interpolation and the complex accumulate per pixel
+            f2 MP = pk2(kMagic + (float)cen, kMagic + (float)cen);
+            const f2 WIN2 = pk2((float)win, (float)win);
 #pragma unroll 1
             for (int pl = 0; pl < count; ++pl) {
                 const Prm &q = S.prm[stage * kChunk + pl];
-                const float4 k0 = q.k0, k1 = q.k1;
-                const float mp = kMagic + (float)(pl * win + cen);
-                const float xA = xc * k0.x;
+                f2 C1, C2, C3, C4, BT, PHT, AA, BB;
+                lds2x2(&q.k0, C1, C2);
+                lds2x2(&q.k1, C3, C4);
+                lds2x2(&q.k2, BT, PHT);
+                lds2x2(&q.k3, AA, BB);
+                const f2 XA = fmul2(XC2, AA);
 #pragma unroll
-                for (int j = 0; j < kPix; ++j) {
-                    const float n = fmaf(yc[j], k0.y, xA + qq[j]);
-                    float poly = NTERMS == 4 ? fmaf(n, fmaf(n, k1.y, k1.x), k0.w) : fmaf(n, k1.x, k0.w);
-                    poly = fmaf(n, poly, k0.z);
-                    const float dR = n * poly;
-                    float b = fmaf(dR, bpm, k1.z);  // bin position relative to the window middle
+                for (int h = 0; h < kPix / 2; ++h) {
+                    const f2 n = ffma2(YC2[h], BB, fadd2(XA, QQ2[h]));
+                    f2 poly = NTERMS == 4 ? ffma2(n, ffma2(n, C4, C3), C2) : ffma2(n, C3, C2);
+                    poly = ffma2(n, poly, C1);
+                    const f2 dR = fmul2(n, poly);
+                    f2 b2 = ffma2(dR, BPM2, BT);  // bin positions relative to the window middle
+                    const f2 ph2 = ffma2(dR, KL2, ffma2(dR, KH2, PHT));
+                    float bb[2], ph[2];
+                    upk2(b2, bb[0], bb[1]);
+                    upk2(ph2, ph[0], ph[1]);
                     if (CHECKED) {
-                        const float bc = fminf(fmaxf(b, -cenf), wmax - cenf);
-                        clamped |= !(bc == b);
-                        b = bc;
+#pragma unroll
+                        for (int u = 0; u < 2; ++u) {
+                            const float bc = fminf(fmaxf(bb[u], -cenf), wmax - cenf);
+                            clamped |= !(bc == bb[u]);
+                            bb[u] = bc;
+                        }
+                        b2 = pk2(bb[0], bb[1]);
                     }
-                    const float t = b + mp;
-                    const float4 v = lds128((__float_as_uint(t) << 4) + sbase);
-                    const float sr = fmaf(b, v.z, v.x);
-                    const float si = fmaf(b, v.w, v.y);
-                    float ph = fmaf(dR, kph_hi, k1.w);
-                    ph = fmaf(dR, kph_lo, ph);
-                    float sn, cs;
-                    __sincosf(ph, &sn, &cs);
-                    acc_r[j] = fmaf(sr, cs, fmaf(-si, sn, acc_r[j]));
-                    acc_i[j] = fmaf(sr, sn, fmaf(si, cs, acc_i[j]));
+                    const f2 t2 = fadd2(b2, MP);
+                    float tt[2];
+                    upk2(t2, tt[0], tt[1]);
+#pragma unroll
+                    for (int u = 0; u < 2; ++u) {
+                        const int j = 2 * h + u;
+                        const float4 v = lds128((__float_as_uint(tt[u]) << 4) + sbase);
+                        const float sr = fmaf(bb[u], v.z, v.x);
+                        const float si = fmaf(bb[u], v.w, v.y);
+                        float sn, cs;
+                        __sincosf(ph[u], &sn, &cs);
+                        acc_r[j] = fmaf(sr, cs, fmaf(-si, sn, acc_r[j]));
+                        acc_i[j] = fmaf(sr, sn, fmaf(si, cs, acc_i[j]));
+                    }
                 }
+                MP = fadd2(MP, WIN2);
             }
         } else if (MODE == SARBP_MODE_FP32) {
 #pragma unroll 1
