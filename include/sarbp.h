@@ -158,7 +158,7 @@ sarbp_status sarbp_range_compress(sarbp_ctx *ctx, const sarbp_radar *radar,
  * program whose own allocator already reserved the GPU's memory, or a
  * latency-bound loop that must not stall on an allocation.  Same kernels and
  * results as sarbp_range_compress, but all scratch (filter spectrum, FFT
- * twiddles, upsampling ramp, a batch of pulse spectra) lives in one fixed
+ * phase table for twiddles and upsampling ramp, a batch of pulse spectra) lives in one fixed
  * SARBP_NOALLOC_SCRATCH_BYTES device array that every GPU loading the library
  * holds until exit.  Pointers must be device memory; the call is asynchronous
  * on `stream` (NULL: the default stream) except when the radar/layout tables
@@ -166,8 +166,8 @@ sarbp_status sarbp_range_compress(sarbp_ctx *ctx, const sarbp_radar *radar,
  * device current) looks up the array's address; make it before any stream
  * capture.  Calls share the array: calls that overlap on the GPU race.
  * Returns SARBP_ERR_UNSUPPORTED when the tables and one pulse spectrum,
- * 8*nfft*(upsample + 3) bytes, exceed the array (the FFT itself is limited to
- * nfft <= 16384, which always fits). */
+ * 8*(2*nfft + 256 + upsample*nfft/256) bytes, exceed the array (the FFT itself
+ * is limited to nfft <= 16384, which always fits). */
 #define SARBP_NOALLOC_SCRATCH_BYTES (4u << 20)
 sarbp_status sarbp_range_compress_noalloc(const sarbp_radar *radar, const sarbp_complex64 *echo,
                                           int32_t np, int32_t ns, int32_t storage, void *rc_out,

@@ -56,7 +56,7 @@ struct RcTables {
     bool valid = false;
     int nfft = 0, L = 0, nc = 0, shift = 0;
     double kr = 0, fs = 0, tc = 0, tp = 0;
-    DevBuf filt, tw, ramp;
+    DevBuf filt, etab;
 };
 
 }  // namespace
@@ -189,26 +189,26 @@ sarbp_status ensure_tables(sarbp_ctx *ctx, const sarbp_radar *r, const sarbp_rc_
         }
     }
     host_fft(h, -1);
-    std::vector<float2> g(N), tw(N), ramp((size_t)L * N);
+    std::vector<float2> g(N), et((size_t)sarbp::rc_etab_size(L, N));
     for (int k = 0; k < N; ++k) {
         const long long m = ((long long)k * lay.shift) % N;
         const double a = -2.0 * kPi * (double)m / (double)N;
         const std::complex<double> v = std::conj(h[k]) * std::complex<double>(std::cos(a), std::sin(a)) / (double)N;
         g[k] = make_float2((float)v.real(), (float)v.imag());
-        const double b = -2.0 * kPi * (double)k / (double)N;
-        tw[k] = make_float2((float)std::cos(b), (float)std::sin(b));
     }
-    for (size_t m = 0; m < (size_t)L * N; ++m) {
-        const double a = 2.0 * kPi * (double)m / ((double)L * N);
-        ramp[m] = make_float2((float)std::cos(a), (float)std::sin(a));
+    // E^m = e^{+j2pi m/(L N)}: et[i] = E^i (i < 256), et[256 + i] = E^{256 i}
+    const double LN = (double)L * N;
+    for (int i = 0; i < 256; ++i)
+        et[i] = make_float2((float)std::cos(2.0 * kPi * i / LN), (float)std::sin(2.0 * kPi * i / LN));
+    for (size_t i = 256; i < et.size(); ++i) {
+        const double a = 2.0 * kPi * (double)(256 * (i - 256)) / LN;
+        et[i] = make_float2((float)std::cos(a), (float)std::sin(a));
     }
     SARBP_CUDA(ctx, t.filt.ensure(sizeof(float2) * N), "alloc filter");
-    SARBP_CUDA(ctx, t.tw.ensure(sizeof(float2) * N), "alloc twiddles");
-    SARBP_CUDA(ctx, t.ramp.ensure(sizeof(float2) * ramp.size()), "alloc ramp");
+    SARBP_CUDA(ctx, t.etab.ensure(sizeof(float2) * et.size()), "alloc phase table");
     SARBP_CUDA(ctx, cudaMemcpy(t.filt.ptr, g.data(), sizeof(float2) * N, cudaMemcpyHostToDevice), "upload filter");
-    SARBP_CUDA(ctx, cudaMemcpy(t.tw.ptr, tw.data(), sizeof(float2) * N, cudaMemcpyHostToDevice), "upload twiddles");
-    SARBP_CUDA(ctx, cudaMemcpy(t.ramp.ptr, ramp.data(), sizeof(float2) * ramp.size(), cudaMemcpyHostToDevice),
-               "upload ramp");
+    SARBP_CUDA(ctx, cudaMemcpy(t.etab.ptr, et.data(), sizeof(float2) * et.size(), cudaMemcpyHostToDevice),
+               "upload phase table");
     t.valid = true;
     t.nfft = N;
     t.L = L;
@@ -271,11 +271,11 @@ sarbp_status rc_device(sarbp_ctx *ctx, const sarbp_radar *r, const sarbp_rc_layo
         plan.nbins = lay.nbins;
         plan.storage = storage;
         SARBP_CUDA(ctx, sarbp::launch_rc_forward(plan, echo + (size_t)p0 * ns, ctx->tables.filt.as<float2>(),
-                                                 ctx->tables.tw.as<float2>(), ctx->spec.as<float2>(),
+                                                 ctx->tables.etab.as<float2>(), ctx->spec.as<float2>(),
                                                  scale ? scale + p0 : nullptr, s),
                    "range compression (forward)");
-        SARBP_CUDA(ctx, sarbp::launch_rc_inverse(plan, ctx->spec.as<float2>(), ctx->tables.tw.as<float2>(),
-                                                 ctx->tables.ramp.as<float2>(), scale ? scale + p0 : nullptr,
+        SARBP_CUDA(ctx, sarbp::launch_rc_inverse(plan, ctx->spec.as<float2>(), ctx->tables.etab.as<float2>(),
+                                                 scale ? scale + p0 : nullptr,
                                                  static_cast<char *>(rc_out) + (size_t)p0 * lay.nbins * esize, s),
                    "range compression (inverse)");
         ctx->launches += 2;
@@ -310,8 +310,6 @@ sarbp_status bp_device(sarbp_ctx *ctx, const sarbp_radar *r, const sarbp_rc_view
     }
     if (rc.nbins % 4 != 0) return fail(ctx, SARBP_ERR_UNSUPPORTED, "nbins must be a multiple of 4");
     if (((uintptr_t)rc.data & 15) != 0) return fail(ctx, SARBP_ERR_INVALID_ARGUMENT, "rc data must be 16-byte aligned");
-    int tx, ty;
-    sarbp::bp_tile_dims(mode, &tx, &ty);
     BpPlan p;
     std::memset(&p, 0, sizeof p);
     p.rc = rc.data;
@@ -349,11 +347,8 @@ sarbp_status bp_device(sarbp_ctx *ctx, const sarbp_radar *r, const sarbp_rc_view
     SARBP_CUDA(ctx, ctx->pref.ensure(sizeof(float) * 8 * (size_t)np), "alloc pulse references");
     p.pref = ctx->pref.as<float4>();
 
-    // Staging window: bins a tile can touch for one pulse, bounded over all pulses
-    // from the grid's extreme line-of-sight directions (sampled on a 9x9 lattice).
-    const double hx = 0.5 * (tx - 1), hy = 0.5 * (ty - 1);
+    // Line-of-sight extremes over the grid (9x9 lattice of grid points, all pulses).
     const double lux = std::sqrt(p.g.g11), luy = std::sqrt(p.g.g22);
-    const double qq_max = hx * hx * p.g.g11 + 2 * hx * hy * std::fabs(p.g.g12) + hy * hy * p.g.g22;
     double cx = 0, sy = 0, rmin = 1e300, rmax = 0;
     for (int i = 0; i < np; ++i) {
         const double *a = apc_host + 3 * (size_t)i;
@@ -372,28 +367,55 @@ sarbp_status bp_device(sarbp_ctx *ctx, const sarbp_radar *r, const sarbp_rc_view
             }
         }
     }
-    const double tile_diag = std::sqrt(qq_max);
-    const double rmin_tile = rmin - tile_diag;
-    if (mode == SARBP_MODE_SPLIT || mode == SARBP_MODE_FP16STORE || mode == SARBP_MODE_FP32 || mode == SARBP_MODE_FP64) {
-        if (!(rmin_tile > 20.0 * tile_diag))
-            return fail(ctx, SARBP_ERR_UNSUPPORTED, "an antenna position is within 20 tile diagonals of the grid");
-    }
     cx = std::min(1.0, cx * 1.05 + 0.01);
     sy = std::min(1.0, sy * 1.05 + 0.01);
     const double bpm = 2.0 / r->c * rc.bin_rate;
-    const double half = bpm * (lux * hx * cx + luy * hy * sy + qq_max / (2 * rmin_tile)) * 1.03 + 2.0;
-    if (!(half < 4096.0)) return fail(ctx, SARBP_ERR_UNSUPPORTED, "tile spans too many range bins");
-    int win = (int)std::ceil(2 * half) + 8;
-    win = (win + 3) & ~3;
-    if (sarbp::bp_smem_bytes(mode, win) > (size_t)(227u << 10))
-        return fail(ctx, SARBP_ERR_UNSUPPORTED, "tile spans too many range bins (%d) for shared memory", win);
-    p.win = win;
-    // series terms: dR error ~ R (5/128) e^4 for 3 terms, e = |n|/R^2 <= (2 diag R + diag^2)/R^2
-    const double e = (2 * tile_diag * rmax + qq_max) / (rmin_tile * rmin_tile);
-    // 3 terms when their truncation stays below 1e-6 m (2e-4 rad of C-band phase)
-    p.nterms = (rmax * 0.0390625 * e * e * e * e < 1e-6) ? 3 : 4;
-    if (rmax * 0.02734375 * std::pow(e, 5) > 1e-7)
-        return fail(ctx, SARBP_ERR_UNSUPPORTED, "tiles too large for the differential-range series");
+    // Tile choice: the tallest tile (32 x 64, 32 x 32, 32 x 16 pixels) whose
+    // differential-range series truncation stays below kSeriesTol metres and
+    // whose staging window fits shared memory.  Series remainder after k terms
+    // of sqrt(1+e)-1 times R: R (5/128) e^4 (k = 3), R (7/256) e^5 (k = 4), with
+    // e = |n|/R^2 <= (2 diag R + diag^2)/R^2 over the tile.
+    constexpr double kSeriesTol = 5e-7;  // 1.1e-4 rad of C-band phase at the tile corners
+    const char *why = "no tile size fits";
+    bool chosen = false;
+    for (int pix : {8, 4, 2}) {
+        int tx, ty;
+        sarbp::bp_tile_dims(pix, &tx, &ty);
+        const double hx = 0.5 * (tx - 1), hy = 0.5 * (ty - 1);
+        const double qq_max = hx * hx * p.g.g11 + 2 * hx * hy * std::fabs(p.g.g12) + hy * hy * p.g.g22;
+        const double tile_diag = std::sqrt(qq_max);
+        const double rmin_tile = rmin - tile_diag;
+        if (!(rmin_tile > 20.0 * tile_diag)) {
+            why = "an antenna position is within 20 tile diagonals of the grid";
+            continue;
+        }
+        const double half = bpm * (lux * hx * cx + luy * hy * sy + qq_max / (2 * rmin_tile)) * 1.03 + 2.0;
+        if (!(half < 4096.0)) {
+            why = "tile spans too many range bins";
+            continue;
+        }
+        int win = (int)std::ceil(2 * half) + 8;
+        win = (win + 3) & ~3;
+        if (sarbp::bp_smem_bytes(mode, win) > (size_t)(227u << 10)) {
+            why = "tile spans too many range bins for shared memory";
+            continue;
+        }
+        const double e = (2 * tile_diag * rmax + qq_max) / (rmin_tile * rmin_tile);
+        const bool split = mode == SARBP_MODE_SPLIT || mode == SARBP_MODE_FP16STORE;
+        if (split && rmax * 0.02734375 * std::pow(e, 5) > kSeriesTol) {
+            why = "tiles too large for the differential-range series";
+            continue;
+        }
+        p.pix = pix;
+        p.win = win;
+        p.nterms = (rmax * 0.0390625 * e * e * e * e < kSeriesTol) ? 3 : 4;
+        chosen = true;
+        break;
+    }
+    if (!chosen) return fail(ctx, SARBP_ERR_UNSUPPORTED, "%s", why);
+    int tx, ty;
+    sarbp::bp_tile_dims(p.pix, &tx, &ty);
+    const int win = p.win;
 
     // pulse segments: fill at least ~2 waves of CTAs
     const int tiles = ((g->nx + tx - 1) / tx) * ((g->ny + ty - 1) / ty);
@@ -482,8 +504,7 @@ sarbp_status sarbp_destroy(sarbp_ctx *ctx) {
     cudaSetDevice(ctx->device);
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
     for (DevBuf *b : {&ctx->echo, &ctx->spec, &ctx->rc, &ctx->scale, &ctx->apc, &ctx->image, &ctx->partial,
-                      &ctx->errword, &ctx->power, &ctx->targets, &ctx->pref, &ctx->tables.filt, &ctx->tables.tw,
-                      &ctx->tables.ramp})
+                      &ctx->errword, &ctx->power, &ctx->targets, &ctx->pref, &ctx->tables.filt, &ctx->tables.etab})
         b->release();
     for (cudaEvent_t &e : ctx->ev)
         if (e) cudaEventDestroy(e);
@@ -517,8 +538,7 @@ size_t sarbp_device_bytes(const sarbp_ctx *ctx) {
     if (!ctx) return 0;
     size_t t = 0;
     for (const DevBuf *b : {&ctx->echo, &ctx->spec, &ctx->rc, &ctx->scale, &ctx->apc, &ctx->image, &ctx->partial,
-                            &ctx->errword, &ctx->power, &ctx->targets, &ctx->pref, &ctx->tables.filt, &ctx->tables.tw,
-                            &ctx->tables.ramp})
+                            &ctx->errword, &ctx->power, &ctx->targets, &ctx->pref, &ctx->tables.filt, &ctx->tables.etab})
         t += b->bytes;
     return t;
 }

@@ -42,9 +42,7 @@ namespace {
 
 constexpr int kThreads = 256;
 constexpr int kWarps = kThreads / 32;
-constexpr int kTileX = 32;  // pixels along x (columns)
-constexpr int kTileY = 64;  // pixels along y (rows)
-constexpr int kPix = kTileX * kTileY / kThreads;  // 8 pixels per thread
+constexpr int kTileX = 32;  // pixels along x (columns); tile height is 8 * PIX rows
 constexpr int kChunk = 16;  // pulses per staged chunk
 constexpr int kPerWarp = kChunk / kWarps;  // pulses each warp prepares
 constexpr int kStages = 3;  // raw-window ring depth
@@ -221,9 +219,10 @@ __global__ void pulse_ref_kernel(const double *__restrict__ apc, int np, BpGeom 
 
 // Per-(tile, pulse) geometry, window and TMA issue for this warp's pulses of
 // one chunk.  Every warp arrives once on the stage's barrier.
-template <int MODE, int STORE>
+template <int MODE, int STORE, int PIX>
 __device__ __forceinline__ void produce(const BpPlan &P, const Smem &S, int stage, int p0, int count,
                                         const TileGeo &T) {
+    constexpr int kTileY = 8 * PIX;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int win = P.win;
     const int esize = STORE == SARBP_STORE_C64 ? 8 : 4;
@@ -354,9 +353,11 @@ __device__ __forceinline__ void convert(const Smem &S, int stage, int sbuf, int 
     }
 }
 
-template <int MODE, int STORE, int NTERMS, bool CHECKED>
+template <int MODE, int STORE, int NTERMS, bool CHECKED, int PIX>
 __global__ void __launch_bounds__(kThreads, 2)
     bp_kernel(const __grid_constant__ BpPlan P, int tiles_y, int pulses_per_seg, float qq_max) {
+    constexpr int kPix = PIX;  // pixels per thread, all in one column
+    constexpr int kTileY = 8 * PIX;
     extern __shared__ __align__(128) unsigned char smem_raw[];
     const int win = P.win;
     const Smem S = carve(smem_raw, win);
@@ -441,7 +442,7 @@ __global__ void __launch_bounds__(kThreads, 2)
         QQ2[h] = pk2(qq[2 * h], qq[2 * h + 1]);
     }
 
-    if (nchunks > 0) produce<MODE, STORE>(P, S, 0, p_begin, min(kChunk, p_end - p_begin), T);
+    if (nchunks > 0) produce<MODE, STORE, PIX>(P, S, 0, p_begin, min(kChunk, p_end - p_begin), T);
 
     bool failed = false;
     bool clamped = false;
@@ -453,7 +454,7 @@ __global__ void __launch_bounds__(kThreads, 2)
         const int count = min(kChunk, p_end - pc0);
         if (c + 1 < nchunks) {
             const int pn = pc0 + kChunk;
-            produce<MODE, STORE>(P, S, (c + 1) % kStages, pn, min(kChunk, p_end - pn), T);
+            produce<MODE, STORE, PIX>(P, S, (c + 1) % kStages, pn, min(kChunk, p_end - pn), T);
         }
         const bool ok = mbar_wait_bounded(smem_addr(&S.bar[stage]), (c / kStages) & 1, 2000000000ull);
         if (!ok) { failed = true; }
@@ -617,9 +618,9 @@ __global__ void reduce_segments_kernel(const float2 *__restrict__ partial, int s
     }
 }
 
-template <int MODE, int STORE, int NTERMS, bool CHECKED>
+template <int MODE, int STORE, int NTERMS, bool CHECKED, int PIX>
 cudaError_t launch_variant(const BpPlan &p, cudaStream_t s, int tiles, int tiles_y, int pps, float qq_max) {
-    auto k = bp_kernel<MODE, STORE, NTERMS, CHECKED>;
+    auto k = bp_kernel<MODE, STORE, NTERMS, CHECKED, PIX>;
     const size_t smem = bp_smem_bytes(MODE, p.win);
     cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
@@ -628,20 +629,36 @@ cudaError_t launch_variant(const BpPlan &p, cudaStream_t s, int tiles, int tiles
     return cudaGetLastError();
 }
 
-template <int MODE, int STORE>
+template <int MODE, int STORE, int PIX>
 cudaError_t launch_split(const BpPlan &p, cudaStream_t s, int tiles, int tiles_y, int pps, float qq_max) {
     if (p.checked)
-        return p.nterms == 3 ? launch_variant<MODE, STORE, 3, true>(p, s, tiles, tiles_y, pps, qq_max)
-                             : launch_variant<MODE, STORE, 4, true>(p, s, tiles, tiles_y, pps, qq_max);
-    return p.nterms == 3 ? launch_variant<MODE, STORE, 3, false>(p, s, tiles, tiles_y, pps, qq_max)
-                         : launch_variant<MODE, STORE, 4, false>(p, s, tiles, tiles_y, pps, qq_max);
+        return p.nterms == 3 ? launch_variant<MODE, STORE, 3, true, PIX>(p, s, tiles, tiles_y, pps, qq_max)
+                             : launch_variant<MODE, STORE, 4, true, PIX>(p, s, tiles, tiles_y, pps, qq_max);
+    return p.nterms == 3 ? launch_variant<MODE, STORE, 3, false, PIX>(p, s, tiles, tiles_y, pps, qq_max)
+                         : launch_variant<MODE, STORE, 4, false, PIX>(p, s, tiles, tiles_y, pps, qq_max);
+}
+
+template <int PIX>
+cudaError_t launch_pix(const BpPlan &p, cudaStream_t s, int tiles, int tiles_y, int pps, float qq_max) {
+    const bool fp16 = p.storage == SARBP_STORE_C32H;
+    switch (p.mode) {
+        case SARBP_MODE_FP64:
+            return fp16 ? launch_variant<SARBP_MODE_FP64, SARBP_STORE_C32H, 4, false, PIX>(p, s, tiles, tiles_y, pps, qq_max)
+                        : launch_variant<SARBP_MODE_FP64, SARBP_STORE_C64, 4, false, PIX>(p, s, tiles, tiles_y, pps, qq_max);
+        case SARBP_MODE_FP32:
+            return fp16 ? launch_variant<SARBP_MODE_FP32, SARBP_STORE_C32H, 4, false, PIX>(p, s, tiles, tiles_y, pps, qq_max)
+                        : launch_variant<SARBP_MODE_FP32, SARBP_STORE_C64, 4, false, PIX>(p, s, tiles, tiles_y, pps, qq_max);
+        default:
+            return fp16 ? launch_split<SARBP_MODE_SPLIT, SARBP_STORE_C32H, PIX>(p, s, tiles, tiles_y, pps, qq_max)
+                        : launch_split<SARBP_MODE_SPLIT, SARBP_STORE_C64, PIX>(p, s, tiles, tiles_y, pps, qq_max);
+    }
 }
 
 }  // namespace
 
-void bp_tile_dims(int, int *tile_x, int *tile_y) {
+void bp_tile_dims(int pix, int *tile_x, int *tile_y) {
     *tile_x = kTileX;
-    *tile_y = kTileY;
+    *tile_y = 8 * pix;
 }
 
 int bp_pulses_per_chunk(int) { return kChunk; }
@@ -653,36 +670,26 @@ size_t bp_smem_bytes(int, int win) {
 
 cudaError_t launch_bp(const BpPlan &p, cudaStream_t s, int *launches) {
     if (p.np <= 0 || p.g.nx <= 0 || p.g.ny <= 0) return cudaSuccess;
+    if (p.pix != 8 && p.pix != 4 && p.pix != 2) return cudaErrorInvalidValue;
+    const int tile_y = 8 * p.pix;
     const int tiles_x = (p.g.nx + kTileX - 1) / kTileX;
-    const int tiles_y = (p.g.ny + kTileY - 1) / kTileY;
+    const int tiles_y = (p.g.ny + tile_y - 1) / tile_y;
     const int tiles = tiles_x * tiles_y;
     int pps = (p.np + p.segments - 1) / p.segments;
     pps = (pps + kChunk - 1) / kChunk * kChunk;
     // |q|^2 bound over a tile (pixel offsets from the tile centre)
-    const double hx = 0.5 * (kTileX - 1), hy = 0.5 * (kTileY - 1);
+    const double hx = 0.5 * (kTileX - 1), hy = 0.5 * (tile_y - 1);
     const float qq_max = (float)(hx * hx * p.g.g11 + 2.0 * hx * hy * fabs(p.g.g12) + hy * hy * p.g.g22);
     cudaError_t e;
-    const bool fp16 = p.storage == SARBP_STORE_C32H;
     if (p.mode == SARBP_MODE_SPLIT || p.mode == SARBP_MODE_FP16STORE) {
         pulse_ref_kernel<<<(p.np + 127) / 128, 128, 0, s>>>(p.apc, p.np, p.g, p.pref);
         e = cudaGetLastError();
         if (e != cudaSuccess) return e;
         if (launches) ++*launches;
     }
-    switch (p.mode) {
-        case SARBP_MODE_FP64:
-            e = fp16 ? launch_variant<SARBP_MODE_FP64, SARBP_STORE_C32H, 4, false>(p, s, tiles, tiles_y, pps, qq_max)
-                     : launch_variant<SARBP_MODE_FP64, SARBP_STORE_C64, 4, false>(p, s, tiles, tiles_y, pps, qq_max);
-            break;
-        case SARBP_MODE_FP32:
-            e = fp16 ? launch_variant<SARBP_MODE_FP32, SARBP_STORE_C32H, 4, false>(p, s, tiles, tiles_y, pps, qq_max)
-                     : launch_variant<SARBP_MODE_FP32, SARBP_STORE_C64, 4, false>(p, s, tiles, tiles_y, pps, qq_max);
-            break;
-        default:
-            e = fp16 ? launch_split<SARBP_MODE_SPLIT, SARBP_STORE_C32H>(p, s, tiles, tiles_y, pps, qq_max)
-                     : launch_split<SARBP_MODE_SPLIT, SARBP_STORE_C64>(p, s, tiles, tiles_y, pps, qq_max);
-            break;
-    }
+    if (p.pix == 8) e = launch_pix<8>(p, s, tiles, tiles_y, pps, qq_max);
+    else if (p.pix == 4) e = launch_pix<4>(p, s, tiles, tiles_y, pps, qq_max);
+    else e = launch_pix<2>(p, s, tiles, tiles_y, pps, qq_max);
     if (e != cudaSuccess) return e;
     if (launches) ++*launches;
     if (p.segments > 1) {

@@ -5,8 +5,9 @@
 // latency-bound processing loop that must not stall on an allocation (which
 // can synchronise the whole device).  sarbp_range_compress_noalloc serves
 // them.  It runs the same range-compression kernels as sarbp_range_compress,
-// but every byte of scratch it needs -- the matched-filter spectrum, the FFT
-// twiddles, the upsampling phase ramp and a batch of per-pulse spectra --
+// but every byte of scratch it needs -- the matched-filter spectrum, the
+// phase table (FFT twiddles and upsampling ramp) and a batch of per-pulse
+// spectra --
 // lives in the fixed array below, which every GPU that loads this library
 // holds until the process exits.
 //
@@ -51,7 +52,7 @@ TableKey g_keys[kMaxDevices];
 
 // host staging for the tables: static storage, no heap
 std::complex<double> g_h[kMaxN];
-float2 g_filt[kMaxN], g_tw[kMaxN], g_ramp[kMaxL * kMaxN];
+float2 g_filt[kMaxN], g_etab[256 + kMaxL * kMaxN / 256];
 
 constexpr double kPi = 3.14159265358979323846;
 
@@ -75,7 +76,7 @@ void fft_inplace(std::complex<double> *x, int n) {
     }
 }
 
-// Fills g_filt, g_tw, g_ramp for the layout (same tables as the allocating path).
+// Fills g_filt and g_etab for the layout (same tables as the allocating path).
 void build_tables(const sarbp_radar &r, const sarbp_rc_layout &lay) {
     const int N = lay.nfft, L = r.upsample;
     for (int i = 0; i < N; ++i) g_h[i] = 0.0;
@@ -92,12 +93,12 @@ void build_tables(const sarbp_radar &r, const sarbp_rc_layout &lay) {
         const double a = -2.0 * kPi * (double)m / (double)N;
         const std::complex<double> v = std::conj(g_h[k]) * std::complex<double>(std::cos(a), std::sin(a)) / (double)N;
         g_filt[k] = make_float2((float)v.real(), (float)v.imag());
-        const double b = -2.0 * kPi * (double)k / (double)N;
-        g_tw[k] = make_float2((float)std::cos(b), (float)std::sin(b));
     }
-    for (long long m = 0; m < (long long)L * N; ++m) {
-        const double a = 2.0 * kPi * (double)m / ((double)L * N);
-        g_ramp[m] = make_float2((float)std::cos(a), (float)std::sin(a));
+    const double LN = (double)L * N;
+    const int ne = sarbp::rc_etab_size(L, N);
+    for (int i = 0; i < ne; ++i) {
+        const double a = 2.0 * kPi * (double)(i < 256 ? i : 256 * (i - 256)) / LN;
+        g_etab[i] = make_float2((float)std::cos(a), (float)std::sin(a));
     }
 }
 
@@ -123,9 +124,10 @@ extern "C" sarbp_status sarbp_range_compress_noalloc(const sarbp_radar *radar, c
     if (np == 0) return SARBP_OK;
     if (!echo || !rc_out || (storage == SARBP_STORE_C32H && !rc_scale_out)) return SARBP_ERR_INVALID_ARGUMENT;
     if (!sarbp::rc_size_supported(lay.nfft)) return SARBP_ERR_UNSUPPORTED;
-    // tables (filter, twiddles, ramp) plus at least one pulse spectrum must fit
+    // tables (filter spectrum, phase table) plus at least one pulse spectrum must fit
     const size_t N = (size_t)lay.nfft, L = (size_t)radar->upsample;
-    const size_t tables = sizeof(float2) * (2 * N + L * N);
+    const size_t ne = (size_t)sarbp::rc_etab_size((int)L, (int)N);
+    const size_t tables = sizeof(float2) * (N + ne);
     const size_t row = sizeof(float2) * N;
     if (tables + row > kScratchBytes || N > (size_t)kMaxN || L > (size_t)kMaxL) return SARBP_ERR_UNSUPPORTED;
     if (!on_device(echo) || !on_device(rc_out) || (storage == SARBP_STORE_C32H && !on_device(rc_scale_out)))
@@ -148,8 +150,7 @@ extern "C" sarbp_status sarbp_range_compress_noalloc(const sarbp_radar *radar, c
     }
     unsigned char *base = g_dev_scratch[dev];
     float2 *d_filt = reinterpret_cast<float2 *>(base);
-    float2 *d_tw = d_filt + N;
-    float2 *d_ramp = d_tw + N;
+    float2 *d_etab = d_filt + N;
     float2 *d_spec = reinterpret_cast<float2 *>(base + ((tables + 255) & ~size_t(255)));
     const size_t spec_bytes = kScratchBytes - ((tables + 255) & ~size_t(255));
     const int batch = (int)std::max<size_t>(1, std::min<size_t>((size_t)np, spec_bytes / row));
@@ -167,8 +168,7 @@ extern "C" sarbp_status sarbp_range_compress_noalloc(const sarbp_radar *radar, c
         build_tables(*radar, lay);
         // the host staging arrays are reused by the next call: wait for the copies
         if (cudaMemcpyAsync(d_filt, g_filt, sizeof(float2) * N, cudaMemcpyHostToDevice, s) != cudaSuccess ||
-            cudaMemcpyAsync(d_tw, g_tw, sizeof(float2) * N, cudaMemcpyHostToDevice, s) != cudaSuccess ||
-            cudaMemcpyAsync(d_ramp, g_ramp, sizeof(float2) * L * N, cudaMemcpyHostToDevice, s) != cudaSuccess ||
+            cudaMemcpyAsync(d_etab, g_etab, sizeof(float2) * ne, cudaMemcpyHostToDevice, s) != cudaSuccess ||
             cudaStreamSynchronize(s) != cudaSuccess) {
             cudaGetLastError();
             g_have_tables[dev] = false;
@@ -190,8 +190,8 @@ extern "C" sarbp_status sarbp_range_compress_noalloc(const sarbp_radar *radar, c
         plan.nbins = lay.nbins;
         plan.storage = storage;
         float *sc = storage == SARBP_STORE_C32H ? rc_scale_out + p0 : nullptr;
-        if (sarbp::launch_rc_forward(plan, e2 + (size_t)p0 * ns, d_filt, d_tw, d_spec, sc, s) != cudaSuccess ||
-            sarbp::launch_rc_inverse(plan, d_spec, d_tw, d_ramp, sc,
+        if (sarbp::launch_rc_forward(plan, e2 + (size_t)p0 * ns, d_filt, d_etab, d_spec, sc, s) != cudaSuccess ||
+            sarbp::launch_rc_inverse(plan, d_spec, d_etab, sc,
                                      static_cast<char *>(rc_out) + (size_t)p0 * lay.nbins * esize, s) != cudaSuccess) {
             cudaGetLastError();
             return SARBP_ERR_CUDA;

@@ -17,8 +17,11 @@
 //
 // The FFT is a Stockham autosort transform with radix-8 stages (one radix-4
 // or radix-2 stage when log2 N is not a multiple of 3), in place in shared
-// memory with a barrier between each stage's loads and stores.  Twiddles come
-// from a table computed in double precision on the host.
+// memory with a barrier between each stage's loads and stores.  Twiddles and
+// the upsampling phase ramp are both powers of E = e^{j 2 pi / (L N)}; E^m is
+// read from a two-level table held in shared memory, E^m = T_hi[m >> 8] *
+// T_lo[m & 255] (tables computed in double precision on the host), so no
+// FFT stage touches global memory.
 #include "sarbp_internal.h"
 
 namespace sarbp {
@@ -35,9 +38,16 @@ __device__ __forceinline__ float2 mulj(float2 a) {
     return INV ? make_float2(-a.y, a.x) : make_float2(a.y, -a.x);
 }
 
-// one float2 of padding per 32 entries breaks the power-of-two store strides
-__device__ __forceinline__ int pad(int i) { return i + (i >> 5); }
-__host__ __device__ constexpr int padded(int n) { return n + (n >> 5); }
+// one float2 of padding per 8 entries breaks the power-of-two store strides
+__device__ __forceinline__ int pad(int i) { return i + (i >> 3); }
+__host__ __device__ constexpr int padded(int n) { return n + (n >> 3); }
+
+// E^m = e^{+j 2 pi m / (L N)} from the two-level shared-memory table
+struct Etab {
+    const float2 *lo;  // [256] (or L N entries when L N < 256)
+    const float2 *hi;  // [max(1, L N / 256)]
+    __device__ __forceinline__ float2 operator()(int m) const { return cmul(hi[m >> 8], lo[m & 255]); }
+};
 
 template <int R, bool INV>
 struct Dft;
@@ -92,7 +102,7 @@ struct Dft<8, INV> {
 // W_N^{k r N/(Ns R)} (k = j mod Ns), runs a radix-R DFT and writes
 // s[(j - k) R + k + r Ns].
 template <int N, int R, int T, bool INV>
-__device__ __forceinline__ void stage(float2 *s, const float2 *__restrict__ tw, int Ns) {
+__device__ __forceinline__ void stage(float2 *s, const Etab &E, int L, int Ns) {
     constexpr int NB = N / R;
     constexpr int PER = (NB + T - 1) / T;
     float2 v[PER][R];
@@ -114,8 +124,8 @@ __device__ __forceinline__ void stage(float2 *s, const float2 *__restrict__ tw, 
                 const int step = N / (Ns * R);
 #pragma unroll
                 for (int r = 1; r < R; ++r) {
-                    float2 w = __ldg(&tw[k * r * step]);
-                    if (INV) w.y = -w.y;
+                    float2 w = E(L * (k * r * step));  // W_N^{k r step}, forward: conjugate
+                    if (!INV) w.y = -w.y;
                     v[b][r] = cmul(v[b][r], w);
                 }
             }
@@ -140,18 +150,31 @@ struct Log2<1> {
 // Unnormalised in-place FFT of N points held (padded) in shared memory.
 // Caller must have synchronised after filling s; returns synchronised.
 template <int N, int T, bool INV>
-__device__ void fft_smem(float2 *s, const float2 *__restrict__ tw) {
+__device__ void fft_smem(float2 *s, const Etab &E, int L) {
     constexpr int LOG = Log2<N>::value;
     constexpr int N8 = LOG / 3;
     constexpr int REM = LOG % 3;
     int Ns = 1;
 #pragma unroll 1
     for (int i = 0; i < N8; ++i) {
-        stage<N, 8, T, INV>(s, tw, Ns);
+        stage<N, 8, T, INV>(s, E, L, Ns);
         Ns *= 8;
     }
-    if (REM == 2) stage<N, 4, T, INV>(s, tw, Ns);
-    if (REM == 1) stage<N, 2, T, INV>(s, tw, Ns);
+    if (REM == 2) stage<N, 4, T, INV>(s, E, L, Ns);
+    if (REM == 1) stage<N, 2, T, INV>(s, E, L, Ns);
+}
+
+// copies the E tables into shared memory right after the padded data
+template <int N, int T>
+__device__ __forceinline__ Etab load_etab(float2 *sm, const float2 *__restrict__ etab, int L) {
+    const int LN = L * N;
+    const int nlo = LN < 256 ? LN : 256;
+    const int nhi = LN < 256 ? 1 : LN / 256;
+    float2 *lo = sm + padded(N);
+    float2 *hi = lo + 256;
+    for (int i = threadIdx.x; i < nlo; i += T) lo[i] = __ldg(&etab[i]);
+    for (int i = threadIdx.x; i < nhi; i += T) hi[i] = __ldg(&etab[256 + i]);
+    return Etab{lo, hi};
 }
 
 template <int T>
@@ -171,18 +194,19 @@ __device__ __forceinline__ float block_sum(float v, float *red) {
 }
 
 template <int N, int T>
-__global__ void __launch_bounds__(T) rc_forward_kernel(int ns, const float2 *__restrict__ echo,
+__global__ void __launch_bounds__(T) rc_forward_kernel(int ns, int L, const float2 *__restrict__ echo,
                                                        const float2 *__restrict__ filt,
-                                                       const float2 *__restrict__ tw,
+                                                       const float2 *__restrict__ etab,
                                                        float2 *__restrict__ spec,
                                                        float *__restrict__ scale) {
     extern __shared__ float2 sm[];
     __shared__ float red[32];
     const int p = blockIdx.x;
+    const Etab E = load_etab<N, T>(sm, etab, L);
     const float2 *row = echo + (size_t)p * ns;
     for (int i = threadIdx.x; i < N; i += T) sm[pad(i)] = i < ns ? __ldg(&row[i]) : make_float2(0.f, 0.f);
     __syncthreads();
-    fft_smem<N, T, false>(sm, tw);
+    fft_smem<N, T, false>(sm, E, L);
     float2 *out = spec + (size_t)p * N;
     float acc = 0.f;
     for (int k = threadIdx.x; k < N; k += T) {
@@ -202,8 +226,7 @@ __global__ void __launch_bounds__(T) rc_forward_kernel(int ns, const float2 *__r
 template <int N, int T, int STORE>
 __global__ void __launch_bounds__(T) rc_inverse_kernel(int ns, int L, int nbins,
                                                        const float2 *__restrict__ spec,
-                                                       const float2 *__restrict__ tw,
-                                                       const float2 *__restrict__ ramp,
+                                                       const float2 *__restrict__ etab,
                                                        const float *__restrict__ scale,
                                                        void *__restrict__ out) {
     extern __shared__ float2 sm[];
@@ -211,18 +234,20 @@ __global__ void __launch_bounds__(T) rc_inverse_kernel(int ns, int L, int nbins,
     const int r = blockIdx.x - p * L;
     const float2 *in = spec + (size_t)p * N;
     const int LN = L * N;
+    const Etab E = load_etab<N, T>(sm, etab, L);
+    __syncthreads();
     for (int k = threadIdx.x; k < N; k += T) {
         float2 y = __ldg(&in[k]);
         if (r != 0) {
             const int kap = k < N / 2 ? k : k - N;  // MATLAB split floor((N+1)/2) for even N
             int m = (kap * r) % LN;
             if (m < 0) m += LN;
-            y = cmul(y, __ldg(&ramp[m]));
+            y = cmul(y, E(m));
         }
         sm[pad(k)] = y;
     }
     __syncthreads();
-    fft_smem<N, T, true>(sm, tw);
+    fft_smem<N, T, true>(sm, E, L);
     if (STORE == SARBP_STORE_C64) {
         float2 *o = reinterpret_cast<float2 *>(out) + (size_t)p * nbins + r;
         for (int i = threadIdx.x; i < ns; i += T) o[(size_t)L * i] = sm[pad(i)];
@@ -241,34 +266,36 @@ constexpr int threads_for() {
     return N >= 4096 ? 512 : (N >= 512 ? N / 8 : 64);
 }
 
+constexpr size_t kEtabSmem = sizeof(float2) * (256 + 1024);  // L N <= 16 * 16384
+
 template <int N>
-cudaError_t fwd_n(const RcPlan &p, const float2 *echo, const float2 *filt, const float2 *tw,
+cudaError_t fwd_n(const RcPlan &p, const float2 *echo, const float2 *filt, const float2 *etab,
                   float2 *spec, float *scale, cudaStream_t s) {
     constexpr int T = threads_for<N>();
-    const size_t smem = sizeof(float2) * padded(N);
+    const size_t smem = sizeof(float2) * padded(N) + kEtabSmem;
     auto k = rc_forward_kernel<N, T>;
     cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
-    k<<<p.np, T, smem, s>>>(p.ns, echo, filt, tw, spec, scale);
+    k<<<p.np, T, smem, s>>>(p.ns, p.L, echo, filt, etab, spec, scale);
     return cudaGetLastError();
 }
 
 template <int N>
-cudaError_t inv_n(const RcPlan &p, const float2 *spec, const float2 *tw, const float2 *ramp,
-                  const float *scale, void *out, cudaStream_t s) {
+cudaError_t inv_n(const RcPlan &p, const float2 *spec, const float2 *etab, const float *scale, void *out,
+                  cudaStream_t s) {
     constexpr int T = threads_for<N>();
-    const size_t smem = sizeof(float2) * padded(N);
+    const size_t smem = sizeof(float2) * padded(N) + kEtabSmem;
     cudaError_t e;
     if (p.storage == SARBP_STORE_C64) {
         auto k = rc_inverse_kernel<N, T, SARBP_STORE_C64>;
         e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;
-        k<<<p.np * p.L, T, smem, s>>>(p.ns, p.L, p.nbins, spec, tw, ramp, scale, out);
+        k<<<p.np * p.L, T, smem, s>>>(p.ns, p.L, p.nbins, spec, etab, scale, out);
     } else {
         auto k = rc_inverse_kernel<N, T, SARBP_STORE_C32H>;
         e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;
-        k<<<p.np * p.L, T, smem, s>>>(p.ns, p.L, p.nbins, spec, tw, ramp, scale, out);
+        k<<<p.np * p.L, T, smem, s>>>(p.ns, p.L, p.nbins, spec, etab, scale, out);
     }
     return cudaGetLastError();
 }
@@ -294,17 +321,19 @@ bool rc_size_supported(int nfft) {
     }
 
 cudaError_t launch_rc_forward(const RcPlan &p, const float2 *echo, const float2 *filt,
-                              const float2 *tw, float2 *spec, float *scale, cudaStream_t s) {
+                              const float2 *etab, float2 *spec, float *scale, cudaStream_t s) {
     if (p.np <= 0) return cudaSuccess;
-#define SARBP_FWD(N) fwd_n<N>(p, echo, filt, tw, spec, scale, s)
+    if (p.L < 1 || p.L > 16) return cudaErrorInvalidValue;
+#define SARBP_FWD(N) fwd_n<N>(p, echo, filt, etab, spec, scale, s)
     SARBP_RC_SWITCH(p.nfft, SARBP_FWD)
 #undef SARBP_FWD
 }
 
-cudaError_t launch_rc_inverse(const RcPlan &p, const float2 *spec, const float2 *tw,
-                              const float2 *ramp, const float *scale, void *out, cudaStream_t s) {
+cudaError_t launch_rc_inverse(const RcPlan &p, const float2 *spec, const float2 *etab,
+                              const float *scale, void *out, cudaStream_t s) {
     if (p.np <= 0) return cudaSuccess;
-#define SARBP_INV(N) inv_n<N>(p, spec, tw, ramp, scale, out, s)
+    if (p.L < 1 || p.L > 16) return cudaErrorInvalidValue;
+#define SARBP_INV(N) inv_n<N>(p, spec, etab, scale, out, s)
     SARBP_RC_SWITCH(p.nfft, SARBP_INV)
 #undef SARBP_INV
 }

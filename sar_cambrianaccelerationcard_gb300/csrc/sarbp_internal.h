@@ -28,12 +28,15 @@ struct RcPlan {
     int storage;     // sarbp_storage
 };
 
-// Host-side launchers (rc.cu).  spec: scratch [np][nfft] complex; filt: [nfft];
-// tw: FFT twiddles [nfft] (e^{-j2pi k/nfft}); ramp: [L*nfft] (e^{+j2pi m/(L nfft)}).
+// Host-side launchers (rc.cu).  spec: scratch [np][nfft] complex; filt: [nfft]
+// matched-filter spectrum; etab: two-level table of E^m = e^{+j2pi m/(L nfft)}:
+// etab[i] = E^i for i < 256, etab[256 + i] = E^{256 i} for i < L nfft / 256
+// (rc_etab_size entries in all).
 cudaError_t launch_rc_forward(const RcPlan &p, const float2 *echo, const float2 *filt,
-                              const float2 *tw, float2 *spec, float *scale, cudaStream_t s);
-cudaError_t launch_rc_inverse(const RcPlan &p, const float2 *spec, const float2 *tw,
-                              const float2 *ramp, const float *scale, void *out, cudaStream_t s);
+                              const float2 *etab, float2 *spec, float *scale, cudaStream_t s);
+cudaError_t launch_rc_inverse(const RcPlan &p, const float2 *spec, const float2 *etab,
+                              const float *scale, void *out, cudaStream_t s);
+inline int rc_etab_size(int L, int nfft) { return 256 + (L * nfft >= 256 ? L * nfft / 256 : 1); }
 bool rc_size_supported(int nfft);
 
 // ---------------------------------------------------------------- back-projection
@@ -64,12 +67,13 @@ struct BpPlan {
     int win;                 // staged bins per (tile, pulse), multiple of 4
     int nterms;              // polynomial terms for the differential range (3 or 4)
     int checked;             // 1: clamp every interpolation index and report clamps
+    int pix;                 // pixels per thread (8, 4 or 2): tiles of 32 x (8 pix) pixels
     unsigned *err;           // device error word
 };
 
 cudaError_t launch_bp(const BpPlan &p, cudaStream_t s, int *launches);
 // Tile geometry the planner needs to size the staging window.
-void bp_tile_dims(int mode, int *tile_x, int *tile_y);
+void bp_tile_dims(int pix, int *tile_x, int *tile_y);
 size_t bp_smem_bytes(int mode, int win);
 int bp_pulses_per_chunk(int mode);
 

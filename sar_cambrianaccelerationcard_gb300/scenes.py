@@ -198,3 +198,25 @@ def noise_sigma(clean_mean_power: float, snr_db: float) -> float:
     """Noise standard deviation (complex, total) for a given SNR relative to the
     mean noiseless echo power."""
     return math.sqrt(clean_mean_power / (10.0 ** (snr_db / 10.0)))
+
+
+def ground_scene(np_: int = 256, ns: int = 2048, n_img: int = 256, spacing: float = 1.0, altitude: float = 5000.0,
+                 ground_range: float = 10000.0, seed: int = 7, snr_db: float | None = 30.0) -> Scene:
+    """Airborne geometry with the image on the ground (the reference program's
+    data model: antenna at altitude H, pixels at z = 0, 1 m spacing,
+    BPA_CUDA.cpp:26-48), 3x3 targets around the scene centre."""
+    radar = Radar()
+    apc = straight_track(radar, np_)
+    apc[:, 2] = altitude
+    ux = np.array([0.0, spacing, 0.0])
+    uy = np.array([spacing, 0.0, 0.0])
+    centre = np.array([0.0, ground_range, 0.0])
+    grid = Grid(origin=centre - (n_img // 2) * ux - (n_img // 2) * uy, ux=ux, uy=uy, nx=n_img, ny=n_img)
+    r0 = float(np.hypot(ground_range, altitude))
+    t = []
+    for da in (-20.0, 0.0, 20.0):
+        for dr in (-20.0, 0.0, 20.0):
+            t.append((da, ground_range + dr, 0.0, 1.0))
+    t_rec0 = 2.0 * r0 / radar.c + radar.tp / 2.0 - ns / (2.0 * radar.fs)
+    return Scene(name="ground", radar=radar, np_=np_, ns=ns, apc=apc, grid=grid, targets=np.array(t),
+                 t_rec0=t_rec0, snr_db=snr_db, seed=seed)

@@ -25,7 +25,8 @@ def scenes_to_check():
     c.apc = scenes.curved_track(c.radar, c.np_, seed=5)
     d = scenes.config1(np_=100, ns=700)
     d.grid = scenes.centred_grid(d.radar, 77, 130, 0.5)
-    return [a, b, c, d]
+    e = scenes.ground_scene()  # 1 m ground pixels from 5 km altitude: shorter tiles
+    return [a, b, c, d, e]
 
 
 @pytest.mark.parametrize("mode", ["split", "fp16store"])
