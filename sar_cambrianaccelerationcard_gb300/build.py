@@ -32,8 +32,8 @@ def _flags(extra=()):
                    "-I", os.path.join(ROOT, "include"), "-I", CSRC, *extra]
 
 
-def _compile(src: str, extra=()) -> str:
-    obj = os.path.join(BUILD, os.path.splitext(src)[0] + ".o")
+def _compile(src: str, extra=(), build_dir: str = BUILD) -> str:
+    obj = os.path.join(build_dir, os.path.splitext(src)[0] + ".o")
     path = os.path.join(CSRC, src)
     deps = [path] + [os.path.join(CSRC, h) for h in os.listdir(CSRC) if h.endswith(".h")] + \
         [os.path.join(ROOT, "include", "sarbp.h")]
@@ -50,19 +50,21 @@ def _compile(src: str, extra=()) -> str:
     return obj
 
 
-def build(verbose: bool = False, extra=()) -> str:
-    os.makedirs(BUILD, exist_ok=True)
+def build(verbose: bool = False, extra=(), lib: str = LIB, build_dir: str = BUILD) -> str:
+    """Compile (incrementally) and link.  `extra` adds nvcc flags (e.g. -D
+    tuning macros); `lib`/`build_dir` place a variant build elsewhere."""
+    os.makedirs(build_dir, exist_ok=True)
     with cf.ThreadPoolExecutor(max_workers=len(SOURCES)) as ex:
-        objs = list(ex.map(lambda s: _compile(s, extra), SOURCES))
-    if os.path.exists(LIB) and all(os.path.getmtime(LIB) >= os.path.getmtime(o) for o in objs):
-        return LIB
-    cmd = [nvcc(), *ARCH, "-shared", "-o", LIB, *objs, "-cudart", "static"]
+        objs = list(ex.map(lambda s: _compile(s, extra, build_dir), SOURCES))
+    if os.path.exists(lib) and all(os.path.getmtime(lib) >= os.path.getmtime(o) for o in objs):
+        return lib
+    cmd = [nvcc(), *ARCH, "-shared", "-o", lib, *objs, "-cudart", "static"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
     if verbose:
-        print("built", LIB)
-    return LIB
+        print("built", lib)
+    return lib
 
 
 if __name__ == "__main__":

@@ -43,8 +43,15 @@ namespace {
 constexpr int kThreads = 256;
 constexpr int kWarps = kThreads / 32;
 constexpr int kTileX = 32;  // pixels along x (columns); tile height is 8 * PIX rows
-constexpr int kChunk = 16;  // pulses per staged chunk
+#ifndef SARBP_BP_CHUNK
+#define SARBP_BP_CHUNK 16
+#endif
+#ifndef SARBP_BP_MINBLOCKS
+#define SARBP_BP_MINBLOCKS 2
+#endif
+constexpr int kChunk = SARBP_BP_CHUNK;  // pulses per staged chunk (a multiple of 8)
 constexpr int kPerWarp = kChunk / kWarps;  // pulses each warp prepares
+static_assert(kChunk % kWarps == 0 && kPerWarp <= 32, "chunk must split evenly over the warps");
 constexpr int kStages = 3;  // raw-window ring depth
 constexpr float kMagic = 12582912.0f;  // 1.5 * 2^23: adding it rounds to an integer
 constexpr unsigned kMagicBitsShift4 = 0x4B400000u << 4;
@@ -354,7 +361,7 @@ __device__ __forceinline__ void convert(const Smem &S, int stage, int sbuf, int 
 }
 
 template <int MODE, int STORE, int NTERMS, bool CHECKED, int PIX>
-__global__ void __launch_bounds__(kThreads, 2)
+__global__ void __launch_bounds__(kThreads, SARBP_BP_MINBLOCKS)
     bp_kernel(const __grid_constant__ BpPlan P, int tiles_y, int pulses_per_seg, float qq_max) {
     constexpr int kPix = PIX;  // pixels per thread, all in one column
     constexpr int kTileY = 8 * PIX;

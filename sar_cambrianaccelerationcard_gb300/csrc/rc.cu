@@ -261,9 +261,12 @@ __global__ void __launch_bounds__(T) rc_inverse_kernel(int ns, int L, int nbins,
     }
 }
 
+#ifndef SARBP_RC_BIG_THREADS
+#define SARBP_RC_BIG_THREADS 512
+#endif
 template <int N>
 constexpr int threads_for() {
-    return N >= 4096 ? 512 : (N >= 512 ? N / 8 : 64);
+    return N >= 8192 ? SARBP_RC_BIG_THREADS : (N >= 4096 ? 512 : (N >= 512 ? N / 8 : 64));
 }
 
 constexpr size_t kEtabSmem = sizeof(float2) * (256 + 1024);  // L N <= 16 * 16384
