@@ -442,10 +442,6 @@ __global__ void __launch_bounds__(kThreads, SARBP_BP_MINBLOCKS)
 
     const f2 XC2 = pk2(xc, xc);
     const f2 BPM2 = pk2(bpm, bpm), KH2 = pk2(kph_hi, kph_hi), KL2 = pk2(kph_lo, kph_lo);
-    const f2 NEG1 = pk2(-1.f, -1.f);
-    f2 AR[kPix / 2], AI[kPix / 2];  // SPLIT accumulators, pixel pairs (2h, 2h+1)
-#pragma unroll
-    for (int h = 0; h < kPix / 2; ++h) AR[h] = AI[h] = pk2(0.f, 0.f);
     f2 YC2[kPix / 2], QQ2[kPix / 2];
 #pragma unroll
     for (int h = 0; h < kPix / 2; ++h) {
@@ -510,21 +506,19 @@ __global__ void __launch_bounds__(kThreads, SARBP_BP_MINBLOCKS)
                         b2 = pk2(bb[0], bb[1]);
                     }
                     const f2 t2 = fadd2(b2, MP);
-                    float tt[2], sr[2], si[2], sn[2], cs[2];
+                    float tt[2];
                     upk2(t2, tt[0], tt[1]);
 #pragma unroll
                     for (int u = 0; u < 2; ++u) {
+                        const int j = 2 * h + u;
                         const float4 v = lds128((__float_as_uint(tt[u]) << 4) + sbase);
-                        sr[u] = fmaf(bb[u], v.z, v.x);
-                        si[u] = fmaf(bb[u], v.w, v.y);
-                        __sincosf(ph[u], &sn[u], &cs[u]);
+                        const float sr = fmaf(bb[u], v.z, v.x);
+                        const float si = fmaf(bb[u], v.w, v.y);
+                        float sn, cs;
+                        __sincosf(ph[u], &sn, &cs);
+                        acc_r[j] = fmaf(sr, cs, fmaf(-si, sn, acc_r[j]));
+                        acc_i[j] = fmaf(sr, sn, fmaf(si, cs, acc_i[j]));
                     }
-                    // complex accumulate of the pixel pair: re += sr cs - si sn, im += sr sn + si cs
-                    const f2 SR = pk2(sr[0], sr[1]), SI = pk2(si[0], si[1]);
-                    const f2 SN = pk2(sn[0], sn[1]), CS = pk2(cs[0], cs[1]);
-                    const f2 NSI = fmul2(SI, NEG1);  // exact negation
-                    AR[h] = ffma2(NSI, SN, ffma2(SR, CS, AR[h]));
-                    AI[h] = ffma2(SI, CS, ffma2(SR, SN, AI[h]));
                 }
                 MP = fadd2(MP, WIN2);
             }
@@ -584,13 +578,6 @@ __global__ void __launch_bounds__(kThreads, SARBP_BP_MINBLOCKS)
         }
     }
 
-    if (MODE == SARBP_MODE_SPLIT || MODE == SARBP_MODE_FP16STORE) {
-#pragma unroll
-        for (int h = 0; h < kPix / 2; ++h) {
-            upk2(AR[h], acc_r[2 * h], acc_r[2 * h + 1]);
-            upk2(AI[h], acc_i[2 * h], acc_i[2 * h + 1]);
-        }
-    }
     if (CHECKED && clamped) atomicOr(P.err, kErrIndexClamp);
     if (failed) {
         if (threadIdx.x == 0) {
