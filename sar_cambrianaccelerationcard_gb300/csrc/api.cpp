@@ -295,8 +295,6 @@ sarbp_status check_grid(sarbp_ctx *ctx, const sarbp_grid *g) {
     return SARBP_OK;
 }
 
-double dot3(const double *a, const double *b) { return a[0] * b[0] + a[1] * b[1] + a[2] * b[2]; }
-
 // Back-projection of device-resident rc + apc into a device image.
 sarbp_status bp_device(sarbp_ctx *ctx, const sarbp_radar *r, const sarbp_rc_view &rc, const double *apc_dev,
                        const double *apc_host, const sarbp_grid *g, int mode, float2 *image, int accumulate,
@@ -311,124 +309,22 @@ sarbp_status bp_device(sarbp_ctx *ctx, const sarbp_radar *r, const sarbp_rc_view
     if (rc.nbins % 4 != 0) return fail(ctx, SARBP_ERR_UNSUPPORTED, "nbins must be a multiple of 4");
     if (((uintptr_t)rc.data & 15) != 0) return fail(ctx, SARBP_ERR_INVALID_ARGUMENT, "rc data must be 16-byte aligned");
     BpPlan p;
-    std::memset(&p, 0, sizeof p);
+    std::string why;
+    if (!sarbp::plan_bp(ctx->sms, *r, rc, apc_host, np, *g, mode, 0, p, why))
+        return fail(ctx, SARBP_ERR_UNSUPPORTED, "%s", why.c_str());
     p.rc = rc.data;
     p.scale = rc.scale;
-    p.storage = rc.storage;
     p.np = np;
-    p.nbins = rc.nbins;
-    p.mode = mode;
     p.apc = apc_dev;
-    for (int i = 0; i < 3; ++i) {
-        p.g.origin[i] = g->origin[i];
-        p.g.ux[i] = g->ux[i];
-        p.g.uy[i] = g->uy[i];
-    }
-    p.g.g11 = dot3(g->ux, g->ux);
-    p.g.g12 = dot3(g->ux, g->uy);
-    p.g.g22 = dot3(g->uy, g->uy);
-    p.g.nx = g->nx;
-    p.g.ny = g->ny;
-    p.fc = r->fc;
-    p.c = r->c;
-    p.t0_bins = rc.t0_bins;
-    p.bin_rate = rc.bin_rate;
     p.image = image;
     p.accumulate = accumulate;
     p.err = ctx->errword.as<unsigned>();
     p.checked = ctx->checked;
-    auto split2 = [](double v, float *h, float *l) {
-        *h = (float)v;
-        *l = (float)(v - (double)*h);
-    };
-    split2(2.0 / r->c * rc.bin_rate, &p.kb_h, &p.kb_l);
-    split2(rc.t0_bins * rc.bin_rate, &p.tb_h, &p.tb_l);
-    split2(2.0 * r->fc / r->c, &p.kc_h, &p.kc_l);
     SARBP_CUDA(ctx, ctx->pref.ensure(sizeof(float) * 8 * (size_t)np), "alloc pulse references");
     p.pref = ctx->pref.as<float4>();
-
-    // Line-of-sight extremes over the grid (9x9 lattice of grid points, all pulses).
-    const double lux = std::sqrt(p.g.g11), luy = std::sqrt(p.g.g22);
-    double cx = 0, sy = 0, rmin = 1e300, rmax = 0;
-    for (int i = 0; i < np; ++i) {
-        const double *a = apc_host + 3 * (size_t)i;
-        for (int u = 0; u <= 8; ++u) {
-            for (int v = 0; v <= 8; ++v) {
-                const double fx = (g->nx - 1) * u / 8.0, fy = (g->ny - 1) * v / 8.0;
-                double w[3];
-                for (int k = 0; k < 3; ++k) w[k] = g->origin[k] + fx * g->ux[k] + fy * g->uy[k] - a[k];
-                const double R = std::sqrt(dot3(w, w));
-                rmin = std::min(rmin, R);
-                rmax = std::max(rmax, R);
-                if (R > 0) {
-                    if (lux > 0) cx = std::max(cx, std::fabs(dot3(g->ux, w)) / (R * lux));
-                    if (luy > 0) sy = std::max(sy, std::fabs(dot3(g->uy, w)) / (R * luy));
-                }
-            }
-        }
-    }
-    cx = std::min(1.0, cx * 1.05 + 0.01);
-    sy = std::min(1.0, sy * 1.05 + 0.01);
-    const double bpm = 2.0 / r->c * rc.bin_rate;
-    // Tile choice: the tallest tile (32 x 64, 32 x 32, 32 x 16 pixels) whose
-    // differential-range series truncation stays below kSeriesTol metres and
-    // whose staging window fits shared memory.  Series remainder after k terms
-    // of sqrt(1+e)-1 times R: R (5/128) e^4 (k = 3), R (7/256) e^5 (k = 4), with
-    // e = |n|/R^2 <= (2 diag R + diag^2)/R^2 over the tile.
-    constexpr double kSeriesTol = 5e-7;  // 1.1e-4 rad of C-band phase at the tile corners
-    const char *why = "no tile size fits";
-    bool chosen = false;
-    for (int pix : {8, 4, 2}) {
-        int tx, ty;
-        sarbp::bp_tile_dims(pix, &tx, &ty);
-        const double hx = 0.5 * (tx - 1), hy = 0.5 * (ty - 1);
-        const double qq_max = hx * hx * p.g.g11 + 2 * hx * hy * std::fabs(p.g.g12) + hy * hy * p.g.g22;
-        const double tile_diag = std::sqrt(qq_max);
-        const double rmin_tile = rmin - tile_diag;
-        if (!(rmin_tile > 20.0 * tile_diag)) {
-            why = "an antenna position is within 20 tile diagonals of the grid";
-            continue;
-        }
-        const double half = bpm * (lux * hx * cx + luy * hy * sy + qq_max / (2 * rmin_tile)) * 1.03 + 2.0;
-        if (!(half < 4096.0)) {
-            why = "tile spans too many range bins";
-            continue;
-        }
-        int win = (int)std::ceil(2 * half) + 8;
-        win = (win + 3) & ~3;
-        if (sarbp::bp_smem_bytes(mode, win) > (size_t)(227u << 10)) {
-            why = "tile spans too many range bins for shared memory";
-            continue;
-        }
-        const double e = (2 * tile_diag * rmax + qq_max) / (rmin_tile * rmin_tile);
-        const bool split = mode == SARBP_MODE_SPLIT || mode == SARBP_MODE_FP16STORE;
-        if (split && rmax * 0.02734375 * std::pow(e, 5) > kSeriesTol) {
-            why = "tiles too large for the differential-range series";
-            continue;
-        }
-        p.pix = pix;
-        p.win = win;
-        p.nterms = (rmax * 0.0390625 * e * e * e * e < kSeriesTol) ? 3 : 4;
-        chosen = true;
-        break;
-    }
-    if (!chosen) return fail(ctx, SARBP_ERR_UNSUPPORTED, "%s", why);
-    int tx, ty;
-    sarbp::bp_tile_dims(p.pix, &tx, &ty);
-    const int win = p.win;
-
-    // pulse segments: fill at least ~2 waves of CTAs
-    const int tiles = ((g->nx + tx - 1) / tx) * ((g->ny + ty - 1) / ty);
-    const int chunk = sarbp::bp_pulses_per_chunk(mode);
-    int cta_per_sm = 2;
-    const size_t smem = sarbp::bp_smem_bytes(mode, win);
-    if (smem > 0) cta_per_sm = std::max<int>(1, std::min<int>(3, (int)((227u << 10) / (smem + 1024))));
-    const int want = 2 * ctx->sms * cta_per_sm;
-    int segments = 1;
-    while (tiles * segments < want && np / (segments * 2) >= 4 * chunk) segments *= 2;
-    p.segments = segments;
-    if (segments > 1) {
-        SARBP_CUDA(ctx, ctx->partial.ensure(sizeof(float2) * (size_t)segments * g->nx * g->ny), "alloc partial images");
+    if (p.segments > 1) {
+        SARBP_CUDA(ctx, ctx->partial.ensure(sizeof(float2) * (size_t)p.segments * g->nx * g->ny),
+                   "alloc partial images");
         p.partial = ctx->partial.as<float2>();
     }
     int launches = 0;

@@ -1,0 +1,129 @@
+// plan.cpp -- host-side planning of a back-projection launch (shared by the
+// one-shot API and the serving loop).
+//
+// From the radar, the range-compressed data layout, the APC track and the
+// pixel grid it derives everything the BP kernel needs that does not change
+// from launch to launch: grid metric terms, float-pair constants, the tile
+// height (32 x 64, 32 x 32 or 32 x 16 pixels), the staging window per
+// (tile, pulse), the number of series terms and the pulse segmentation.
+#include <cmath>
+#include <cstring>
+#include <string>
+
+#include "sarbp_internal.h"
+
+namespace sarbp {
+namespace {
+double dot3(const double *a, const double *b) { return a[0] * b[0] + a[1] * b[1] + a[2] * b[2]; }
+}  // namespace
+
+bool plan_bp(int sms, const sarbp_radar &r, const sarbp_rc_view &rc, const double *apc_host, int np,
+             const sarbp_grid &g, int mode, int pulses_per_launch, BpPlan &p, std::string &why) {
+    std::memset(&p, 0, sizeof p);
+    p.storage = rc.storage;
+    p.nbins = rc.nbins;
+    p.mode = mode;
+    for (int i = 0; i < 3; ++i) {
+        p.g.origin[i] = g.origin[i];
+        p.g.ux[i] = g.ux[i];
+        p.g.uy[i] = g.uy[i];
+    }
+    p.g.g11 = dot3(g.ux, g.ux);
+    p.g.g12 = dot3(g.ux, g.uy);
+    p.g.g22 = dot3(g.uy, g.uy);
+    p.g.nx = g.nx;
+    p.g.ny = g.ny;
+    p.fc = r.fc;
+    p.c = r.c;
+    p.t0_bins = rc.t0_bins;
+    p.bin_rate = rc.bin_rate;
+    auto split2 = [](double v, float *h, float *l) {
+        *h = (float)v;
+        *l = (float)(v - (double)*h);
+    };
+    split2(2.0 / r.c * rc.bin_rate, &p.kb_h, &p.kb_l);
+    split2(rc.t0_bins * rc.bin_rate, &p.tb_h, &p.tb_l);
+    split2(2.0 * r.fc / r.c, &p.kc_h, &p.kc_l);
+
+    // Line-of-sight extremes over the grid (9x9 lattice of grid points, all pulses).
+    const double lux = std::sqrt(p.g.g11), luy = std::sqrt(p.g.g22);
+    double cx = 0, sy = 0, rmin = 1e300, rmax = 0;
+    for (int i = 0; i < np; ++i) {
+        const double *a = apc_host + 3 * (size_t)i;
+        for (int u = 0; u <= 8; ++u) {
+            for (int v = 0; v <= 8; ++v) {
+                const double fx = (g.nx - 1) * u / 8.0, fy = (g.ny - 1) * v / 8.0;
+                double w[3];
+                for (int k = 0; k < 3; ++k) w[k] = g.origin[k] + fx * g.ux[k] + fy * g.uy[k] - a[k];
+                const double R = std::sqrt(dot3(w, w));
+                rmin = std::min(rmin, R);
+                rmax = std::max(rmax, R);
+                if (R > 0) {
+                    if (lux > 0) cx = std::max(cx, std::fabs(dot3(g.ux, w)) / (R * lux));
+                    if (luy > 0) sy = std::max(sy, std::fabs(dot3(g.uy, w)) / (R * luy));
+                }
+            }
+        }
+    }
+    cx = std::min(1.0, cx * 1.05 + 0.01);
+    sy = std::min(1.0, sy * 1.05 + 0.01);
+    const double bpm = 2.0 / r.c * rc.bin_rate;
+    // Tile choice: the tallest tile (32 x 64, 32 x 32, 32 x 16 pixels) whose
+    // differential-range series truncation stays below kSeriesTol metres and
+    // whose staging window fits shared memory.  Series remainder after k terms
+    // of sqrt(1+e)-1 times R: R (5/128) e^4 (k = 3), R (7/256) e^5 (k = 4), with
+    // e = |n|/R^2 <= (2 diag R + diag^2)/R^2 over the tile.
+    constexpr double kSeriesTol = 5e-7;  // 1.1e-4 rad of C-band phase at the tile corners
+    why = "no tile size fits";
+    bool chosen = false;
+    for (int pix : {8, 4, 2}) {
+        int tx, ty;
+        bp_tile_dims(pix, &tx, &ty);
+        const double hx = 0.5 * (tx - 1), hy = 0.5 * (ty - 1);
+        const double qq_max = hx * hx * p.g.g11 + 2 * hx * hy * std::fabs(p.g.g12) + hy * hy * p.g.g22;
+        const double tile_diag = std::sqrt(qq_max);
+        const double rmin_tile = rmin - tile_diag;
+        if (!(rmin_tile > 20.0 * tile_diag)) {
+            why = "an antenna position is within 20 tile diagonals of the grid";
+            continue;
+        }
+        const double half = bpm * (lux * hx * cx + luy * hy * sy + qq_max / (2 * rmin_tile)) * 1.03 + 2.0;
+        if (!(half < 4096.0)) {
+            why = "tile spans too many range bins";
+            continue;
+        }
+        int win = (int)std::ceil(2 * half) + 8;
+        win = (win + 3) & ~3;
+        if (bp_smem_bytes(mode, win) > (size_t)(227u << 10)) {
+            why = "tile spans too many range bins for shared memory";
+            continue;
+        }
+        const double e = (2 * tile_diag * rmax + qq_max) / (rmin_tile * rmin_tile);
+        const bool split = mode == SARBP_MODE_SPLIT || mode == SARBP_MODE_FP16STORE;
+        if (split && rmax * 0.02734375 * std::pow(e, 5) > kSeriesTol) {
+            why = "tiles too large for the differential-range series";
+            continue;
+        }
+        p.pix = pix;
+        p.win = win;
+        p.nterms = (rmax * 0.0390625 * e * e * e * e < kSeriesTol) ? 3 : 4;
+        chosen = true;
+        break;
+    }
+    if (!chosen) return false;
+    int tx, ty;
+    bp_tile_dims(p.pix, &tx, &ty);
+    // pulse segments: fill at least ~2 waves of CTAs
+    const int tiles = ((g.nx + tx - 1) / tx) * ((g.ny + ty - 1) / ty);
+    const int chunk = bp_pulses_per_chunk(mode);
+    const size_t smem = bp_smem_bytes(mode, p.win);
+    const int cta_per_sm = std::max<int>(1, std::min<int>(3, (int)((227u << 10) / (smem + 1024))));
+    const int want = 2 * sms * cta_per_sm;
+    const int npl = pulses_per_launch > 0 ? pulses_per_launch : np;
+    int segments = 1;
+    while (tiles * segments < want && npl / (segments * 2) >= 4 * chunk) segments *= 2;
+    p.segments = segments;
+    return true;
+}
+
+}  // namespace sarbp

@@ -5,6 +5,8 @@
 #include <cuda_fp16.h>
 #include <stdint.h>
 
+#include <string>
+
 #include "sarbp.h"
 
 namespace sarbp {
@@ -72,6 +74,12 @@ struct BpPlan {
 };
 
 cudaError_t launch_bp(const BpPlan &p, cudaStream_t s, int *launches);
+// Host planning (plan.cpp): fills every BpPlan field that does not depend on
+// buffers (geometry, constants, tile height, window, series terms, segments
+// for launches of `pulses_per_launch` pulses; 0 = all np).  On failure returns
+// false with the reason in `why`.
+bool plan_bp(int sms, const sarbp_radar &r, const sarbp_rc_view &rc, const double *apc_host, int np,
+             const sarbp_grid &g, int mode, int pulses_per_launch, BpPlan &p, std::string &why);
 // Tile geometry the planner needs to size the staging window.
 void bp_tile_dims(int pix, int *tile_x, int *tile_y);
 size_t bp_smem_bytes(int mode, int win);
