@@ -202,6 +202,73 @@ sarbp_status sarbp_synthesize_echo(sarbp_ctx *ctx, const sarbp_radar *radar,
                                    double snr_db, uint64_t seed,
                                    sarbp_complex64 *echo_out, void *stream);
 
+/* ------------------------------------------------------------- serving -- */
+
+/* A persistent imaging service on one device.  A worker thread admits
+ * submitted jobs while the device-memory budget and the job slots allow,
+ * keeps each admitted job's echo, range-compressed data and partial image
+ * resident, and advances all admitted jobs together: every step back-projects
+ * the next `pulses_per_step` pulses of each job (accumulating into its image),
+ * with the step's launches for all jobs captured in one CUDA graph (one branch
+ * per job, so their work overlaps on the device).  Jobs that arrive while
+ * others run join at the next step.  Each job's result is the same whatever
+ * else runs with it (its launches and their order do not depend on the mix).
+ * Submit, poll, wait and cancel may be called from any host thread. */
+typedef struct sarbp_server sarbp_server;
+
+typedef struct sarbp_server_config {
+    int32_t device;
+    int32_t max_jobs;           /* jobs resident at once (slots), 1..64 */
+    uint64_t hbm_budget_bytes;  /* device memory the server may hold for jobs */
+    int32_t pulses_per_step;    /* pulses per job per step (multiple of 16); 0: 512 */
+    int32_t use_graphs;         /* 1: capture each step's launches in a CUDA graph; 0: plain streams */
+} sarbp_server_config;
+
+typedef struct sarbp_job {
+    sarbp_radar radar;
+    sarbp_grid grid;
+    const sarbp_complex64 *echo; /* host [np][ns]; must stay valid until the job ends (pinned: async upload) */
+    const double *apc;           /* host [np][3] */
+    sarbp_complex64 *image;      /* host [ny][nx] result */
+    int32_t np, ns;
+    int32_t mode;                /* SARBP_MODE_SPLIT or SARBP_MODE_FP16STORE */
+    int32_t reserved;
+} sarbp_job;
+
+typedef struct sarbp_job_stats {
+    int32_t status;          /* the job's sarbp_status */
+    int32_t steps;           /* back-projection steps the job took */
+    double queued_ms;        /* submit -> admitted */
+    double latency_ms;       /* submit -> image in host memory */
+    double updates;          /* nx * ny * np */
+    uint64_t device_bytes;   /* admission footprint */
+} sarbp_job_stats;
+
+typedef struct sarbp_server_stats {
+    uint64_t submitted, completed, failed, rejected, cancelled;
+    uint64_t steps, graph_launches;
+    double updates;          /* pixel*pulse updates of completed jobs */
+    double busy_s;           /* wall time with at least one job admitted */
+    uint64_t bytes_in_use, peak_bytes;
+    int32_t active, queued, peak_active, reserved;
+} sarbp_server_stats;
+
+sarbp_status sarbp_server_create(sarbp_server **out, const sarbp_server_config *cfg);
+/* Finishes admitted jobs, cancels queued ones, stops the worker. */
+sarbp_status sarbp_server_destroy(sarbp_server *srv);
+/* Validates and plans the job, queues it.  SARBP_ERR_BUDGET if the job alone
+ * exceeds the budget. */
+sarbp_status sarbp_server_submit(sarbp_server *srv, const sarbp_job *job, uint64_t *ticket);
+/* SARBP_OK when done, SARBP_ERR_NOT_READY while queued or running, else the job's error. */
+sarbp_status sarbp_server_poll(sarbp_server *srv, uint64_t ticket);
+/* Waits up to timeout_ms (< 0: forever); SARBP_ERR_TIMEOUT if still running.
+ * On completion fills stats (may be NULL), returns the job's status and
+ * releases the ticket. */
+sarbp_status sarbp_server_wait(sarbp_server *srv, uint64_t ticket, int32_t timeout_ms, sarbp_job_stats *stats);
+/* Cancels a queued job (SARBP_ERR_NOT_READY if it was already admitted). */
+sarbp_status sarbp_server_cancel(sarbp_server *srv, uint64_t ticket);
+sarbp_status sarbp_server_get_stats(sarbp_server *srv, sarbp_server_stats *out);
+
 /* ------------------------------------------------- reference-layout shim -- */
 
 /* Byte-for-byte layout of the reference's SARParams (BPA_CUDA.h:28-50):

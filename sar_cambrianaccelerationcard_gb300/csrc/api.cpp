@@ -26,7 +26,6 @@ using sarbp::RcPlan;
 
 namespace {
 
-constexpr double kPi = 3.14159265358979323846;
 constexpr size_t kSpecScratchBudget = size_t(256) << 20;  // bytes of spectrum scratch per batch
 
 struct DevBuf {
@@ -150,28 +149,6 @@ sarbp_status layout(sarbp_ctx *ctx, const sarbp_radar *r, int32_t ns, sarbp_rc_l
     return SARBP_OK;
 }
 
-// iterative radix-2 FFT on the host (double), unnormalised, sign -1 forward
-void host_fft(std::vector<std::complex<double>> &x, int sign) {
-    const size_t n = x.size();
-    for (size_t i = 1, j = 0; i < n; ++i) {
-        size_t bit = n >> 1;
-        for (; j & bit; bit >>= 1) j ^= bit;
-        j ^= bit;
-        if (i < j) std::swap(x[i], x[j]);
-    }
-    for (size_t len = 2; len <= n; len <<= 1) {
-        for (size_t i = 0; i < n; i += len) {
-            for (size_t k = 0; k < len / 2; ++k) {
-                const double a = sign * 2.0 * kPi * (double)k / (double)len;
-                const std::complex<double> w(std::cos(a), std::sin(a));
-                const std::complex<double> u = x[i + k], v = x[i + k + len / 2] * w;
-                x[i + k] = u + v;
-                x[i + k + len / 2] = u - v;
-            }
-        }
-    }
-}
-
 sarbp_status ensure_tables(sarbp_ctx *ctx, const sarbp_radar *r, const sarbp_rc_layout &lay) {
     RcTables &t = ctx->tables;
     if (t.valid && t.nfft == lay.nfft && t.L == r->upsample && t.nc == lay.nc && t.shift == lay.shift &&
@@ -179,31 +156,8 @@ sarbp_status ensure_tables(sarbp_ctx *ctx, const sarbp_radar *r, const sarbp_rc_
         return SARBP_OK;
     t.valid = false;
     const int N = lay.nfft, L = r->upsample;
-    // matched-filter spectrum G[k] = conj(H[k]) e^{-j2pi k shift/N} / N
-    std::vector<std::complex<double>> h(N);
-    for (int i = 0; i < lay.nc; ++i) {
-        const double u = (double)i / r->fs;
-        if (u >= 0.0 && u < r->tp) {
-            const double ph = kPi * r->kr * (u - r->tc) * (u - r->tc);
-            h[i] = std::complex<double>(std::cos(ph), std::sin(ph));
-        }
-    }
-    host_fft(h, -1);
-    std::vector<float2> g(N), et((size_t)sarbp::rc_etab_size(L, N));
-    for (int k = 0; k < N; ++k) {
-        const long long m = ((long long)k * lay.shift) % N;
-        const double a = -2.0 * kPi * (double)m / (double)N;
-        const std::complex<double> v = std::conj(h[k]) * std::complex<double>(std::cos(a), std::sin(a)) / (double)N;
-        g[k] = make_float2((float)v.real(), (float)v.imag());
-    }
-    // E^m = e^{+j2pi m/(L N)}: et[i] = E^i (i < 256), et[256 + i] = E^{256 i}
-    const double LN = (double)L * N;
-    for (int i = 0; i < 256; ++i)
-        et[i] = make_float2((float)std::cos(2.0 * kPi * i / LN), (float)std::sin(2.0 * kPi * i / LN));
-    for (size_t i = 256; i < et.size(); ++i) {
-        const double a = 2.0 * kPi * (double)(256 * (i - 256)) / LN;
-        et[i] = make_float2((float)std::cos(a), (float)std::sin(a));
-    }
+    std::vector<float2> g, et;
+    sarbp::rc_tables_host(*r, lay, g, et);
     SARBP_CUDA(ctx, t.filt.ensure(sizeof(float2) * N), "alloc filter");
     SARBP_CUDA(ctx, t.etab.ensure(sizeof(float2) * et.size()), "alloc phase table");
     SARBP_CUDA(ctx, cudaMemcpy(t.filt.ptr, g.data(), sizeof(float2) * N, cudaMemcpyHostToDevice), "upload filter");

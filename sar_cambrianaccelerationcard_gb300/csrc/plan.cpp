@@ -7,8 +7,10 @@
 // height (32 x 64, 32 x 32 or 32 x 16 pixels), the staging window per
 // (tile, pulse), the number of series terms and the pulse segmentation.
 #include <cmath>
+#include <complex>
 #include <cstring>
 #include <string>
+#include <vector>
 
 #include "sarbp_internal.h"
 
@@ -124,6 +126,49 @@ bool plan_bp(int sms, const sarbp_radar &r, const sarbp_rc_view &rc, const doubl
     while (tiles * segments < want && npl / (segments * 2) >= 4 * chunk) segments *= 2;
     p.segments = segments;
     return true;
+}
+
+void rc_tables_host(const sarbp_radar &r, const sarbp_rc_layout &lay, std::vector<float2> &filt,
+                    std::vector<float2> &etab) {
+    constexpr double kPi = 3.14159265358979323846;
+    const int N = lay.nfft, L = r.upsample;
+    std::vector<std::complex<double>> h(N);
+    for (int i = 0; i < lay.nc && i < N; ++i) {
+        const double u = (double)i / r.fs;
+        if (u >= 0.0 && u < r.tp) {
+            const double ph = kPi * r.kr * (u - r.tc) * (u - r.tc);
+            h[i] = std::complex<double>(std::cos(ph), std::sin(ph));
+        }
+    }
+    // radix-2 forward transform of the chirp (unnormalised)
+    for (int i = 1, j = 0; i < N; ++i) {
+        int bit = N >> 1;
+        for (; j & bit; bit >>= 1) j ^= bit;
+        j ^= bit;
+        if (i < j) std::swap(h[i], h[j]);
+    }
+    for (int len = 2; len <= N; len <<= 1)
+        for (int i = 0; i < N; i += len)
+            for (int k = 0; k < len / 2; ++k) {
+                const double a = -2.0 * kPi * (double)k / (double)len;
+                const std::complex<double> w(std::cos(a), std::sin(a));
+                const std::complex<double> u = h[i + k], v = h[i + k + len / 2] * w;
+                h[i + k] = u + v;
+                h[i + k + len / 2] = u - v;
+            }
+    filt.resize(N);
+    for (int k = 0; k < N; ++k) {
+        const long long m = ((long long)k * lay.shift) % N;
+        const double a = -2.0 * kPi * (double)m / (double)N;
+        const std::complex<double> v = std::conj(h[k]) * std::complex<double>(std::cos(a), std::sin(a)) / (double)N;
+        filt[k] = make_float2((float)v.real(), (float)v.imag());
+    }
+    etab.resize(rc_etab_size(L, N));
+    const double LN = (double)L * N;
+    for (size_t i = 0; i < etab.size(); ++i) {
+        const double a = 2.0 * kPi * (double)(i < 256 ? i : 256 * (i - 256)) / LN;
+        etab[i] = make_float2((float)std::cos(a), (float)std::sin(a));
+    }
 }
 
 }  // namespace sarbp

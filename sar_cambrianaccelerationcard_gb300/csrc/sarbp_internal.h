@@ -6,6 +6,7 @@
 #include <stdint.h>
 
 #include <string>
+#include <vector>
 
 #include "sarbp.h"
 
@@ -80,6 +81,9 @@ cudaError_t launch_bp(const BpPlan &p, cudaStream_t s, int *launches);
 // false with the reason in `why`.
 bool plan_bp(int sms, const sarbp_radar &r, const sarbp_rc_view &rc, const double *apc_host, int np,
              const sarbp_grid &g, int mode, int pulses_per_launch, BpPlan &p, std::string &why);
+// Matched-filter spectrum [nfft] and phase table [rc_etab_size] for a layout (plan.cpp).
+void rc_tables_host(const sarbp_radar &r, const sarbp_rc_layout &lay, std::vector<float2> &filt,
+                    std::vector<float2> &etab);
 // Tile geometry the planner needs to size the staging window.
 void bp_tile_dims(int pix, int *tile_x, int *tile_y);
 size_t bp_smem_bytes(int mode, int win);
