@@ -71,6 +71,30 @@ class Target(ctypes.Structure):
     _fields_ = [("x", ctypes.c_double), ("y", ctypes.c_double), ("z", ctypes.c_double), ("amp", ctypes.c_double)]
 
 
+class ServerConfig(ctypes.Structure):
+    _fields_ = [("device", ctypes.c_int32), ("max_jobs", ctypes.c_int32), ("hbm_budget_bytes", ctypes.c_uint64),
+                ("pulses_per_step", ctypes.c_int32), ("use_graphs", ctypes.c_int32)]
+
+
+class Job(ctypes.Structure):
+    _fields_ = [("radar", Radar), ("grid", Grid), ("echo", ctypes.c_void_p), ("apc", ctypes.c_void_p),
+                ("image", ctypes.c_void_p), ("np", ctypes.c_int32), ("ns", ctypes.c_int32),
+                ("mode", ctypes.c_int32), ("reserved", ctypes.c_int32)]
+
+
+class JobStats(ctypes.Structure):
+    _fields_ = [("status", ctypes.c_int32), ("steps", ctypes.c_int32), ("queued_ms", ctypes.c_double),
+                ("latency_ms", ctypes.c_double), ("updates", ctypes.c_double), ("device_bytes", ctypes.c_uint64)]
+
+
+class ServerStats(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_uint64) for n in ("submitted", "completed", "failed", "rejected", "cancelled",
+                                               "steps", "graph_launches")] + \
+               [("updates", ctypes.c_double), ("busy_s", ctypes.c_double), ("bytes_in_use", ctypes.c_uint64),
+                ("peak_bytes", ctypes.c_uint64), ("active", ctypes.c_int32), ("queued", ctypes.c_int32),
+                ("peak_active", ctypes.c_int32), ("reserved", ctypes.c_int32)]
+
+
 class RefParams(ctypes.Structure):
     """Byte layout of the reference's SARParams (code/SAR_BP/CUDA/BPA_CUDA.h:28-50)."""
     _fields_ = [(n, ctypes.c_float) for n in ("c", "fc", "lam", "Kr", "Tr", "Br", "Fr", "vr", "H", "La",
@@ -116,6 +140,14 @@ SIGNATURES = {
     "sarbp_synthesize_echo": ([ctypes.c_void_p, ctypes.POINTER(Radar), ctypes.c_void_p, ctypes.c_int32,
                                ctypes.c_int32, ctypes.c_void_p, ctypes.c_int32, ctypes.c_double, ctypes.c_uint64,
                                ctypes.c_void_p, ctypes.c_void_p], ctypes.c_int),
+    "sarbp_server_create": ([ctypes.POINTER(ctypes.c_void_p), ctypes.POINTER(ServerConfig)], ctypes.c_int),
+    "sarbp_server_destroy": ([ctypes.c_void_p], ctypes.c_int),
+    "sarbp_server_submit": ([ctypes.c_void_p, ctypes.POINTER(Job), ctypes.POINTER(ctypes.c_uint64)], ctypes.c_int),
+    "sarbp_server_poll": ([ctypes.c_void_p, ctypes.c_uint64], ctypes.c_int),
+    "sarbp_server_wait": ([ctypes.c_void_p, ctypes.c_uint64, ctypes.c_int32, ctypes.POINTER(JobStats)],
+                          ctypes.c_int),
+    "sarbp_server_cancel": ([ctypes.c_void_p, ctypes.c_uint64], ctypes.c_int),
+    "sarbp_server_get_stats": ([ctypes.c_void_p, ctypes.POINTER(ServerStats)], ctypes.c_int),
     "sarbp_launch_back_projection": ([ctypes.c_void_p, ctypes.c_void_p, ctypes.POINTER(RefParams),
                                       ctypes.c_int32, ctypes.c_int32], ctypes.c_int),
     "sarbp_launch_generate_echo": ([ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
@@ -325,3 +357,73 @@ def image_scene(ctx: Context, scene: scenes.Scene, echo, mode: int, image=None, 
 
 def nan_to_none(x):
     return None if x is None or (isinstance(x, float) and math.isnan(x)) else x
+
+
+class Server:
+    """Continuous-batching imaging service (sarbp_server_* in include/sarbp.h)."""
+
+    def __init__(self, device: int = 0, max_jobs: int = 16, hbm_budget_bytes: int = 64 << 30,
+                 pulses_per_step: int = 512, use_graphs: bool = True):
+        self.lib = load()
+        cfg = ServerConfig(device, max_jobs, hbm_budget_bytes, pulses_per_step, int(use_graphs))
+        h = ctypes.c_void_p()
+        st = self.lib.sarbp_server_create(ctypes.byref(h), ctypes.byref(cfg))
+        if st != OK:
+            raise SarbpError(st, f"sarbp_server_create: {self.lib.sarbp_status_string(st).decode()}")
+        self.h = h
+        self._keep = {}  # ticket -> buffers that must outlive the job
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.sarbp_server_destroy(self.h)
+            self.h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def submit(self, radar: Radar, grid: Grid, echo, apc, mode: int = MODE_SPLIT, image=None) -> int:
+        """echo: numpy complex64 [np][ns], or a (pinned) float32 tensor [np][2 ns]."""
+        if isinstance(echo, np.ndarray):
+            if echo.dtype != np.complex64 or echo.ndim != 2:
+                raise ValueError("echo must be complex64 [np][ns]")
+            np_, ns = echo.shape
+        else:
+            np_, ns = int(echo.shape[0]), int(echo.shape[1]) // 2
+        if image is None:
+            image = np.zeros((grid.ny, grid.nx), dtype=np.complex64)
+        apc = np.ascontiguousarray(apc, dtype=np.float64)
+        j = Job()
+        j.radar, j.grid = radar, grid
+        j.echo, j.apc, j.image = _ptr(echo), _ptr(apc), _ptr(image)
+        j.np, j.ns, j.mode = np_, ns, mode
+        t = ctypes.c_uint64()
+        st = self.lib.sarbp_server_submit(self.h, ctypes.byref(j), ctypes.byref(t))
+        if st != OK:
+            raise SarbpError(st, f"submit: {self.lib.sarbp_status_string(st).decode()}")
+        self._keep[t.value] = (echo, apc, image)
+        return t.value
+
+    def poll(self, ticket: int) -> int:
+        return self.lib.sarbp_server_poll(self.h, ticket)
+
+    def cancel(self, ticket: int) -> int:
+        return self.lib.sarbp_server_cancel(self.h, ticket)
+
+    def wait(self, ticket: int, timeout_ms: int = -1):
+        """Returns (status, JobStats, image)."""
+        s = JobStats()
+        st = self.lib.sarbp_server_wait(self.h, ticket, timeout_ms, ctypes.byref(s))
+        if st == ERR_TIMEOUT:
+            return st, s, None
+        _, _, image = self._keep.pop(ticket, (None, None, None))
+        return st, s, image
+
+    def stats(self) -> ServerStats:
+        s = ServerStats()
+        st = self.lib.sarbp_server_get_stats(self.h, ctypes.byref(s))
+        if st != OK:
+            raise SarbpError(st, "stats")
+        return s

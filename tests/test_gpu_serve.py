@@ -1,0 +1,108 @@
+"""Serving loop (sarbp_server_*): continuous batching of uneven imaging jobs.
+
+* A job's image is the same alone and in a mix (bit for bit: its launches and
+  their order do not depend on the other jobs), and matches the one-shot
+  sarbp_image result within -100 dB (only the sub-aperture summation order
+  differs).
+* Admission respects the device-memory budget; a job larger than the budget is
+  rejected at submit; queued jobs can be cancelled; admitted jobs overlap
+  (more than one resident at once) and steps run as CUDA graphs.
+"""
+import numpy as np
+import pytest
+
+from sar_cambrianaccelerationcard_gb300 import metrics, sarbp, scenes
+
+pytestmark = pytest.mark.gpu
+
+
+def job_scene(np_, ns, n_img, seed):
+    s = scenes.config1(np_=np_, ns=ns, n_img=n_img, seed=seed, snr_db=20.0)
+    return s
+
+
+@pytest.fixture(scope="module")
+def jobs():
+    ctx = sarbp.Context(0)
+    specs = [(512, 1024, 256, 11), (256, 2048, 128, 12), (768, 1024, 320, 13), (320, 1536, 200, 14),
+             (512, 1024, 96, 15)]
+    out = []
+    for np_, ns, n, seed in specs:
+        s = job_scene(np_, ns, n, seed)
+        echo = sarbp.synthesize(ctx, s)
+        one_shot = sarbp.image_scene(ctx, s, echo, sarbp.MODE_SPLIT)
+        out.append((s, echo, one_shot))
+    ctx.close()
+    return out
+
+
+def submit(srv, s, echo, mode=sarbp.MODE_SPLIT):
+    r, g, _ = sarbp.scene_args(s)
+    return srv.submit(r, g, echo, s.apc, mode)
+
+
+def test_alone_equals_in_mix(jobs):
+    s0, e0, one_shot = jobs[0]
+    with sarbp.Server(0, max_jobs=8, hbm_budget_bytes=8 << 30, pulses_per_step=128) as srv:
+        t = submit(srv, s0, e0)
+        st, stats, alone = srv.wait(t)
+        assert st == sarbp.OK and stats.steps == 4
+        tickets = [submit(srv, s, e) for (s, e, _) in jobs[1:3]]
+        t0 = submit(srv, s0, e0)
+        tickets += [submit(srv, s, e) for (s, e, _) in jobs[3:]]
+        st, _, mixed = srv.wait(t0)
+        assert st == sarbp.OK
+        others = [srv.wait(t) for t in tickets]
+        assert all(o[0] == sarbp.OK for o in others)
+        stat = srv.stats()
+        assert stat.peak_active >= 2, "jobs overlapped on the device"
+        assert stat.graph_launches > 0
+    assert np.array_equal(alone, mixed)
+    assert metrics.rel_l2_db(alone, one_shot) <= -100.0
+    # every job in the mix matches its one-shot image
+    for (s, e, ref), (st, _, img) in zip([jobs[1], jobs[2], jobs[3], jobs[4]], others):
+        assert metrics.rel_l2_db(img, ref) <= -100.0
+
+
+def test_fp16_storage_jobs(jobs):
+    s, e, _ = jobs[1]
+    ctx = sarbp.Context(0)
+    ref = sarbp.image_scene(ctx, s, e, sarbp.MODE_FP16STORE)
+    ctx.close()
+    with sarbp.Server(0, max_jobs=2, hbm_budget_bytes=4 << 30, pulses_per_step=64) as srv:
+        st, _, img = srv.wait(submit(srv, s, e, sarbp.MODE_FP16STORE))
+    assert st == sarbp.OK
+    assert metrics.rel_l2_db(img, ref) <= -100.0
+
+
+def test_budget_admission_and_rejection(jobs):
+    s, e, ref = jobs[0]
+    with sarbp.Server(0, max_jobs=8, hbm_budget_bytes=8 << 30, pulses_per_step=128) as probe:
+        t = submit(probe, s, e)
+        _, stats, _ = probe.wait(t)
+    one = stats.device_bytes
+    # room for one job at a time: the second waits for the first to finish
+    with sarbp.Server(0, max_jobs=8, hbm_budget_bytes=int(one * 1.5), pulses_per_step=128) as srv:
+        ts = [submit(srv, s, e) for _ in range(3)]
+        res = [srv.wait(t) for t in ts]
+        assert all(r[0] == sarbp.OK for r in res)
+        st = srv.stats()
+        assert st.peak_active == 1 and st.peak_bytes <= int(one * 1.5)
+        assert all(np.array_equal(r[2], res[0][2]) for r in res)
+    with sarbp.Server(0, max_jobs=2, hbm_budget_bytes=one // 2) as srv:
+        with pytest.raises(sarbp.SarbpError) as err:
+            submit(srv, s, e)
+        assert err.value.status == sarbp.ERR_BUDGET
+
+
+def test_cancel_and_poll(jobs):
+    s, e, _ = jobs[0]
+    with sarbp.Server(0, max_jobs=1, hbm_budget_bytes=8 << 30, pulses_per_step=16) as srv:
+        a = submit(srv, s, e)
+        b = submit(srv, s, e)
+        assert srv.cancel(b) in (sarbp.OK, sarbp.ERR_NOT_READY)
+        st_b, _, _ = srv.wait(b)
+        st_a, _, _ = srv.wait(a)
+        assert st_a == sarbp.OK
+        assert st_b in (sarbp.OK, sarbp.ERR_CANCELLED)
+        assert srv.poll(a) == sarbp.ERR_INVALID_ARGUMENT  # released by wait
