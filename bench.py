@@ -51,6 +51,10 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-probe", action="store_true", help="skip the issue-rate probe (profiling runs)")
+    ap.add_argument("--serve", action="store_true",
+                    help="serving stream (config 4): Poisson arrivals at swept rates, p50/p99 latency")
+    ap.add_argument("--rates", default="10,20,30,40", help="arrival rates (jobs/s) for --serve")
+    ap.add_argument("--jobs", type=int, default=60, help="jobs per rate for --serve")
     return ap.parse_args()
 
 
@@ -365,10 +369,100 @@ def run_ours(args):
     return 0
 
 
+def serve_requests(ctx, n_req, seed=4):
+    """Config-4 request pool: aperture U[256, 8192] pulses x U[2048, 8192] samples,
+    grid side log-uniform in [256, 4096], 9-200 targets, 20 dB SNR."""
+    import torch
+    from sar_cambrianaccelerationcard_gb300 import sarbp, scenes
+    rng = np.random.default_rng(seed)
+    reqs = []
+    for i in range(n_req):
+        np_ = int(rng.integers(256, 8193)) // 16 * 16
+        ns = int(rng.integers(2048, 8193)) // 4 * 4
+        side = int(round(math.exp(rng.uniform(math.log(256), math.log(4096))))) // 32 * 32
+        nt = int(rng.integers(9, 201))
+        radar = scenes.Radar()
+        grid = scenes.centred_grid(radar, side, side, 0.25)
+        sc = scenes.Scene(name=f"req{i}", radar=radar, np_=np_, ns=ns, apc=scenes.straight_track(radar, np_),
+                          grid=grid, targets=scenes.random_targets(grid, nt, seed + 1000 + i),
+                          t_rec0=scenes.centred_record_start(radar, ns), snr_db=20.0, seed=seed + 1000 + i)
+        dev = torch.empty((np_, ns * 2), dtype=torch.float32, device="cuda")
+        sarbp.synthesize(ctx, sc, out=dev)
+        ctx.synchronize()
+        host = torch.empty((np_, ns * 2), dtype=torch.float32, pin_memory=True)
+        host.copy_(dev)
+        img = torch.empty((side, side * 2), dtype=torch.float32, pin_memory=True)
+        reqs.append((sc, host, img))
+        del dev
+    return reqs
+
+
+def run_serve(args):
+    """Serving stream: a submitter thread draws Poisson arrivals and submits
+    requests to one sarbp server; latency is submit -> image in host memory."""
+    import threading
+    import torch
+    from sar_cambrianaccelerationcard_gb300 import sarbp
+    torch.cuda.set_device(0)
+    ctx = sarbp.Context(0)
+    reqs = serve_requests(ctx, 24)
+    ctx.close()
+    torch.cuda.empty_cache()
+    out = []
+    for rate in [float(r) for r in args.rates.split(",")]:
+        srv = sarbp.Server(0, max_jobs=16, hbm_budget_bytes=96 << 30, pulses_per_step=512)
+        rng = np.random.default_rng(int(rate * 1000))
+        order = rng.integers(0, len(reqs), args.jobs)
+        gaps = rng.exponential(1.0 / rate, args.jobs)
+        tickets = []
+        t_first = time.perf_counter()
+
+        def submitter():
+            t_next = time.perf_counter()
+            for k in range(args.jobs):
+                t_next += gaps[k]
+                d = t_next - time.perf_counter()
+                if d > 0:
+                    time.sleep(d)
+                sc, host, img = reqs[order[k]]
+                r, g, _ = sarbp.scene_args(sc)
+                tickets.append(srv.submit(r, g, host, sc.apc, sarbp.MODE_SPLIT, image=img))
+
+        th = threading.Thread(target=submitter)
+        th.start()
+        th.join()
+        lat, upd = [], 0.0
+        for t in tickets:
+            st, js, _ = srv.wait(t, 600000)
+            if st == sarbp.OK:
+                lat.append(js.latency_ms)
+                upd += js.updates
+        t_last = time.perf_counter()
+        stats = srv.stats()
+        srv.close()
+        lat.sort()
+        pct = lambda q: lat[min(len(lat) - 1, int(q * len(lat)))] if lat else None
+        out.append({"rate_jobs_s": rate, "jobs": len(lat), "p50_ms": pct(0.50), "p99_ms": pct(0.99),
+                    "mean_ms": sum(lat) / len(lat) if lat else None,
+                    "gpix_pulse_s": upd / (t_last - t_first) / 1e9,
+                    "busy_gpix_pulse_s": stats.updates / max(stats.busy_s, 1e-9) / 1e9,
+                    "peak_active": stats.peak_active, "graph_launches": stats.graph_launches,
+                    "peak_gb": stats.peak_bytes / 2**30})
+    line = {"metric": "serving p50/p99 latency and aggregate Gpix*pulse/s", "mode": "split",
+            "workload": "config 4: Poisson arrivals, 256-8192 pulses x 2048-8192 samples, grids 256^2-4096^2 "
+                        "log-uniform at 0.25 m, 9-200 targets, 20 dB SNR; 24 distinct requests drawn at random",
+            "server": {"max_jobs": 16, "hbm_budget_gb": 96, "pulses_per_step": 512, "graphs": True},
+            "sweep": out}
+    print(json.dumps(line))
+    return 0
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         return run_reference(args)
+    if args.serve:
+        return run_serve(args)
     return run_ours(args)
 
 

@@ -36,6 +36,12 @@ def jobs():
     return out
 
 
+def wait(srv, t):
+    res = srv.wait(t, 120000)
+    assert res[0] != sarbp.ERR_TIMEOUT, "job did not finish within 120 s"
+    return res
+
+
 def submit(srv, s, echo, mode=sarbp.MODE_SPLIT):
     r, g, _ = sarbp.scene_args(s)
     return srv.submit(r, g, echo, s.apc, mode)
@@ -45,14 +51,14 @@ def test_alone_equals_in_mix(jobs):
     s0, e0, one_shot = jobs[0]
     with sarbp.Server(0, max_jobs=8, hbm_budget_bytes=8 << 30, pulses_per_step=128) as srv:
         t = submit(srv, s0, e0)
-        st, stats, alone = srv.wait(t)
+        st, stats, alone = wait(srv, t)
         assert st == sarbp.OK and stats.steps == 4
         tickets = [submit(srv, s, e) for (s, e, _) in jobs[1:3]]
         t0 = submit(srv, s0, e0)
         tickets += [submit(srv, s, e) for (s, e, _) in jobs[3:]]
-        st, _, mixed = srv.wait(t0)
+        st, _, mixed = wait(srv, t0)
         assert st == sarbp.OK
-        others = [srv.wait(t) for t in tickets]
+        others = [wait(srv, t) for t in tickets]
         assert all(o[0] == sarbp.OK for o in others)
         stat = srv.stats()
         assert stat.peak_active >= 2, "jobs overlapped on the device"
@@ -70,7 +76,7 @@ def test_fp16_storage_jobs(jobs):
     ref = sarbp.image_scene(ctx, s, e, sarbp.MODE_FP16STORE)
     ctx.close()
     with sarbp.Server(0, max_jobs=2, hbm_budget_bytes=4 << 30, pulses_per_step=64) as srv:
-        st, _, img = srv.wait(submit(srv, s, e, sarbp.MODE_FP16STORE))
+        st, _, img = wait(srv, submit(srv, s, e, sarbp.MODE_FP16STORE))
     assert st == sarbp.OK
     assert metrics.rel_l2_db(img, ref) <= -100.0
 
@@ -79,12 +85,12 @@ def test_budget_admission_and_rejection(jobs):
     s, e, ref = jobs[0]
     with sarbp.Server(0, max_jobs=8, hbm_budget_bytes=8 << 30, pulses_per_step=128) as probe:
         t = submit(probe, s, e)
-        _, stats, _ = probe.wait(t)
+        _, stats, _ = wait(probe, t)
     one = stats.device_bytes
     # room for one job at a time: the second waits for the first to finish
     with sarbp.Server(0, max_jobs=8, hbm_budget_bytes=int(one * 1.5), pulses_per_step=128) as srv:
         ts = [submit(srv, s, e) for _ in range(3)]
-        res = [srv.wait(t) for t in ts]
+        res = [wait(srv, t) for t in ts]
         assert all(r[0] == sarbp.OK for r in res)
         st = srv.stats()
         assert st.peak_active == 1 and st.peak_bytes <= int(one * 1.5)
@@ -101,8 +107,8 @@ def test_cancel_and_poll(jobs):
         a = submit(srv, s, e)
         b = submit(srv, s, e)
         assert srv.cancel(b) in (sarbp.OK, sarbp.ERR_NOT_READY)
-        st_b, _, _ = srv.wait(b)
-        st_a, _, _ = srv.wait(a)
+        st_b, _, _ = wait(srv, b)
+        st_a, _, _ = wait(srv, a)
         assert st_a == sarbp.OK
         assert st_b in (sarbp.OK, sarbp.ERR_CANCELLED)
         assert srv.poll(a) == sarbp.ERR_INVALID_ARGUMENT  # released by wait
