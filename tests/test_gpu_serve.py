@@ -24,8 +24,10 @@ def job_scene(np_, ns, n_img, seed):
 @pytest.fixture(scope="module")
 def jobs():
     ctx = sarbp.Context(0)
-    specs = [(512, 1024, 256, 11), (256, 2048, 128, 12), (768, 1024, 320, 13), (320, 1536, 200, 14),
-             (512, 1024, 96, 15)]
+    # large enough (~1e10 pixel*pulse updates, several ms each) that jobs are
+    # still resident when the next submissions arrive
+    specs = [(1024, 2048, 1024, 11), (2048, 2048, 2048, 12), (1536, 4096, 1536, 13), (2048, 1024, 2048, 14),
+             (1024, 1024, 512, 15)]
     out = []
     for np_, ns, n, seed in specs:
         s = job_scene(np_, ns, n, seed)
@@ -52,7 +54,7 @@ def test_alone_equals_in_mix(jobs):
     with sarbp.Server(0, max_jobs=8, hbm_budget_bytes=8 << 30, pulses_per_step=128) as srv:
         t = submit(srv, s0, e0)
         st, stats, alone = wait(srv, t)
-        assert st == sarbp.OK and stats.steps == 4
+        assert st == sarbp.OK and stats.steps == 8
         tickets = [submit(srv, s, e) for (s, e, _) in jobs[1:3]]
         t0 = submit(srv, s0, e0)
         tickets += [submit(srv, s, e) for (s, e, _) in jobs[3:]]
