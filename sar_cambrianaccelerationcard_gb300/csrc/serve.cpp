@@ -8,17 +8,19 @@
 //     segments) and build the range-compression tables on the host, compute
 //     the device footprint, queue the job;
 //   * admission (worker): in arrival order, every queued job that fits the
-//     free budget and a free slot is admitted -- device buffers come from the
-//     stream-ordered pool, the echo and APC track are uploaded, the echo is
-//     range-compressed into the job's resident buffer;
+//     free budget and a free slot is admitted -- on an admission stream that
+//     runs beside the steps, device buffers come from the stream-ordered pool,
+//     the echo and APC track are uploaded and the echo is range-compressed
+//     into the job's resident buffer; the job joins the steps once that work
+//     has completed;
 //   * steps (worker): each step back-projects the next pulses_per_step pulses
 //     of every admitted job into its resident image (accumulate after the
 //     first step).  The step's launches are captured into one CUDA graph with
 //     a branch per job on its own lane stream, so jobs overlap on the device;
 //     at most two steps are in flight;
-//   * completion: after a job's last step its image is copied back and an
-//     event recorded; when the event completes the job's memory returns to the
-//     budget and waiters are released.
+//   * completion: after a job's last step its image is copied back on a
+//     download stream and an event recorded; when the event completes the
+//     job's memory returns to the budget and waiters are released.
 // Every job is computed by the same launches in the same order whatever else
 // runs beside it, so its image does not depend on the mix.
 #include <cuda_runtime.h>
@@ -47,7 +49,7 @@ double ms_between(Clock::time_point a, Clock::time_point b) {
 
 size_t align256(size_t v) { return (v + 255) & ~size_t(255); }
 
-enum class JobState { Queued, Active, Finishing, Done, Failed, Cancelled };
+enum class JobState { Queued, Loading, Active, Finishing, Done, Failed, Cancelled };
 
 struct Job {
     uint64_t id = 0;
@@ -71,6 +73,7 @@ struct Job {
     int next_pulse = 0;
     int steps = 0;
     cudaEvent_t done_ev = nullptr;
+    cudaEvent_t ready_ev = nullptr;  // echo uploaded and range-compressed
     JobState state = JobState::Queued;
     sarbp_status status = SARBP_OK;
     std::string msg;
@@ -91,7 +94,9 @@ struct sarbp_server {
     std::map<uint64_t, Job *> jobs;       // every unreleased ticket
     uint64_t next_id = 1;
     size_t in_use = 0;
-    cudaStream_t s0 = nullptr;
+    cudaStream_t s0 = nullptr;            // back-projection steps (graphs)
+    cudaStream_t sa = nullptr;            // admission: allocation, upload, range compression
+    cudaStream_t sd = nullptr;            // image downloads and frees
     std::vector<cudaStream_t> lanes;
     std::vector<cudaEvent_t> join;        // one per lane
     cudaEvent_t fork = nullptr;
@@ -134,9 +139,10 @@ size_t job_bytes(const Job &j) {
     return b;
 }
 
-// Enqueue admission work for j on s0: carve buffers, upload, range-compress.
+// Enqueue admission work for j on the admission stream: carve buffers, upload,
+// range-compress, then record the job's ready event.
 sarbp_status admit(sarbp_server *S, Job *j) {
-    cudaError_t e = cudaMallocAsync((void **)&j->dev, j->bytes, S->s0);
+    cudaError_t e = cudaMallocAsync((void **)&j->dev, j->bytes, S->sa);
     if (e != cudaSuccess) {
         cudaGetLastError();
         return SARBP_ERR_OUT_OF_MEMORY;
@@ -159,13 +165,13 @@ sarbp_status admit(sarbp_server *S, Job *j) {
     j->d_filt = (float2 *)take(j->filt.size() * 8);
     j->d_etab = (float2 *)take(j->etab.size() * 8);
     j->d_err = (unsigned *)take(sizeof(unsigned));
-    e = cudaMemcpyAsync(j->d_echo, j->desc.echo, np * ns * 8, cudaMemcpyHostToDevice, S->s0);
-    if (e == cudaSuccess) e = cudaMemcpyAsync(j->d_apc, j->desc.apc, np * 24, cudaMemcpyHostToDevice, S->s0);
+    e = cudaMemcpyAsync(j->d_echo, j->desc.echo, np * ns * 8, cudaMemcpyHostToDevice, S->sa);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(j->d_apc, j->desc.apc, np * 24, cudaMemcpyHostToDevice, S->sa);
     if (e == cudaSuccess)
-        e = cudaMemcpyAsync(j->d_filt, j->filt.data(), j->filt.size() * 8, cudaMemcpyHostToDevice, S->s0);
+        e = cudaMemcpyAsync(j->d_filt, j->filt.data(), j->filt.size() * 8, cudaMemcpyHostToDevice, S->sa);
     if (e == cudaSuccess)
-        e = cudaMemcpyAsync(j->d_etab, j->etab.data(), j->etab.size() * 8, cudaMemcpyHostToDevice, S->s0);
-    if (e == cudaSuccess) e = cudaMemsetAsync(j->d_err, 0, sizeof(unsigned), S->s0);
+        e = cudaMemcpyAsync(j->d_etab, j->etab.data(), j->etab.size() * 8, cudaMemcpyHostToDevice, S->sa);
+    if (e == cudaSuccess) e = cudaMemsetAsync(j->d_err, 0, sizeof(unsigned), S->sa);
     for (size_t p0 = 0; e == cudaSuccess && p0 < np; p0 += S->spec_rows) {
         sarbp::RcPlan rp;
         rp.np = (int)std::min(S->spec_rows, np - p0);
@@ -175,11 +181,12 @@ sarbp_status admit(sarbp_server *S, Job *j) {
         rp.nbins = (int)nb;
         rp.storage = j->storage;
         float *sc = j->storage == SARBP_STORE_C32H ? j->d_scale + p0 : nullptr;
-        e = sarbp::launch_rc_forward(rp, j->d_echo + p0 * ns, j->d_filt, j->d_etab, S->d_spec, sc, S->s0);
+        e = sarbp::launch_rc_forward(rp, j->d_echo + p0 * ns, j->d_filt, j->d_etab, S->d_spec, sc, S->sa);
         if (e == cudaSuccess)
             e = sarbp::launch_rc_inverse(rp, S->d_spec, j->d_etab, sc,
-                                         static_cast<char *>(j->d_rc) + p0 * nb * j->esize, S->s0);
+                                         static_cast<char *>(j->d_rc) + p0 * nb * j->esize, S->sa);
     }
+    if (e == cudaSuccess) e = cudaEventRecord(j->ready_ev, S->sa);
     if (e != cudaSuccess) {
         cudaGetLastError();
         return SARBP_ERR_CUDA;
@@ -208,7 +215,7 @@ cudaError_t launch_step(Job *j, int p0, int p1, cudaStream_t s) {
 }
 
 void release(sarbp_server *S, Job *j) {
-    if (j->dev) cudaFreeAsync(j->dev, S->s0);
+    if (j->dev) cudaFreeAsync(j->dev, S->sd);  // after the download, which waited for the last step
     j->dev = nullptr;
     S->in_use -= j->bytes;
     if (j->lane >= 0) j->lane = -1;
@@ -240,6 +247,8 @@ void worker_main(sarbp_server *S) {
                 ++it;
             }
         }
+        for (Job *j : S->active)
+            if (j->state == JobState::Loading && cudaEventQuery(j->ready_ev) == cudaSuccess) j->state = JobState::Active;
         if (S->active.empty() && S->busy) {
             S->st.busy_s += std::chrono::duration<double>(Clock::now() - S->busy_since).count();
             S->busy = false;
@@ -258,7 +267,7 @@ void worker_main(sarbp_server *S) {
             const sarbp_status st = admit(S, j);
             if (st != SARBP_OK) {
                 fail_job(j, st, "admission failed");
-                if (j->dev) cudaFreeAsync(j->dev, S->s0);
+                if (j->dev) cudaFreeAsync(j->dev, S->sa);
                 j->dev = nullptr;
                 S->st.failed++;
                 S->cv_done.notify_all();
@@ -266,7 +275,7 @@ void worker_main(sarbp_server *S) {
             }
             lane_busy[lane] = true;
             j->lane = lane;
-            j->state = JobState::Active;
+            j->state = JobState::Loading;
             j->t_admit = Clock::now();
             S->in_use += j->bytes;
             S->st.peak_bytes = std::max<uint64_t>(S->st.peak_bytes, S->in_use);
@@ -326,6 +335,9 @@ void worker_main(sarbp_server *S) {
                 if (g) cudaGraphDestroy(g);
             }
             S->st.steps++;
+            if (e != cudaSuccess) cudaGetLastError();
+            cudaEventRecord(S->step_ev[par], S->s0);
+            bool waited = false;
             for (Job *j : step) {
                 if (e != cudaSuccess) {
                     fail_job(j, SARBP_ERR_CUDA, cudaGetErrorString(e));
@@ -333,18 +345,19 @@ void worker_main(sarbp_server *S) {
                 }
                 j->steps++;
                 j->next_pulse = std::min(j->desc.np, j->next_pulse + pps);
-                if (j->next_pulse >= j->desc.np) {  // last step: copy the image back
+                if (j->next_pulse >= j->desc.np) {  // last step: copy the image back on the download stream
                     const size_t npix = (size_t)j->desc.grid.nx * j->desc.grid.ny;
-                    cudaError_t ce = cudaMemcpyAsync(j->desc.image, j->d_img, npix * 8, cudaMemcpyDeviceToHost, S->s0);
+                    cudaError_t ce = waited ? cudaSuccess : cudaStreamWaitEvent(S->sd, S->step_ev[par], 0);
+                    waited = true;
                     if (ce == cudaSuccess)
-                        ce = cudaMemcpyAsync(j->h_err, j->d_err, sizeof(unsigned), cudaMemcpyDeviceToHost, S->s0);
-                    if (ce == cudaSuccess) ce = cudaEventRecord(j->done_ev, S->s0);
+                        ce = cudaMemcpyAsync(j->desc.image, j->d_img, npix * 8, cudaMemcpyDeviceToHost, S->sd);
+                    if (ce == cudaSuccess)
+                        ce = cudaMemcpyAsync(j->h_err, j->d_err, sizeof(unsigned), cudaMemcpyDeviceToHost, S->sd);
+                    if (ce == cudaSuccess) ce = cudaEventRecord(j->done_ev, S->sd);
                     if (ce != cudaSuccess) fail_job(j, SARBP_ERR_CUDA, cudaGetErrorString(ce));
                     else j->state = JobState::Finishing;
                 }
             }
-            if (e != cudaSuccess) cudaGetLastError();
-            cudaEventRecord(S->step_ev[par], S->s0);
             S->step_pending[par] = true;
             S->step_parity ^= 1;
             // failed jobs leave the active set
@@ -352,6 +365,7 @@ void worker_main(sarbp_server *S) {
                 Job *j = *it;
                 if (j->state == JobState::Failed) {
                     cudaStreamSynchronize(S->s0);
+                    cudaStreamWaitEvent(S->sd, S->step_ev[par], 0);
                     lane_busy[j->lane] = false;
                     release(S, j);
                     S->st.failed++;
@@ -366,12 +380,12 @@ void worker_main(sarbp_server *S) {
         // 4. nothing to launch: wait for a completion, new work or stop
         Job *oldest = nullptr;
         for (Job *j : S->active)
-            if (j->state == JobState::Finishing) {
+            if (j->state == JobState::Finishing || j->state == JobState::Loading) {
                 oldest = j;
                 break;
             }
         if (oldest) {
-            cudaEvent_t ev = oldest->done_ev;
+            cudaEvent_t ev = oldest->state == JobState::Loading ? oldest->ready_ev : oldest->done_ev;
             lk.unlock();
             cudaEventSynchronize(ev);
             lk.lock();
@@ -406,7 +420,9 @@ sarbp_status sarbp_server_create(sarbp_server **out, const sarbp_server_config *
     S->cfg = *cfg;
     if (S->cfg.pulses_per_step == 0) S->cfg.pulses_per_step = 512;
     S->sms = prop.multiProcessorCount;
-    bool ok = cudaStreamCreateWithFlags(&S->s0, cudaStreamNonBlocking) == cudaSuccess;
+    bool ok = cudaStreamCreateWithFlags(&S->s0, cudaStreamNonBlocking) == cudaSuccess &&
+              cudaStreamCreateWithFlags(&S->sa, cudaStreamNonBlocking) == cudaSuccess &&
+              cudaStreamCreateWithFlags(&S->sd, cudaStreamNonBlocking) == cudaSuccess;
     S->lanes.resize(S->cfg.max_jobs);
     S->join.resize(S->cfg.max_jobs);
     for (int i = 0; ok && i < S->cfg.max_jobs; ++i) {
@@ -450,10 +466,12 @@ sarbp_status sarbp_server_destroy(sarbp_server *S) {
     S->cv_work.notify_all();
     if (S->worker.joinable()) S->worker.join();
     cudaSetDevice(S->cfg.device);
-    if (S->s0) cudaStreamSynchronize(S->s0);
+    for (cudaStream_t st : {S->sa, S->s0, S->sd})
+        if (st) cudaStreamSynchronize(st);
     for (auto &kv : S->jobs) {
         Job *j = kv.second;
         if (j->done_ev) cudaEventDestroy(j->done_ev);
+        if (j->ready_ev) cudaEventDestroy(j->ready_ev);
         if (j->h_err) cudaFreeHost(j->h_err);
         delete j;
     }
@@ -466,7 +484,8 @@ sarbp_status sarbp_server_destroy(sarbp_server *S) {
     if (S->fork) cudaEventDestroy(S->fork);
     for (cudaEvent_t e : S->step_ev)
         if (e) cudaEventDestroy(e);
-    if (S->s0) cudaStreamDestroy(S->s0);
+    for (cudaStream_t st : {S->s0, S->sa, S->sd})
+        if (st) cudaStreamDestroy(st);
     delete S;
     return SARBP_OK;
 }
@@ -514,9 +533,11 @@ sarbp_status sarbp_server_submit(sarbp_server *S, const sarbp_job *job, uint64_t
     }
     cudaSetDevice(S->cfg.device);
     if (cudaEventCreateWithFlags(&j->done_ev, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&j->ready_ev, cudaEventDisableTiming) != cudaSuccess ||
         cudaMallocHost(&j->h_err, sizeof(unsigned)) != cudaSuccess) {
         cudaGetLastError();
         if (j->done_ev) cudaEventDestroy(j->done_ev);
+        if (j->ready_ev) cudaEventDestroy(j->ready_ev);
         delete j;
         return SARBP_ERR_CUDA;
     }
@@ -526,6 +547,7 @@ sarbp_status sarbp_server_submit(sarbp_server *S, const sarbp_job *job, uint64_t
         std::lock_guard<std::mutex> lk(S->mu);
         if (S->stop) {
             cudaEventDestroy(j->done_ev);
+            cudaEventDestroy(j->ready_ev);
             cudaFreeHost(j->h_err);
             delete j;
             return SARBP_ERR_CANCELLED;
@@ -581,6 +603,7 @@ sarbp_status sarbp_server_wait(sarbp_server *S, uint64_t ticket, int32_t timeout
     S->jobs.erase(it);
     lk.unlock();
     if (j->done_ev) cudaEventDestroy(j->done_ev);
+    if (j->ready_ev) cudaEventDestroy(j->ready_ev);
     if (j->h_err) cudaFreeHost(j->h_err);
     delete j;
     return st;
