@@ -167,7 +167,7 @@ sarbp_status sarbp_range_compress(sarbp_ctx *ctx, const sarbp_radar *radar,
  * capture.  Calls share the array: calls that overlap on the GPU race.
  * Returns SARBP_ERR_UNSUPPORTED when the tables and one pulse spectrum,
  * 8*(2*nfft + 256 + upsample*nfft/256) bytes, exceed the array (the FFT itself
- * is limited to nfft <= 16384, which always fits). */
+ * is limited to nfft <= 32768, which always fits). */
 #define SARBP_NOALLOC_SCRATCH_BYTES (4u << 20)
 sarbp_status sarbp_range_compress_noalloc(const sarbp_radar *radar, const sarbp_complex64 *echo,
                                           int32_t np, int32_t ns, int32_t storage, void *rc_out,

@@ -205,19 +205,22 @@ sarbp_status finish(sarbp_ctx *ctx, cudaStream_t s, bool sync) {
 sarbp_status rc_device(sarbp_ctx *ctx, const sarbp_radar *r, const sarbp_rc_layout &lay, const float2 *echo,
                        int np, int ns, int storage, void *rc_out, float *scale_out, cudaStream_t s) {
     if (!sarbp::rc_size_supported(lay.nfft))
-        return fail(ctx, SARBP_ERR_UNSUPPORTED, "range FFT size %d not supported (max 16384: ns + tp*fs - 1 <= 16384)",
+        return fail(ctx, SARBP_ERR_UNSUPPORTED, "range FFT size %d not supported (max 32768: ns + tp*fs - 1 <= 32768)",
                     lay.nfft);
     sarbp_status st = ensure_tables(ctx, r, lay);
     if (st != SARBP_OK) return st;
     const size_t row = sizeof(float2) * (size_t)lay.nfft;
     const int batch = (int)std::max<size_t>(1, std::min<size_t>((size_t)np, kSpecScratchBudget / row));
-    SARBP_CUDA(ctx, ctx->spec.ensure(row * (size_t)batch), "alloc spectrum scratch");
+    // spectra [batch][nfft], then the split path's per-half bounds [2 batch]
+    SARBP_CUDA(ctx, ctx->spec.ensure(row * (size_t)batch + sizeof(float) * 2 * (size_t)batch), "alloc spectrum scratch");
+    float *bound2 = reinterpret_cast<float *>(static_cast<char *>(ctx->spec.ptr) + row * (size_t)batch);
     float *scale = scale_out;
     if (storage == SARBP_STORE_C32H && !scale) return fail(ctx, SARBP_ERR_INVALID_ARGUMENT, "fp16 storage needs a scale array");
     const size_t esize = storage == SARBP_STORE_C64 ? 8 : 4;
     cudaEventRecord(ctx->ev[0], s);
     for (int p0 = 0; p0 < np; p0 += batch) {
-        RcPlan plan;
+        RcPlan plan{};
+        plan.bound2 = bound2;
         plan.np = std::min(batch, np - p0);
         plan.ns = ns;
         plan.nfft = lay.nfft;

@@ -31,7 +31,7 @@ namespace {
 
 constexpr size_t kScratchBytes = size_t(4) << 20;  // SARBP_NOALLOC_SCRATCH_BYTES
 constexpr int kMaxDevices = 64;
-constexpr int kMaxN = 16384;  // largest range FFT the kernels support
+constexpr int kMaxN = 32768;  // largest range FFT the kernels support
 constexpr int kMaxL = 16;
 
 static __device__ __align__(256) unsigned char g_rc_scratch[kScratchBytes];
@@ -129,7 +129,8 @@ extern "C" sarbp_status sarbp_range_compress_noalloc(const sarbp_radar *radar, c
     const size_t ne = (size_t)sarbp::rc_etab_size((int)L, (int)N);
     const size_t tables = sizeof(float2) * (N + ne);
     const size_t row = sizeof(float2) * N;
-    if (tables + row > kScratchBytes || N > (size_t)kMaxN || L > (size_t)kMaxL) return SARBP_ERR_UNSUPPORTED;
+    if (tables + row + 2 * sizeof(float) + 256 > kScratchBytes || N > (size_t)kMaxN || L > (size_t)kMaxL)
+        return SARBP_ERR_UNSUPPORTED;
     if (!on_device(echo) || !on_device(rc_out) || (storage == SARBP_STORE_C32H && !on_device(rc_scale_out)))
         return SARBP_ERR_INVALID_ARGUMENT;  // device memory only: a host buffer would need a staging copy
 
@@ -153,7 +154,9 @@ extern "C" sarbp_status sarbp_range_compress_noalloc(const sarbp_radar *radar, c
     float2 *d_etab = d_filt + N;
     float2 *d_spec = reinterpret_cast<float2 *>(base + ((tables + 255) & ~size_t(255)));
     const size_t spec_bytes = kScratchBytes - ((tables + 255) & ~size_t(255));
-    const int batch = (int)std::max<size_t>(1, std::min<size_t>((size_t)np, spec_bytes / row));
+    // per pulse: one spectrum row and two split-path bounds
+    const int batch = (int)std::max<size_t>(1, std::min<size_t>((size_t)np, spec_bytes / (row + 2 * sizeof(float))));
+    float *d_bound2 = reinterpret_cast<float *>(reinterpret_cast<char *>(d_spec) + row * (size_t)batch);
 
     TableKey key;
     key.nfft = lay.nfft;
@@ -182,7 +185,8 @@ extern "C" sarbp_status sarbp_range_compress_noalloc(const sarbp_radar *radar, c
     const size_t esize = storage == SARBP_STORE_C64 ? 8 : 4;
     const float2 *e2 = reinterpret_cast<const float2 *>(echo);
     for (int p0 = 0; p0 < np; p0 += batch) {
-        sarbp::RcPlan plan;
+        sarbp::RcPlan plan{};
+        plan.bound2 = d_bound2;
         plan.np = std::min(batch, np - p0);
         plan.ns = ns;
         plan.nfft = lay.nfft;

@@ -22,6 +22,15 @@
 // read from a two-level table held in shared memory, E^m = T_hi[m >> 8] *
 // T_lo[m & 255] (tables computed in double precision on the host), so no
 // FFT stage touches global memory.
+//
+// N = 32768 (shared memory holds 16384 points) is split by one radix-2 stage:
+// the forward runs two CTAs per pulse on the half-size inputs x[n] + x[n+M] and
+// (x[n] - x[n+M]) W_N^n, giving the even and odd spectral bins; the inverse
+// runs a 2-CTA cluster per (pulse, phase) on the even and odd bins and forms
+// y[i] = A[i] + W_N^{-i} B[i], y[i+M] = A[i] - W_N^{-i} B[i] with the partner's
+// half read through distributed shared memory.
+#include <cooperative_groups.h>
+
 #include "sarbp_internal.h"
 
 namespace sarbp {
@@ -42,11 +51,17 @@ __device__ __forceinline__ float2 mulj(float2 a) {
 __device__ __forceinline__ int pad(int i) { return i + (i >> 3); }
 __host__ __device__ constexpr int padded(int n) { return n + (n >> 3); }
 
+// table slot of entry i: one spare slot per 8 entries, so the strided gathers
+// of the later FFT stages (index steps of 8, 32, 256) spread over the banks
+__device__ __forceinline__ int tslot(int i) { return i + (i >> 3); }
+
 // E^m = e^{+j 2 pi m / (L N)} from the two-level shared-memory table
 struct Etab {
-    const float2 *lo;  // [256] (or L N entries when L N < 256)
-    const float2 *hi;  // [max(1, L N / 256)]
-    __device__ __forceinline__ float2 operator()(int m) const { return cmul(hi[m >> 8], lo[m & 255]); }
+    const float2 *lo;  // E^i, i < 256 (or L N entries when L N < 256), slot tslot(i)
+    const float2 *hi;  // E^{256 i}, i < max(1, L N / 256), slot tslot(i)
+    __device__ __forceinline__ float2 operator()(int m) const {
+        return cmul(hi[tslot(m >> 8)], lo[tslot(m & 255)]);
+    }
 };
 
 template <int R, bool INV>
@@ -121,13 +136,26 @@ __device__ __forceinline__ void stage(float2 *s, const Etab &E, int L, int Ns) {
         if (PER * T == NB || j < NB) {
             const int k = j & (Ns - 1);
             if (Ns > 1) {
-                const int step = N / (Ns * R);
-#pragma unroll
-                for (int r = 1; r < R; ++r) {
-                    float2 w = E(L * (k * r * step));  // W_N^{k r step}, forward: conjugate
-                    if (!INV) w.y = -w.y;
-                    v[b][r] = cmul(v[b][r], w);
+                // twiddles W_N^{k r step}, r = 1..R-1 (forward: conjugated): w, w^2 and
+                // w^4 from the table, the others as products
+                const int m1 = L * (k * (N / (Ns * R)));
+                float2 w[R];
+                w[1] = E(m1);
+                if (!INV) w[1].y = -w[1].y;
+                if (R >= 4) {
+                    w[2] = E(2 * m1);
+                    if (!INV) w[2].y = -w[2].y;
+                    w[3] = cmul(w[1], w[2]);
                 }
+                if (R >= 8) {
+                    w[4] = E(4 * m1);
+                    if (!INV) w[4].y = -w[4].y;
+                    w[5] = cmul(w[1], w[4]);
+                    w[6] = cmul(w[2], w[4]);
+                    w[7] = cmul(w[3], w[4]);
+                }
+#pragma unroll
+                for (int r = 1; r < R; ++r) v[b][r] = cmul(v[b][r], w[r]);
             }
             Dft<R, INV>::run(v[b]);
             const int base = (j - k) * R + k;
@@ -171,9 +199,9 @@ __device__ __forceinline__ Etab load_etab(float2 *sm, const float2 *__restrict__
     const int nlo = LN < 256 ? LN : 256;
     const int nhi = LN < 256 ? 1 : LN / 256;
     float2 *lo = sm + padded(N);
-    float2 *hi = lo + 256;
-    for (int i = threadIdx.x; i < nlo; i += T) lo[i] = __ldg(&etab[i]);
-    for (int i = threadIdx.x; i < nhi; i += T) hi[i] = __ldg(&etab[256 + i]);
+    float2 *hi = lo + 288;
+    for (int i = threadIdx.x; i < nlo; i += T) lo[tslot(i)] = __ldg(&etab[i]);
+    for (int i = threadIdx.x; i < nhi; i += T) hi[tslot(i)] = __ldg(&etab[256 + i]);
     return Etab{lo, hi};
 }
 
@@ -261,6 +289,106 @@ __global__ void __launch_bounds__(T) rc_inverse_kernel(int ns, int L, int nbins,
     }
 }
 
+namespace cg = cooperative_groups;
+
+// N = 2M forward: CTA pair (h = 0, 1) per pulse; h = 0 yields X[2k], h = 1 X[2k+1].
+// bound2[2p + h] receives the CTA's part of sum_k |Y[k]|.
+template <int M, int T>
+__global__ void __launch_bounds__(T) rc_forward2_kernel(int ns, int L, const float2 *__restrict__ echo,
+                                                        const float2 *__restrict__ filt,
+                                                        const float2 *__restrict__ etab,
+                                                        float2 *__restrict__ spec, float *__restrict__ bound2) {
+    extern __shared__ float2 sm[];
+    __shared__ float red[32];
+    const int h = blockIdx.x & 1, p = blockIdx.x >> 1;
+    const Etab E = load_etab<M, T>(sm, etab, 2 * L);
+    __syncthreads();
+    const float2 *row = echo + (size_t)p * ns;
+    for (int i = threadIdx.x; i < M; i += T) {
+        const float2 a = i < ns ? __ldg(&row[i]) : make_float2(0.f, 0.f);
+        const float2 b = i + M < ns ? __ldg(&row[i + M]) : make_float2(0.f, 0.f);
+        float2 v;
+        if (h == 0) {
+            v = cadd(a, b);
+        } else {
+            float2 w = E(L * i);  // W_N^i = conj(E^{L i})
+            w.y = -w.y;
+            v = cmul(csub(a, b), w);
+        }
+        sm[pad(i)] = v;
+    }
+    __syncthreads();
+    fft_smem<M, T, false>(sm, E, 2 * L);
+    float2 *out = spec + (size_t)p * (2 * M);
+    float acc = 0.f;
+    for (int k = threadIdx.x; k < M; k += T) {
+        const int idx = 2 * k + h;
+        const float2 y = cmul(sm[pad(k)], __ldg(&filt[idx]));
+        out[idx] = y;
+        acc += sqrtf(fmaf(y.x, y.x, y.y * y.y));
+    }
+    const float bound = block_sum<T>(acc, red);
+    if (threadIdx.x == 0) bound2[2 * p + h] = bound;
+}
+
+// N = 2M inverse: cluster of two CTAs per (pulse, phase r).  CTA h transforms
+// the bins 2k + h, then each CTA writes half of the outputs using both halves.
+template <int M, int T, int STORE>
+__global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(T)
+    rc_inverse2_kernel(int ns, int L, int nbins, const float2 *__restrict__ spec, const float2 *__restrict__ etab,
+                       const float *__restrict__ bound2, float *__restrict__ scale, void *__restrict__ out) {
+    extern __shared__ float2 sm[];
+    cg::cluster_group cluster = cg::this_cluster();
+    const int h = (int)cluster.block_rank();
+    const int pr = blockIdx.x >> 1;
+    const int p = pr / L, r = pr - p * L;
+    constexpr int N = 2 * M;
+    const int LN = L * N;
+    const Etab E = load_etab<M, T>(sm, etab, 2 * L);
+    __syncthreads();
+    const float2 *in = spec + (size_t)p * N;
+    for (int k = threadIdx.x; k < M; k += T) {
+        const int idx = 2 * k + h;
+        float2 y = __ldg(&in[idx]);
+        if (r != 0) {
+            const int kap = idx < N / 2 ? idx : idx - N;
+            int m = (int)(((long long)kap * r) % LN);
+            if (m < 0) m += LN;
+            y = cmul(y, E(m));
+        }
+        sm[pad(k)] = y;
+    }
+    __syncthreads();
+    fft_smem<M, T, true>(sm, E, 2 * L);
+    cluster.sync();  // both halves transformed
+    const float2 *A = cluster.map_shared_rank(sm, 0);
+    const float2 *B = cluster.map_shared_rank(sm, 1);
+    float inv = 1.f;
+    if (STORE == SARBP_STORE_C32H) {
+        const float bound = __ldg(&bound2[2 * p]) + __ldg(&bound2[2 * p + 1]);
+        float sc = 1.f;
+        if (bound > 0.f && isfinite(bound)) sc = exp2f(ceilf(log2f(bound) - 14.f));
+        inv = 1.f / sc;
+        if (r == 0 && h == 0 && threadIdx.x == 0) scale[p] = sc;
+    }
+    const int i0 = h * (M / 2), i1 = i0 + M / 2;
+    for (int i = i0 + threadIdx.x; i < i1; i += T) {
+        const float2 a = A[pad(i)];
+        const float2 t = cmul(E(L * i), B[pad(i)]);  // W_N^{-i} B[i]
+        const float2 y0 = cadd(a, t), y1 = csub(a, t);
+        if (STORE == SARBP_STORE_C64) {
+            float2 *o = reinterpret_cast<float2 *>(out) + (size_t)p * nbins + r;
+            if (i < ns) o[(size_t)L * i] = y0;
+            if (i + M < ns) o[(size_t)L * (i + M)] = y1;
+        } else {
+            __half2 *o = reinterpret_cast<__half2 *>(out) + (size_t)p * nbins + r;
+            if (i < ns) o[(size_t)L * i] = __floats2half2_rn(y0.x * inv, y0.y * inv);
+            if (i + M < ns) o[(size_t)L * (i + M)] = __floats2half2_rn(y1.x * inv, y1.y * inv);
+        }
+    }
+    cluster.sync();  // the partner has finished reading this CTA's shared memory
+}
+
 #ifndef SARBP_RC_BIG_THREADS
 #define SARBP_RC_BIG_THREADS 512
 #endif
@@ -269,7 +397,7 @@ constexpr int threads_for() {
     return N >= 8192 ? SARBP_RC_BIG_THREADS : (N >= 4096 ? 512 : (N >= 512 ? N / 8 : 64));
 }
 
-constexpr size_t kEtabSmem = sizeof(float2) * (256 + 1024);  // L N <= 16 * 16384
+constexpr size_t kEtabSmem = sizeof(float2) * (288 + 1152);  // slots of 256 + 1024 entries (L N <= 16 * 16384)
 
 template <int N>
 cudaError_t fwd_n(const RcPlan &p, const float2 *echo, const float2 *filt, const float2 *etab,
@@ -303,10 +431,42 @@ cudaError_t inv_n(const RcPlan &p, const float2 *spec, const float2 *etab, const
     return cudaGetLastError();
 }
 
+template <int M>
+cudaError_t fwd2(const RcPlan &p, const float2 *echo, const float2 *filt, const float2 *etab, float2 *spec,
+                 float *bound2, cudaStream_t s) {
+    constexpr int T = threads_for<M>();
+    const size_t smem = sizeof(float2) * padded(M) + kEtabSmem;
+    auto k = rc_forward2_kernel<M, T>;
+    cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    k<<<2 * p.np, T, smem, s>>>(p.ns, p.L, echo, filt, etab, spec, bound2);
+    return cudaGetLastError();
+}
+
+template <int M>
+cudaError_t inv2(const RcPlan &p, const float2 *spec, const float2 *etab, const float *bound2, float *scale,
+                 void *out, cudaStream_t s) {
+    constexpr int T = threads_for<M>();
+    const size_t smem = sizeof(float2) * padded(M) + kEtabSmem;
+    cudaError_t e;
+    if (p.storage == SARBP_STORE_C64) {
+        auto k = rc_inverse2_kernel<M, T, SARBP_STORE_C64>;
+        e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+        k<<<2 * p.np * p.L, T, smem, s>>>(p.ns, p.L, p.nbins, spec, etab, bound2, scale, out);
+    } else {
+        auto k = rc_inverse2_kernel<M, T, SARBP_STORE_C32H>;
+        e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+        k<<<2 * p.np * p.L, T, smem, s>>>(p.ns, p.L, p.nbins, spec, etab, bound2, scale, out);
+    }
+    return cudaGetLastError();
+}
+
 }  // namespace
 
 bool rc_size_supported(int nfft) {
-    return nfft >= 64 && nfft <= 16384 && (nfft & (nfft - 1)) == 0;
+    return nfft >= 64 && nfft <= 32768 && (nfft & (nfft - 1)) == 0;
 }
 
 #define SARBP_RC_SWITCH(N_, CALL)      \
@@ -327,6 +487,10 @@ cudaError_t launch_rc_forward(const RcPlan &p, const float2 *echo, const float2 
                               const float2 *etab, float2 *spec, float *scale, cudaStream_t s) {
     if (p.np <= 0) return cudaSuccess;
     if (p.L < 1 || p.L > 16) return cudaErrorInvalidValue;
+    if (p.nfft == 32768) {
+        if (!p.bound2) return cudaErrorInvalidValue;
+        return fwd2<16384>(p, echo, filt, etab, spec, p.bound2, s);
+    }
 #define SARBP_FWD(N) fwd_n<N>(p, echo, filt, etab, spec, scale, s)
     SARBP_RC_SWITCH(p.nfft, SARBP_FWD)
 #undef SARBP_FWD
@@ -336,6 +500,10 @@ cudaError_t launch_rc_inverse(const RcPlan &p, const float2 *spec, const float2 
                               const float *scale, void *out, cudaStream_t s) {
     if (p.np <= 0) return cudaSuccess;
     if (p.L < 1 || p.L > 16) return cudaErrorInvalidValue;
+    if (p.nfft == 32768) {
+        if (!p.bound2) return cudaErrorInvalidValue;
+        return inv2<16384>(p, spec, etab, p.bound2, const_cast<float *>(scale), out, s);
+    }
 #define SARBP_INV(N) inv_n<N>(p, spec, etab, scale, out, s)
     SARBP_RC_SWITCH(p.nfft, SARBP_INV)
 #undef SARBP_INV

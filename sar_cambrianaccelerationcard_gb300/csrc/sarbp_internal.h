@@ -29,6 +29,7 @@ struct RcPlan {
     int L;           // upsampling factor
     int nbins;       // L * ns
     int storage;     // sarbp_storage
+    float *bound2;   // [2 np] scratch for the split (nfft = 32768) path, else unused
 };
 
 // Host-side launchers (rc.cu).  spec: scratch [np][nfft] complex; filt: [nfft]
@@ -39,6 +40,8 @@ cudaError_t launch_rc_forward(const RcPlan &p, const float2 *echo, const float2 
                               const float2 *etab, float2 *spec, float *scale, cudaStream_t s);
 cudaError_t launch_rc_inverse(const RcPlan &p, const float2 *spec, const float2 *etab,
                               const float *scale, void *out, cudaStream_t s);
+// The split path (nfft = 32768) writes the FP16 scale in the inverse, so the
+// scale pointer passed to launch_rc_inverse must be writable there.
 inline int rc_etab_size(int L, int nfft) { return 256 + (L * nfft >= 256 ? L * nfft / 256 : 1); }
 bool rc_size_supported(int nfft);
 

@@ -105,6 +105,7 @@ struct sarbp_server {
     bool step_pending[2] = {false, false};
     cudaGraphExec_t exec = nullptr;
     float2 *d_spec = nullptr;             // range-compression spectrum scratch
+    float *d_bound2 = nullptr;            // split-path bounds for the scratch rows
     size_t spec_rows = 0;
     sarbp_server_stats st{};
     Clock::time_point busy_since;
@@ -113,8 +114,8 @@ struct sarbp_server {
 
 namespace {
 
-constexpr size_t kSpecRows = 256;  // pulses per range-compression batch (scratch rows of 16384 points)
-constexpr int kMaxN = 16384;
+constexpr size_t kSpecRows = 256;  // pulses per range-compression batch (scratch rows of up to 32768 points)
+constexpr int kMaxN = 32768;
 
 void fail_job(Job *j, sarbp_status st, const std::string &msg) {
     j->status = st;
@@ -173,7 +174,8 @@ sarbp_status admit(sarbp_server *S, Job *j) {
         e = cudaMemcpyAsync(j->d_etab, j->etab.data(), j->etab.size() * 8, cudaMemcpyHostToDevice, S->sa);
     if (e == cudaSuccess) e = cudaMemsetAsync(j->d_err, 0, sizeof(unsigned), S->sa);
     for (size_t p0 = 0; e == cudaSuccess && p0 < np; p0 += S->spec_rows) {
-        sarbp::RcPlan rp;
+        sarbp::RcPlan rp{};
+        rp.bound2 = S->d_bound2;
         rp.np = (int)std::min(S->spec_rows, np - p0);
         rp.ns = (int)ns;
         rp.nfft = j->lay.nfft;
@@ -433,7 +435,8 @@ sarbp_status sarbp_server_create(sarbp_server **out, const sarbp_server_config *
          cudaEventCreateWithFlags(&S->step_ev[0], cudaEventDisableTiming) == cudaSuccess &&
          cudaEventCreateWithFlags(&S->step_ev[1], cudaEventDisableTiming) == cudaSuccess;
     S->spec_rows = kSpecRows;
-    ok = ok && cudaMalloc(&S->d_spec, sizeof(float2) * kSpecRows * kMaxN) == cudaSuccess;
+    ok = ok && cudaMalloc(&S->d_spec, sizeof(float2) * kSpecRows * kMaxN + sizeof(float) * 2 * kSpecRows) == cudaSuccess;
+    if (ok) S->d_bound2 = reinterpret_cast<float *>(S->d_spec + kSpecRows * kMaxN);
     if (ok) {  // keep freed job memory in the pool for the next admissions
         cudaMemPool_t pool;
         if (cudaDeviceGetDefaultMemPool(&pool, cfg->device) == cudaSuccess) {

@@ -166,8 +166,8 @@ def test_invalid_arguments(ctx, c1):
     with pytest.raises(sarbp.SarbpError) as e:
         ctx.backproject(r, rc32, bad, g, sarbp.MODE_SPLIT, lay.t0_bins, lay.bin_rate)
     assert e.value.status == sarbp.ERR_INVALID_ARGUMENT
-    with pytest.raises(sarbp.SarbpError) as e:   # range FFT beyond 16384 points
-        ctx.range_compress(r, np.zeros((2, 16000), np.complex64))
+    with pytest.raises(sarbp.SarbpError) as e:   # range FFT beyond 32768 points
+        ctx.range_compress(r, np.zeros((2, 40000), np.complex64))
     assert e.value.status == sarbp.ERR_UNSUPPORTED
     # the context stays usable after errors
     img = ctx.backproject(r, rc32[:8].copy(), s.apc[:8].copy(), g, sarbp.MODE_SPLIT, lay.t0_bins, lay.bin_rate)

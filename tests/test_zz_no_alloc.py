@@ -68,6 +68,6 @@ def test_noalloc_rejects_host_pointers_and_oversize():
     host_out = np.zeros((4, 8 * 256), np.complex64)
     assert lib.sarbp_range_compress_noalloc(ctypes.byref(r), host_echo.ctypes.data, 4, 256, 0,
                                             host_out.ctypes.data, None, None) == sarbp.ERR_INVALID_ARGUMENT
-    # a range FFT beyond 16384 points is rejected before touching any memory
-    assert lib.sarbp_range_compress_noalloc(ctypes.byref(r), host_echo.ctypes.data, 4, 16000, 0,
+    # a range FFT beyond 32768 points is rejected before touching any memory
+    assert lib.sarbp_range_compress_noalloc(ctypes.byref(r), host_echo.ctypes.data, 4, 40000, 0,
                                             host_out.ctypes.data, None, None) == sarbp.ERR_UNSUPPORTED
