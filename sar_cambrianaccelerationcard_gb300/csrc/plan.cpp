@@ -78,7 +78,11 @@ bool plan_bp(int sms, const sarbp_radar &r, const sarbp_rc_view &rc, const doubl
     constexpr double kSeriesTol = 5e-7;  // 1.1e-4 rad of C-band phase at the tile corners
     why = "no tile size fits";
     bool chosen = false;
+#ifdef SARBP_BP_FORCE_PIX
+    for (int pix : {SARBP_BP_FORCE_PIX}) {  // tuning builds only
+#else
     for (int pix : {8, 4, 2}) {
+#endif
         int tx, ty;
         bp_tile_dims(pix, &tx, &ty);
         const double hx = 0.5 * (tx - 1), hy = 0.5 * (ty - 1);
