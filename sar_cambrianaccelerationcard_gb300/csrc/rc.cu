@@ -115,18 +115,24 @@ struct Dft<8, INV> {
 
 // One Stockham stage: butterfly j reads s[j + r*N/R], applies twiddles
 // W_N^{k r N/(Ns R)} (k = j mod Ns), runs a radix-R DFT and writes
-// s[(j - k) R + k + r Ns].
-template <int N, int R, int T, bool INV>
-__device__ __forceinline__ void stage(float2 *s, const Etab &E, int L, int Ns) {
+// s[(j - k) R + k + r Ns].  Ns is a compile-time constant, so with the padding
+// pad(i) = i + i/8 every r-offset is an immediate: pad(j + r N/R) =
+// pad(j) + r padded(N/R) and pad(base + r Ns) = pad(base) + r (Ns + Ns/8) for
+// Ns >= 8 (pad(base) + r for Ns = 1, where base is a multiple of 8).
+template <int N, int R, int T, bool INV, int Ns>
+__device__ __forceinline__ void stage(float2 *s, const Etab &E, int L) {
     constexpr int NB = N / R;
     constexpr int PER = (NB + T - 1) / T;
+    constexpr int LD = padded(NB);
+    constexpr int ST = Ns >= 8 ? Ns + Ns / 8 : 1;
     float2 v[PER][R];
 #pragma unroll
     for (int b = 0; b < PER; ++b) {
         const int j = threadIdx.x + b * T;
         if (PER * T == NB || j < NB) {
+            const float2 *src = s + pad(j);
 #pragma unroll
-            for (int r = 0; r < R; ++r) v[b][r] = s[pad(j + r * NB)];
+            for (int r = 0; r < R; ++r) v[b][r] = src[r * LD];
         }
     }
     __syncthreads();
@@ -158,38 +164,34 @@ __device__ __forceinline__ void stage(float2 *s, const Etab &E, int L, int Ns) {
                 for (int r = 1; r < R; ++r) v[b][r] = cmul(v[b][r], w[r]);
             }
             Dft<R, INV>::run(v[b]);
-            const int base = (j - k) * R + k;
+            float2 *dst = s + pad((j - k) * R + k);
 #pragma unroll
-            for (int r = 0; r < R; ++r) s[pad(base + r * Ns)] = v[b][r];
+            for (int r = 0; r < R; ++r) dst[r * ST] = v[b][r];
         }
     }
     __syncthreads();
 }
 
-template <int N>
-struct Log2 {
-    static constexpr int value = 1 + Log2<N / 2>::value;
-};
-template <>
-struct Log2<1> {
-    static constexpr int value = 0;
+// radix-8 stages while 8 * Ns <= N, then one radix-4 or radix-2 stage
+template <int N, int T, bool INV, int Ns>
+struct Stages {
+    __device__ __forceinline__ static void run(float2 *s, const Etab &E, int L) {
+        if constexpr (Ns * 8 <= N) {
+            stage<N, 8, T, INV, Ns>(s, E, L);
+            Stages<N, T, INV, Ns * 8>::run(s, E, L);
+        } else if constexpr (Ns * 4 == N) {
+            stage<N, 4, T, INV, Ns>(s, E, L);
+        } else if constexpr (Ns * 2 == N) {
+            stage<N, 2, T, INV, Ns>(s, E, L);
+        }
+    }
 };
 
 // Unnormalised in-place FFT of N points held (padded) in shared memory.
 // Caller must have synchronised after filling s; returns synchronised.
 template <int N, int T, bool INV>
 __device__ void fft_smem(float2 *s, const Etab &E, int L) {
-    constexpr int LOG = Log2<N>::value;
-    constexpr int N8 = LOG / 3;
-    constexpr int REM = LOG % 3;
-    int Ns = 1;
-#pragma unroll 1
-    for (int i = 0; i < N8; ++i) {
-        stage<N, 8, T, INV>(s, E, L, Ns);
-        Ns *= 8;
-    }
-    if (REM == 2) stage<N, 4, T, INV>(s, E, L, Ns);
-    if (REM == 1) stage<N, 2, T, INV>(s, E, L, Ns);
+    Stages<N, T, INV, 1>::run(s, E, L);
 }
 
 // copies the E tables into shared memory right after the padded data
@@ -268,9 +270,7 @@ __global__ void __launch_bounds__(T) rc_inverse_kernel(int ns, int L, int nbins,
         float2 y = __ldg(&in[k]);
         if (r != 0) {
             const int kap = k < N / 2 ? k : k - N;  // MATLAB split floor((N+1)/2) for even N
-            int m = (kap * r) % LN;
-            if (m < 0) m += LN;
-            y = cmul(y, E(m));
+            y = cmul(y, E((kap * r) & (LN - 1)));  // LN is a power of two
         }
         sm[pad(k)] = y;
     }
@@ -352,9 +352,7 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(T)
         float2 y = __ldg(&in[idx]);
         if (r != 0) {
             const int kap = idx < N / 2 ? idx : idx - N;
-            int m = (int)(((long long)kap * r) % LN);
-            if (m < 0) m += LN;
-            y = cmul(y, E(m));
+            y = cmul(y, E((kap * r) & (LN - 1)));  // LN is a power of two
         }
         sm[pad(k)] = y;
     }
