@@ -37,6 +37,18 @@ sys.path.insert(0, ROOT)
 # and 3 MUFU operations (a square-root-class op, sin, cos).
 FP32_OPS_PER_UPDATE = 19
 MUFU_OPS_PER_UPDATE = 3
+# DRAM bytes (read + write) per launch measured by ncu (dram__bytes_read.sum +
+# dram__bytes_write.sum, one-pass capture of the full-size launch) on GB300 for
+# the default workload (4096 pulses x 8192 samples -> 4096^2, complex64 rows).
+# BP: 236.3 MB read + 115.6 MB written (part of the image is still in L2 when
+# the launch ends); the algorithmic bytes are each pulse's swath bins once
+# (227.9 MB) plus the image (134.2 MB).
+# Range compression (two 2048-pulse batches of forward + inverse): 2 x
+# (134.6 + 208.4 + 268.6 + 1014.2) MB.
+MEASURED_TRAFFIC = {
+    ("full", "split"): {"bp": 236301312 + 115647232,
+                        "rc": 2 * (134575872 + 208381184 + 268595200 + 1014241280)},
+}
 
 
 def parse():
@@ -139,26 +151,39 @@ def workload(size):
     return scenes.config2()
 
 
-def cpu_sample(scene, threads=None):
-    """FP64 oracle back-projection of a 128x128 tile (all pulses) of the scene,
-    on range-compressed data computed by the oracle.  Returns (updates/s,
-    cores, description, seconds)."""
+def cpu_tile_side(orc, scene, rc, seconds: float) -> int:
+    """Side of the centred square tile whose FP64 oracle back-projection (all
+    pulses) takes about `seconds` on this host, from a 64x64 probe; a
+    multiple of 32, capped at the image."""
+    g = scene.grid
+    probe = min(64, g.nx, g.ny)
+    t = time.perf_counter()
+    orc.backproject(scene, rc, (g.nx // 2 - probe // 2, g.ny // 2 - probe // 2, probe, probe))
+    rate = probe * probe * scene.np_ / max(time.perf_counter() - t, 1e-6)
+    side = int(math.sqrt(seconds * rate / scene.np_)) // 32 * 32
+    return max(32, min(side, g.nx, g.ny))
+
+
+def cpu_sample(scene, threads=None, seconds: float = 12.0):
+    """FP64 oracle back-projection of a centred square tile (all pulses) of the
+    scene, sized for about `seconds` of host work, on range-compressed data
+    computed by the oracle.  Returns (updates/s, cores, description, seconds)."""
     from oracle import oracle as orc
     if threads:
         orc.set_threads(threads)
     cores = orc.threads()
     g = scene.grid
-    w = h = 128
-    x0, y0 = g.nx // 2 - w // 2, g.ny // 2 - h // 2
     # range-compress the pulses once (untimed setup): oracle FP64 chain
     echo = orc.echo(scene)
     rc = orc.range_compress(scene, echo)
+    w = h = cpu_tile_side(orc, scene, rc, seconds)
+    x0, y0 = g.nx // 2 - w // 2, g.ny // 2 - h // 2
     t = time.perf_counter()
     orc.backproject(scene, rc, (x0, y0, w, h))
     dt = time.perf_counter() - t
     upd = w * h * scene.np_
     desc = (f"FP64 oracle BP (restated BPA_SAR.m:177-197, linear interpolation) over a {w}x{h}-pixel tile "
-            f"x all {scene.np_} pulses of the same scene ({upd:.3g} updates), {cores} OpenMP threads")
+            f"x all {scene.np_} pulses of the same scene ({upd:.3g} updates, {dt:.1f} s), {cores} OpenMP threads")
     return upd / dt, cores, desc, dt, rc, (x0, y0, w, h)
 
 
@@ -172,7 +197,7 @@ def run_reference(args):
     echo = orc.echo(scene)
     rc = orc.range_compress(scene, echo)
     g = scene.grid
-    w = h = 128 if args.size == "full" else 64
+    w = h = cpu_tile_side(orc, scene, rc, 5.0)  # ~5 s of host work per step
     region = (g.nx // 2 - w // 2, g.ny // 2 - h // 2, w, h)
     for _ in range(args.warmup):
         orc.backproject(scene, rc, region)
@@ -190,7 +215,8 @@ def run_reference(args):
         "config": {"workload": f"stripmap BP {scene.np_} pulses x {scene.ns} samples -> {g.nx}x{g.ny} image",
                    "mode": "fp64-cpu", "sample_tile": [w, h]},
         "cpu_baseline": {"value": v, "unit": "Gpix*pulse/s", "cores": cores, "kind": "port",
-                         "sample": f"{w}x{h} tile x {scene.np_} pulses per step (range compression untimed)"},
+                         "sample": f"{w}x{h} tile x {scene.np_} pulses per step ({upd:.3g} updates, "
+                                   f"{dt:.1f} s; range compression untimed)"},
         "e2e": {"value": v, "unit": "Gpix*pulse/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line))
@@ -319,13 +345,24 @@ def run_ours(args):
                "h2d_bytes_per_step": scene.np_ * scene.ns * 8 + scene.np_ * 24,
                "d2h_bytes_per_step": g.nx * g.ny * 8, "ms_per_step": e2e_s * 1e3}
 
+    # algorithmic BP bytes per launch: for every pulse the range bins between
+    # the nearest and farthest pixel (9x9 lattice over the grid), read once,
+    # plus the image written once
+    fx, fy = np.meshgrid(np.linspace(0, g.nx - 1, 9), np.linspace(0, g.ny - 1, 9))
+    pts = scene.grid.origin + fx.reshape(-1, 1) * scene.grid.ux + fy.reshape(-1, 1) * scene.grid.uy
+    rng = np.linalg.norm(pts[None, :, :] - scene.apc[:, None, :], axis=2)
+    span_bins = np.minimum(lay.nbins, (rng.max(axis=1) - rng.min(axis=1)) * 2.0 / scene.radar.c * lay.bin_rate)
+    bp_alg_bytes = int(span_bins.sum() * esize + g.nx * g.ny * 8)
+
     # --- roofline: issue-rate ceiling from live microbenchmarks
     fp32_rate, mufu_rate, sms = (1.0, 1.0, 0) if args.no_probe else ctx.probe_issue_rates()
     peak = min(fp32_rate / FP32_OPS_PER_UPDATE, mufu_rate / MUFU_OPS_PER_UPDATE) / 1e9
     bp_rate = updates / (bp_ms_each * 1e-3) / 1e9 if bp_ms_each else None
     roofline = {
         "bound": "issue (FP32+MUFU)", "achieved": bp_rate, "peak": peak, "unit": "Gpix*pulse/s",
-        "frac": (bp_rate / peak) if bp_rate else None, "traffic": None,
+        "frac": (bp_rate / peak) if bp_rate else None,
+        "traffic": MEASURED_TRAFFIC.get((args.size, args.mode), {}).get("bp"),
+        "traffic_algorithmic": bp_alg_bytes,
         "peak_source": (f"measured live: FP32 FMA {fp32_rate / 1e12:.1f} T lanes/s, MUFU {mufu_rate / 1e12:.2f} T "
                         f"lanes/s on {sms} SMs; peak = min(FP32/{FP32_OPS_PER_UPDATE}, MUFU/{MUFU_OPS_PER_UPDATE})"),
         "kernel": "bp_kernel<SPLIT>",
@@ -337,7 +374,8 @@ def run_ours(args):
     rc_bytes = scene.np_ * scene.ns * 8 + scene.np_ * lay.nbins * esize
     roofline_rc = {"bound": "hbm", "achieved": rc_bytes / (rc_ms * 1e-3) / 1e9 if rc_ms else None, "peak": hbm,
                    "unit": "GB/s", "frac": (rc_bytes / (rc_ms * 1e-3) / 1e9 / hbm) if (rc_ms and hbm) else None,
-                   "traffic": None, "kernel": "rc_forward + rc_inverse", "ms": rc_ms}
+                   "traffic": MEASURED_TRAFFIC.get((args.size, args.mode), {}).get("rc"),
+                   "kernel": "rc_forward + rc_inverse", "ms": rc_ms}
 
     cpu = None
     if rank == 0 and not args.no_cpu:
