@@ -182,6 +182,53 @@ sarbp_status sarbp_backproject(sarbp_ctx *ctx, const sarbp_radar *radar,
                                const sarbp_grid *grid, int32_t mode,
                                sarbp_complex64 *image, int32_t accumulate, void *stream);
 
+/* Per-pulse corrections applied inside back-projection: the motion-compensation
+ * / autofocus hook on the APC track.  Pulse p's slant range becomes
+ * |apc_p - pix| + drange[p] (metres; shifts the range bin and the carrier
+ * phase) and its phase gains dphase[p] (radians).  Either pointer may be NULL;
+ * host or device memory.  The reference has no counterpart: its APC track is
+ * implicit in SARParams (BPA_CUDA.cpp:35-42) and the MATLAB script uses the
+ * nominal track (BPA_SAR.m:83,182). */
+typedef struct sarbp_pulse_corr {
+    const double *drange;  /* [np] or NULL */
+    const double *dphase;  /* [np] or NULL */
+} sarbp_pulse_corr;
+
+/* sarbp_backproject with per-pulse corrections (corr may be NULL). */
+sarbp_status sarbp_backproject_ex(sarbp_ctx *ctx, const sarbp_radar *radar,
+                                  const sarbp_rc_view *rc, const double *apc,
+                                  const sarbp_grid *grid, int32_t mode,
+                                  const sarbp_pulse_corr *corr,
+                                  sarbp_complex64 *image, int32_t accumulate, void *stream);
+
+/* Weighted projection, the adjoint of back-projection: for every pulse p,
+ * out[p] = sum over pixels of conj(weight[pixel]) * S_p(bin) exp(j phase_p),
+ * the pulse's back-projected term with corrections.  With weight = |I|^2 I this
+ * is the per-pulse gradient of the image sharpness sum |I|^4:
+ * d/d dphase[p] = -4 Im(out[p]).  SPLIT or FP16STORE arithmetic (mode), sums
+ * over tiles in FP64 in a fixed order.  weight [ny][nx] complex64 (host or
+ * device); out [np] complex128 as (re, im) pairs (host or device). */
+sarbp_status sarbp_project_weighted(sarbp_ctx *ctx, const sarbp_radar *radar,
+                                    const sarbp_rc_view *rc, const double *apc,
+                                    const sarbp_grid *grid, int32_t mode,
+                                    const sarbp_pulse_corr *corr,
+                                    const sarbp_complex64 *weight, double *out, void *stream);
+
+/* Autofocus: per-pulse phase errors estimated by maximising the image
+ * sharpness sum |I|^4.  Each iteration back-projects with the current phases,
+ * forms W = |I|^2 I, projects it onto every pulse (sarbp_project_weighted) and
+ * sets dphase[p] -= arg(out[p]), then removes the mean phase.
+ * dphase [np] (host) holds the starting phases and receives the estimate;
+ * drange [np] (host, may be NULL) is a fixed range correction; image
+ * [ny][nx] (host or device, may be NULL) receives the image with the final
+ * phases; sharpness [iterations + 1] (host, may be NULL) receives sum |I|^4
+ * before each update and for the final image.  Synchronous. */
+sarbp_status sarbp_autofocus(sarbp_ctx *ctx, const sarbp_radar *radar,
+                             const sarbp_rc_view *rc, const double *apc,
+                             const sarbp_grid *grid, int32_t mode, int32_t iterations,
+                             const double *drange, double *dphase,
+                             sarbp_complex64 *image, double *sharpness, void *stream);
+
 /* The SAR_BP entry point: echo + APC track + radar + grid in, complex image out.
  * Range compression (storage chosen by mode) followed by back-projection
  * (SAR_Processor::processImage + applyBPAlgorithm, BPA_CUDA.cpp:70-90). */

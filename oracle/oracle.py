@@ -57,6 +57,12 @@ def lib():
                    ctypes.c_int, _dp]
         L.orc_backproject.argtypes = [_dp] + bp_args
         L.orc_backproject_c64.argtypes = [_fp] + bp_args
+        corr_args = [ctypes.c_int, ctypes.c_int, _dp, _dp, _dp, _dp,
+                     ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                     ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_double,
+                     ctypes.c_int, _dp, _dp]
+        L.orc_backproject_corr.argtypes = [_dp] + corr_args + [_dp]
+        L.orc_project_weighted.argtypes = [_dp] + corr_args + [_dp, _dp]
         L.orc_set_threads.argtypes = [ctypes.c_int]
         L.orc_get_threads.restype = ctypes.c_int
         _lib = L
@@ -158,6 +164,46 @@ def backproject_raw(rc, apc, origin, ux, uy, region, fc, c, t0, binrate,
     return img
 
 
+def _opt(a):
+    return None if a is None else _d(np.ascontiguousarray(a, dtype=np.float64))
+
+
+def backproject_corr_raw(rc, apc, origin, ux, uy, region, fc, c, t0, binrate,
+                         drange=None, dphase=None, interp: int = 0) -> np.ndarray:
+    """Back-projection with per-pulse range (m) and phase (rad) corrections."""
+    apc = np.ascontiguousarray(apc, dtype=np.float64)
+    x0, y0, w, h = (int(v) for v in region)
+    img = np.zeros((h, w), dtype=np.complex128)
+    rcc = _c128(rc)
+    np_, nbins = rcc.shape
+    dr = None if drange is None else np.ascontiguousarray(drange, dtype=np.float64)
+    dp = None if dphase is None else np.ascontiguousarray(dphase, dtype=np.float64)
+    lib().orc_backproject_corr(_d(rcc.view(np.float64)), np_, nbins, _d(apc), _opt(origin), _opt(ux), _opt(uy),
+                               x0, y0, w, h, fc, c, t0, binrate, int(interp),
+                               None if dr is None else _d(dr), None if dp is None else _d(dp),
+                               _d(img.view(np.float64)))
+    return img
+
+
+def project_weighted_raw(rc, apc, origin, ux, uy, region, fc, c, t0, binrate, weight,
+                         drange=None, dphase=None, interp: int = 0) -> np.ndarray:
+    """out[p] = sum over the region of conj(weight) * pulse p's term."""
+    apc = np.ascontiguousarray(apc, dtype=np.float64)
+    x0, y0, w, h = (int(v) for v in region)
+    wt = _c128(weight)
+    assert wt.shape == (h, w)
+    rcc = _c128(rc)
+    np_, nbins = rcc.shape
+    out = np.zeros(np_, dtype=np.complex128)
+    dr = None if drange is None else np.ascontiguousarray(drange, dtype=np.float64)
+    dp = None if dphase is None else np.ascontiguousarray(dphase, dtype=np.float64)
+    lib().orc_project_weighted(_d(rcc.view(np.float64)), np_, nbins, _d(apc), _opt(origin), _opt(ux), _opt(uy),
+                               x0, y0, w, h, fc, c, t0, binrate, int(interp),
+                               None if dr is None else _d(dr), None if dp is None else _d(dp),
+                               _d(wt.view(np.float64)), _d(out.view(np.complex128).view(np.float64)))
+    return out
+
+
 # ------------------------------------------------------- product profile --
 
 def echo(scene, noise: bool = True) -> np.ndarray:
@@ -193,3 +239,41 @@ def backproject(scene, rc, region=None) -> np.ndarray:
 
 def image(scene, echo_data, region=None) -> np.ndarray:
     return backproject(scene, range_compress(scene, echo_data), region)
+
+
+def backproject_corr(scene, rc, drange=None, dphase=None, region=None) -> np.ndarray:
+    g = scene.grid
+    lay = scene.layout
+    if region is None:
+        region = (0, 0, g.nx, g.ny)
+    return backproject_corr_raw(rc, scene.apc, g.origin, g.ux, g.uy, region, scene.radar.fc, scene.radar.c,
+                                lay.t0_bins, lay.bin_rate, drange, dphase)
+
+
+def project_weighted(scene, rc, weight, drange=None, dphase=None) -> np.ndarray:
+    g = scene.grid
+    lay = scene.layout
+    return project_weighted_raw(rc, scene.apc, g.origin, g.ux, g.uy, (0, 0, g.nx, g.ny), scene.radar.fc,
+                                scene.radar.c, lay.t0_bins, lay.bin_rate, weight, drange, dphase)
+
+
+def autofocus(scene, rc, iterations: int, dphase=None, drange=None):
+    """Sharpness-maximising per-pulse phase estimation, the FP64 statement of
+    the product's sarbp_autofocus: each iteration images with the current
+    phases, forms W = |I|^2 I, projects it onto every pulse
+    (c_p = sum conj(W) term_p) and sets dphase[p] -= arg(c_p), then removes
+    the mean.  Returns (dphase, sharpness per iteration, final image)."""
+    np_ = rc.shape[0]
+    ph = np.zeros(np_) if dphase is None else np.array(dphase, dtype=np.float64)
+    sharp = []
+    for _ in range(iterations):
+        img = backproject_corr(scene, rc, drange, ph)
+        a2 = np.abs(img) ** 2
+        sharp.append(float(np.sum(a2 * a2)))
+        cp = project_weighted(scene, rc, a2 * img, drange, ph)
+        ph = ph - np.angle(cp)
+        ph -= ph.mean()
+    img = backproject_corr(scene, rc, drange, ph)
+    a2 = np.abs(img) ** 2
+    sharp.append(float(np.sum(a2 * a2)))
+    return ph, sharp, img

@@ -20,7 +20,7 @@
 
 static int g_threads = 0;
 
-int orc_version(void) { return 3; }
+int orc_version(void) { return 4; }
 
 void orc_set_threads(int n) { g_threads = n; }
 
@@ -261,6 +261,48 @@ double orc_mean_power(const double *x, int64_t count)
 
 static long long round_half_away(double v) { return (long long)(v >= 0.0 ? floor(v + 0.5) : ceil(v - 0.5)); }
 
+/* Sample of pulse p at pixel (px, py, pz) times its phase term, with the
+ * optional per-pulse corrections: slant range R + drange[p], phase
+ * 2 pi frac(2 fc R / c) + dphase[p].  Linear interpolation (zero outside the
+ * row) or the script's nearest bin (BPA_SAR.m:184-188, 1-based round). */
+#define ORC_TERM(LOAD_RE, LOAD_IM, p, px, py, pz, out_r, out_i)                              \
+    do {                                                                                     \
+        const double *a_ = apc + 3 * (size_t)(p);                                            \
+        double dx_ = a_[0] - (px), dy_ = a_[1] - (py), dz_ = a_[2] - (pz);                   \
+        double r_ = sqrt(dx_ * dx_ + dy_ * dy_ + dz_ * dz_);                                 \
+        if (drange) r_ += drange[p];                                                         \
+        double b_ = (2.0 * r_ / c - t0) * binrate;                                           \
+        double sr_ = 0.0, si_ = 0.0;                                                         \
+        size_t rowoff_ = (size_t)nbins * (size_t)(p);                                        \
+        if (interp == ORC_INTERP_LINEAR) {                                                   \
+            double fl_ = floor(b_);                                                          \
+            double f_ = b_ - fl_;                                                            \
+            if (fl_ >= -1.0 && fl_ <= (double)nbins - 1.0) {                                 \
+                long long i0_ = (long long)fl_;                                              \
+                if (i0_ >= 0) {                                                              \
+                    sr_ += (1.0 - f_) * LOAD_RE(rowoff_ + (size_t)i0_);                      \
+                    si_ += (1.0 - f_) * LOAD_IM(rowoff_ + (size_t)i0_);                      \
+                }                                                                            \
+                if (i0_ + 1 <= nbins - 1) {                                                  \
+                    sr_ += f_ * LOAD_RE(rowoff_ + (size_t)(i0_ + 1));                        \
+                    si_ += f_ * LOAD_IM(rowoff_ + (size_t)(i0_ + 1));                        \
+                }                                                                            \
+            }                                                                                \
+        } else {                                                                             \
+            long long idx_ = round_half_away(b_) - 1;                                        \
+            if (idx_ >= 0 && idx_ < nbins) {                                                 \
+                sr_ = LOAD_RE(rowoff_ + (size_t)idx_);                                       \
+                si_ = LOAD_IM(rowoff_ + (size_t)idx_);                                       \
+            }                                                                                \
+        }                                                                                    \
+        double cyc_ = 2.0 * fc * r_ / c;                                                     \
+        double ph_ = ORC_TWO_PI * (cyc_ - floor(cyc_)) + (dphase ? dphase[p] : 0.0);         \
+        double s_, co_;                                                                      \
+        sincos(ph_, &s_, &co_);                                                              \
+        (out_r) = sr_ * co_ - si_ * s_;                                                      \
+        (out_i) = sr_ * s_ + si_ * co_;                                                      \
+    } while (0)
+
 #define ORC_BP_BODY(LOAD_RE, LOAD_IM)                                                        \
     _Pragma("omp parallel for collapse(2) schedule(static) num_threads(orc_get_threads())") \
     for (int yy = 0; yy < h; ++yy) {                                                         \
@@ -270,38 +312,10 @@ static long long round_half_away(double v) { return (long long)(v >= 0.0 ? floor
             double pz = origin[2] + (double)(x0 + xx) * ux[2] + (double)(y0 + yy) * uy[2];   \
             double acc_r = 0.0, acc_i = 0.0;                                                 \
             for (int p = 0; p < np; ++p) {                                                   \
-                const double *a = apc + 3 * (size_t)p;                                       \
-                double dx = a[0] - px, dy = a[1] - py, dz = a[2] - pz;                       \
-                double r = sqrt(dx * dx + dy * dy + dz * dz);                                \
-                double b = (2.0 * r / c - t0) * binrate;                                     \
-                double sr = 0.0, si = 0.0;                                                   \
-                size_t rowoff = (size_t)nbins * (size_t)p;                                   \
-                if (interp == ORC_INTERP_LINEAR) {                                           \
-                    double fl = floor(b);                                                    \
-                    double f = b - fl;                                                       \
-                    if (fl >= -1.0 && fl <= (double)nbins - 1.0) {                           \
-                        long long i0 = (long long)fl;                                        \
-                        if (i0 >= 0) {                                                       \
-                            sr += (1.0 - f) * LOAD_RE(rowoff + (size_t)i0);                  \
-                            si += (1.0 - f) * LOAD_IM(rowoff + (size_t)i0);                  \
-                        }                                                                    \
-                        if (i0 + 1 <= nbins - 1) {                                           \
-                            sr += f * LOAD_RE(rowoff + (size_t)(i0 + 1));                    \
-                            si += f * LOAD_IM(rowoff + (size_t)(i0 + 1));                    \
-                        }                                                                    \
-                    }                                                                        \
-                } else {                                                                     \
-                    long long idx = round_half_away(b) - 1;                                  \
-                    if (idx >= 0 && idx < nbins) {                                           \
-                        sr = LOAD_RE(rowoff + (size_t)idx);                                  \
-                        si = LOAD_IM(rowoff + (size_t)idx);                                  \
-                    }                                                                        \
-                }                                                                            \
-                double cyc = 2.0 * fc * r / c;                                               \
-                double s, co;                                                                \
-                sincos(ORC_TWO_PI * (cyc - floor(cyc)), &s, &co);                            \
-                acc_r += sr * co - si * s;                                                   \
-                acc_i += sr * s + si * co;                                                   \
+                double tr, ti;                                                               \
+                ORC_TERM(LOAD_RE, LOAD_IM, p, px, py, pz, tr, ti);                           \
+                acc_r += tr;                                                                 \
+                acc_i += ti;                                                                 \
             }                                                                                \
             img[2 * ((size_t)yy * w + xx)] = acc_r;                                          \
             img[2 * ((size_t)yy * w + xx) + 1] = acc_i;                                      \
@@ -319,6 +333,7 @@ void orc_backproject(const double *rc, int np, int nbins, const double *apc,
                      double fc, double c, double t0, double binrate, int interp,
                      double *img)
 {
+    const double *drange = NULL, *dphase = NULL;
     ORC_BP_BODY(LD_D_RE, LD_D_IM)
 }
 
@@ -328,5 +343,47 @@ void orc_backproject_c64(const float *rc, int np, int nbins, const double *apc,
                          double fc, double c, double t0, double binrate, int interp,
                          double *img)
 {
+    const double *drange = NULL, *dphase = NULL;
     ORC_BP_BODY(LD_F_RE, LD_F_IM)
+}
+
+/* Back-projection with per-pulse corrections (either array may be NULL). */
+void orc_backproject_corr(const double *rc, int np, int nbins, const double *apc,
+                          const double *origin, const double *ux, const double *uy,
+                          int x0, int y0, int w, int h,
+                          double fc, double c, double t0, double binrate, int interp,
+                          const double *drange, const double *dphase, double *img)
+{
+    ORC_BP_BODY(LD_D_RE, LD_D_IM)
+}
+
+/* Weighted projection, the adjoint of back-projection over the region:
+ * out[p] = sum_{pixels} conj(weight[pixel]) * term_p(pixel), term_p the pulse's
+ * interpolated sample times its phase term (with corrections).  For the image
+ * I = sum_p term_p exp(j phi_p) and weight W = |I|^2 I, d/dphi_p sum |I|^4 =
+ * -4 Im(out[p]).  weight: [h][w] complex, out: [np] complex. */
+void orc_project_weighted(const double *rc, int np, int nbins, const double *apc,
+                          const double *origin, const double *ux, const double *uy,
+                          int x0, int y0, int w, int h,
+                          double fc, double c, double t0, double binrate, int interp,
+                          const double *drange, const double *dphase, const double *weight, double *out)
+{
+#pragma omp parallel for schedule(static) num_threads(orc_get_threads())
+    for (int p = 0; p < np; ++p) {
+        double cr = 0.0, ci = 0.0;
+        for (int yy = 0; yy < h; ++yy) {
+            for (int xx = 0; xx < w; ++xx) {
+                double px = origin[0] + (double)(x0 + xx) * ux[0] + (double)(y0 + yy) * uy[0];
+                double py = origin[1] + (double)(x0 + xx) * ux[1] + (double)(y0 + yy) * uy[1];
+                double pz = origin[2] + (double)(x0 + xx) * ux[2] + (double)(y0 + yy) * uy[2];
+                double tr, ti;
+                ORC_TERM(LD_D_RE, LD_D_IM, p, px, py, pz, tr, ti);
+                const double wr = weight[2 * ((size_t)yy * w + xx)], wi = weight[2 * ((size_t)yy * w + xx) + 1];
+                cr += wr * tr + wi * ti;
+                ci += wr * ti - wi * tr;
+            }
+        }
+        out[2 * p] = cr;
+        out[2 * p + 1] = ci;
+    }
 }

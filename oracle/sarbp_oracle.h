@@ -109,6 +109,25 @@ void orc_backproject_c64(const float *rc, int np, int nbins, const double *apc,
                          double fc, double c, double t0, double binrate, int interp,
                          double *img);
 
+/* Back-projection with per-pulse corrections (motion compensation / autofocus
+ * output; either array may be NULL): R_p = |apc_p - pix| + drange[p] for the bin
+ * and the carrier phase, and dphase[p] added to the phase. */
+void orc_backproject_corr(const double *rc, int np, int nbins, const double *apc,
+                          const double *origin, const double *ux, const double *uy,
+                          int x0, int y0, int w, int h,
+                          double fc, double c, double t0, double binrate, int interp,
+                          const double *drange, const double *dphase, double *img);
+
+/* Adjoint of orc_backproject_corr over the region: out[p] (complex) =
+ * sum over pixels of conj(weight) * S_p(b) * exp(j phase_p).  With
+ * weight = |I|^2 I this is the per-pulse gradient of the sharpness sum |I|^4:
+ * d/d dphase[p] = -4 Im(out[p]). */
+void orc_project_weighted(const double *rc, int np, int nbins, const double *apc,
+                          const double *origin, const double *ux, const double *uy,
+                          int x0, int y0, int w, int h,
+                          double fc, double c, double t0, double binrate, int interp,
+                          const double *drange, const double *dphase, const double *weight, double *out);
+
 #ifdef __cplusplus
 }
 #endif

@@ -67,6 +67,7 @@ struct sarbp_ctx {
     cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
     std::string err;
     DevBuf echo, spec, rc, scale, apc, image, partial, errword, power, targets, pref;
+    DevBuf corr, weight, proj, projout, sharp;  // per-pulse corrections, projection and autofocus scratch
     RcTables tables;
     int64_t launches = 0;
     int checked = 0;  // SARBP_BOUNDS_CHECK=1 at creation: clamped, self-reporting BP kernels
@@ -255,7 +256,7 @@ sarbp_status check_grid(sarbp_ctx *ctx, const sarbp_grid *g) {
 // Back-projection of device-resident rc + apc into a device image.
 sarbp_status bp_device(sarbp_ctx *ctx, const sarbp_radar *r, const sarbp_rc_view &rc, const double *apc_dev,
                        const double *apc_host, const sarbp_grid *g, int mode, float2 *image, int accumulate,
-                       cudaStream_t s) {
+                       cudaStream_t s, const double *dr_dev = nullptr, const double *dph_dev = nullptr) {
     const int np = rc.np;
     if (g->nx == 0 || g->ny == 0) return SARBP_OK;
     if (np == 0) {
@@ -277,6 +278,8 @@ sarbp_status bp_device(sarbp_ctx *ctx, const sarbp_radar *r, const sarbp_rc_view
     p.accumulate = accumulate;
     p.err = ctx->errword.as<unsigned>();
     p.checked = ctx->checked;
+    p.drange = dr_dev;
+    p.dphase = dph_dev;
     SARBP_CUDA(ctx, ctx->pref.ensure(sizeof(float) * 8 * (size_t)np), "alloc pulse references");
     p.pref = ctx->pref.as<float4>();
     if (p.segments > 1) {
@@ -290,6 +293,128 @@ sarbp_status bp_device(sarbp_ctx *ctx, const sarbp_radar *r, const sarbp_rc_view
     cudaEventRecord(ctx->ev[3], s);
     ctx->timed_bp = true;
     ctx->launches += launches;
+    return SARBP_OK;
+}
+
+// Weighted projection of device-resident rc + apc against a device weight
+// image into out[np] (device, complex128).
+sarbp_status project_device(sarbp_ctx *ctx, const sarbp_radar *r, const sarbp_rc_view &rc, const double *apc_dev,
+                            const double *apc_host, const sarbp_grid *g, int mode, const float2 *weight,
+                            double2 *out, cudaStream_t s, const double *dr_dev, const double *dph_dev) {
+    const int np = rc.np;
+    if (np == 0) return SARBP_OK;
+    if (rc.nbins % 4 != 0) return fail(ctx, SARBP_ERR_UNSUPPORTED, "nbins must be a multiple of 4");
+    if (((uintptr_t)rc.data & 15) != 0) return fail(ctx, SARBP_ERR_INVALID_ARGUMENT, "rc data must be 16-byte aligned");
+    BpPlan p;
+    std::string why;
+    if (!sarbp::plan_bp(ctx->sms, *r, rc, apc_host, np, *g, mode, 0, p, why))
+        return fail(ctx, SARBP_ERR_UNSUPPORTED, "%s", why.c_str());
+    p.rc = rc.data;
+    p.scale = rc.scale;
+    p.np = np;
+    p.apc = apc_dev;
+    p.err = ctx->errword.as<unsigned>();
+    p.checked = 0;
+    p.drange = dr_dev;
+    p.dphase = dph_dev;
+    p.weight = weight;
+    SARBP_CUDA(ctx, ctx->pref.ensure(sizeof(float) * 8 * (size_t)np), "alloc pulse references");
+    p.pref = ctx->pref.as<float4>();
+    SARBP_CUDA(ctx, ctx->proj.ensure(sizeof(float2) * sarbp::bp_tiles(p) * (size_t)np), "alloc projection scratch");
+    p.proj = ctx->proj.as<float2>();
+    int launches = 0;
+    SARBP_CUDA(ctx, sarbp::launch_project(p, out, s, &launches), "projection launch");
+    ctx->launches += launches;
+    return SARBP_OK;
+}
+
+// Device-side inputs of a back-projection-type call (uploads of host arrays
+// into the context's buffers) after validation.
+struct BpInputs {
+    sarbp_rc_view v{};
+    const double *apc_dev = nullptr, *apc_host = nullptr;
+    std::vector<double> apc_h;
+    const double *dr_dev = nullptr, *dph_dev = nullptr;
+    bool any_host = false;
+};
+
+sarbp_status stage_bp_inputs(sarbp_ctx *ctx, const sarbp_radar *radar, const sarbp_rc_view *rc, const double *apc,
+                             const sarbp_grid *grid, int32_t mode, const sarbp_pulse_corr *corr, cudaStream_t s,
+                             BpInputs &in) {
+    sarbp_status st = check_radar(ctx, radar);
+    if (st != SARBP_OK) return st;
+    if (!rc) return fail(ctx, SARBP_ERR_INVALID_ARGUMENT, "rc view is null");
+    st = check_grid(ctx, grid);
+    if (st != SARBP_OK) return st;
+    if (mode < SARBP_MODE_FP64 || mode > SARBP_MODE_FP16STORE)
+        return fail(ctx, SARBP_ERR_INVALID_ARGUMENT, "unknown mode %d", mode);
+    if (rc->np < 0 || rc->nbins < 0) return fail(ctx, SARBP_ERR_INVALID_ARGUMENT, "negative rc size");
+    if (rc->storage != SARBP_STORE_C64 && rc->storage != SARBP_STORE_C32H)
+        return fail(ctx, SARBP_ERR_INVALID_ARGUMENT, "unknown storage %d", rc->storage);
+    if (mode == SARBP_MODE_FP16STORE && rc->storage != SARBP_STORE_C32H)
+        return fail(ctx, SARBP_ERR_INVALID_ARGUMENT, "FP16STORE mode needs SARBP_STORE_C32H data");
+    if (!(rc->bin_rate > 0) || !std::isfinite(rc->t0_bins))
+        return fail(ctx, SARBP_ERR_INVALID_ARGUMENT, "rc bin_rate must be > 0 and t0_bins finite");
+    if (rc->np > 0 && (!rc->data || !apc)) return fail(ctx, SARBP_ERR_INVALID_ARGUMENT, "rc data and apc must be non-null");
+    if (rc->np > 0 && rc->nbins < 2) return fail(ctx, SARBP_ERR_INVALID_ARGUMENT, "nbins must be >= 2");
+    if (rc->storage == SARBP_STORE_C32H && rc->np > 0 && !rc->scale)
+        return fail(ctx, SARBP_ERR_INVALID_ARGUMENT, "fp16 storage needs a scale array");
+    const size_t esize = rc->storage == SARBP_STORE_C64 ? 8 : 4;
+    const int np = rc->np;
+    in.v = *rc;
+    in.apc_host = apc;
+    in.apc_dev = apc;
+    if (np == 0) return SARBP_OK;
+    // APC: always needed on the host for planning, and on the device for the kernel
+    if (is_device_ptr(apc)) {
+        in.apc_h.resize((size_t)3 * np);
+        SARBP_CUDA(ctx, cudaMemcpyAsync(in.apc_h.data(), apc, sizeof(double) * 3 * np, cudaMemcpyDeviceToHost, s),
+                   "read apc");
+        SARBP_CUDA(ctx, cudaStreamSynchronize(s), "read apc");
+        in.apc_host = in.apc_h.data();
+    } else {
+        SARBP_CUDA(ctx, ctx->apc.ensure(sizeof(double) * 3 * np), "alloc apc");
+        SARBP_CUDA(ctx, cudaMemcpyAsync(ctx->apc.ptr, apc, sizeof(double) * 3 * np, cudaMemcpyHostToDevice, s),
+                   "upload apc");
+        in.apc_dev = ctx->apc.as<double>();
+        in.any_host = true;
+    }
+    for (size_t i = 0; i < (size_t)3 * np; ++i)
+        if (!std::isfinite(in.apc_host[i])) return fail(ctx, SARBP_ERR_INVALID_ARGUMENT, "apc must be finite");
+    if (!is_device_ptr(rc->data)) {
+        SARBP_CUDA(ctx, ctx->rc.ensure(esize * (size_t)np * rc->nbins), "alloc rc");
+        SARBP_CUDA(ctx, cudaMemcpyAsync(ctx->rc.ptr, rc->data, esize * (size_t)np * rc->nbins, cudaMemcpyHostToDevice, s),
+                   "upload rc");
+        in.v.data = ctx->rc.ptr;
+        in.any_host = true;
+    }
+    if (rc->storage == SARBP_STORE_C32H && !is_device_ptr(rc->scale)) {
+        SARBP_CUDA(ctx, ctx->scale.ensure(sizeof(float) * np), "alloc scale");
+        SARBP_CUDA(ctx, cudaMemcpyAsync(ctx->scale.ptr, rc->scale, sizeof(float) * np, cudaMemcpyHostToDevice, s),
+                   "upload scale");
+        in.v.scale = ctx->scale.as<float>();
+        in.any_host = true;
+    }
+    if (corr && (corr->drange || corr->dphase)) {
+        SARBP_CUDA(ctx, ctx->corr.ensure(sizeof(double) * 2 * (size_t)np), "alloc corrections");
+        const double *src[2] = {corr->drange, corr->dphase};
+        const double **dst[2] = {&in.dr_dev, &in.dph_dev};
+        for (int k = 0; k < 2; ++k) {
+            if (!src[k]) continue;
+            if (is_device_ptr(src[k])) {
+                *dst[k] = src[k];
+            } else {
+                for (int i = 0; i < np; ++i)
+                    if (!std::isfinite(src[k][i]))
+                        return fail(ctx, SARBP_ERR_INVALID_ARGUMENT, "pulse corrections must be finite");
+                double *d = ctx->corr.as<double>() + (size_t)k * np;
+                SARBP_CUDA(ctx, cudaMemcpyAsync(d, src[k], sizeof(double) * np, cudaMemcpyHostToDevice, s),
+                           "upload corrections");
+                *dst[k] = d;
+                in.any_host = true;
+            }
+        }
+    }
     return SARBP_OK;
 }
 
@@ -450,74 +575,24 @@ sarbp_status sarbp_range_compress(sarbp_ctx *ctx, const sarbp_radar *radar, cons
     return finish(ctx, s, !dev_in || !dev_out || !dev_sc);
 }
 
-sarbp_status sarbp_backproject(sarbp_ctx *ctx, const sarbp_radar *radar, const sarbp_rc_view *rc,
-                               const double *apc, const sarbp_grid *grid, int32_t mode, sarbp_complex64 *image,
-                               int32_t accumulate, void *stream) {
+sarbp_status sarbp_backproject_ex(sarbp_ctx *ctx, const sarbp_radar *radar, const sarbp_rc_view *rc,
+                                  const double *apc, const sarbp_grid *grid, int32_t mode,
+                                  const sarbp_pulse_corr *corr, sarbp_complex64 *image, int32_t accumulate,
+                                  void *stream) {
     if (!ctx) return SARBP_ERR_INVALID_ARGUMENT;
     ctx->err.clear();
     cudaSetDevice(ctx->device);
-    sarbp_status st = check_radar(ctx, radar);
+    cudaStream_t s = pick_stream(ctx, stream);
+    if (grid && (size_t)grid->nx * grid->ny > 0 && !image)
+        return fail(ctx, SARBP_ERR_INVALID_ARGUMENT, "image is null");
+    BpInputs in;
+    sarbp_status st = stage_bp_inputs(ctx, radar, rc, apc, grid, mode, corr, s, in);
     if (st != SARBP_OK) return st;
-    if (!rc) return fail(ctx, SARBP_ERR_INVALID_ARGUMENT, "rc view is null");
-    st = check_grid(ctx, grid);
-    if (st != SARBP_OK) return st;
-    if (mode < SARBP_MODE_FP64 || mode > SARBP_MODE_FP16STORE)
-        return fail(ctx, SARBP_ERR_INVALID_ARGUMENT, "unknown mode %d", mode);
-    if (rc->np < 0 || rc->nbins < 0) return fail(ctx, SARBP_ERR_INVALID_ARGUMENT, "negative rc size");
-    if (rc->storage != SARBP_STORE_C64 && rc->storage != SARBP_STORE_C32H)
-        return fail(ctx, SARBP_ERR_INVALID_ARGUMENT, "unknown storage %d", rc->storage);
-    if (mode == SARBP_MODE_FP16STORE && rc->storage != SARBP_STORE_C32H)
-        return fail(ctx, SARBP_ERR_INVALID_ARGUMENT, "FP16STORE mode needs SARBP_STORE_C32H data");
-    if (!(rc->bin_rate > 0) || !std::isfinite(rc->t0_bins))
-        return fail(ctx, SARBP_ERR_INVALID_ARGUMENT, "rc bin_rate must be > 0 and t0_bins finite");
     const size_t npix = (size_t)grid->nx * grid->ny;
     if (npix == 0) return SARBP_OK;
-    if (!image) return fail(ctx, SARBP_ERR_INVALID_ARGUMENT, "image is null");
-    if (rc->np > 0 && (!rc->data || !apc)) return fail(ctx, SARBP_ERR_INVALID_ARGUMENT, "rc data and apc must be non-null");
-    if (rc->np > 0 && rc->nbins < 2) return fail(ctx, SARBP_ERR_INVALID_ARGUMENT, "nbins must be >= 2");
-    if (rc->storage == SARBP_STORE_C32H && rc->np > 0 && !rc->scale)
-        return fail(ctx, SARBP_ERR_INVALID_ARGUMENT, "fp16 storage needs a scale array");
-    cudaStream_t s = pick_stream(ctx, stream);
-    const size_t esize = rc->storage == SARBP_STORE_C64 ? 8 : 4;
-    const int np = rc->np;
-    bool any_host = false;
-    // APC: always needed on the host for planning, and on the device for the kernel
-    std::vector<double> apc_h;
-    const double *apc_host = apc, *apc_dev = apc;
-    if (np > 0) {
-        if (is_device_ptr(apc)) {
-            apc_h.resize((size_t)3 * np);
-            SARBP_CUDA(ctx, cudaMemcpyAsync(apc_h.data(), apc, sizeof(double) * 3 * np, cudaMemcpyDeviceToHost, s),
-                       "read apc");
-            SARBP_CUDA(ctx, cudaStreamSynchronize(s), "read apc");
-            apc_host = apc_h.data();
-        } else {
-            SARBP_CUDA(ctx, ctx->apc.ensure(sizeof(double) * 3 * np), "alloc apc");
-            SARBP_CUDA(ctx, cudaMemcpyAsync(ctx->apc.ptr, apc, sizeof(double) * 3 * np, cudaMemcpyHostToDevice, s),
-                       "upload apc");
-            apc_dev = ctx->apc.as<double>();
-            any_host = true;
-        }
-        for (size_t i = 0; i < (size_t)3 * np; ++i)
-            if (!std::isfinite(apc_host[i])) return fail(ctx, SARBP_ERR_INVALID_ARGUMENT, "apc must be finite");
-    }
-    sarbp_rc_view v = *rc;
-    if (np > 0 && !is_device_ptr(rc->data)) {
-        SARBP_CUDA(ctx, ctx->rc.ensure(esize * (size_t)np * rc->nbins), "alloc rc");
-        SARBP_CUDA(ctx, cudaMemcpyAsync(ctx->rc.ptr, rc->data, esize * (size_t)np * rc->nbins, cudaMemcpyHostToDevice, s),
-                   "upload rc");
-        v.data = ctx->rc.ptr;
-        any_host = true;
-    }
-    if (np > 0 && rc->storage == SARBP_STORE_C32H && !is_device_ptr(rc->scale)) {
-        SARBP_CUDA(ctx, ctx->scale.ensure(sizeof(float) * np), "alloc scale");
-        SARBP_CUDA(ctx, cudaMemcpyAsync(ctx->scale.ptr, rc->scale, sizeof(float) * np, cudaMemcpyHostToDevice, s),
-                   "upload scale");
-        v.scale = ctx->scale.as<float>();
-        any_host = true;
-    }
     float2 *d_img = reinterpret_cast<float2 *>(image);
     const bool dev_img = is_device_ptr(image);
+    bool any_host = in.any_host;
     if (!dev_img) {
         SARBP_CUDA(ctx, ctx->image.ensure(sizeof(float2) * npix), "alloc image");
         d_img = ctx->image.as<float2>();
@@ -526,11 +601,141 @@ sarbp_status sarbp_backproject(sarbp_ctx *ctx, const sarbp_radar *radar, const s
         any_host = true;
     }
     ctx->timed_rc = false;
-    st = bp_device(ctx, radar, v, apc_dev, apc_host, grid, mode, d_img, accumulate, s);
+    st = bp_device(ctx, radar, in.v, in.apc_dev, in.apc_host, grid, mode, d_img, accumulate, s, in.dr_dev, in.dph_dev);
     if (st != SARBP_OK) return st;
     if (!dev_img)
         SARBP_CUDA(ctx, cudaMemcpyAsync(image, d_img, sizeof(float2) * npix, cudaMemcpyDeviceToHost, s), "download image");
     return finish(ctx, s, any_host);
+}
+
+sarbp_status sarbp_backproject(sarbp_ctx *ctx, const sarbp_radar *radar, const sarbp_rc_view *rc,
+                               const double *apc, const sarbp_grid *grid, int32_t mode, sarbp_complex64 *image,
+                               int32_t accumulate, void *stream) {
+    return sarbp_backproject_ex(ctx, radar, rc, apc, grid, mode, nullptr, image, accumulate, stream);
+}
+
+sarbp_status sarbp_project_weighted(sarbp_ctx *ctx, const sarbp_radar *radar, const sarbp_rc_view *rc,
+                                    const double *apc, const sarbp_grid *grid, int32_t mode,
+                                    const sarbp_pulse_corr *corr, const sarbp_complex64 *weight, double *out,
+                                    void *stream) {
+    if (!ctx) return SARBP_ERR_INVALID_ARGUMENT;
+    ctx->err.clear();
+    cudaSetDevice(ctx->device);
+    if (mode != SARBP_MODE_SPLIT && mode != SARBP_MODE_FP16STORE)
+        return fail(ctx, SARBP_ERR_UNSUPPORTED, "weighted projection runs in SPLIT or FP16STORE mode");
+    cudaStream_t s = pick_stream(ctx, stream);
+    BpInputs in;
+    sarbp_status st = stage_bp_inputs(ctx, radar, rc, apc, grid, mode, corr, s, in);
+    if (st != SARBP_OK) return st;
+    const int np = rc->np;
+    if (np == 0) return SARBP_OK;
+    if (!out) return fail(ctx, SARBP_ERR_INVALID_ARGUMENT, "out is null");
+    const size_t npix = (size_t)grid->nx * grid->ny;
+    bool any_host = in.any_host;
+    double2 *d_out = reinterpret_cast<double2 *>(out);
+    const bool dev_out = is_device_ptr(out);
+    if (!dev_out) {
+        SARBP_CUDA(ctx, ctx->projout.ensure(sizeof(double2) * np), "alloc projection output");
+        d_out = ctx->projout.as<double2>();
+        any_host = true;
+    }
+    if (npix == 0) {
+        SARBP_CUDA(ctx, cudaMemsetAsync(d_out, 0, sizeof(double2) * np, s), "clear projection");
+    } else {
+        if (!weight) return fail(ctx, SARBP_ERR_INVALID_ARGUMENT, "weight is null");
+        const float2 *d_w = reinterpret_cast<const float2 *>(weight);
+        if (!is_device_ptr(weight)) {
+            SARBP_CUDA(ctx, ctx->weight.ensure(sizeof(float2) * npix), "alloc weight");
+            SARBP_CUDA(ctx, cudaMemcpyAsync(ctx->weight.ptr, weight, sizeof(float2) * npix, cudaMemcpyHostToDevice, s),
+                       "upload weight");
+            d_w = ctx->weight.as<float2>();
+            any_host = true;
+        }
+        st = project_device(ctx, radar, in.v, in.apc_dev, in.apc_host, grid, mode, d_w, d_out, s, in.dr_dev,
+                            in.dph_dev);
+        if (st != SARBP_OK) return st;
+    }
+    if (!dev_out)
+        SARBP_CUDA(ctx, cudaMemcpyAsync(out, d_out, sizeof(double2) * np, cudaMemcpyDeviceToHost, s), "download projection");
+    return finish(ctx, s, any_host);
+}
+
+sarbp_status sarbp_autofocus(sarbp_ctx *ctx, const sarbp_radar *radar, const sarbp_rc_view *rc, const double *apc,
+                             const sarbp_grid *grid, int32_t mode, int32_t iterations, const double *drange,
+                             double *dphase, sarbp_complex64 *image, double *sharpness, void *stream) {
+    if (!ctx) return SARBP_ERR_INVALID_ARGUMENT;
+    ctx->err.clear();
+    cudaSetDevice(ctx->device);
+    if (mode != SARBP_MODE_SPLIT && mode != SARBP_MODE_FP16STORE)
+        return fail(ctx, SARBP_ERR_UNSUPPORTED, "autofocus runs in SPLIT or FP16STORE mode");
+    if (iterations < 0 || iterations > 1000) return fail(ctx, SARBP_ERR_INVALID_ARGUMENT, "iterations out of range");
+    if (!dphase) return fail(ctx, SARBP_ERR_INVALID_ARGUMENT, "dphase is null");
+    if (is_device_ptr(dphase) || (drange && is_device_ptr(drange)) || (sharpness && is_device_ptr(sharpness)))
+        return fail(ctx, SARBP_ERR_INVALID_ARGUMENT, "dphase, drange and sharpness are host arrays");
+    cudaStream_t s = pick_stream(ctx, stream);
+    sarbp_pulse_corr c0{drange, nullptr};
+    BpInputs in;
+    sarbp_status st = stage_bp_inputs(ctx, radar, rc, apc, grid, mode, &c0, s, in);
+    if (st != SARBP_OK) return st;
+    const int np = rc->np;
+    const size_t npix = (size_t)grid->nx * grid->ny;
+    if (np == 0 || npix == 0) return finish(ctx, s, true);
+    std::vector<double> ph(dphase, dphase + np);
+    for (double v : ph)
+        if (!std::isfinite(v)) return fail(ctx, SARBP_ERR_INVALID_ARGUMENT, "dphase must be finite");
+    // device state: phases (in the second half of the correction buffer, which
+    // stage_bp_inputs sized for 2 np), image, weights, projection, sharpness partials
+    SARBP_CUDA(ctx, ctx->corr.ensure(sizeof(double) * 2 * (size_t)np), "alloc corrections");
+    double *d_ph = ctx->corr.as<double>() + np;
+    const bool dev_img = is_device_ptr(image);
+    float2 *d_img = dev_img ? reinterpret_cast<float2 *>(image) : nullptr;
+    if (!dev_img) {
+        SARBP_CUDA(ctx, ctx->image.ensure(sizeof(float2) * npix), "alloc image");
+        d_img = ctx->image.as<float2>();
+    }
+    SARBP_CUDA(ctx, ctx->weight.ensure(sizeof(float2) * npix), "alloc weight");
+    SARBP_CUDA(ctx, ctx->projout.ensure(sizeof(double2) * np), "alloc projection output");
+    const int nb = sarbp::sharpness_blocks(npix);
+    SARBP_CUDA(ctx, ctx->sharp.ensure(sizeof(double) * nb), "alloc sharpness");
+    std::vector<double2> cp(np);
+    std::vector<double> part(nb);
+    float2 *d_w = ctx->weight.as<float2>();
+    for (int it = 0; it <= iterations; ++it) {
+        SARBP_CUDA(ctx, cudaMemcpyAsync(d_ph, ph.data(), sizeof(double) * np, cudaMemcpyHostToDevice, s), "upload phases");
+        st = bp_device(ctx, radar, in.v, in.apc_dev, in.apc_host, grid, mode, d_img, 0, s, in.dr_dev, d_ph);
+        if (st != SARBP_OK) return st;
+        const bool last = it == iterations;
+        SARBP_CUDA(ctx, sarbp::launch_sharpness_weight(d_img, npix, last ? nullptr : d_w, ctx->sharp.as<double>(), s),
+                   "sharpness");
+        ctx->launches += 1;
+        if (!last) {
+            st = project_device(ctx, radar, in.v, in.apc_dev, in.apc_host, grid, mode, d_w, ctx->projout.as<double2>(),
+                                s, in.dr_dev, d_ph);
+            if (st != SARBP_OK) return st;
+            SARBP_CUDA(ctx, cudaMemcpyAsync(cp.data(), ctx->projout.ptr, sizeof(double2) * np, cudaMemcpyDeviceToHost, s),
+                       "download projection");
+        }
+        SARBP_CUDA(ctx, cudaMemcpyAsync(part.data(), ctx->sharp.ptr, sizeof(double) * nb, cudaMemcpyDeviceToHost, s),
+                   "download sharpness");
+        SARBP_CUDA(ctx, cudaStreamSynchronize(s), "autofocus iteration");
+        st = check_errword(ctx);
+        if (st != SARBP_OK) return st;
+        double sum = 0.0;
+        for (double v : part) sum += v;
+        if (sharpness) sharpness[it] = sum;
+        if (last) break;
+        double mean = 0.0;
+        for (int p = 0; p < np; ++p) {
+            ph[p] -= std::atan2(cp[p].y, cp[p].x);
+            mean += ph[p];
+        }
+        mean /= np;
+        for (int p = 0; p < np; ++p) ph[p] -= mean;
+    }
+    std::copy(ph.begin(), ph.end(), dphase);
+    if (image && !dev_img)
+        SARBP_CUDA(ctx, cudaMemcpyAsync(image, d_img, sizeof(float2) * npix, cudaMemcpyDeviceToHost, s), "download image");
+    return finish(ctx, s, true);
 }
 
 sarbp_status sarbp_image(sarbp_ctx *ctx, const sarbp_radar *radar, const sarbp_complex64 *echo, int32_t np,

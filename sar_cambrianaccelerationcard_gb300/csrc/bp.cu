@@ -63,6 +63,7 @@ struct __align__(16) Prm {
     float4 k2;     // SPLIT: bin', bin', phT, phT
     float4 k3;     // SPLIT: A, A, B, B
     double ax, ay, az;  // FP64: APC position
+    double dr, dph;     // FP64: per-pulse range (m) and phase (rad) corrections
     int ws;        // first bin of the window
     int lo, hi;    // copied part of the window [lo, hi) relative to ws
     float scale;   // FP16 storage scale
@@ -165,6 +166,7 @@ struct Smem {
     unsigned char *raw;  // [kStages][kChunk][win] * 8 bytes
     Prm *prm;            // [kStages][kChunk]
     uint64_t *bar;       // [kStages]
+    float2 *red;         // [2][kWarps][kChunk] per-warp pulse sums (weighted projection)
 };
 
 __device__ __forceinline__ Smem carve(unsigned char *base, int win) {
@@ -173,6 +175,7 @@ __device__ __forceinline__ Smem carve(unsigned char *base, int win) {
     s.raw = base + (size_t)2 * kChunk * win * 16;
     s.prm = reinterpret_cast<Prm *>(s.raw + (size_t)kStages * kChunk * win * 8);
     s.bar = reinterpret_cast<uint64_t *>(s.prm + kStages * kChunk);
+    s.red = reinterpret_cast<float2 *>(s.bar + kStages);
     return s;
 }
 
@@ -212,16 +215,26 @@ __device__ __forceinline__ ff ff_mul_f(ff a, float b) {
 //   a0 = |O - apc|^2, a1 = 2 ux.(O - apc), a2 = 2 uy.(O - apc)
 // stored as float pairs: pref[2p] = (a0h, a0l, a1h, a1l), pref[2p+1] = (a2h, a2l, 0, 0).
 // With (xT, yT) a tile centre in pixel units, R_T^2 = a0 + xT a1 + yT a2 + |q_T|^2.
-__global__ void pulse_ref_kernel(const double *__restrict__ apc, int np, BpGeom g, float4 *__restrict__ pref) {
+// Per-pulse references for the SPLIT path.  The optional corrections enter
+// as a bin offset db = drange * (2 bin_rate / c) and a phase offset
+// dph = 2 pi frac(drange * 2 fc / c) + dphase (wrapped to [-pi, pi]), applied to
+// the tile-centre bin and phase, so they cost nothing per update.
+__global__ void pulse_ref_kernel(const double *__restrict__ apc, int np, BpGeom g, const double *__restrict__ drange,
+                                 const double *__restrict__ dphase, double bins_per_m, double cyc_per_m,
+                                 float4 *__restrict__ pref) {
     const int p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= np) return;
+    const double dr = drange ? drange[p] : 0.0;
+    const double cyc = dr * cyc_per_m;
+    double dph = 2.0 * CUDART_PI * (cyc - rint(cyc)) + (dphase ? dphase[p] : 0.0);
+    dph -= 2.0 * CUDART_PI * rint(dph * (0.5 / CUDART_PI));
     const double wx = g.origin[0] - apc[3 * p], wy = g.origin[1] - apc[3 * p + 1], wz = g.origin[2] - apc[3 * p + 2];
     const double a0 = fma(wx, wx, fma(wy, wy, wz * wz));
     const double a1 = 2.0 * (g.ux[0] * wx + g.ux[1] * wy + g.ux[2] * wz);
     const double a2 = 2.0 * (g.uy[0] * wx + g.uy[1] * wy + g.uy[2] * wz);
     const float a0h = (float)a0, a1h = (float)a1, a2h = (float)a2;
     pref[2 * p] = make_float4(a0h, (float)(a0 - (double)a0h), a1h, (float)(a1 - (double)a1h));
-    pref[2 * p + 1] = make_float4(a2h, (float)(a2 - (double)a2h), 0.f, 0.f);
+    pref[2 * p + 1] = make_float4(a2h, (float)(a2 - (double)a2h), (float)(dr * bins_per_m), (float)dph);
 }
 
 // Per-(tile, pulse) geometry, window and TMA issue for this warp's pulses of
@@ -257,13 +270,13 @@ __device__ __forceinline__ void produce(const BpPlan &P, const Smem &S, int stag
             const float kbh = P.kb_h, kbl = P.kb_l;
             float ph_ = r * kbh;
             float pl_ = fmaf(r, kbh, -ph_) + fmaf(r, kbl, corr * kbh);
-            const ff bT = ff_add(quick_two_sum(ph_, pl_), ff{-P.tb_h, -P.tb_l});
+            const ff bT = ff_add(ff_add(quick_two_sum(ph_, pl_), ff{-P.tb_h, -P.tb_l}), ff{r1v.z, 0.f});
             // carrier phase 2 pi frac(R_T * 2 fc / c)
             const float kch = P.kc_h, kcl = P.kc_l;
             const float cy = r * kch;
             const float cy_e = fmaf(r, kch, -cy) + fmaf(r, kcl, corr * kch);
             const float fr = (cy - rintf(cy)) + cy_e;
-            const float phT = fr * 6.28318530717958647692f;
+            const float phT = fmaf(fr, 6.28318530717958647692f, r1v.w);
             const float iR = 1.0f / r;
             const float A = r0v.z + 2.f * (T.xT * (float)P.g.g11 + T.yT * (float)P.g.g12);
             const float B = r1v.x + 2.f * (T.xT * (float)P.g.g12 + T.yT * (float)P.g.g22);
@@ -287,7 +300,9 @@ __device__ __forceinline__ void produce(const BpPlan &P, const Smem &S, int stag
         } else {
             const double ax = __ldg(&P.apc[3 * p]), ay = __ldg(&P.apc[3 * p + 1]), az = __ldg(&P.apc[3 * p + 2]);
             const double wx = T.pcx - ax, wy = T.pcy - ay, wz = T.pcz - az;
-            const double R = sqrt(fma(wx, wx, fma(wy, wy, wz * wz)));
+            const double dr = P.drange ? __ldg(&P.drange[p]) : 0.0;
+            const double dph = P.dphase ? __ldg(&P.dphase[p]) : 0.0;
+            const double R = sqrt(fma(wx, wx, fma(wy, wy, wz * wz))) + dr;
             const float iR = (float)(1.0 / R);
             const float wxf = (float)wx, wyf = (float)wy, wzf = (float)wz;
             const float A = 2.f * ((float)P.g.ux[0] * wxf + (float)P.g.ux[1] * wyf + (float)P.g.ux[2] * wzf);
@@ -299,9 +314,15 @@ __device__ __forceinline__ void produce(const BpPlan &P, const Smem &S, int stag
             ws &= ~3LL;
             const long long need_end = (long long)ceilf(fminf(bTf + half, 1.0e9f)) + 2;
             sane = isfinite(R) && R > 0.0 && isfinite(half) && need_end - ws <= win;
-            if (MODE == SARBP_MODE_FP32)
+            if (MODE == SARBP_MODE_FP32) {
+                const double kph_d = 4.0 * CUDART_PI * P.fc / P.c;
                 q.k0 = make_float4((float)ax, (float)ay, (float)az,
-                                   (float)(-P.t0_bins * P.bin_rate - (double)ws - 0.5 - (double)cen));
+                                   (float)(dr * (2.0 / P.c * P.bin_rate) - P.t0_bins * P.bin_rate - (double)ws - 0.5 -
+                                           (double)cen));
+                q.k1 = make_float4((float)(kph_d * dr + dph), 0.f, 0.f, 0.f);
+            }
+            q.dr = dr;
+            q.dph = dph;
             q.ax = ax;
             q.ay = ay;
             q.az = az;
@@ -360,9 +381,29 @@ __device__ __forceinline__ void convert(const Smem &S, int stage, int sbuf, int 
     }
 }
 
-template <int MODE, int STORE, int NTERMS, bool CHECKED, int PIX>
+// Sum of the warps' projections for the pulses of one chunk into
+// proj[tile][pulse] (fixed order: deterministic).
+__device__ __forceinline__ void flush_projection(const BpPlan &P, const Smem &S, int buf, int p0, int count) {
+    const int t = threadIdx.x;
+    if (t < count) {
+        float sr = 0.f, si = 0.f;
+#pragma unroll
+        for (int w = 0; w < kWarps; ++w) {
+            const float2 v = S.red[(buf * kWarps + w) * kChunk + t];
+            sr += v.x;
+            si += v.y;
+        }
+        P.proj[(size_t)blockIdx.x * P.np + p0 + t] = make_float2(sr, si);
+    }
+}
+
+// ADJ: weighted projection (the adjoint) instead of back-projection: every
+// pixel's term of pulse p is multiplied by conj(weight[pixel]) and summed over
+// the tile into proj[tile][p] (SPLIT / FP16STORE arithmetic).
+template <int MODE, int STORE, int NTERMS, bool CHECKED, int PIX, bool ADJ = false>
 __global__ void __launch_bounds__(kThreads, SARBP_BP_MINBLOCKS)
     bp_kernel(const __grid_constant__ BpPlan P, int tiles_y, int pulses_per_seg, float qq_max) {
+    static_assert(!ADJ || MODE == SARBP_MODE_SPLIT || MODE == SARBP_MODE_FP16STORE, "projection: split arithmetic");
     constexpr int kPix = PIX;  // pixels per thread, all in one column
     constexpr int kTileY = 8 * PIX;
     extern __shared__ __align__(128) unsigned char smem_raw[];
@@ -429,6 +470,19 @@ __global__ void __launch_bounds__(kThreads, SARBP_BP_MINBLOCKS)
     const float kph_lo = (float)(kph_d - (double)kph_hi);
     const float wmax = (float)(win - 2);
 
+    // weighted projection: conj(weight) of this thread's pixels (zero outside the grid)
+    float wr[ADJ ? kPix : 1], wi[ADJ ? kPix : 1];
+    if constexpr (ADJ) {
+#pragma unroll
+        for (int j = 0; j < kPix; ++j) {
+            const int x = tx * kTileX + xl, y = ty * kTileY + ((warp >> 2) + 2 * j) * 4 + ly;
+            float2 w = make_float2(0.f, 0.f);
+            if (x < P.g.nx && y < P.g.ny) w = __ldg(&P.weight[(size_t)y * P.g.nx + x]);
+            wr[j] = w.x;
+            wi[j] = w.y;
+        }
+    }
+
     float fpy[kPix], fpz[kPix], fpxx[kPix];
     if (MODE == SARBP_MODE_FP32) {
 #pragma unroll
@@ -468,6 +522,9 @@ __global__ void __launch_bounds__(kThreads, SARBP_BP_MINBLOCKS)
         if (__syncthreads_or(failed)) { failed = true; break; }
         convert<MODE, STORE>(S, stage, sbuf, count, win, win_magic);
         __syncthreads();
+        if constexpr (ADJ) {  // every warp has finished chunk c-1: combine its pulse sums
+            if (c > 0) flush_projection(P, S, (c - 1) & 1, pc0 - kChunk, kChunk);
+        }
 
         const float4 *stg = S.staged + (size_t)sbuf * kChunk * win;
         const unsigned sbase = smem_addr(stg) - kMagicBitsShift4;
@@ -485,6 +542,7 @@ __global__ void __launch_bounds__(kThreads, SARBP_BP_MINBLOCKS)
                 lds2x2(&q.k2, BT, PHT);
                 lds2x2(&q.k3, AA, BB);
                 const f2 XA = fmul2(XC2, AA);
+                float tr = 0.f, ti = 0.f;  // projection: this thread's sum for the pulse
 #pragma unroll
                 for (int h = 0; h < kPix / 2; ++h) {
                     const f2 n = ffma2(YC2[h], BB, fadd2(XA, QQ2[h]));
@@ -516,9 +574,23 @@ __global__ void __launch_bounds__(kThreads, SARBP_BP_MINBLOCKS)
                         const float si = fmaf(bb[u], v.w, v.y);
                         float sn, cs;
                         __sincosf(ph[u], &sn, &cs);
-                        acc_r[j] = fmaf(sr, cs, fmaf(-si, sn, acc_r[j]));
-                        acc_i[j] = fmaf(sr, sn, fmaf(si, cs, acc_i[j]));
+                        if constexpr (ADJ) {
+                            const float ur = fmaf(sr, cs, -si * sn), ui = fmaf(sr, sn, si * cs);
+                            tr = fmaf(wr[j], ur, fmaf(wi[j], ui, tr));
+                            ti = fmaf(wr[j], ui, fmaf(-wi[j], ur, ti));
+                        } else {
+                            acc_r[j] = fmaf(sr, cs, fmaf(-si, sn, acc_r[j]));
+                            acc_i[j] = fmaf(sr, sn, fmaf(si, cs, acc_i[j]));
+                        }
                     }
+                }
+                if constexpr (ADJ) {
+#pragma unroll
+                    for (int o = 16; o > 0; o >>= 1) {
+                        tr += __shfl_xor_sync(0xffffffffu, tr, o);
+                        ti += __shfl_xor_sync(0xffffffffu, ti, o);
+                    }
+                    if (lane == 0) S.red[((c & 1) * kWarps + warp) * kChunk + pl] = make_float2(tr, ti);
                 }
                 MP = fadd2(MP, WIN2);
             }
@@ -527,6 +599,7 @@ __global__ void __launch_bounds__(kThreads, SARBP_BP_MINBLOCKS)
             for (int pl = 0; pl < count; ++pl) {
                 const Prm &q = S.prm[stage * kChunk + pl];
                 const float4 k0 = q.k0;
+                const float phc = q.k1.x;  // per-pulse phase correction
                 const float mp = kMagic + (float)(pl * win + cen);
                 const float kph = (float)kph_d;
 #pragma unroll
@@ -540,7 +613,7 @@ __global__ void __launch_bounds__(kThreads, SARBP_BP_MINBLOCKS)
                     const float sr = fmaf(b, v.z, v.x);
                     const float si = fmaf(b, v.w, v.y);
                     float sn, cs;
-                    sincosf(kph * R, &sn, &cs);
+                    sincosf(fmaf(kph, R, phc), &sn, &cs);
                     acc_r[j] = fmaf(sr, cs, fmaf(-si, sn, acc_r[j]));
                     acc_i[j] = fmaf(sr, sn, fmaf(si, cs, acc_i[j]));
                 }
@@ -550,7 +623,7 @@ __global__ void __launch_bounds__(kThreads, SARBP_BP_MINBLOCKS)
 #pragma unroll 1
             for (int pl = 0; pl < count; ++pl) {
                 const Prm &q = S.prm[stage * kChunk + pl];
-                const double ax = q.ax, ay = q.ay, az = q.az;
+                const double ax = q.ax, ay = q.ay, az = q.az, dr = q.dr, dph_pi = q.dph / CUDART_PI;
                 const double boff = -P.t0_bins * P.bin_rate - (double)q.ws;
                 const float4 *st = stg + pl * win;
 #pragma unroll
@@ -560,7 +633,7 @@ __global__ void __launch_bounds__(kThreads, SARBP_BP_MINBLOCKS)
                     const double py = P.g.origin[1] + xi * P.g.ux[1] + yi * P.g.uy[1];
                     const double pz = P.g.origin[2] + xi * P.g.ux[2] + yi * P.g.uy[2];
                     const double dx = ax - px, dy = ay - py, dz = az - pz;
-                    const double R = sqrt(dx * dx + dy * dy + dz * dz);
+                    const double R = sqrt(dx * dx + dy * dy + dz * dz) + dr;
                     double b = fma(R, 2.0 / P.c * P.bin_rate, boff) - 0.5;
                     b = fmin(fmax(b, 0.0), (double)(win - 2));
                     const double r0 = rint(b);
@@ -570,7 +643,7 @@ __global__ void __launch_bounds__(kThreads, SARBP_BP_MINBLOCKS)
                     const double si = fma(f, (double)v.w, (double)v.y);
                     const double cyc = cyc_per_m * R;
                     double sn, cs;
-                    sincospi(2.0 * (cyc - rint(cyc)), &sn, &cs);
+                    sincospi(2.0 * (cyc - rint(cyc)) + dph_pi, &sn, &cs);
                     dacc_r[j] = fma(sr, cs, fma(-si, sn, dacc_r[j]));
                     dacc_i[j] = fma(sr, sn, fma(si, cs, dacc_i[j]));
                 }
@@ -586,6 +659,15 @@ __global__ void __launch_bounds__(kThreads, SARBP_BP_MINBLOCKS)
             for (int s = 0; s < kStages; ++s) mbar_wait_bounded(smem_addr(&S.bar[s]), 0, 500000000ull);
         }
         __syncthreads();
+        return;
+    }
+
+    if constexpr (ADJ) {
+        if (nchunks > 0) {
+            __syncthreads();
+            const int last = nchunks - 1;
+            flush_projection(P, S, last & 1, p_begin + last * kChunk, min(kChunk, p_end - p_begin - last * kChunk));
+        }
         return;
     }
 
@@ -625,9 +707,9 @@ __global__ void reduce_segments_kernel(const float2 *__restrict__ partial, int s
     }
 }
 
-template <int MODE, int STORE, int NTERMS, bool CHECKED, int PIX>
+template <int MODE, int STORE, int NTERMS, bool CHECKED, int PIX, bool ADJ = false>
 cudaError_t launch_variant(const BpPlan &p, cudaStream_t s, int tiles, int tiles_y, int pps, float qq_max) {
-    auto k = bp_kernel<MODE, STORE, NTERMS, CHECKED, PIX>;
+    auto k = bp_kernel<MODE, STORE, NTERMS, CHECKED, PIX, ADJ>;
     const size_t smem = bp_smem_bytes(MODE, p.win);
     cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
@@ -661,7 +743,78 @@ cudaError_t launch_pix(const BpPlan &p, cudaStream_t s, int tiles, int tiles_y, 
     }
 }
 
+// out[p] = sum over tiles of proj[tile][p], accumulated in FP64 in tile order.
+__global__ void proj_reduce_kernel(const float2 *__restrict__ proj, int tiles, int np, double2 *__restrict__ out) {
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= np) return;
+    double sr = 0.0, si = 0.0;
+    for (int t = 0; t < tiles; ++t) {
+        const float2 v = __ldg(&proj[(size_t)t * np + p]);
+        sr += v.x;
+        si += v.y;
+    }
+    out[p] = make_double2(sr, si);
+}
+
+template <int STORE, int PIX>
+cudaError_t launch_proj_pix(const BpPlan &p, cudaStream_t s, int tiles, int tiles_y, int pps, float qq_max) {
+    return p.nterms == 3 ? launch_variant<SARBP_MODE_SPLIT, STORE, 3, false, PIX, true>(p, s, tiles, tiles_y, pps, qq_max)
+                         : launch_variant<SARBP_MODE_SPLIT, STORE, 4, false, PIX, true>(p, s, tiles, tiles_y, pps, qq_max);
+}
+
+void launch_geometry(const BpPlan &p, int *tiles, int *tiles_y, int *pps, float *qq_max) {
+    const int tile_y = 8 * p.pix;
+    const int tiles_x = (p.g.nx + kTileX - 1) / kTileX;
+    *tiles_y = (p.g.ny + tile_y - 1) / tile_y;
+    *tiles = tiles_x * *tiles_y;
+    int n = (p.np + p.segments - 1) / p.segments;
+    *pps = (n + kChunk - 1) / kChunk * kChunk;
+    // |q|^2 bound over a tile (pixel offsets from the tile centre)
+    const double hx = 0.5 * (kTileX - 1), hy = 0.5 * (tile_y - 1);
+    *qq_max = (float)(hx * hx * p.g.g11 + 2.0 * hx * hy * fabs(p.g.g12) + hy * hy * p.g.g22);
+}
+
+cudaError_t launch_pulse_refs(const BpPlan &p, cudaStream_t s) {
+    pulse_ref_kernel<<<(p.np + 127) / 128, 128, 0, s>>>(p.apc, p.np, p.g, p.drange, p.dphase,
+                                                         2.0 / p.c * p.bin_rate, 2.0 * p.fc / p.c, p.pref);
+    return cudaGetLastError();
+}
+
 }  // namespace
+
+size_t bp_tiles(const BpPlan &p) {
+    int tiles, tiles_y, pps;
+    float qq;
+    launch_geometry(p, &tiles, &tiles_y, &pps, &qq);
+    return (size_t)tiles;
+}
+
+cudaError_t launch_project(const BpPlan &p, double2 *out, cudaStream_t s, int *launches) {
+    if (p.np <= 0) return cudaSuccess;
+    if (p.mode != SARBP_MODE_SPLIT && p.mode != SARBP_MODE_FP16STORE) return cudaErrorInvalidValue;
+    if (p.pix != 8 && p.pix != 4 && p.pix != 2) return cudaErrorInvalidValue;
+    if (!p.weight || !p.proj || !out) return cudaErrorInvalidValue;
+    if (p.g.nx <= 0 || p.g.ny <= 0) return cudaMemsetAsync(out, 0, sizeof(double2) * p.np, s);
+    int tiles, tiles_y, pps;
+    float qq_max;
+    launch_geometry(p, &tiles, &tiles_y, &pps, &qq_max);
+    cudaError_t e = launch_pulse_refs(p, s);
+    if (e != cudaSuccess) return e;
+    if (launches) ++*launches;
+    const bool fp16 = p.storage == SARBP_STORE_C32H;
+    if (p.pix == 8) e = fp16 ? launch_proj_pix<SARBP_STORE_C32H, 8>(p, s, tiles, tiles_y, pps, qq_max)
+                             : launch_proj_pix<SARBP_STORE_C64, 8>(p, s, tiles, tiles_y, pps, qq_max);
+    else if (p.pix == 4) e = fp16 ? launch_proj_pix<SARBP_STORE_C32H, 4>(p, s, tiles, tiles_y, pps, qq_max)
+                                  : launch_proj_pix<SARBP_STORE_C64, 4>(p, s, tiles, tiles_y, pps, qq_max);
+    else e = fp16 ? launch_proj_pix<SARBP_STORE_C32H, 2>(p, s, tiles, tiles_y, pps, qq_max)
+                  : launch_proj_pix<SARBP_STORE_C64, 2>(p, s, tiles, tiles_y, pps, qq_max);
+    if (e != cudaSuccess) return e;
+    if (launches) ++*launches;
+    proj_reduce_kernel<<<(p.np + 255) / 256, 256, 0, s>>>(p.proj, tiles, p.np, out);
+    e = cudaGetLastError();
+    if (launches) ++*launches;
+    return e;
+}
 
 void bp_tile_dims(int pix, int *tile_x, int *tile_y) {
     *tile_x = kTileX;
@@ -672,25 +825,18 @@ int bp_pulses_per_chunk(int) { return kChunk; }
 
 size_t bp_smem_bytes(int, int win) {
     return (size_t)2 * kChunk * win * 16 + (size_t)kStages * kChunk * win * 8 + kStages * kChunk * sizeof(Prm) +
-           kStages * sizeof(uint64_t);
+           kStages * sizeof(uint64_t) + 2 * kWarps * kChunk * sizeof(float2);
 }
 
 cudaError_t launch_bp(const BpPlan &p, cudaStream_t s, int *launches) {
     if (p.np <= 0 || p.g.nx <= 0 || p.g.ny <= 0) return cudaSuccess;
     if (p.pix != 8 && p.pix != 4 && p.pix != 2) return cudaErrorInvalidValue;
-    const int tile_y = 8 * p.pix;
-    const int tiles_x = (p.g.nx + kTileX - 1) / kTileX;
-    const int tiles_y = (p.g.ny + tile_y - 1) / tile_y;
-    const int tiles = tiles_x * tiles_y;
-    int pps = (p.np + p.segments - 1) / p.segments;
-    pps = (pps + kChunk - 1) / kChunk * kChunk;
-    // |q|^2 bound over a tile (pixel offsets from the tile centre)
-    const double hx = 0.5 * (kTileX - 1), hy = 0.5 * (tile_y - 1);
-    const float qq_max = (float)(hx * hx * p.g.g11 + 2.0 * hx * hy * fabs(p.g.g12) + hy * hy * p.g.g22);
+    int tiles, tiles_y, pps;
+    float qq_max;
+    launch_geometry(p, &tiles, &tiles_y, &pps, &qq_max);
     cudaError_t e;
     if (p.mode == SARBP_MODE_SPLIT || p.mode == SARBP_MODE_FP16STORE) {
-        pulse_ref_kernel<<<(p.np + 127) / 128, 128, 0, s>>>(p.apc, p.np, p.g, p.pref);
-        e = cudaGetLastError();
+        e = launch_pulse_refs(p, s);
         if (e != cudaSuccess) return e;
         if (launches) ++*launches;
     }

@@ -75,9 +75,18 @@ struct BpPlan {
     int checked;             // 1: clamp every interpolation index and report clamps
     int pix;                 // pixels per thread (8, 4 or 2): tiles of 32 x (8 pix) pixels
     unsigned *err;           // device error word
+    const double *drange;    // [np] device, per-pulse range corrections (m), or null
+    const double *dphase;    // [np] device, per-pulse phase corrections (rad), or null
+    const float2 *weight;    // [ny][nx] device, projection weights (launch_project only)
+    float2 *proj;            // [tiles][np] device scratch of tile sums (launch_project only)
 };
 
 cudaError_t launch_bp(const BpPlan &p, cudaStream_t s, int *launches);
+// Weighted projection (adjoint of back-projection, SPLIT / FP16STORE arithmetic):
+// out[p] = sum over pixels of conj(weight) * pulse p's term, via p.proj
+// ([bp_tiles(p)][np] float2 scratch) and a fixed-order reduction in FP64.
+cudaError_t launch_project(const BpPlan &p, double2 *out, cudaStream_t s, int *launches);
+size_t bp_tiles(const BpPlan &p);
 // Host planning (plan.cpp): fills every BpPlan field that does not depend on
 // buffers (geometry, constants, tile height, window, series terms, segments
 // for launches of `pulses_per_launch` pulses; 0 = all np).  On failure returns
@@ -101,6 +110,11 @@ cudaError_t launch_echo_noise(float2 *echo, int64_t count, const double *power_a
                               double snr_db, uint64_t seed, cudaStream_t s);
 cudaError_t launch_ref_echo(float2 *Srnm, const float *Ptarget, const float *ta, const float *tr,
                             const sarbp_ref_params &p, int Mslow, int Nfast, cudaStream_t s);
+
+// ---------------------------------------------------------------- autofocus (autofocus.cu)
+// w = |img|^2 img (w may be null); partial[sharpness_blocks(n)] = per-block sums of |img|^4.
+int sharpness_blocks(size_t n);
+cudaError_t launch_sharpness_weight(const float2 *img, size_t n, float2 *w, double *partial, cudaStream_t s);
 
 // ---------------------------------------------------------------- probes
 cudaError_t run_issue_probe(int sms, double *fp32_lanes_per_s, double *mufu_lanes_per_s,

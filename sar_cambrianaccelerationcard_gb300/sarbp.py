@@ -61,6 +61,10 @@ class RcLayout(ctypes.Structure):
                 ("nbins", ctypes.c_int32), ("t0_bins", ctypes.c_double), ("bin_rate", ctypes.c_double)]
 
 
+class PulseCorr(ctypes.Structure):
+    _fields_ = [("drange", ctypes.c_void_p), ("dphase", ctypes.c_void_p)]
+
+
 class RcView(ctypes.Structure):
     _fields_ = [("data", ctypes.c_void_p), ("scale", ctypes.c_void_p), ("storage", ctypes.c_int32),
                 ("np", ctypes.c_int32), ("nbins", ctypes.c_int32), ("reserved", ctypes.c_int32),
@@ -134,6 +138,15 @@ SIGNATURES = {
     "sarbp_backproject": ([ctypes.c_void_p, ctypes.POINTER(Radar), ctypes.POINTER(RcView), ctypes.c_void_p,
                            ctypes.POINTER(Grid), ctypes.c_int32, ctypes.c_void_p, ctypes.c_int32,
                            ctypes.c_void_p], ctypes.c_int),
+    "sarbp_backproject_ex": ([ctypes.c_void_p, ctypes.POINTER(Radar), ctypes.POINTER(RcView), ctypes.c_void_p,
+                              ctypes.POINTER(Grid), ctypes.c_int32, ctypes.POINTER(PulseCorr), ctypes.c_void_p,
+                              ctypes.c_int32, ctypes.c_void_p], ctypes.c_int),
+    "sarbp_project_weighted": ([ctypes.c_void_p, ctypes.POINTER(Radar), ctypes.POINTER(RcView), ctypes.c_void_p,
+                                ctypes.POINTER(Grid), ctypes.c_int32, ctypes.POINTER(PulseCorr), ctypes.c_void_p,
+                                ctypes.c_void_p, ctypes.c_void_p], ctypes.c_int),
+    "sarbp_autofocus": ([ctypes.c_void_p, ctypes.POINTER(Radar), ctypes.POINTER(RcView), ctypes.c_void_p,
+                         ctypes.POINTER(Grid), ctypes.c_int32, ctypes.c_int32, ctypes.c_void_p, ctypes.c_void_p,
+                         ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p], ctypes.c_int),
     "sarbp_image": ([ctypes.c_void_p, ctypes.POINTER(Radar), ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32,
                      ctypes.c_void_p, ctypes.POINTER(Grid), ctypes.c_int32, ctypes.c_void_p, ctypes.c_void_p],
                     ctypes.c_int),
@@ -277,8 +290,8 @@ class Context:
                                                  _ptr(out), _ptr(scale), stream), "range_compress")
         return (out, scale) if storage == STORE_C32H else out
 
-    def backproject(self, radar: Radar, rc, apc, grid: Grid, mode: int, t0_bins: float, bin_rate: float,
-                    scale=None, image=None, accumulate: bool = False, stream=None):
+    @staticmethod
+    def _rc_view(rc, scale, t0_bins: float, bin_rate: float) -> RcView:
         v = RcView()
         if isinstance(rc, np.ndarray) and rc.dtype == np.float16:
             v.storage = STORE_C32H
@@ -289,12 +302,61 @@ class Context:
         v.data = _ptr(rc)
         v.scale = _ptr(scale)
         v.t0_bins, v.bin_rate = t0_bins, bin_rate
+        return v
+
+    @staticmethod
+    def _corr(drange, dphase):
+        if drange is None and dphase is None:
+            return None, ()
+        keep = tuple(None if a is None else (a if not isinstance(a, np.ndarray)
+                                             else np.ascontiguousarray(a, dtype=np.float64))
+                     for a in (drange, dphase))
+        c = PulseCorr()
+        c.drange, c.dphase = _ptr(keep[0]), _ptr(keep[1])
+        return c, keep
+
+    def backproject(self, radar: Radar, rc, apc, grid: Grid, mode: int, t0_bins: float, bin_rate: float,
+                    scale=None, image=None, accumulate: bool = False, stream=None, drange=None, dphase=None):
+        v = self._rc_view(rc, scale, t0_bins, bin_rate)
         if image is None:
             image = np.zeros((grid.ny, grid.nx), dtype=np.complex64)
-        self.check(self.lib.sarbp_backproject(self.h, ctypes.byref(radar), ctypes.byref(v), _ptr(apc),
-                                              ctypes.byref(grid), mode, _ptr(image), int(accumulate), stream),
-                   "backproject")
+        corr, _keep = self._corr(drange, dphase)
+        if corr is None:
+            self.check(self.lib.sarbp_backproject(self.h, ctypes.byref(radar), ctypes.byref(v), _ptr(apc),
+                                                  ctypes.byref(grid), mode, _ptr(image), int(accumulate), stream),
+                       "backproject")
+        else:
+            self.check(self.lib.sarbp_backproject_ex(self.h, ctypes.byref(radar), ctypes.byref(v), _ptr(apc),
+                                                     ctypes.byref(grid), mode, ctypes.byref(corr), _ptr(image),
+                                                     int(accumulate), stream), "backproject_ex")
         return image
+
+    def project_weighted(self, radar: Radar, rc, apc, grid: Grid, mode: int, t0_bins: float, bin_rate: float,
+                         weight, scale=None, drange=None, dphase=None, out=None, stream=None):
+        """out[p] = sum over pixels of conj(weight) * pulse p's term (complex128 [np])."""
+        v = self._rc_view(rc, scale, t0_bins, bin_rate)
+        if out is None:
+            out = np.zeros(v.np, dtype=np.complex128)
+        corr, _keep = self._corr(drange, dphase)
+        self.check(self.lib.sarbp_project_weighted(self.h, ctypes.byref(radar), ctypes.byref(v), _ptr(apc),
+                                                   ctypes.byref(grid), mode,
+                                                   ctypes.byref(corr) if corr is not None else None,
+                                                   _ptr(weight), _ptr(out), stream), "project_weighted")
+        return out
+
+    def autofocus(self, radar: Radar, rc, apc, grid: Grid, mode: int, t0_bins: float, bin_rate: float,
+                  iterations: int, scale=None, dphase=None, drange=None, image=None, stream=None):
+        """Sharpness autofocus: returns (dphase [np], sharpness [iterations + 1], image)."""
+        v = self._rc_view(rc, scale, t0_bins, bin_rate)
+        ph = np.zeros(v.np) if dphase is None else np.array(dphase, dtype=np.float64)
+        dr = None if drange is None else np.ascontiguousarray(drange, dtype=np.float64)
+        sharp = np.zeros(iterations + 1)
+        if image is None:
+            image = np.zeros((grid.ny, grid.nx), dtype=np.complex64)
+        self.check(self.lib.sarbp_autofocus(self.h, ctypes.byref(radar), ctypes.byref(v), _ptr(apc),
+                                            ctypes.byref(grid), mode, int(iterations), _ptr(dr), _ptr(ph),
+                                            _ptr(image), _ptr(sharp), stream), "autofocus")
+        return ph, sharp, image
 
     def image(self, radar: Radar, echo, apc, grid: Grid, mode: int, image=None, stream=None):
         np_, ns = echo.shape
