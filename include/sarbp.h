@@ -237,6 +237,44 @@ sarbp_status sarbp_image(sarbp_ctx *ctx, const sarbp_radar *radar,
                          const double *apc, const sarbp_grid *grid, int32_t mode,
                          sarbp_complex64 *image, void *stream);
 
+/* ------------------------------------------------------ omega-K imager -- */
+
+/* Parameters of the omega-K (Stolt) imager (WKParams, wk.cc:59-66 and
+ * readParams, readfile/read.cc).  kr carries the sign of the reference's
+ * parameter file (paras.txt: Kr = -7.2135e11 for the RADARSAT-1 scene), so the
+ * reference-function phase is 4 pi r0 / c sqrt((f0 + fr)^2 - c^2 fa^2 / (4 vr^2))
+ * + pi fr^2 / kr (task/compression.cc:17-73; mian_wka_sinc.m step 2). */
+typedef struct sarbp_wk_params {
+    double fr;    /* range sampling rate Fr (Hz) */
+    double prf;   /* azimuth sampling rate (Hz) */
+    double f0;    /* carrier frequency (Hz) */
+    double r0;    /* reference slant range R0 (m) */
+    double kr;    /* range FM rate (Hz/s), parameter-file sign */
+    double c;     /* propagation speed (m/s) */
+    double vr;    /* effective radar velocity (m/s); the reference fixes 7062 */
+    double f_nc;  /* Doppler centroid (Hz); the reference fixes -6900 */
+    int32_t taps; /* Stolt sinc taps P (the reference uses 6) */
+    int32_t reserved;
+} sarbp_wk_params;
+
+/* Padded image size of an na x nr echo: na + 2 round(na / 6), nr + 2 round(nr / 3)
+ * (preprocess.cc:22-25).  Supported when both sides are powers of two <= 16384
+ * or other lengths <= 8192. */
+sarbp_status sarbp_wk_padded_size(int32_t na, int32_t nr, int32_t *na_pad, int32_t *nr_pad);
+
+/* The omega-K imager (process_wk, wk.cc:43-343, without its text I/O): zero
+ * padding and azimuth down-conversion by exp(-j 2 pi f_nc ta), 2-D FFT,
+ * reference-function multiply, Stolt mapping with a taps-point sinc
+ * (taps at clip(floor(n - delta + k - taps/2), 0, nr_pad - 1)), 2-D IFFT (1/(na_pad nr_pad)).
+ * echo [na][nr], image [na_pad][nr_pad]; host or device pointers. */
+sarbp_status sarbp_wk_image(sarbp_ctx *ctx, const sarbp_wk_params *params, const sarbp_complex64 *echo,
+                            int32_t na, int32_t nr, sarbp_complex64 *image, void *stream);
+
+/* Batched 1-D DFT along the rows of data [rows][n], in place: forward
+ * (unnormalised) or inverse (times 1/n), any supported n (see above). */
+sarbp_status sarbp_dft(sarbp_ctx *ctx, sarbp_complex64 *data, int32_t rows, int32_t n, int32_t inverse,
+                       void *stream);
+
 /* ------------------------------------------------------ echo synthesiser -- */
 
 /* Point-target echo with FP64 phase (BPA_SAR.m:80-89; replaces

@@ -51,6 +51,12 @@ struct DevBuf {
     T *as() const { return static_cast<T *>(ptr); }
 };
 
+struct DftCache {
+    int n = 0, m = 0;
+    uint64_t used = 0;
+    DevBuf etab, chirp, kf, ki;
+};
+
 struct RcTables {
     bool valid = false;
     int nfft = 0, L = 0, nc = 0, shift = 0;
@@ -68,6 +74,9 @@ struct sarbp_ctx {
     std::string err;
     DevBuf echo, spec, rc, scale, apc, image, partial, errword, power, targets, pref;
     DevBuf corr, weight, proj, projout, sharp;  // per-pulse corrections, projection and autofocus scratch
+    DevBuf wk0, wk1, wkrow, wktab;                // omega-K ping-pong buffers and tables
+    DftCache dft[4];
+    uint64_t dft_clock = 0;
     RcTables tables;
     int64_t launches = 0;
     int checked = 0;  // SARBP_BOUNDS_CHECK=1 at creation: clamped, self-reporting BP kernels
@@ -418,6 +427,53 @@ sarbp_status stage_bp_inputs(sarbp_ctx *ctx, const sarbp_radar *radar, const sar
     return SARBP_OK;
 }
 
+// DFT plan for rows of length n (tables cached per length in the context).
+sarbp_status get_dft(sarbp_ctx *ctx, int n, sarbp::DftPlan &p) {
+    if (!sarbp::dft_size_supported(n))
+        return fail(ctx, SARBP_ERR_UNSUPPORTED, "DFT length %d not supported (powers of two <= 16384, others <= 8192)", n);
+    DftCache *slot = nullptr;
+    for (auto &c : ctx->dft)
+        if (c.n == n) slot = &c;
+    if (!slot) {
+        slot = &ctx->dft[0];
+        for (auto &c : ctx->dft)
+            if (c.used < slot->used) slot = &c;
+        std::vector<float2> etab, chirp, kf, ki;
+        sarbp::dft_tables_host(n, etab, chirp, kf, ki);
+        slot->n = 0;
+        SARBP_CUDA(ctx, slot->etab.ensure(sizeof(float2) * etab.size()), "alloc DFT tables");
+        SARBP_CUDA(ctx, cudaMemcpy(slot->etab.ptr, etab.data(), sizeof(float2) * etab.size(), cudaMemcpyHostToDevice),
+                   "upload DFT tables");
+        slot->m = sarbp::dft_bluestein_size(n);
+        if (slot->m) {
+            SARBP_CUDA(ctx, slot->chirp.ensure(sizeof(float2) * n), "alloc DFT tables");
+            SARBP_CUDA(ctx, slot->kf.ensure(sizeof(float2) * slot->m), "alloc DFT tables");
+            SARBP_CUDA(ctx, slot->ki.ensure(sizeof(float2) * slot->m), "alloc DFT tables");
+            SARBP_CUDA(ctx, cudaMemcpy(slot->chirp.ptr, chirp.data(), sizeof(float2) * n, cudaMemcpyHostToDevice),
+                       "upload DFT tables");
+            SARBP_CUDA(ctx, cudaMemcpy(slot->kf.ptr, kf.data(), sizeof(float2) * slot->m, cudaMemcpyHostToDevice),
+                       "upload DFT tables");
+            SARBP_CUDA(ctx, cudaMemcpy(slot->ki.ptr, ki.data(), sizeof(float2) * slot->m, cudaMemcpyHostToDevice),
+                       "upload DFT tables");
+        }
+        slot->n = n;
+    }
+    slot->used = ++ctx->dft_clock;
+    p.n = n;
+    p.m = slot->m;
+    p.etab = slot->etab.as<float2>();
+    p.chirp = slot->chirp.as<float2>();
+    p.kfwd = slot->kf.as<float2>();
+    p.kinv = slot->ki.as<float2>();
+    return SARBP_OK;
+}
+
+void wk_pads(int na, int nr, int *pa, int *pr) {
+    // round(Na / 6.0f), round(Nr / 3.0f) as the reference computes them (float, half away from zero)
+    *pa = (int)std::lround((float)na / 6.0f);
+    *pr = (int)std::lround((float)nr / 3.0f);
+}
+
 std::mutex g_shim_mu;
 sarbp_ctx *g_shim_ctx = nullptr;
 int g_shim_dev = -1;
@@ -736,6 +792,135 @@ sarbp_status sarbp_autofocus(sarbp_ctx *ctx, const sarbp_radar *radar, const sar
     if (image && !dev_img)
         SARBP_CUDA(ctx, cudaMemcpyAsync(image, d_img, sizeof(float2) * npix, cudaMemcpyDeviceToHost, s), "download image");
     return finish(ctx, s, true);
+}
+
+sarbp_status sarbp_wk_padded_size(int32_t na, int32_t nr, int32_t *na_pad, int32_t *nr_pad) {
+    if (na <= 0 || nr <= 0 || !na_pad || !nr_pad) return SARBP_ERR_INVALID_ARGUMENT;
+    int pa, pr;
+    wk_pads(na, nr, &pa, &pr);
+    const long long NA = (long long)na + 2LL * pa, NR = (long long)nr + 2LL * pr;
+    if (NA > (1 << 30) || NR > (1 << 30)) return SARBP_ERR_UNSUPPORTED;
+    *na_pad = (int32_t)NA;
+    *nr_pad = (int32_t)NR;
+    return sarbp::dft_size_supported((int)NA) && sarbp::dft_size_supported((int)NR) ? SARBP_OK : SARBP_ERR_UNSUPPORTED;
+}
+
+sarbp_status sarbp_dft(sarbp_ctx *ctx, sarbp_complex64 *data, int32_t rows, int32_t n, int32_t inverse, void *stream) {
+    if (!ctx) return SARBP_ERR_INVALID_ARGUMENT;
+    ctx->err.clear();
+    cudaSetDevice(ctx->device);
+    if (rows < 0 || n < 1) return fail(ctx, SARBP_ERR_INVALID_ARGUMENT, "rows must be >= 0 and n >= 1");
+    if (rows == 0 || n == 1) return SARBP_OK;
+    if (!data) return fail(ctx, SARBP_ERR_INVALID_ARGUMENT, "data is null");
+    sarbp::DftPlan p;
+    sarbp_status st = get_dft(ctx, n, p);
+    if (st != SARBP_OK) return st;
+    cudaStream_t s = pick_stream(ctx, stream);
+    const size_t bytes = sizeof(float2) * (size_t)rows * n;
+    float2 *d = reinterpret_cast<float2 *>(data);
+    const bool dev = is_device_ptr(data);
+    if (!dev) {
+        SARBP_CUDA(ctx, ctx->wk0.ensure(bytes), "alloc DFT buffer");
+        d = ctx->wk0.as<float2>();
+        SARBP_CUDA(ctx, cudaMemcpyAsync(d, data, bytes, cudaMemcpyHostToDevice, s), "upload DFT rows");
+    }
+    SARBP_CUDA(ctx, sarbp::launch_dft_rows(p, d, rows, n, inverse != 0, inverse ? 1.0f / (float)n : 1.0f, s),
+               "DFT launch");
+    ctx->launches += 1;
+    if (!dev) SARBP_CUDA(ctx, cudaMemcpyAsync(data, d, bytes, cudaMemcpyDeviceToHost, s), "download DFT rows");
+    return finish(ctx, s, !dev);
+}
+
+sarbp_status sarbp_wk_image(sarbp_ctx *ctx, const sarbp_wk_params *w, const sarbp_complex64 *echo, int32_t na,
+                            int32_t nr, sarbp_complex64 *image, void *stream) {
+    constexpr double kPi = 3.14159265358979323846;
+    if (!ctx) return SARBP_ERR_INVALID_ARGUMENT;
+    ctx->err.clear();
+    cudaSetDevice(ctx->device);
+    if (!w) return fail(ctx, SARBP_ERR_INVALID_ARGUMENT, "params is null");
+    const double vals[8] = {w->fr, w->prf, w->f0, w->r0, w->kr, w->c, w->vr, w->f_nc};
+    for (double v : vals)
+        if (!std::isfinite(v)) return fail(ctx, SARBP_ERR_INVALID_ARGUMENT, "omega-K parameters must be finite");
+    if (!(w->fr > 0) || !(w->prf > 0) || !(w->f0 > 0) || !(w->c > 0) || !(w->vr > 0) || w->kr == 0.0)
+        return fail(ctx, SARBP_ERR_INVALID_ARGUMENT, "fr, prf, f0, c, vr must be > 0 and kr != 0");
+    if (w->taps < 1 || w->taps > 32) return fail(ctx, SARBP_ERR_INVALID_ARGUMENT, "taps must be in [1, 32]");
+    if (na <= 0 || nr <= 0) return fail(ctx, SARBP_ERR_INVALID_ARGUMENT, "echo size must be > 0");
+    if (!echo || !image) return fail(ctx, SARBP_ERR_INVALID_ARGUMENT, "echo and image must be non-null");
+    int32_t NA, NR;
+    if (sarbp_wk_padded_size(na, nr, &NA, &NR) != SARBP_OK)
+        return fail(ctx, SARBP_ERR_UNSUPPORTED, "padded size %d x %d not supported", NA, NR);
+    if (sarbp::wk_stolt_smem(NR) > (size_t)(227u << 10))
+        return fail(ctx, SARBP_ERR_UNSUPPORTED, "range size %d too large for the Stolt stage", NR);
+    int pa, pr;
+    wk_pads(na, nr, &pa, &pr);
+    sarbp::DftPlan pa_plan, pr_plan;
+    sarbp_status st = get_dft(ctx, NR, pr_plan);
+    if (st != SARBP_OK) return st;
+    st = get_dft(ctx, NA, pa_plan);
+    if (st != SARBP_OK) return st;
+    cudaStream_t s = pick_stream(ctx, stream);
+    // host tables (FP64): row phasors exp(-j 2 pi f_nc ta_m), ta_m = (m - NA/2) / prf;
+    // frequency axes as the reference builds them (fftshifted index, wk.cc:181-205)
+    std::vector<float2> rowphase(NA);
+    std::vector<double> tab(3 * (size_t)NR + NA);
+    double *col_f2 = tab.data(), *col_ph = col_f2 + NR, *col_fr = col_ph + NR, *row_q = col_fr + NR;
+    for (int m = 0; m < NA; ++m) {
+        const double ta = (double)(m - NA / 2) / w->prf;
+        const double cyc = -w->f_nc * ta;
+        const double a = 2.0 * kPi * (cyc - std::nearbyint(cyc));
+        rowphase[m] = make_float2((float)std::cos(a), (float)std::sin(a));
+        const int idx = m < NA / 2 ? m + NA / 2 : m - NA / 2;
+        const double fa = w->f_nc + (double)(idx - NA / 2) * (w->prf / NA);
+        row_q[m] = w->c * w->c / (4.0 * w->vr * w->vr) * fa * fa;
+    }
+    for (int n = 0; n < NR; ++n) {
+        const int idx = n < NR / 2 ? n + NR / 2 : n - NR / 2;
+        const double fr = (double)(idx - NR / 2) * (w->fr / NR);
+        col_f2[n] = (w->f0 + fr) * (w->f0 + fr);
+        col_ph[n] = kPi * fr * fr / w->kr;
+        col_fr[n] = fr;
+    }
+    const size_t npix = (size_t)NA * NR;
+    SARBP_CUDA(ctx, ctx->wk0.ensure(sizeof(float2) * npix), "alloc omega-K buffer");
+    SARBP_CUDA(ctx, ctx->wk1.ensure(sizeof(float2) * npix), "alloc omega-K buffer");
+    SARBP_CUDA(ctx, ctx->wkrow.ensure(sizeof(float2) * NA), "alloc omega-K tables");
+    SARBP_CUDA(ctx, ctx->wktab.ensure(sizeof(double) * tab.size()), "alloc omega-K tables");
+    SARBP_CUDA(ctx, cudaMemcpyAsync(ctx->wkrow.ptr, rowphase.data(), sizeof(float2) * NA, cudaMemcpyHostToDevice, s),
+               "upload omega-K tables");
+    SARBP_CUDA(ctx, cudaMemcpyAsync(ctx->wktab.ptr, tab.data(), sizeof(double) * tab.size(), cudaMemcpyHostToDevice, s),
+               "upload omega-K tables");
+    const double *d_tab = ctx->wktab.as<double>();
+    const float2 *d_echo = reinterpret_cast<const float2 *>(echo);
+    bool any_host = true;  // the host tables above are staged through pageable memory
+    if (!is_device_ptr(echo)) {
+        SARBP_CUDA(ctx, ctx->echo.ensure(sizeof(float2) * (size_t)na * nr), "alloc echo");
+        SARBP_CUDA(ctx, cudaMemcpyAsync(ctx->echo.ptr, echo, sizeof(float2) * (size_t)na * nr, cudaMemcpyHostToDevice, s),
+                   "upload echo");
+        d_echo = ctx->echo.as<float2>();
+    }
+    float2 *A = ctx->wk0.as<float2>(), *B = ctx->wk1.as<float2>();
+    const bool dev_img = is_device_ptr(image);
+    float2 *out = dev_img ? reinterpret_cast<float2 *>(image) : B;
+    cudaEventRecord(ctx->ev[0], s);
+    SARBP_CUDA(ctx, sarbp::launch_wk_pad(d_echo, na, nr, pa, pr, NA, NR, ctx->wkrow.as<float2>(), A, s), "omega-K pad");
+    SARBP_CUDA(ctx, sarbp::launch_dft_rows(pr_plan, A, NA, NR, false, 1.0f, s), "range FFT");
+    SARBP_CUDA(ctx, sarbp::launch_transpose(A, B, NA, NR, s), "transpose");
+    SARBP_CUDA(ctx, sarbp::launch_dft_rows(pa_plan, B, NR, NA, false, 1.0f, s), "azimuth FFT");
+    SARBP_CUDA(ctx, sarbp::launch_transpose(B, A, NR, NA, s), "transpose");
+    SARBP_CUDA(ctx, sarbp::launch_wk_stolt(A, B, NA, NR, d_tab, d_tab + NR, d_tab + 2 * NR, d_tab + 3 * NR,
+                                            4.0 * kPi * w->r0 / w->c, w->f0, NR / w->fr, w->taps, s),
+               "reference-function multiply and Stolt mapping");
+    SARBP_CUDA(ctx, sarbp::launch_dft_rows(pr_plan, B, NA, NR, true, 1.0f / (float)NR, s), "range IFFT");
+    SARBP_CUDA(ctx, sarbp::launch_transpose(B, A, NA, NR, s), "transpose");
+    SARBP_CUDA(ctx, sarbp::launch_dft_rows(pa_plan, A, NR, NA, true, 1.0f / (float)NA, s), "azimuth IFFT");
+    SARBP_CUDA(ctx, sarbp::launch_transpose(A, out, NR, NA, s), "transpose");
+    cudaEventRecord(ctx->ev[1], s);
+    ctx->timed_rc = true;  // sarbp_last_timings reports the omega-K time in its rc slot
+    ctx->timed_bp = false;
+    ctx->launches += 10;
+    if (!dev_img)
+        SARBP_CUDA(ctx, cudaMemcpyAsync(image, out, sizeof(float2) * npix, cudaMemcpyDeviceToHost, s), "download image");
+    return finish(ctx, s, any_host);
 }
 
 sarbp_status sarbp_image(sarbp_ctx *ctx, const sarbp_radar *radar, const sarbp_complex64 *echo, int32_t np,

@@ -17,6 +17,27 @@
 namespace sarbp {
 namespace {
 double dot3(const double *a, const double *b) { return a[0] * b[0] + a[1] * b[1] + a[2] * b[2]; }
+
+// In-place radix-2 forward DFT (unnormalised) of a power-of-two length, FP64.
+void fft_pow2_host(std::vector<std::complex<double>> &h) {
+    constexpr double kPi = 3.14159265358979323846;
+    const int N = (int)h.size();
+    for (int i = 1, j = 0; i < N; ++i) {
+        int bit = N >> 1;
+        for (; j & bit; bit >>= 1) j ^= bit;
+        j ^= bit;
+        if (i < j) std::swap(h[i], h[j]);
+    }
+    for (int len = 2; len <= N; len <<= 1)
+        for (int i = 0; i < N; i += len)
+            for (int k = 0; k < len / 2; ++k) {
+                const double a = -2.0 * kPi * (double)k / (double)len;
+                const std::complex<double> w(std::cos(a), std::sin(a));
+                const std::complex<double> u = h[i + k], v = h[i + k + len / 2] * w;
+                h[i + k] = u + v;
+                h[i + k + len / 2] = u - v;
+            }
+}
 }  // namespace
 
 bool plan_bp(int sms, const sarbp_radar &r, const sarbp_rc_view &rc, const double *apc_host, int np,
@@ -144,22 +165,7 @@ void rc_tables_host(const sarbp_radar &r, const sarbp_rc_layout &lay, std::vecto
             h[i] = std::complex<double>(std::cos(ph), std::sin(ph));
         }
     }
-    // radix-2 forward transform of the chirp (unnormalised)
-    for (int i = 1, j = 0; i < N; ++i) {
-        int bit = N >> 1;
-        for (; j & bit; bit >>= 1) j ^= bit;
-        j ^= bit;
-        if (i < j) std::swap(h[i], h[j]);
-    }
-    for (int len = 2; len <= N; len <<= 1)
-        for (int i = 0; i < N; i += len)
-            for (int k = 0; k < len / 2; ++k) {
-                const double a = -2.0 * kPi * (double)k / (double)len;
-                const std::complex<double> w(std::cos(a), std::sin(a));
-                const std::complex<double> u = h[i + k], v = h[i + k + len / 2] * w;
-                h[i + k] = u + v;
-                h[i + k + len / 2] = u - v;
-            }
+    fft_pow2_host(h);  // forward transform of the chirp (unnormalised)
     filt.resize(N);
     for (int k = 0; k < N; ++k) {
         const long long m = ((long long)k * lay.shift) % N;
@@ -167,6 +173,44 @@ void rc_tables_host(const sarbp_radar &r, const sarbp_rc_layout &lay, std::vecto
         const std::complex<double> v = std::conj(h[k]) * std::complex<double>(std::cos(a), std::sin(a)) / (double)N;
         filt[k] = make_float2((float)v.real(), (float)v.imag());
     }
+    fft_etab_host(L, N, etab);
+}
+
+void dft_tables_host(int n, std::vector<float2> &etab, std::vector<float2> &chirp, std::vector<float2> &kfwd,
+                     std::vector<float2> &kinv) {
+    constexpr double kPi = 3.14159265358979323846;
+    const int m = dft_bluestein_size(n);
+    fft_etab_host(1, m ? m : n, etab);
+    chirp.clear();
+    kfwd.clear();
+    kinv.clear();
+    if (!m) return;
+    // w_j = e^{j pi j^2 / n}; j^2 reduced modulo 2n in integers keeps the angle exact
+    std::vector<std::complex<double>> w(n), b(m), bc(m);
+    chirp.resize(n);
+    for (int j = 0; j < n; ++j) {
+        const long long r = ((long long)j * j) % (2LL * n);
+        const double a = kPi * (double)r / (double)n;
+        w[j] = std::complex<double>(std::cos(a), std::sin(a));
+        chirp[j] = make_float2((float)w[j].real(), (float)w[j].imag());
+    }
+    for (int j = 0; j < n; ++j) {
+        b[j] = w[j];
+        if (j > 0) b[m - j] = w[j];
+    }
+    for (int j = 0; j < m; ++j) bc[j] = std::conj(b[j]);
+    fft_pow2_host(b);
+    fft_pow2_host(bc);
+    kfwd.resize(m);
+    kinv.resize(m);
+    for (int j = 0; j < m; ++j) {
+        kfwd[j] = make_float2((float)(b[j].real() / m), (float)(b[j].imag() / m));
+        kinv[j] = make_float2((float)(bc[j].real() / m), (float)(bc[j].imag() / m));
+    }
+}
+
+void fft_etab_host(int L, int N, std::vector<float2> &etab) {
+    constexpr double kPi = 3.14159265358979323846;
     etab.resize(rc_etab_size(L, N));
     const double LN = (double)L * N;
     for (size_t i = 0; i < etab.size(); ++i) {

@@ -33,244 +33,10 @@
 // half read through distributed shared memory.
 #include <cooperative_groups.h>
 
-#include "sarbp_internal.h"
+#include "fft_smem.cuh"
 
 namespace sarbp {
 namespace {
-
-__device__ __forceinline__ float2 cmul(float2 a, float2 b) {
-    return make_float2(fmaf(a.x, b.x, -a.y * b.y), fmaf(a.x, b.y, a.y * b.x));
-}
-__device__ __forceinline__ float2 cadd(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
-__device__ __forceinline__ float2 csub(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
-// multiply by -j (forward kernel) or +j (inverse kernel)
-template <bool INV>
-__device__ __forceinline__ float2 mulj(float2 a) {
-    return INV ? make_float2(-a.y, a.x) : make_float2(a.y, -a.x);
-}
-
-// Shared-memory layout of the transform points: point x lives in slot sw(x),
-// an XOR swizzle inside each run of 16 float2 (128 bytes).  A half-warp of
-// 64-bit accesses then touches 16 distinct bank pairs for every access pattern
-// of the transform: contiguous runs (loads of every stage, stores of the later
-// stages) and the stride-8 / stride-64 stores of the first two radix-8 stages.
-// The swizzle only changes bits 0..3 and depends on bits 4..6, so
-// sw(x + c) = sw(x) + c for any multiple c of 128.
-__host__ __device__ constexpr int sw(int x) { return x ^ (((x >> 4) & 7) | ((x >> 3) & 8)); }
-
-// table slot of entry i: one spare slot per 8 entries, so strided gathers
-// spread over the banks
-__device__ __forceinline__ int tslot(int i) { return i + (i >> 3); }
-
-constexpr int kWlo = 128;  // low level of the transform twiddle table
-
-// Shared-memory tables.  E^m = e^{+j 2 pi m / (L N)} (upsampling ramp, split
-// combine) from E^m = T_hi[m >> 8] * T_lo[m & 255]; the transform twiddles
-// W^m = e^{+j 2 pi m / N} = E^{L m} from W^m = W_hi[m >> 7] * W_lo[m & 127].
-struct Etab {
-    const float2 *lo;   // E^i, i < 256 (or L N entries when L N < 256), slot tslot(i)
-    const float2 *hi;   // E^{256 i}, i < max(1, L N / 256), slot tslot(i)
-    const float2 *wlo;  // W^i, i < min(N, 128)
-    const float2 *whi;  // W^{128 i}, i < max(1, N / 128)
-    __device__ __forceinline__ float2 operator()(int m) const {
-        return cmul(hi[tslot(m >> 8)], lo[tslot(m & 255)]);
-    }
-    __device__ __forceinline__ float2 w(int m) const { return cmul(whi[m >> 7], wlo[m & (kWlo - 1)]); }
-};
-
-template <int R, bool INV>
-struct Dft;
-
-template <bool INV>
-struct Dft<2, INV> {
-    __device__ __forceinline__ static void run(float2 *v) {
-        float2 a = v[0], b = v[1];
-        v[0] = cadd(a, b);
-        v[1] = csub(a, b);
-    }
-};
-
-template <bool INV>
-struct Dft<4, INV> {
-    __device__ __forceinline__ static void run(float2 *v) {
-        float2 t0 = cadd(v[0], v[2]), t1 = csub(v[0], v[2]);
-        float2 t2 = cadd(v[1], v[3]), t3 = mulj<INV>(csub(v[1], v[3]));
-        v[0] = cadd(t0, t2);
-        v[2] = csub(t0, t2);
-        v[1] = cadd(t1, t3);
-        v[3] = csub(t1, t3);
-    }
-};
-
-template <bool INV>
-struct Dft<8, INV> {
-    __device__ __forceinline__ static void run(float2 *v) {
-        float2 e[4] = {v[0], v[2], v[4], v[6]};
-        float2 o[4] = {v[1], v[3], v[5], v[7]};
-        Dft<4, INV>::run(e);
-        Dft<4, INV>::run(o);
-        const float h = 0.70710678118654752440f;
-        // W8^1, W8^2, W8^3 for the chosen direction
-        float2 o1 = INV ? make_float2(h * (o[1].x - o[1].y), h * (o[1].x + o[1].y))
-                        : make_float2(h * (o[1].x + o[1].y), h * (o[1].y - o[1].x));
-        float2 o2 = mulj<INV>(o[2]);
-        float2 o3 = INV ? make_float2(-h * (o[3].x + o[3].y), h * (o[3].x - o[3].y))
-                        : make_float2(h * (o[3].y - o[3].x), -h * (o[3].x + o[3].y));
-        v[0] = cadd(e[0], o[0]);
-        v[4] = csub(e[0], o[0]);
-        v[1] = cadd(e[1], o1);
-        v[5] = csub(e[1], o1);
-        v[2] = cadd(e[2], o2);
-        v[6] = csub(e[2], o2);
-        v[3] = cadd(e[3], o3);
-        v[7] = csub(e[3], o3);
-    }
-};
-
-// Twiddles W^{m r}, r = 1..R-1 (forward: conjugated) for a butterfly whose
-// base exponent is m: w, w^2, w^4 from the table, the others as products.
-// lo1/lo2/lo4 are the low-level table entries when the caller hoisted them.
-template <int R, bool INV, bool HOISTED_LO>
-__device__ __forceinline__ void twiddles(const Etab &E, int m, float2 lo1, float2 lo2, float2 lo4, float2 *w) {
-    w[1] = HOISTED_LO ? cmul(E.whi[m >> 7], lo1) : E.w(m);
-    if (!INV) w[1].y = -w[1].y;
-    if (R >= 4) {
-        w[2] = HOISTED_LO ? cmul(E.whi[(2 * m) >> 7], lo2) : E.w(2 * m);
-        if (!INV) w[2].y = -w[2].y;
-        w[3] = cmul(w[1], w[2]);
-    }
-    if (R >= 8) {
-        w[4] = HOISTED_LO ? cmul(E.whi[(4 * m) >> 7], lo4) : E.w(4 * m);
-        if (!INV) w[4].y = -w[4].y;
-        w[5] = cmul(w[1], w[4]);
-        w[6] = cmul(w[2], w[4]);
-        w[7] = cmul(w[3], w[4]);
-    }
-}
-
-// One Stockham stage: butterfly j reads s[j + r*N/R], applies twiddles
-// W_N^{k r N/(Ns R)} (k = j mod Ns), runs a radix-R DFT and writes
-// s[(j - k) R + k + r Ns] (slots through sw()).  Ns is a compile-time
-// constant: offsets that are multiples of 128 points pass through sw()
-// unchanged and become immediates.  When T is a multiple of Ns every
-// butterfly of a thread has the same k and the twiddles are computed once.
-template <int N, int R, int T, bool INV, int Ns>
-__device__ __forceinline__ void stage(float2 *s, const Etab &E) {
-    constexpr int NB = N / R;
-    constexpr int PER = (NB + T - 1) / T;
-    constexpr int C = N / (Ns * R);  // k -> twiddle exponent step
-    float2 v[PER][R];
-#pragma unroll
-    for (int b = 0; b < PER; ++b) {
-        const int j = threadIdx.x + b * T;
-        if (PER * T == NB || j < NB) {
-            if constexpr (NB % 128 == 0) {
-                const float2 *src = s + sw(j);
-#pragma unroll
-                for (int r = 0; r < R; ++r) v[b][r] = src[r * NB];
-            } else {
-#pragma unroll
-                for (int r = 0; r < R; ++r) v[b][r] = s[sw(j + r * NB)];
-            }
-        }
-    }
-    __syncthreads();
-    float2 w[R];
-    constexpr bool kSameK = Ns > 1 && T % Ns == 0;
-    // k = j when Ns >= NB (last stage); the low table level is then fixed per thread
-    constexpr bool kHoistLo = Ns > 1 && !kSameK && Ns >= NB && N >= kWlo && (C * T) % kWlo == 0;
-    float2 lo1 = make_float2(1.f, 0.f), lo2 = lo1, lo4 = lo1;
-    if constexpr (kSameK) {
-        twiddles<R, INV, false>(E, C * (int)(threadIdx.x & (Ns - 1)), lo1, lo2, lo4, w);
-    } else if constexpr (kHoistLo) {
-        const int m = C * (int)threadIdx.x;
-        lo1 = E.wlo[m & (kWlo - 1)];
-        if (R >= 4) lo2 = E.wlo[(2 * m) & (kWlo - 1)];
-        if (R >= 8) lo4 = E.wlo[(4 * m) & (kWlo - 1)];
-    }
-#pragma unroll
-    for (int b = 0; b < PER; ++b) {
-        const int j = threadIdx.x + b * T;
-        if (PER * T == NB || j < NB) {
-            const int k = j & (Ns - 1);
-            if constexpr (Ns > 1) {
-                if constexpr (!kSameK) twiddles<R, INV, kHoistLo>(E, C * k, lo1, lo2, lo4, w);
-#pragma unroll
-                for (int r = 1; r < R; ++r) v[b][r] = cmul(v[b][r], w[r]);
-            }
-            Dft<R, INV>::run(v[b]);
-            const int x0 = (j - k) * R + k;
-            if constexpr (Ns % 128 == 0) {
-                float2 *dst = s + sw(x0);
-#pragma unroll
-                for (int r = 0; r < R; ++r) dst[r * Ns] = v[b][r];
-            } else {
-#pragma unroll
-                for (int r = 0; r < R; ++r) s[sw(x0 + r * Ns)] = v[b][r];
-            }
-        }
-    }
-    __syncthreads();
-}
-
-// radix-8 stages while 8 * Ns <= N, then one radix-4 or radix-2 stage
-template <int N, int T, bool INV, int Ns>
-struct Stages {
-    __device__ __forceinline__ static void run(float2 *s, const Etab &E) {
-        if constexpr (Ns * 8 <= N) {
-            stage<N, 8, T, INV, Ns>(s, E);
-            Stages<N, T, INV, Ns * 8>::run(s, E);
-        } else if constexpr (Ns * 4 == N) {
-            stage<N, 4, T, INV, Ns>(s, E);
-        } else if constexpr (Ns * 2 == N) {
-            stage<N, 2, T, INV, Ns>(s, E);
-        }
-    }
-};
-
-// Unnormalised in-place FFT of N points held (swizzled) in shared memory.
-// Caller must have synchronised after filling s; returns synchronised.
-template <int N, int T, bool INV>
-__device__ void fft_smem(float2 *s, const Etab &E) {
-    Stages<N, T, INV, 1>::run(s, E);
-}
-
-// Shared memory after the N points: E low/high levels (slots through
-// tslot), W low/high levels, and the per-CTA ramp table of the inverse.
-constexpr int kEloSlots = 288, kEhiSlots = 1152, kWhiMax = 128, kRampMax = 64;
-constexpr size_t kTabSmem = sizeof(float2) * (kEloSlots + kEhiSlots + kWlo + kWhiMax + kRampMax);
-template <int N>
-__device__ __forceinline__ float2 *ramp_slots(float2 *sm) {
-    return sm + N + kEloSlots + kEhiSlots + kWlo + kWhiMax;
-}
-
-// Fills the E tables from global memory, then derives the W tables
-// (W^m = E^{L m}).  Contains one block barrier; the caller synchronises again
-// before the W tables are read.
-template <int N, int T>
-__device__ __forceinline__ Etab load_etab(float2 *sm, const float2 *__restrict__ etab, int L) {
-    static_assert(N / kWlo <= kWhiMax, "W table too small");
-    const int LN = L * N;
-    const int nlo = LN < 256 ? LN : 256;
-    const int nhi = LN < 256 ? 1 : LN / 256;
-    float2 *lo = sm + N;
-    float2 *hi = lo + kEloSlots;
-    float2 *wlo = hi + kEhiSlots;
-    float2 *whi = wlo + kWlo;
-    for (int i = threadIdx.x; i < nlo; i += T) lo[tslot(i)] = __ldg(&etab[i]);
-    for (int i = threadIdx.x; i < nhi; i += T) hi[tslot(i)] = __ldg(&etab[256 + i]);
-    __syncthreads();
-    const Etab E{lo, hi, wlo, whi};
-    constexpr int nwlo = N < kWlo ? N : kWlo;
-    constexpr int nwhi = N < kWlo ? 1 : N / kWlo;
-    for (int i = threadIdx.x; i < nwlo + nwhi; i += T) {
-        if (i < nwlo)
-            wlo[i] = E(L * i);
-        else
-            whi[i - nwlo] = E((L * kWlo * (i - nwlo)) & (LN - 1));
-    }
-    return E;
-}
 
 template <int T>
 __device__ __forceinline__ float block_sum(float v, float *red) {

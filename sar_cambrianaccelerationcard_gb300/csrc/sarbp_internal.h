@@ -93,6 +93,8 @@ size_t bp_tiles(const BpPlan &p);
 // false with the reason in `why`.
 bool plan_bp(int sms, const sarbp_radar &r, const sarbp_rc_view &rc, const double *apc_host, int np,
              const sarbp_grid &g, int mode, int pulses_per_launch, BpPlan &p, std::string &why);
+// Two-level table of E^m = e^{+j 2 pi m / (L N)} ([rc_etab_size(L, N)] entries, plan.cpp).
+void fft_etab_host(int L, int N, std::vector<float2> &etab);
 // Matched-filter spectrum [nfft] and phase table [rc_etab_size] for a layout (plan.cpp).
 void rc_tables_host(const sarbp_radar &r, const sarbp_rc_layout &lay, std::vector<float2> &filt,
                     std::vector<float2> &etab);
@@ -110,6 +112,32 @@ cudaError_t launch_echo_noise(float2 *echo, int64_t count, const double *power_a
                               double snr_db, uint64_t seed, cudaStream_t s);
 cudaError_t launch_ref_echo(float2 *Srnm, const float *Ptarget, const float *ta, const float *tr,
                             const sarbp_ref_params &p, int Mslow, int Nfast, cudaStream_t s);
+
+// ---------------------------------------------------------------- omega-K (wk.cu)
+// Batched 1-D DFT along rows: power-of-two n <= 16384 (m = 0) in shared memory,
+// other n <= 8192 by Bluestein through m-point FFTs (m = pow2 >= 2n - 1).
+struct DftPlan {
+    int n, m;
+    const float2 *etab;   // [rc_etab_size(1, m ? m : n)] E table of the shared-memory FFT
+    const float2 *chirp;  // [n] w_j = e^{j pi j^2 / n} (Bluestein)
+    const float2 *kfwd;   // [m] FFT_m of the circular kernel w, / m (Bluestein forward)
+    const float2 *kinv;   // [m] FFT_m of conj(w), / m (Bluestein inverse)
+};
+bool dft_size_supported(int n);
+int dft_bluestein_size(int n);
+// host FP64 tables for a DftPlan of length n (plan.cpp)
+void dft_tables_host(int n, std::vector<float2> &etab, std::vector<float2> &chirp, std::vector<float2> &kfwd,
+                     std::vector<float2> &kinv);
+// rows x n in place (row stride ld): forward unnormalised, or inverse; times scale
+cudaError_t launch_dft_rows(const DftPlan &p, float2 *data, int rows, long long ld, bool inverse, float scale,
+                            cudaStream_t s);
+cudaError_t launch_transpose(const float2 *in, float2 *out, int rows, int cols, cudaStream_t s);
+cudaError_t launch_wk_pad(const float2 *echo, int na, int nr, int pa, int pr, int NA, int NR, const float2 *rowphase,
+                          float2 *out, cudaStream_t s);
+size_t wk_stolt_smem(int NR);
+cudaError_t launch_wk_stolt(const float2 *in, float2 *out, int NA, int NR, const double *col_f2, const double *col_ph,
+                            const double *col_fr, const double *row_q, double a4r, double f0, double inv_gap, int taps,
+                            cudaStream_t s);
 
 // ---------------------------------------------------------------- autofocus (autofocus.cu)
 // w = |img|^2 img (w may be null); partial[sharpness_blocks(n)] = per-block sums of |img|^4.

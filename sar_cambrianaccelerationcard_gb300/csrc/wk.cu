@@ -1,0 +1,282 @@
+// wk.cu -- omega-K (Stolt) imager on sm_103a.
+//
+// Implements the reference's omega-K path (code/SAR_WK/wk_v5.2.3/wk.cc:43-343,
+// specified by code/SAR_WK/matlab/mian_wka_sinc.m): zero padding and azimuth
+// down-conversion (task/preprocess.cc:17-167), 2-D FFT (task/fft.cc:18+),
+// reference-function multiply (task/compression.cc:17-73), Stolt mapping with
+// a P-tap sinc kernel (task/stolt.cc:324+) and 2-D IFFT.
+//
+// GPU design (data [Na][Nr] complex64 in HBM, ping-pong between two buffers):
+//   * 1-D DFTs run along rows, one CTA per row, in shared memory: the
+//     Stockham FFT of fft_smem.cuh for power-of-two lengths (<= 16384), and
+//     Bluestein's chirp-z form for other lengths n <= 8192: the row times the
+//     chirp conj(w), w_j = e^{j pi j^2 / n}, is convolved with w through one
+//     forward and one inverse power-of-two FFT of M >= 2n - 1 points held in
+//     the same shared memory, with the convolution kernel's spectrum
+//     precomputed in FP64 on the host.  Azimuth transforms run on transposed
+//     data (32 x 32-tile transposes through shared memory).
+//   * The reference-function multiply and the Stolt interpolation are one
+//     kernel per azimuth-frequency row: sqrt((f0+fr)^2 - c^2 fa^2 / (4 Vr^2))
+//     is evaluated once per sample in FP64 and gives both the phase
+//     theta = 4 pi R0 / c * root + pi fr^2 / kr (reduced modulo 2 pi in FP64,
+//     rotated in FP32) and the Stolt shift delta = (root - f0 - fr) Nr / Fr;
+//     the multiplied row is staged in shared memory and each output sums P
+//     taps at clip(floor(n - delta + k - P/2), 0, Nr - 1) weighted by
+//     sin(pi u) / (pi u), u = (n - delta) - tap, as the reference's gather /
+//     sinc / reduce chain does.  One sin per output: away from the row edges
+//     the taps' sines differ only in sign.
+#include <algorithm>
+
+#include "fft_smem.cuh"
+
+namespace sarbp {
+namespace {
+
+// ------------------------------------------------------------------ DFT rows
+
+template <int N>
+constexpr int dft_threads() {
+    return N >= 8192 ? 1024 : (N >= 4096 ? 512 : (N >= 512 ? N / 8 : 64));
+}
+
+// Power-of-two row transform: row r of data (stride ld) in place, times scale.
+template <int N, int T, bool INV>
+__global__ void __launch_bounds__(T) dft_pow2_kernel(float2 *__restrict__ data, long long ld, float scale,
+                                                     const float2 *__restrict__ etab) {
+    extern __shared__ float2 sm[];
+    const Etab E = load_etab<N, T>(sm, etab, 1);
+    float2 *row = data + (size_t)blockIdx.x * ld;
+    for (int i = threadIdx.x; i < N; i += T) sm[sw(i)] = row[i];
+    __syncthreads();
+    fft_smem<N, T, INV>(sm, E);
+    for (int i = threadIdx.x; i < N; i += T) {
+        const float2 v = sm[sw(i)];
+        row[i] = make_float2(v.x * scale, v.y * scale);
+    }
+}
+
+// Bluestein row transform of length n through M-point FFTs.
+//   forward: X[k] = conj(w_k) sum_j (x_j conj(w_j)) w_{k-j}
+//   inverse: X[k] = w_k sum_j (x_j w_j) conj(w_{k-j})
+// chirp[j] = w_j (j < n); kspec = FFT_M of the circular kernel (w or conj(w)),
+// divided by M (the inverse FFT's normalisation).
+template <int M, int T, bool INV>
+__global__ void __launch_bounds__(T) dft_bluestein_kernel(float2 *__restrict__ data, long long ld, int n,
+                                                          float scale, const float2 *__restrict__ etab,
+                                                          const float2 *__restrict__ chirp,
+                                                          const float2 *__restrict__ kspec) {
+    extern __shared__ float2 sm[];
+    const Etab E = load_etab<M, T>(sm, etab, 1);
+    float2 *row = data + (size_t)blockIdx.x * ld;
+    for (int i = threadIdx.x; i < M; i += T) {
+        float2 v = make_float2(0.f, 0.f);
+        if (i < n) {
+            float2 w = __ldg(&chirp[i]);
+            if (!INV) w.y = -w.y;
+            v = cmul(row[i], w);
+        }
+        sm[sw(i)] = v;
+    }
+    __syncthreads();
+    fft_smem<M, T, false>(sm, E);
+    for (int i = threadIdx.x; i < M; i += T) sm[sw(i)] = cmul(sm[sw(i)], __ldg(&kspec[i]));
+    __syncthreads();
+    fft_smem<M, T, true>(sm, E);
+    for (int i = threadIdx.x; i < n; i += T) {
+        float2 w = __ldg(&chirp[i]);
+        if (!INV) w.y = -w.y;
+        const float2 v = cmul(sm[sw(i)], w);
+        row[i] = make_float2(v.x * scale, v.y * scale);
+    }
+}
+
+template <int N, bool INV>
+cudaError_t pow2_n(const DftPlan &p, float2 *data, int rows, long long ld, float scale, cudaStream_t s) {
+    constexpr int T = dft_threads<N>();
+    const size_t smem = sizeof(float2) * N + kTabSmem;
+    auto k = dft_pow2_kernel<N, T, INV>;
+    cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    k<<<rows, T, smem, s>>>(data, ld, scale, p.etab);
+    return cudaGetLastError();
+}
+
+template <int M, bool INV>
+cudaError_t blue_m(const DftPlan &p, float2 *data, int rows, long long ld, float scale, cudaStream_t s) {
+    constexpr int T = dft_threads<M>();
+    const size_t smem = sizeof(float2) * M + kTabSmem;
+    auto k = dft_bluestein_kernel<M, T, INV>;
+    cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    k<<<rows, T, smem, s>>>(data, ld, p.n, scale, p.etab, p.chirp, INV ? p.kinv : p.kfwd);
+    return cudaGetLastError();
+}
+
+template <bool INV>
+cudaError_t dft_dispatch(const DftPlan &p, float2 *data, int rows, long long ld, float scale, cudaStream_t s) {
+#define SARBP_DFT_CASE(F, V) \
+    case V: return F<V, INV>(p, data, rows, ld, scale, s);
+    if (p.m == 0) {
+        switch (p.n) {
+            SARBP_DFT_CASE(pow2_n, 2) SARBP_DFT_CASE(pow2_n, 4) SARBP_DFT_CASE(pow2_n, 8)
+            SARBP_DFT_CASE(pow2_n, 16) SARBP_DFT_CASE(pow2_n, 32) SARBP_DFT_CASE(pow2_n, 64)
+            SARBP_DFT_CASE(pow2_n, 128) SARBP_DFT_CASE(pow2_n, 256) SARBP_DFT_CASE(pow2_n, 512)
+            SARBP_DFT_CASE(pow2_n, 1024) SARBP_DFT_CASE(pow2_n, 2048) SARBP_DFT_CASE(pow2_n, 4096)
+            SARBP_DFT_CASE(pow2_n, 8192) SARBP_DFT_CASE(pow2_n, 16384)
+            default: return cudaErrorInvalidValue;
+        }
+    }
+    switch (p.m) {
+        SARBP_DFT_CASE(blue_m, 4) SARBP_DFT_CASE(blue_m, 8) SARBP_DFT_CASE(blue_m, 16)
+        SARBP_DFT_CASE(blue_m, 32) SARBP_DFT_CASE(blue_m, 64) SARBP_DFT_CASE(blue_m, 128)
+        SARBP_DFT_CASE(blue_m, 256) SARBP_DFT_CASE(blue_m, 512) SARBP_DFT_CASE(blue_m, 1024)
+        SARBP_DFT_CASE(blue_m, 2048) SARBP_DFT_CASE(blue_m, 4096) SARBP_DFT_CASE(blue_m, 8192)
+        SARBP_DFT_CASE(blue_m, 16384)
+        default: return cudaErrorInvalidValue;
+    }
+#undef SARBP_DFT_CASE
+}
+
+// ------------------------------------------------------------------ transpose
+
+constexpr int kTile = 32;
+
+// out[c][r] = in[r][c] for a dense rows x cols matrix.
+__global__ void __launch_bounds__(kTile * 8) transpose_kernel(const float2 *__restrict__ in, float2 *__restrict__ out,
+                                                               int rows, int cols) {
+    __shared__ float2 t[kTile][kTile + 1];
+    const int c0 = blockIdx.x * kTile, r0 = blockIdx.y * kTile;
+    for (int i = threadIdx.y; i < kTile; i += 8) {
+        const int r = r0 + i, c = c0 + threadIdx.x;
+        if (r < rows && c < cols) t[i][threadIdx.x] = in[(size_t)r * cols + c];
+    }
+    __syncthreads();
+    for (int i = threadIdx.y; i < kTile; i += 8) {
+        const int c = c0 + i, r = r0 + threadIdx.x;
+        if (c < cols && r < rows) out[(size_t)c * rows + r] = t[threadIdx.x][i];
+    }
+}
+
+// ------------------------------------------------------------------ pad + down-conversion
+
+// out[m][n] = echo[m - pa][n - pr] * rowphase[m] inside the echo, 0 in the padding.
+__global__ void wk_pad_kernel(const float2 *__restrict__ echo, int na, int nr, int pa, int pr, int NA, int NR,
+                              const float2 *__restrict__ rowphase, float2 *__restrict__ out) {
+    const size_t total = (size_t)NA * NR;
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total; i += (size_t)gridDim.x * blockDim.x) {
+        const int m = (int)(i / NR), n = (int)(i - (size_t)m * NR);
+        const int a = m - pa, r = n - pr;
+        float2 v = make_float2(0.f, 0.f);
+        if (a >= 0 && a < na && r >= 0 && r < nr) v = cmul(__ldg(&echo[(size_t)a * nr + r]), __ldg(&rowphase[m]));
+        out[i] = v;
+    }
+}
+
+// ------------------------------------------------------------------ RFM + Stolt
+
+constexpr int kStoltThreads = 512;
+
+// One CTA per azimuth-frequency row m of in/out ([NA][NR]).
+//   col_f2[n]  = (f0 + fr_n)^2,  col_ph[n] = pi fr_n^2 / kr,  col_fr[n] = fr_n
+//   row_q[m]   = c^2 fa_m^2 / (4 Vr^2)
+__global__ void __launch_bounds__(kStoltThreads) wk_stolt_kernel(const float2 *__restrict__ in,
+                                                                  float2 *__restrict__ out, int NR,
+                                                                  const double *__restrict__ col_f2,
+                                                                  const double *__restrict__ col_ph,
+                                                                  const double *__restrict__ col_fr,
+                                                                  const double *__restrict__ row_q, double a4r,
+                                                                  double f0, double inv_gap, int taps) {
+    extern __shared__ float2 sm[];
+    float *sdelta = reinterpret_cast<float *>(sm + NR);
+    const int m = blockIdx.x;
+    const double q = row_q[m];
+    const float2 *src = in + (size_t)m * NR;
+    constexpr double kTwoPi = 6.283185307179586476925;
+    for (int n = threadIdx.x; n < NR; n += kStoltThreads) {
+        const double root = sqrt(fmax(col_f2[n] - q, 0.0));
+        double th = fma(a4r, root, col_ph[n]);
+        th -= kTwoPi * rint(th * (1.0 / kTwoPi));
+        float sn, cs;
+        sincosf((float)th, &sn, &cs);
+        sm[n] = cmul(__ldg(&src[n]), make_float2(cs, sn));
+        sdelta[n] = (float)((root - f0 - col_fr[n]) * inv_gap);
+    }
+    __syncthreads();
+    float2 *dst = out + (size_t)m * NR;
+    const float half = 0.5f * (float)taps;
+    for (int n = threadIdx.x; n < NR; n += kStoltThreads) {
+        // centre c = n - delta = fl + f, f in [0, 1)
+        const float nd = -sdelta[n];
+        const float fnd = floorf(nd);
+        const float f = nd - fnd;
+        const int fl = n + (int)fnd;
+        const float s0 = sinpif(f);  // sin(pi (f + o)) = (-1)^o s0 for integer o
+        float2 acc = make_float2(0.f, 0.f);
+        for (int k = 0; k < taps; ++k) {
+            // tap floor(c + k - taps/2), clipped to the row (stolt.cc: arange, floor, clip)
+            const int t = fl + (int)floorf(f + ((float)k - half));
+            const int idx = min(max(t, 0), NR - 1);
+            const float u = f + (float)(fl - idx);  // c - idx
+            float w;
+            if (u == 0.f) {
+                w = 1.f;
+            } else {
+                const float s = (idx == t) ? (((fl - idx) & 1) ? -s0 : s0) : sinpif(u);
+                w = s / (3.14159265358979323846f * u);
+            }
+            const float2 v = sm[idx];
+            acc.x = fmaf(w, v.x, acc.x);
+            acc.y = fmaf(w, v.y, acc.y);
+        }
+        dst[n] = acc;
+    }
+}
+
+}  // namespace
+
+bool dft_size_supported(int n) {
+    if (n < 2 || n > 16384) return false;
+    if ((n & (n - 1)) == 0) return true;
+    return n <= 8192;
+}
+
+int dft_bluestein_size(int n) {
+    if ((n & (n - 1)) == 0) return 0;
+    int m = 4;
+    while (m < 2 * n - 1) m <<= 1;
+    return m;
+}
+
+cudaError_t launch_dft_rows(const DftPlan &p, float2 *data, int rows, long long ld, bool inverse, float scale,
+                            cudaStream_t s) {
+    if (rows <= 0) return cudaSuccess;
+    return inverse ? dft_dispatch<true>(p, data, rows, ld, scale, s) : dft_dispatch<false>(p, data, rows, ld, scale, s);
+}
+
+cudaError_t launch_transpose(const float2 *in, float2 *out, int rows, int cols, cudaStream_t s) {
+    dim3 grid((cols + kTile - 1) / kTile, (rows + kTile - 1) / kTile);
+    transpose_kernel<<<grid, dim3(kTile, 8), 0, s>>>(in, out, rows, cols);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_wk_pad(const float2 *echo, int na, int nr, int pa, int pr, int NA, int NR, const float2 *rowphase,
+                          float2 *out, cudaStream_t s) {
+    const size_t total = (size_t)NA * NR;
+    const int blocks = (int)std::min<size_t>((total + 255) / 256, (size_t)152 * 16);
+    wk_pad_kernel<<<blocks, 256, 0, s>>>(echo, na, nr, pa, pr, NA, NR, rowphase, out);
+    return cudaGetLastError();
+}
+
+size_t wk_stolt_smem(int NR) { return (size_t)NR * (sizeof(float2) + sizeof(float)); }
+
+cudaError_t launch_wk_stolt(const float2 *in, float2 *out, int NA, int NR, const double *col_f2, const double *col_ph,
+                            const double *col_fr, const double *row_q, double a4r, double f0, double inv_gap, int taps,
+                            cudaStream_t s) {
+    const size_t smem = wk_stolt_smem(NR);
+    cudaError_t e = cudaFuncSetAttribute(wk_stolt_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    wk_stolt_kernel<<<NA, kStoltThreads, smem, s>>>(in, out, NR, col_f2, col_ph, col_fr, row_q, a4r, f0, inv_gap, taps);
+    return cudaGetLastError();
+}
+
+}  // namespace sarbp

@@ -61,6 +61,22 @@ class RcLayout(ctypes.Structure):
                 ("nbins", ctypes.c_int32), ("t0_bins", ctypes.c_double), ("bin_rate", ctypes.c_double)]
 
 
+class WkParams(ctypes.Structure):
+    _fields_ = [("fr", ctypes.c_double), ("prf", ctypes.c_double), ("f0", ctypes.c_double),
+                ("r0", ctypes.c_double), ("kr", ctypes.c_double), ("c", ctypes.c_double),
+                ("vr", ctypes.c_double), ("f_nc", ctypes.c_double), ("taps", ctypes.c_int32),
+                ("reserved", ctypes.c_int32)]
+
+
+def wk_params(p) -> WkParams:
+    """WkParams from any object with fr, prf, f0, r0, kr, c, vr, f_nc, taps."""
+    w = WkParams()
+    for f in ("fr", "prf", "f0", "r0", "kr", "c", "vr", "f_nc"):
+        setattr(w, f, float(getattr(p, f)))
+    w.taps = int(p.taps)
+    return w
+
+
 class PulseCorr(ctypes.Structure):
     _fields_ = [("drange", ctypes.c_void_p), ("dphase", ctypes.c_void_p)]
 
@@ -147,6 +163,12 @@ SIGNATURES = {
     "sarbp_autofocus": ([ctypes.c_void_p, ctypes.POINTER(Radar), ctypes.POINTER(RcView), ctypes.c_void_p,
                          ctypes.POINTER(Grid), ctypes.c_int32, ctypes.c_int32, ctypes.c_void_p, ctypes.c_void_p,
                          ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p], ctypes.c_int),
+    "sarbp_wk_padded_size": ([ctypes.c_int32, ctypes.c_int32, ctypes.POINTER(ctypes.c_int32),
+                              ctypes.POINTER(ctypes.c_int32)], ctypes.c_int),
+    "sarbp_wk_image": ([ctypes.c_void_p, ctypes.POINTER(WkParams), ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32,
+                        ctypes.c_void_p, ctypes.c_void_p], ctypes.c_int),
+    "sarbp_dft": ([ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32, ctypes.c_void_p],
+                  ctypes.c_int),
     "sarbp_image": ([ctypes.c_void_p, ctypes.POINTER(Radar), ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32,
                      ctypes.c_void_p, ctypes.POINTER(Grid), ctypes.c_int32, ctypes.c_void_p, ctypes.c_void_p],
                     ctypes.c_int),
@@ -357,6 +379,28 @@ class Context:
                                             ctypes.byref(grid), mode, int(iterations), _ptr(dr), _ptr(ph),
                                             _ptr(image), _ptr(sharp), stream), "autofocus")
         return ph, sharp, image
+
+    def wk_padded_size(self, na: int, nr: int):
+        a, b = ctypes.c_int32(), ctypes.c_int32()
+        st = self.lib.sarbp_wk_padded_size(int(na), int(nr), ctypes.byref(a), ctypes.byref(b))
+        return a.value, b.value, st
+
+    def wk_image(self, params, echo, image=None, stream=None):
+        """Omega-K image [na_pad][nr_pad] complex64 of echo [na][nr]."""
+        w = params if isinstance(params, WkParams) else wk_params(params)
+        na, nr = echo.shape
+        NA, NR, _ = self.wk_padded_size(na, nr)
+        if image is None:
+            image = np.zeros((NA, NR), dtype=np.complex64)
+        self.check(self.lib.sarbp_wk_image(self.h, ctypes.byref(w), _ptr(echo), na, nr, _ptr(image), stream),
+                   "wk_image")
+        return image
+
+    def dft(self, data, inverse: bool = False, stream=None):
+        """In-place batched DFT along the rows of data [rows][n] (complex64)."""
+        rows, n = data.shape
+        self.check(self.lib.sarbp_dft(self.h, _ptr(data), rows, n, int(inverse), stream), "dft")
+        return data
 
     def image(self, radar: Radar, echo, apc, grid: Grid, mode: int, image=None, stream=None):
         np_, ns = echo.shape

@@ -1,0 +1,100 @@
+"""GPU parity of the omega-K imager and its batched DFT against FP64 numpy /
+the omega-K oracle (oracle/wk.py).
+
+Tolerances (relative L2): DFT <= -110 dB (FP32 transforms of up to 16384
+points); omega-K image <= -80 dB against the FP64 restatement (FP32 FFTs, FP64
+phases, FP32 Stolt weights)."""
+import os
+
+import numpy as np
+import pytest
+
+from oracle import wk
+from sar_cambrianaccelerationcard_gb300 import metrics, sarbp
+
+pytestmark = pytest.mark.gpu
+
+GOLDEN = os.path.join(os.path.dirname(__file__), "golden", "wk_cd_crop.npz")
+
+
+@pytest.fixture(scope="module")
+def ctx():
+    c = sarbp.Context(0)
+    yield c
+    c.close()
+
+
+def rand(shape, seed):
+    rng = np.random.default_rng(seed)
+    return (rng.standard_normal(shape) + 1j * rng.standard_normal(shape)).astype(np.complex64)
+
+
+@pytest.mark.parametrize("n", [2, 8, 64, 512, 4096, 16384, 3, 5, 7, 100, 106, 214, 854, 1000, 3414, 8191])
+def test_dft_rows(ctx, n):
+    rows = max(1, min(64, 65536 // n))
+    x = rand((rows, n), n)
+    ref = np.fft.fft(x.astype(np.complex128), axis=1)
+    got = ctx.dft(x.copy())
+    err = metrics.rel_l2_db(got, ref)
+    back = ctx.dft(got.copy(), inverse=True)
+    err_inv = metrics.rel_l2_db(back, x.astype(np.complex128))
+    print(f"dft n {n}: forward {err:.1f} dB, round trip {err_inv:.1f} dB")
+    assert err <= -110.0
+    assert err_inv <= -110.0
+
+
+def test_dft_rejects_unsupported(ctx):
+    with pytest.raises(sarbp.SarbpError):
+        ctx.dft(np.zeros((2, 8193), dtype=np.complex64))
+
+
+def test_wk_golden_crop(ctx):
+    """The reference's RADARSAT-1 echo (96 x 64 crop): GPU against the FP64 image."""
+    g = np.load(GOLDEN)
+    img = ctx.wk_image(wk.radarsat1(), g["echo"])
+    err = metrics.rel_l2_db(img, g["image"])
+    print("wk golden crop rel-L2 dB", err)
+    assert img.shape == (128, 106)
+    assert err <= -80.0
+
+
+@pytest.mark.parametrize("shape,taps", [((768, 512), 6), ((300, 200), 6), ((128, 96), 5), ((64, 256), 8)])
+def test_wk_matches_oracle(ctx, shape, taps):
+    p = wk.radarsat1()
+    p.taps = taps
+    echo = rand(shape, 7 + taps)
+    ref = wk.wk_image(echo.astype(np.complex128), p)
+    img = ctx.wk_image(p, echo)
+    err = metrics.rel_l2_db(img, ref)
+    print(f"wk {shape} taps {taps} rel-L2 dB {err:.1f}")
+    assert err <= -80.0
+
+
+def test_wk_device_pointers(ctx):
+    torch = pytest.importorskip("torch")
+    p = wk.radarsat1()
+    echo = rand((192, 128), 3)
+    host = ctx.wk_image(p, echo)
+    NA, NR, _ = ctx.wk_padded_size(192, 128)
+    d_echo = torch.from_numpy(echo.view(np.float32)).cuda()
+    d_img = torch.empty((NA, NR * 2), dtype=torch.float32, device="cuda")
+    w = sarbp.wk_params(p)
+    ctx.check(ctx.lib.sarbp_wk_image(ctx.h, sarbp.ctypes.byref(w), d_echo.data_ptr(), 192, 128, d_img.data_ptr(), None),
+              "wk device")
+    ctx.synchronize()
+    dev = d_img.cpu().numpy().view(np.complex64)
+    assert np.array_equal(dev, host)
+
+
+def test_wk_rejects_bad_arguments(ctx):
+    p = wk.radarsat1()
+    with pytest.raises(sarbp.SarbpError):
+        q = wk.radarsat1()
+        q.taps = 0
+        ctx.wk_image(q, rand((64, 64), 1))
+    with pytest.raises(sarbp.SarbpError):
+        q = wk.radarsat1()
+        q.prf = float("nan")
+        ctx.wk_image(q, rand((64, 64), 1))
+    with pytest.raises(sarbp.SarbpError):  # padded range size 10924 > 8192 and not a power of two
+        ctx.wk_image(p, rand((8, 6554), 1))
