@@ -58,7 +58,7 @@ def build(verbose: bool = False, extra=(), lib: str = LIB, build_dir: str = BUIL
         objs = list(ex.map(lambda s: _compile(s, extra, build_dir), SOURCES))
     if os.path.exists(lib) and all(os.path.getmtime(lib) >= os.path.getmtime(o) for o in objs):
         return lib
-    cmd = [nvcc(), *ARCH, "-shared", "-o", lib, *objs, "-cudart", "static"]
+    cmd = [nvcc(), *ARCH, "-shared", "-o", lib, *objs, "-cudart", "static", "-Xlinker", "--no-undefined"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
