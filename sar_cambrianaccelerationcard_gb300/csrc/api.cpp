@@ -861,9 +861,12 @@ sarbp_status sarbp_wk_image(sarbp_ctx *ctx, const sarbp_wk_params *w, const sarb
     cudaStream_t s = pick_stream(ctx, stream);
     // host tables (FP64): row phasors exp(-j 2 pi f_nc ta_m), ta_m = (m - NA/2) / prf;
     // frequency axes as the reference builds them (fftshifted index, wk.cc:181-205)
-    std::vector<float2> rowphase(NA);
+    const double a4r = 4.0 * kPi * w->r0 / w->c;
+    std::vector<float2> rowphase(NA), row_qf(NA), col_ip(NR);
+    std::vector<float> col_c(NR);
     std::vector<double> tab(3 * (size_t)NR + NA);
     double *col_f2 = tab.data(), *col_ph = col_f2 + NR, *col_fr = col_ph + NR, *row_q = col_fr + NR;
+    double qmax = 0.0, pmin = 1e300;
     for (int m = 0; m < NA; ++m) {
         const double ta = (double)(m - NA / 2) / w->prf;
         const double cyc = -w->f_nc * ta;
@@ -872,20 +875,41 @@ sarbp_status sarbp_wk_image(sarbp_ctx *ctx, const sarbp_wk_params *w, const sarb
         const int idx = m < NA / 2 ? m + NA / 2 : m - NA / 2;
         const double fa = w->f_nc + (double)(idx - NA / 2) * (w->prf / NA);
         row_q[m] = w->c * w->c / (4.0 * w->vr * w->vr) * fa * fa;
+        const float qh = (float)row_q[m];
+        row_qf[m] = make_float2(qh, (float)(row_q[m] - (double)qh));
+        qmax = std::max(qmax, row_q[m]);
     }
     for (int n = 0; n < NR; ++n) {
         const int idx = n < NR / 2 ? n + NR / 2 : n - NR / 2;
         const double fr = (double)(idx - NR / 2) * (w->fr / NR);
-        col_f2[n] = (w->f0 + fr) * (w->f0 + fr);
+        const double P = w->f0 + fr;
+        col_f2[n] = P * P;
         col_ph[n] = kPi * fr * fr / w->kr;
         col_fr[n] = fr;
+        const double th = a4r * P + col_ph[n];
+        col_c[n] = (float)(th - 2.0 * kPi * std::nearbyint(th / (2.0 * kPi)));
+        const double ip = 1.0 / P;
+        const float iph = (float)ip;
+        col_ip[n] = make_float2(iph, (float)(ip - (double)iph));
+        pmin = std::min(pmin, P);
     }
+    // float-float Stolt stage when the mapping is a small correction (eps <= 1e-2), else FP64
+    const bool ff_stolt = pmin > 0.0 && qmax / (pmin * pmin) <= 1e-2;
     const size_t npix = (size_t)NA * NR;
     SARBP_CUDA(ctx, ctx->wk0.ensure(sizeof(float2) * npix), "alloc omega-K buffer");
     SARBP_CUDA(ctx, ctx->wk1.ensure(sizeof(float2) * npix), "alloc omega-K buffer");
-    SARBP_CUDA(ctx, ctx->wkrow.ensure(sizeof(float2) * NA), "alloc omega-K tables");
+    const size_t row_bytes = sizeof(float2) * 2 * NA, col_bytes = (sizeof(float) + sizeof(float2)) * NR;
+    SARBP_CUDA(ctx, ctx->wkrow.ensure(row_bytes + col_bytes), "alloc omega-K tables");
     SARBP_CUDA(ctx, ctx->wktab.ensure(sizeof(double) * tab.size()), "alloc omega-K tables");
-    SARBP_CUDA(ctx, cudaMemcpyAsync(ctx->wkrow.ptr, rowphase.data(), sizeof(float2) * NA, cudaMemcpyHostToDevice, s),
+    float2 *d_rowphase = ctx->wkrow.as<float2>(), *d_rowq = d_rowphase + NA, *d_colip = d_rowq + NA;
+    float *d_colc = reinterpret_cast<float *>(d_colip + NR);
+    SARBP_CUDA(ctx, cudaMemcpyAsync(d_rowphase, rowphase.data(), sizeof(float2) * NA, cudaMemcpyHostToDevice, s),
+               "upload omega-K tables");
+    SARBP_CUDA(ctx, cudaMemcpyAsync(d_rowq, row_qf.data(), sizeof(float2) * NA, cudaMemcpyHostToDevice, s),
+               "upload omega-K tables");
+    SARBP_CUDA(ctx, cudaMemcpyAsync(d_colip, col_ip.data(), sizeof(float2) * NR, cudaMemcpyHostToDevice, s),
+               "upload omega-K tables");
+    SARBP_CUDA(ctx, cudaMemcpyAsync(d_colc, col_c.data(), sizeof(float) * NR, cudaMemcpyHostToDevice, s),
                "upload omega-K tables");
     SARBP_CUDA(ctx, cudaMemcpyAsync(ctx->wktab.ptr, tab.data(), sizeof(double) * tab.size(), cudaMemcpyHostToDevice, s),
                "upload omega-K tables");
@@ -902,14 +926,27 @@ sarbp_status sarbp_wk_image(sarbp_ctx *ctx, const sarbp_wk_params *w, const sarb
     const bool dev_img = is_device_ptr(image);
     float2 *out = dev_img ? reinterpret_cast<float2 *>(image) : B;
     cudaEventRecord(ctx->ev[0], s);
-    SARBP_CUDA(ctx, sarbp::launch_wk_pad(d_echo, na, nr, pa, pr, NA, NR, ctx->wkrow.as<float2>(), A, s), "omega-K pad");
-    SARBP_CUDA(ctx, sarbp::launch_dft_rows(pr_plan, A, NA, NR, false, 1.0f, s), "range FFT");
+    // padding rows stay zero through the range FFT; the echo rows are padded,
+    // down-converted and transformed in one pass
+    SARBP_CUDA(ctx, cudaMemsetAsync(A, 0, sizeof(float2) * (size_t)pa * NR, s), "clear padding");
+    SARBP_CUDA(ctx, cudaMemsetAsync(A + (size_t)(pa + na) * NR, 0, sizeof(float2) * (size_t)(NA - pa - na) * NR, s),
+               "clear padding");
+    sarbp::DftIo io;
+    io.src = d_echo;
+    io.src_cols = nr;
+    io.col0 = pr;
+    io.rowmul = d_rowphase + pa;
+    SARBP_CUDA(ctx, sarbp::launch_dft_rows(pr_plan, A + (size_t)pa * NR, na, NR, false, 1.0f, s, io), "range FFT");
     SARBP_CUDA(ctx, sarbp::launch_transpose(A, B, NA, NR, s), "transpose");
     SARBP_CUDA(ctx, sarbp::launch_dft_rows(pa_plan, B, NR, NA, false, 1.0f, s), "azimuth FFT");
     SARBP_CUDA(ctx, sarbp::launch_transpose(B, A, NR, NA, s), "transpose");
-    SARBP_CUDA(ctx, sarbp::launch_wk_stolt(A, B, NA, NR, d_tab, d_tab + NR, d_tab + 2 * NR, d_tab + 3 * NR,
-                                            4.0 * kPi * w->r0 / w->c, w->f0, NR / w->fr, w->taps, s),
-               "reference-function multiply and Stolt mapping");
+    if (ff_stolt)
+        SARBP_CUDA(ctx, sarbp::launch_wk_stolt_ff(A, B, NA, NR, d_colc, d_colip, d_rowq, a4r, NR / w->fr, w->taps, s),
+                   "reference-function multiply and Stolt mapping");
+    else
+        SARBP_CUDA(ctx, sarbp::launch_wk_stolt(A, B, NA, NR, d_tab, d_tab + NR, d_tab + 2 * NR, d_tab + 3 * NR, a4r,
+                                                w->f0, NR / w->fr, w->taps, s),
+                   "reference-function multiply and Stolt mapping");
     SARBP_CUDA(ctx, sarbp::launch_dft_rows(pr_plan, B, NA, NR, true, 1.0f / (float)NR, s), "range IFFT");
     SARBP_CUDA(ctx, sarbp::launch_transpose(B, A, NA, NR, s), "transpose");
     SARBP_CUDA(ctx, sarbp::launch_dft_rows(pa_plan, A, NR, NA, true, 1.0f / (float)NA, s), "azimuth IFFT");
@@ -917,7 +954,7 @@ sarbp_status sarbp_wk_image(sarbp_ctx *ctx, const sarbp_wk_params *w, const sarb
     cudaEventRecord(ctx->ev[1], s);
     ctx->timed_rc = true;  // sarbp_last_timings reports the omega-K time in its rc slot
     ctx->timed_bp = false;
-    ctx->launches += 10;
+    ctx->launches += 9;
     if (!dev_img)
         SARBP_CUDA(ctx, cudaMemcpyAsync(image, out, sizeof(float2) * npix, cudaMemcpyDeviceToHost, s), "download image");
     return finish(ctx, s, any_host);

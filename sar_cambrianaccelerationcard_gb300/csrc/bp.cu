@@ -37,6 +37,8 @@
 
 #include <math_constants.h>
 
+#include "ffloat.cuh"
+
 namespace sarbp {
 namespace {
 
@@ -185,31 +187,6 @@ struct TileGeo {
     float xT, yT;           // tile centre in pixel units from the grid origin (exact)
     float qqh, qql;         // |xT ux + yT uy|^2 as a float pair
 };
-
-// Float-float ("double-float") arithmetic on the FP32 pipe: a value is h + l
-// with |l| <= ulp(h)/2, about 48 significant bits.  Error-free transforms
-// (Knuth two-sum, FMA two-product).
-struct ff {
-    float h, l;
-};
-__device__ __forceinline__ ff two_sum(float a, float b) {
-    const float s = a + b;
-    const float bb = s - a;
-    return {s, (a - (s - bb)) + (b - bb)};
-}
-__device__ __forceinline__ ff quick_two_sum(float a, float b) {
-    const float s = a + b;
-    return {s, b - (s - a)};
-}
-__device__ __forceinline__ ff ff_add(ff a, ff b) {
-    const ff s = two_sum(a.h, b.h);
-    return quick_two_sum(s.h, s.l + (a.l + b.l));
-}
-__device__ __forceinline__ ff ff_mul_f(ff a, float b) {
-    const float p = a.h * b;
-    const float e = fmaf(a.h, b, -p);
-    return quick_two_sum(p, fmaf(a.l, b, e));
-}
 
 // Per-pulse reference (FP64), relative to the grid origin O:
 //   a0 = |O - apc|^2, a1 = 2 ux.(O - apc), a2 = 2 uy.(O - apc)

@@ -123,6 +123,15 @@ struct DftPlan {
     const float2 *kfwd;   // [m] FFT_m of the circular kernel w, / m (Bluestein forward)
     const float2 *kinv;   // [m] FFT_m of conj(w), / m (Bluestein inverse)
 };
+// Optional input of a row transform: element i of row b is src[b][i - col0] *
+// rowmul[b] inside [col0, col0 + src_cols) and 0 outside (fused zero padding
+// and azimuth down-conversion); src = null transforms the rows in place.
+struct DftIo {
+    const float2 *src = nullptr;
+    int src_cols = 0;
+    int col0 = 0;
+    const float2 *rowmul = nullptr;
+};
 bool dft_size_supported(int n);
 int dft_bluestein_size(int n);
 // host FP64 tables for a DftPlan of length n (plan.cpp)
@@ -130,11 +139,14 @@ void dft_tables_host(int n, std::vector<float2> &etab, std::vector<float2> &chir
                      std::vector<float2> &kinv);
 // rows x n in place (row stride ld): forward unnormalised, or inverse; times scale
 cudaError_t launch_dft_rows(const DftPlan &p, float2 *data, int rows, long long ld, bool inverse, float scale,
-                            cudaStream_t s);
+                            cudaStream_t s, const DftIo &io = DftIo());
 cudaError_t launch_transpose(const float2 *in, float2 *out, int rows, int cols, cudaStream_t s);
-cudaError_t launch_wk_pad(const float2 *echo, int na, int nr, int pa, int pr, int NA, int NR, const float2 *rowphase,
-                          float2 *out, cudaStream_t s);
 size_t wk_stolt_smem(int NR);
+// FP32 / float-float form of the Stolt stage (eps = q / (f0 + fr)^2 <= 1e-2):
+// col_c = (A (f0 + fr) + pi fr^2 / kr) mod 2 pi, col_ip = 1 / (f0 + fr) and row_q as float pairs.
+cudaError_t launch_wk_stolt_ff(const float2 *in, float2 *out, int NA, int NR, const float *col_c,
+                               const float2 *col_ip, const float2 *row_q, double a4r, double nr_over_fr, int taps,
+                               cudaStream_t s);
 cudaError_t launch_wk_stolt(const float2 *in, float2 *out, int NA, int NR, const double *col_f2, const double *col_ph,
                             const double *col_fr, const double *row_q, double a4r, double f0, double inv_gap, int taps,
                             cudaStream_t s);

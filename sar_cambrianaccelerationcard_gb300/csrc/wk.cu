@@ -28,6 +28,7 @@
 #include <algorithm>
 
 #include "fft_smem.cuh"
+#include "ffloat.cuh"
 
 namespace sarbp {
 namespace {
@@ -39,14 +40,24 @@ constexpr int dft_threads() {
     return N >= 8192 ? 1024 : (N >= 4096 ? 512 : (N >= 512 ? N / 8 : 64));
 }
 
+// Element i of the transformed row b: the row itself, or (fused padding and
+// azimuth down-conversion) src[b][i - col0] * rowmul[b] inside the source
+// columns and 0 outside.
+__device__ __forceinline__ float2 dft_input(const DftIo &io, const float2 *row, int b, int i) {
+    if (!io.src) return row[i];
+    const int c = i - io.col0;
+    if (c < 0 || c >= io.src_cols) return make_float2(0.f, 0.f);
+    return cmul(__ldg(&io.src[(size_t)b * io.src_cols + c]), __ldg(&io.rowmul[b]));
+}
+
 // Power-of-two row transform: row r of data (stride ld) in place, times scale.
 template <int N, int T, bool INV>
 __global__ void __launch_bounds__(T) dft_pow2_kernel(float2 *__restrict__ data, long long ld, float scale,
-                                                     const float2 *__restrict__ etab) {
+                                                     const float2 *__restrict__ etab, DftIo io) {
     extern __shared__ float2 sm[];
     const Etab E = load_etab<N, T>(sm, etab, 1);
     float2 *row = data + (size_t)blockIdx.x * ld;
-    for (int i = threadIdx.x; i < N; i += T) sm[sw(i)] = row[i];
+    for (int i = threadIdx.x; i < N; i += T) sm[sw(i)] = dft_input(io, row, blockIdx.x, i);
     __syncthreads();
     fft_smem<N, T, INV>(sm, E);
     for (int i = threadIdx.x; i < N; i += T) {
@@ -64,7 +75,7 @@ template <int M, int T, bool INV>
 __global__ void __launch_bounds__(T) dft_bluestein_kernel(float2 *__restrict__ data, long long ld, int n,
                                                           float scale, const float2 *__restrict__ etab,
                                                           const float2 *__restrict__ chirp,
-                                                          const float2 *__restrict__ kspec) {
+                                                          const float2 *__restrict__ kspec, DftIo io) {
     extern __shared__ float2 sm[];
     const Etab E = load_etab<M, T>(sm, etab, 1);
     float2 *row = data + (size_t)blockIdx.x * ld;
@@ -73,7 +84,7 @@ __global__ void __launch_bounds__(T) dft_bluestein_kernel(float2 *__restrict__ d
         if (i < n) {
             float2 w = __ldg(&chirp[i]);
             if (!INV) w.y = -w.y;
-            v = cmul(row[i], w);
+            v = cmul(dft_input(io, row, blockIdx.x, i), w);
         }
         sm[sw(i)] = v;
     }
@@ -91,31 +102,34 @@ __global__ void __launch_bounds__(T) dft_bluestein_kernel(float2 *__restrict__ d
 }
 
 template <int N, bool INV>
-cudaError_t pow2_n(const DftPlan &p, float2 *data, int rows, long long ld, float scale, cudaStream_t s) {
+cudaError_t pow2_n(const DftPlan &p, float2 *data, int rows, long long ld, float scale, const DftIo &io,
+                   cudaStream_t s) {
     constexpr int T = dft_threads<N>();
     const size_t smem = sizeof(float2) * N + kTabSmem;
     auto k = dft_pow2_kernel<N, T, INV>;
     cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
-    k<<<rows, T, smem, s>>>(data, ld, scale, p.etab);
+    k<<<rows, T, smem, s>>>(data, ld, scale, p.etab, io);
     return cudaGetLastError();
 }
 
 template <int M, bool INV>
-cudaError_t blue_m(const DftPlan &p, float2 *data, int rows, long long ld, float scale, cudaStream_t s) {
+cudaError_t blue_m(const DftPlan &p, float2 *data, int rows, long long ld, float scale, const DftIo &io,
+                   cudaStream_t s) {
     constexpr int T = dft_threads<M>();
     const size_t smem = sizeof(float2) * M + kTabSmem;
     auto k = dft_bluestein_kernel<M, T, INV>;
     cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
-    k<<<rows, T, smem, s>>>(data, ld, p.n, scale, p.etab, p.chirp, INV ? p.kinv : p.kfwd);
+    k<<<rows, T, smem, s>>>(data, ld, p.n, scale, p.etab, p.chirp, INV ? p.kinv : p.kfwd, io);
     return cudaGetLastError();
 }
 
 template <bool INV>
-cudaError_t dft_dispatch(const DftPlan &p, float2 *data, int rows, long long ld, float scale, cudaStream_t s) {
+cudaError_t dft_dispatch(const DftPlan &p, float2 *data, int rows, long long ld, float scale, const DftIo &io,
+                         cudaStream_t s) {
 #define SARBP_DFT_CASE(F, V) \
-    case V: return F<V, INV>(p, data, rows, ld, scale, s);
+    case V: return F<V, INV>(p, data, rows, ld, scale, io, s);
     if (p.m == 0) {
         switch (p.n) {
             SARBP_DFT_CASE(pow2_n, 2) SARBP_DFT_CASE(pow2_n, 4) SARBP_DFT_CASE(pow2_n, 8)
@@ -157,52 +171,14 @@ __global__ void __launch_bounds__(kTile * 8) transpose_kernel(const float2 *__re
     }
 }
 
-// ------------------------------------------------------------------ pad + down-conversion
-
-// out[m][n] = echo[m - pa][n - pr] * rowphase[m] inside the echo, 0 in the padding.
-__global__ void wk_pad_kernel(const float2 *__restrict__ echo, int na, int nr, int pa, int pr, int NA, int NR,
-                              const float2 *__restrict__ rowphase, float2 *__restrict__ out) {
-    const size_t total = (size_t)NA * NR;
-    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total; i += (size_t)gridDim.x * blockDim.x) {
-        const int m = (int)(i / NR), n = (int)(i - (size_t)m * NR);
-        const int a = m - pa, r = n - pr;
-        float2 v = make_float2(0.f, 0.f);
-        if (a >= 0 && a < na && r >= 0 && r < nr) v = cmul(__ldg(&echo[(size_t)a * nr + r]), __ldg(&rowphase[m]));
-        out[i] = v;
-    }
-}
-
 // ------------------------------------------------------------------ RFM + Stolt
 
 constexpr int kStoltThreads = 512;
 
-// One CTA per azimuth-frequency row m of in/out ([NA][NR]).
-//   col_f2[n]  = (f0 + fr_n)^2,  col_ph[n] = pi fr_n^2 / kr,  col_fr[n] = fr_n
-//   row_q[m]   = c^2 fa_m^2 / (4 Vr^2)
-__global__ void __launch_bounds__(kStoltThreads) wk_stolt_kernel(const float2 *__restrict__ in,
-                                                                  float2 *__restrict__ out, int NR,
-                                                                  const double *__restrict__ col_f2,
-                                                                  const double *__restrict__ col_ph,
-                                                                  const double *__restrict__ col_fr,
-                                                                  const double *__restrict__ row_q, double a4r,
-                                                                  double f0, double inv_gap, int taps) {
-    extern __shared__ float2 sm[];
-    float *sdelta = reinterpret_cast<float *>(sm + NR);
-    const int m = blockIdx.x;
-    const double q = row_q[m];
-    const float2 *src = in + (size_t)m * NR;
-    constexpr double kTwoPi = 6.283185307179586476925;
-    for (int n = threadIdx.x; n < NR; n += kStoltThreads) {
-        const double root = sqrt(fmax(col_f2[n] - q, 0.0));
-        double th = fma(a4r, root, col_ph[n]);
-        th -= kTwoPi * rint(th * (1.0 / kTwoPi));
-        float sn, cs;
-        sincosf((float)th, &sn, &cs);
-        sm[n] = cmul(__ldg(&src[n]), make_float2(cs, sn));
-        sdelta[n] = (float)((root - f0 - col_fr[n]) * inv_gap);
-    }
-    __syncthreads();
-    float2 *dst = out + (size_t)m * NR;
+// Stolt taps of one row: out[n] = sum over k of w_k sm[idx_k],
+// idx_k = clip(floor(n - delta[n] + k - taps/2), 0, NR - 1),
+// w_k = sin(pi u) / (pi u), u = n - delta[n] - idx_k.
+__device__ __forceinline__ void stolt_taps(const float2 *sm, const float *sdelta, float2 *dst, int NR, int taps) {
     const float half = 0.5f * (float)taps;
     for (int n = threadIdx.x; n < NR; n += kStoltThreads) {
         // centre c = n - delta = fl + f, f in [0, 1)
@@ -232,6 +208,81 @@ __global__ void __launch_bounds__(kStoltThreads) wk_stolt_kernel(const float2 *_
     }
 }
 
+// One CTA per azimuth-frequency row m of in/out ([NA][NR]).
+//   col_f2[n]  = (f0 + fr_n)^2,  col_ph[n] = pi fr_n^2 / kr,  col_fr[n] = fr_n
+//   row_q[m]   = c^2 fa_m^2 / (4 Vr^2)
+__global__ void __launch_bounds__(kStoltThreads) wk_stolt_kernel(const float2 *__restrict__ in,
+                                                                  float2 *__restrict__ out, int NR,
+                                                                  const double *__restrict__ col_f2,
+                                                                  const double *__restrict__ col_ph,
+                                                                  const double *__restrict__ col_fr,
+                                                                  const double *__restrict__ row_q, double a4r,
+                                                                  double f0, double inv_gap, int taps) {
+    extern __shared__ float2 sm[];
+    float *sdelta = reinterpret_cast<float *>(sm + NR);
+    const int m = blockIdx.x;
+    const double q = row_q[m];
+    const float2 *src = in + (size_t)m * NR;
+    constexpr double kTwoPi = 6.283185307179586476925;
+    for (int n = threadIdx.x; n < NR; n += kStoltThreads) {
+        const double root = sqrt(fmax(col_f2[n] - q, 0.0));
+        double th = fma(a4r, root, col_ph[n]);
+        th -= kTwoPi * rint(th * (1.0 / kTwoPi));
+        float sn, cs;
+        sincosf((float)th, &sn, &cs);
+        sm[n] = cmul(__ldg(&src[n]), make_float2(cs, sn));
+        sdelta[n] = (float)((root - f0 - col_fr[n]) * inv_gap);
+    }
+    __syncthreads();
+    stolt_taps(sm, sdelta, out + (size_t)m * NR, NR, taps);
+}
+
+// The same stage without FP64 arithmetic per sample.  With P = f0 + fr_n,
+// eps = q_m / P^2 and s = sqrt(1 - eps):
+//   root = P - u h,  u = q_m / P,  h = 1 / (1 + s) = 1/2 + eps / (2 (1 + s)^2)
+//   theta = [A P + pi fr^2 / kr] - A u / 2 - A u (h - 1/2)
+// The bracket is a per-column table reduced modulo 2 pi in FP64 on the host;
+// A u / 2 (~1e5 rad) is formed and reduced in float-float; the last term
+// (A u eps / 8, tens of radians when eps <= 1e-2) is FP32.
+//   col_c[n] = (A P + pi fr^2 / kr) mod 2 pi,  col_ip[n] = 1 / P (float pair)
+//   row_q[m] = q_m (float pair),  a2 = A / 2 (float pair)
+__global__ void __launch_bounds__(kStoltThreads) wk_stolt_ff_kernel(const float2 *__restrict__ in,
+                                                                     float2 *__restrict__ out, int NR,
+                                                                     const float *__restrict__ col_c,
+                                                                     const float2 *__restrict__ col_ip,
+                                                                     const float2 *__restrict__ row_q, float a2h,
+                                                                     float a2l, float a, float nr_over_fr,
+                                                                     int taps) {
+    extern __shared__ float2 sm[];
+    float *sdelta = reinterpret_cast<float *>(sm + NR);
+    const int m = blockIdx.x;
+    const float2 qv = __ldg(&row_q[m]);
+    const ff q{qv.x, qv.y};
+    const ff a2{a2h, a2l};
+    const ff two_pi{6.28318548202514648438f, -1.74845553e-07f};
+    const float2 *src = in + (size_t)m * NR;
+    for (int n = threadIdx.x; n < NR; n += kStoltThreads) {
+        const float2 ipv = __ldg(&col_ip[n]);
+        const ff u = ff_mul(q, ff{ipv.x, ipv.y});
+        const float eps = u.h * ipv.x;
+        const float sq = sqrtf(1.f - eps);
+        const float op = 1.f + sq;
+        const float h = 1.f / op;
+        const float hm = eps * (0.5f * h * h);  // h - 1/2
+        const ff d = ff_mul(u, a2);             // A u / 2
+        const float k = rintf(d.h * 0.159154943091895335769f);
+        const ff dr = ff_add(d, ff_mul_f(two_pi, -k));
+        float th = __ldg(&col_c[n]) - (dr.h + dr.l) - a * u.h * hm;
+        th -= 6.28318530717958647692f * rintf(th * 0.159154943091895335769f);
+        float sn, cs;
+        __sincosf(th, &sn, &cs);
+        sm[n] = cmul(__ldg(&src[n]), make_float2(cs, sn));
+        sdelta[n] = -u.h * h * nr_over_fr;  // (root - P) Nr / Fr
+    }
+    __syncthreads();
+    stolt_taps(sm, sdelta, out + (size_t)m * NR, NR, taps);
+}
+
 }  // namespace
 
 bool dft_size_supported(int n) {
@@ -248,9 +299,10 @@ int dft_bluestein_size(int n) {
 }
 
 cudaError_t launch_dft_rows(const DftPlan &p, float2 *data, int rows, long long ld, bool inverse, float scale,
-                            cudaStream_t s) {
+                            cudaStream_t s, const DftIo &io) {
     if (rows <= 0) return cudaSuccess;
-    return inverse ? dft_dispatch<true>(p, data, rows, ld, scale, s) : dft_dispatch<false>(p, data, rows, ld, scale, s);
+    return inverse ? dft_dispatch<true>(p, data, rows, ld, scale, io, s)
+                   : dft_dispatch<false>(p, data, rows, ld, scale, io, s);
 }
 
 cudaError_t launch_transpose(const float2 *in, float2 *out, int rows, int cols, cudaStream_t s) {
@@ -259,15 +311,20 @@ cudaError_t launch_transpose(const float2 *in, float2 *out, int rows, int cols, 
     return cudaGetLastError();
 }
 
-cudaError_t launch_wk_pad(const float2 *echo, int na, int nr, int pa, int pr, int NA, int NR, const float2 *rowphase,
-                          float2 *out, cudaStream_t s) {
-    const size_t total = (size_t)NA * NR;
-    const int blocks = (int)std::min<size_t>((total + 255) / 256, (size_t)152 * 16);
-    wk_pad_kernel<<<blocks, 256, 0, s>>>(echo, na, nr, pa, pr, NA, NR, rowphase, out);
+size_t wk_stolt_smem(int NR) { return (size_t)NR * (sizeof(float2) + sizeof(float)); }
+
+cudaError_t launch_wk_stolt_ff(const float2 *in, float2 *out, int NA, int NR, const float *col_c,
+                               const float2 *col_ip, const float2 *row_q, double a4r, double nr_over_fr, int taps,
+                               cudaStream_t s) {
+    const size_t smem = wk_stolt_smem(NR);
+    cudaError_t e = cudaFuncSetAttribute(wk_stolt_ff_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    const double a2 = 0.5 * a4r;
+    const float a2h = (float)a2, a2l = (float)(a2 - (double)a2h);
+    wk_stolt_ff_kernel<<<NA, kStoltThreads, smem, s>>>(in, out, NR, col_c, col_ip, row_q, a2h, a2l, (float)a4r,
+                                                       (float)nr_over_fr, taps);
     return cudaGetLastError();
 }
-
-size_t wk_stolt_smem(int NR) { return (size_t)NR * (sizeof(float2) + sizeof(float)); }
 
 cudaError_t launch_wk_stolt(const float2 *in, float2 *out, int NA, int NR, const double *col_f2, const double *col_ph,
                             const double *col_fr, const double *row_q, double a4r, double f0, double inv_gap, int taps,

@@ -70,6 +70,19 @@ def test_wk_matches_oracle(ctx, shape, taps):
     assert err <= -80.0
 
 
+def test_wk_fp64_stolt_path(ctx):
+    """An airborne L-band case (f0 1.3 GHz, Vr 120 m/s, zero Doppler centroid):
+    the mapping is no longer a small correction (c^2 fa^2 / (4 Vr^2) up to 0.4 of
+    (f0 + fr)^2), so the Stolt stage runs in FP64."""
+    p = wk.WkParams(fr=100e6, prf=1000.0, f0=1.3e9, r0=3000.0, kr=5e12, vr=120.0, f_nc=0.0)
+    echo = rand((192, 160), 21)
+    ref = wk.wk_image(echo.astype(np.complex128), p)
+    img = ctx.wk_image(p, echo)
+    err = metrics.rel_l2_db(img, ref)
+    print("wk fp64 stolt rel-L2 dB", err)
+    assert err <= -80.0
+
+
 def test_wk_device_pointers(ctx):
     torch = pytest.importorskip("torch")
     p = wk.radarsat1()
