@@ -664,7 +664,7 @@ def run_wk(args):
     line = {
         "metric": "omega-K image Mpix/s", "value": npix / (ms * 1e-3) / 1e6, "unit": "Mpix/s", "n_gpus": 1,
         "steps": args.steps, "warmup": max(3, args.warmup), "ms_per_step": ms, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f32 (FP64 phases)", "data": "synthetic (seeded)",
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32 (float-float phases)", "data": "synthetic (seeded)",
         "config": {"workload": f"omega-K RADARSAT-1 parameters, {na} x {nr} echo padded to {NA} x {NR}, Stolt "
                                f"{p.taps}-tap sinc", "l2": "working set 2 x 112 MB plus tables, larger than L2"},
         "accuracy": {"rel_l2_db_vs_fp64_restatement": err},
