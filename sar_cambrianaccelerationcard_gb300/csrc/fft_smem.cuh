@@ -247,5 +247,13 @@ __device__ __forceinline__ Etab load_etab(float2 *sm, const float2 *__restrict__
     return E;
 }
 
+// CTAs per SM that a T-thread kernel holding an N-point transform (plus the
+// tables) aims its register allocation at: two when both fit twice (8192
+// points at 512 threads: 64 registers per thread), else one.
+template <int N, int T>
+constexpr int fft_min_blocks() {
+    return (T * 64 <= 32768 && (size_t)N * 8 + kTabSmem <= (size_t)110 * 1024) ? 2 : 1;
+}
+
 }  // namespace
 }  // namespace sarbp

@@ -55,7 +55,7 @@ __device__ __forceinline__ float block_sum(float v, float *red) {
 }
 
 template <int N, int T>
-__global__ void __launch_bounds__(T) rc_forward_kernel(int ns, int L, const float2 *__restrict__ echo,
+__global__ void __launch_bounds__(T, (fft_min_blocks<N, T>())) rc_forward_kernel(int ns, int L, const float2 *__restrict__ echo,
                                                        const float2 *__restrict__ filt,
                                                        const float2 *__restrict__ etab,
                                                        float2 *__restrict__ spec,
@@ -85,7 +85,7 @@ __global__ void __launch_bounds__(T) rc_forward_kernel(int ns, int L, const floa
 }
 
 template <int N, int T, int STORE>
-__global__ void __launch_bounds__(T) rc_inverse_kernel(int ns, int L, int nbins,
+__global__ void __launch_bounds__(T, (fft_min_blocks<N, T>())) rc_inverse_kernel(int ns, int L, int nbins,
                                                        const float2 *__restrict__ spec,
                                                        const float2 *__restrict__ etab,
                                                        const float *__restrict__ scale,
@@ -241,12 +241,15 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(T)
 #ifndef SARBP_RC_SPLIT_MIN
 #define SARBP_RC_SPLIT_MIN 32768
 #endif
+#ifndef SARBP_RC_8K_THREADS
+#define SARBP_RC_8K_THREADS 1024
+#endif
 #ifndef SARBP_RC_BIG_THREADS
 #define SARBP_RC_BIG_THREADS 1024
 #endif
 template <int N>
 constexpr int threads_for() {
-    return N >= 8192 ? SARBP_RC_BIG_THREADS : (N >= 4096 ? 512 : (N >= 512 ? N / 8 : 64));
+    return N >= 16384 ? SARBP_RC_BIG_THREADS : (N >= 8192 ? SARBP_RC_8K_THREADS : (N >= 4096 ? 512 : (N >= 512 ? N / 8 : 64)));
 }
 
 

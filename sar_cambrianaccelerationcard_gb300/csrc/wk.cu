@@ -35,9 +35,12 @@ namespace {
 
 // ------------------------------------------------------------------ DFT rows
 
+#ifndef SARBP_DFT_T8192
+#define SARBP_DFT_T8192 512
+#endif
 template <int N>
 constexpr int dft_threads() {
-    return N >= 8192 ? 1024 : (N >= 4096 ? 512 : (N >= 512 ? N / 8 : 64));
+    return N >= 16384 ? 1024 : (N >= 8192 ? SARBP_DFT_T8192 : (N >= 4096 ? 512 : (N >= 512 ? N / 8 : 64)));
 }
 
 // Element i of the transformed row b: the row itself, or (fused padding and
@@ -52,7 +55,7 @@ __device__ __forceinline__ float2 dft_input(const DftIo &io, const float2 *row, 
 
 // Power-of-two row transform: row r of data (stride ld) in place, times scale.
 template <int N, int T, bool INV>
-__global__ void __launch_bounds__(T) dft_pow2_kernel(float2 *__restrict__ data, long long ld, float scale,
+__global__ void __launch_bounds__(T, (fft_min_blocks<N, T>())) dft_pow2_kernel(float2 *__restrict__ data, long long ld, float scale,
                                                      const float2 *__restrict__ etab, DftIo io) {
     extern __shared__ float2 sm[];
     const Etab E = load_etab<N, T>(sm, etab, 1);
@@ -72,7 +75,7 @@ __global__ void __launch_bounds__(T) dft_pow2_kernel(float2 *__restrict__ data, 
 // chirp[j] = w_j (j < n); kspec = FFT_M of the circular kernel (w or conj(w)),
 // divided by M (the inverse FFT's normalisation).
 template <int M, int T, bool INV>
-__global__ void __launch_bounds__(T) dft_bluestein_kernel(float2 *__restrict__ data, long long ld, int n,
+__global__ void __launch_bounds__(T, (fft_min_blocks<M, T>())) dft_bluestein_kernel(float2 *__restrict__ data, long long ld, int n,
                                                           float scale, const float2 *__restrict__ etab,
                                                           const float2 *__restrict__ chirp,
                                                           const float2 *__restrict__ kspec, DftIo io) {
