@@ -275,6 +275,37 @@ sarbp_status sarbp_wk_image(sarbp_ctx *ctx, const sarbp_wk_params *params, const
 sarbp_status sarbp_dft(sarbp_ctx *ctx, sarbp_complex64 *data, int32_t rows, int32_t n, int32_t inverse,
                        void *stream);
 
+/* ------------------------------------------------------ CEOS raw ingest -- */
+
+/* Layout of a RADARSAT-1 CEOS raw-data file as the reference's reader sees it
+ * (code/data_process/CEOS/read_CEOS_raw.m:13-16,67-80; its values in
+ * parentheses). */
+typedef struct sarbp_ceos_layout {
+    int32_t file_header;     /* bytes before the first block (16252) */
+    int32_t header;          /* record header bytes per line (192) */
+    int32_t aux;             /* auxiliary bytes per line (50) */
+    int32_t cells;           /* range cells per line, 2 bytes (I, Q) each (9288) */
+    int32_t replica;         /* replica bytes per block (2880) */
+    int32_t replica_line;    /* 1-based line of a block whose record holds the replica, after its aux bytes (7) */
+    int32_t lines_per_block; /* (8) */
+    int32_t agc_byte;        /* 1-based aux byte whose low 6 bits are the AGC code (50) */
+    float gain;              /* gain factor applied with the AGC attenuation (1.5) */
+    int32_t reserved;        /* must be 0 */
+} sarbp_ceos_layout;
+
+/* Decodes range lines [first_line, first_line + nlines) (0-based in the file)
+ * and cells [first_cell, first_cell + ncells) of a CEOS raw-data file into
+ * echo [nlines][ncells] complex64: sample byte d -> 2 (d' - 16 [d' > 7]) + 1
+ * with d' = d & 15 (read_CEOS_raw.m:135-141), times gain 10^(AGC_dB / 20) per
+ * line when apply_agc != 0 (load_DATA_block.m:58-69); agc_db [nlines] (may be
+ * NULL) receives code - 24 [code > 31] (extract_AGC.m:45-58).  raw holds the
+ * file from byte 0 (host or device, raw_bytes long); from host memory only
+ * the blocks holding the requested lines are copied to the device. */
+sarbp_status sarbp_ceos_decode(sarbp_ctx *ctx, const uint8_t *raw, uint64_t raw_bytes,
+                               const sarbp_ceos_layout *layout, int32_t first_line, int32_t nlines,
+                               int32_t first_cell, int32_t ncells, int32_t apply_agc,
+                               sarbp_complex64 *echo, int16_t *agc_db, void *stream);
+
 /* ------------------------------------------------------ echo synthesiser -- */
 
 /* Point-target echo with FP64 phase (BPA_SAR.m:80-89; replaces

@@ -16,7 +16,7 @@ ROOT = os.path.dirname(PKG)
 CSRC = os.path.join(PKG, "csrc")
 BUILD = os.path.join(PKG, "_build")
 LIB = os.path.join(PKG, "libsarbp.so")
-SOURCES = ["rc.cu", "bp.cu", "synth.cu", "probe.cu", "noalloc.cu", "autofocus.cu", "wk.cu", "plan.cpp", "serve.cpp", "api.cpp"]
+SOURCES = ["rc.cu", "bp.cu", "synth.cu", "probe.cu", "noalloc.cu", "autofocus.cu", "wk.cu", "ceos.cu", "plan.cpp", "serve.cpp", "api.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

@@ -960,6 +960,93 @@ sarbp_status sarbp_wk_image(sarbp_ctx *ctx, const sarbp_wk_params *w, const sarb
     return finish(ctx, s, any_host);
 }
 
+sarbp_status sarbp_ceos_decode(sarbp_ctx *ctx, const uint8_t *raw, uint64_t raw_bytes,
+                               const sarbp_ceos_layout *l, int32_t first_line, int32_t nlines, int32_t first_cell,
+                               int32_t ncells, int32_t apply_agc, sarbp_complex64 *echo, int16_t *agc_db,
+                               void *stream) {
+    if (!ctx) return SARBP_ERR_INVALID_ARGUMENT;
+    ctx->err.clear();
+    cudaSetDevice(ctx->device);
+    if (!l) return fail(ctx, SARBP_ERR_INVALID_ARGUMENT, "layout is null");
+    if (l->file_header < 0 || l->header < 0 || l->aux < 1 || l->cells < 1 || l->replica < 0 ||
+        l->lines_per_block < 1 || l->replica_line < 1 || l->replica_line > l->lines_per_block ||
+        l->agc_byte < 1 || l->agc_byte > l->aux || !std::isfinite(l->gain) || l->reserved != 0)
+        return fail(ctx, SARBP_ERR_INVALID_ARGUMENT, "inconsistent CEOS layout");
+    if ((l->file_header | l->header | l->aux | l->replica) & 1)
+        return fail(ctx, SARBP_ERR_UNSUPPORTED, "CEOS layouts with odd header, aux or replica sizes are not supported");
+    if (nlines < 0 || ncells < 0 || first_line < 0 || first_cell < 0 || first_cell + (long long)ncells > l->cells)
+        return fail(ctx, SARBP_ERR_INVALID_ARGUMENT, "line or cell range out of the layout");
+    if (nlines == 0 || ncells == 0) return SARBP_OK;
+    if (!raw || !echo) return fail(ctx, SARBP_ERR_INVALID_ARGUMENT, "raw and echo must be non-null");
+    sarbp::CeosGeom g{};
+    g.header = l->header;
+    g.aux = l->aux;
+    g.replica = l->replica;
+    g.replica_line = l->replica_line;
+    g.lines_per_block = l->lines_per_block;
+    g.agc_byte = l->agc_byte;
+    g.first_line = first_line;
+    g.nlines = nlines;
+    g.first_cell = first_cell;
+    g.ncells = ncells;
+    g.apply_agc = apply_agc != 0;
+    g.line_bytes = (long long)l->header + l->aux + 2LL * l->cells;
+    g.block_bytes = (long long)l->replica + (long long)l->lines_per_block * g.line_bytes;
+    const long long b0 = first_line / l->lines_per_block;
+    const long long b1 = (first_line + (long long)nlines - 1) / l->lines_per_block + 1;
+    const long long lo = l->file_header + b0 * g.block_bytes, hi = l->file_header + b1 * g.block_bytes;
+    if ((unsigned long long)hi > raw_bytes)
+        return fail(ctx, SARBP_ERR_INVALID_ARGUMENT, "raw data end at byte %llu, the lines need %lld",
+                    (unsigned long long)raw_bytes, hi);
+    cudaStream_t s = pick_stream(ctx, stream);
+    bool any_host = false;
+    const unsigned char *d_raw;
+    if (is_device_ptr(raw)) {
+        d_raw = reinterpret_cast<const unsigned char *>(raw);
+        g.raw_offset = -(long long)l->file_header;
+    } else {
+        SARBP_CUDA(ctx, ctx->echo.ensure((size_t)(hi - lo)), "alloc raw buffer");
+        SARBP_CUDA(ctx, cudaMemcpyAsync(ctx->echo.ptr, raw + lo, (size_t)(hi - lo), cudaMemcpyHostToDevice, s),
+                   "upload raw blocks");
+        d_raw = ctx->echo.as<unsigned char>();
+        g.raw_offset = b0 * g.block_bytes;
+        any_host = true;
+    }
+    // gain per AGC code: float(gain) * float(10^(dB / 20)), the reader's float arithmetic
+    float gains[64];
+    for (int code = 0; code < 64; ++code) {
+        const int db = code - 24 * (code > 31);
+        gains[code] = l->gain * (float)std::pow(10.0, db / 20.0);
+    }
+    SARBP_CUDA(ctx, ctx->wkrow.ensure(sizeof gains), "alloc gain table");
+    SARBP_CUDA(ctx, cudaMemcpyAsync(ctx->wkrow.ptr, gains, sizeof gains, cudaMemcpyHostToDevice, s), "upload gains");
+    float2 *d_echo = reinterpret_cast<float2 *>(echo);
+    const size_t out_bytes = sizeof(float2) * (size_t)nlines * ncells;
+    const bool dev_echo = is_device_ptr(echo);
+    if (!dev_echo) {
+        SARBP_CUDA(ctx, ctx->wk0.ensure(out_bytes), "alloc echo");
+        d_echo = ctx->wk0.as<float2>();
+        any_host = true;
+    }
+    short *d_agc = nullptr;
+    if (agc_db) {
+        if (is_device_ptr(agc_db)) {
+            d_agc = reinterpret_cast<short *>(agc_db);
+        } else {
+            SARBP_CUDA(ctx, ctx->sharp.ensure(sizeof(short) * nlines), "alloc agc");
+            d_agc = ctx->sharp.as<short>();
+            any_host = true;
+        }
+    }
+    SARBP_CUDA(ctx, sarbp::launch_ceos_decode(d_raw, g, ctx->wkrow.as<float>(), d_echo, d_agc, s), "CEOS decode");
+    ctx->launches += 1;
+    if (!dev_echo) SARBP_CUDA(ctx, cudaMemcpyAsync(echo, d_echo, out_bytes, cudaMemcpyDeviceToHost, s), "download echo");
+    if (agc_db && d_agc != reinterpret_cast<short *>(agc_db))
+        SARBP_CUDA(ctx, cudaMemcpyAsync(agc_db, d_agc, sizeof(short) * nlines, cudaMemcpyDeviceToHost, s),
+                   "download agc");
+    return finish(ctx, s, any_host);
+}
+
 sarbp_status sarbp_image(sarbp_ctx *ctx, const sarbp_radar *radar, const sarbp_complex64 *echo, int32_t np,
                          int32_t ns, const double *apc, const sarbp_grid *grid, int32_t mode, sarbp_complex64 *image,
                          void *stream) {

@@ -151,6 +151,17 @@ cudaError_t launch_wk_stolt(const float2 *in, float2 *out, int NA, int NR, const
                             const double *col_fr, const double *row_q, double a4r, double f0, double inv_gap, int taps,
                             cudaStream_t s);
 
+// ---------------------------------------------------------------- CEOS decode (ceos.cu)
+struct CeosGeom {
+    int header, aux, replica, replica_line, lines_per_block, agc_byte;
+    int first_line, nlines, first_cell, ncells, apply_agc;
+    long long line_bytes, block_bytes;
+    long long raw_offset;  // offset of the device buffer's byte 0 from the start of the first block
+};
+// echo [nlines][ncells], agc_db [nlines] (may be null); gains[64] = 1.5 10^(dB(code)/20)
+cudaError_t launch_ceos_decode(const unsigned char *raw, const CeosGeom &g, const float *gains, float2 *echo,
+                               short *agc_db, cudaStream_t s);
+
 // ---------------------------------------------------------------- autofocus (autofocus.cu)
 // w = |img|^2 img (w may be null); partial[sharpness_blocks(n)] = per-block sums of |img|^4.
 int sharpness_blocks(size_t n);

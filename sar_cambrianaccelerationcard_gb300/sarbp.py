@@ -77,6 +77,22 @@ def wk_params(p) -> WkParams:
     return w
 
 
+class CeosLayout(ctypes.Structure):
+    _fields_ = [("file_header", ctypes.c_int32), ("header", ctypes.c_int32), ("aux", ctypes.c_int32),
+                ("cells", ctypes.c_int32), ("replica", ctypes.c_int32), ("replica_line", ctypes.c_int32),
+                ("lines_per_block", ctypes.c_int32), ("agc_byte", ctypes.c_int32), ("gain", ctypes.c_float),
+                ("reserved", ctypes.c_int32)]
+
+
+def ceos_layout(l=None) -> CeosLayout:
+    """CeosLayout from an object with the same field names (RADARSAT-1 values by default)."""
+    c = CeosLayout(16252, 192, 50, 9288, 2880, 7, 8, 50, 1.5, 0)
+    if l is not None:
+        for f, _ in CeosLayout._fields_[:-1]:
+            setattr(c, f, getattr(l, f))
+    return c
+
+
 class PulseCorr(ctypes.Structure):
     _fields_ = [("drange", ctypes.c_void_p), ("dphase", ctypes.c_void_p)]
 
@@ -169,6 +185,9 @@ SIGNATURES = {
                         ctypes.c_void_p, ctypes.c_void_p], ctypes.c_int),
     "sarbp_dft": ([ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32, ctypes.c_void_p],
                   ctypes.c_int),
+    "sarbp_ceos_decode": ([ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint64, ctypes.POINTER(CeosLayout),
+                           ctypes.c_int32, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32,
+                           ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p], ctypes.c_int),
     "sarbp_image": ([ctypes.c_void_p, ctypes.POINTER(Radar), ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32,
                      ctypes.c_void_p, ctypes.POINTER(Grid), ctypes.c_int32, ctypes.c_void_p, ctypes.c_void_p],
                     ctypes.c_int),
@@ -395,6 +414,18 @@ class Context:
         self.check(self.lib.sarbp_wk_image(self.h, ctypes.byref(w), _ptr(echo), na, nr, _ptr(image), stream),
                    "wk_image")
         return image
+
+    def ceos_decode(self, raw, first_line: int, nlines: int, first_cell: int, ncells: int, layout=None,
+                    apply_agc: bool = True, stream=None):
+        """(echo [nlines][ncells] complex64, AGC dB [nlines] int16) from CEOS file bytes."""
+        lay = ceos_layout(layout)
+        echo = np.zeros((nlines, ncells), dtype=np.complex64)
+        agc = np.zeros(nlines, dtype=np.int16)
+        nbytes = raw.nbytes if isinstance(raw, np.ndarray) else raw.numel() * raw.element_size()
+        self.check(self.lib.sarbp_ceos_decode(self.h, _ptr(raw), nbytes, ctypes.byref(lay), first_line, nlines,
+                                              first_cell, ncells, int(apply_agc), _ptr(echo), _ptr(agc), stream),
+                   "ceos_decode")
+        return echo, agc
 
     def dft(self, data, inverse: bool = False, stream=None):
         """In-place batched DFT along the rows of data [rows][n] (complex64)."""
