@@ -4,7 +4,7 @@
 // load_DATA_block.m, extract_AGC.m), which reads 8-line blocks with fread,
 // cuts out the replica and decodes in the interpreter.  Here the caller's
 // file bytes (the blocks that hold the wanted lines) are decoded on the
-// device in one pass: one thread per range cell, 2-byte (I, Q) loads
+// device in one pass: four range cells per thread, 2-byte (I, Q) loads
 // (every record offset is even), coalesced along a line.
 //
 // Layout (read_CEOS_raw.m:13-16,67-80): a file header, then blocks of
@@ -21,6 +21,8 @@
 
 namespace sarbp {
 namespace {
+
+constexpr int kCellsPerThread = 4;
 
 __device__ __forceinline__ float ceos_value(unsigned d) {
     const int v = (int)(d & 15u);
@@ -41,9 +43,21 @@ __global__ void ceos_decode_kernel(const unsigned char *__restrict__ raw, CeosGe
     if (agc_db && blockIdx.x == 0 && threadIdx.x == 0) agc_db[line] = (short)((int)code - 24 * (code > 31u));
     const unsigned short *s = reinterpret_cast<const unsigned short *>(raw + smp_off);
     float2 *dst = echo + (size_t)line * g.ncells;
-    for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < g.ncells; c += gridDim.x * blockDim.x) {
-        const unsigned iq = __ldg(&s[c]);  // low byte I, high byte Q (file order)
-        dst[c] = make_float2(ceos_value(iq & 255u) * gain, ceos_value(iq >> 8) * gain);
+    // kCellsPerThread cells per thread, strided by the block (coalesced), loads issued together
+    const int step = blockDim.x;
+    for (int c0 = blockIdx.x * step * kCellsPerThread + threadIdx.x; c0 < g.ncells;
+         c0 += gridDim.x * step * kCellsPerThread) {
+        unsigned iq[kCellsPerThread];
+#pragma unroll
+        for (int u = 0; u < kCellsPerThread; ++u) {
+            const int c = c0 + u * step;
+            iq[u] = c < g.ncells ? __ldg(&s[c]) : 0u;  // low byte I, high byte Q (file order)
+        }
+#pragma unroll
+        for (int u = 0; u < kCellsPerThread; ++u) {
+            const int c = c0 + u * step;
+            if (c < g.ncells) dst[c] = make_float2(ceos_value(iq[u] & 255u) * gain, ceos_value(iq[u] >> 8) * gain);
+        }
     }
 }
 
@@ -53,7 +67,7 @@ cudaError_t launch_ceos_decode(const unsigned char *raw, const CeosGeom &g, cons
                                short *agc_db, cudaStream_t s) {
     if (g.nlines <= 0 || g.ncells <= 0) return cudaSuccess;
     const int threads = 256;
-    const int bx = (g.ncells + threads - 1) / threads;
+    const int bx = (g.ncells + threads * kCellsPerThread - 1) / (threads * kCellsPerThread);
     dim3 grid(bx < 8 ? bx : 8, g.nlines);
     ceos_decode_kernel<<<grid, threads, 0, s>>>(raw, g, gains, echo, agc_db);
     return cudaGetLastError();
