@@ -25,13 +25,15 @@ __device__ __forceinline__ float2 mulj(float2 a) {
 }
 
 // Shared-memory layout of the transform points: point x lives in slot sw(x),
-// an XOR swizzle inside each run of 16 float2 (128 bytes).  A half-warp of
-// 64-bit accesses then touches 16 distinct bank pairs for every access pattern
-// of the transform: contiguous runs (loads of every stage, stores of the later
-// stages) and the stride-8 / stride-64 stores of the first two radix-8 stages.
-// The swizzle only changes bits 0..3 and depends on bits 4..6, so
-// sw(x + c) = sw(x) + c for any multiple c of 128.
-__host__ __device__ constexpr int sw(int x) { return x ^ (((x >> 4) & 7) | ((x >> 3) & 8)); }
+// an XOR swizzle inside each run of 16 float2 (128 bytes):
+// x ^ (t ^ ((t & 4) << 1)) with t = (x >> 4) & 15.  A half-warp of 64-bit
+// accesses then touches 16 distinct bank pairs for every access pattern of the
+// transform: contiguous runs (loads of every stage, stores of the later
+// stages), the stride-8 / stride-64 stores of the first two radix-8 stages and
+// the stride-16 stores of the first radix-16 stage.  The swizzle only changes
+// bits 0..3 and depends on bits 4..7, so sw(x + c) = sw(x) + c for any
+// multiple c of 256.
+__host__ __device__ constexpr int sw(int x) { return x ^ (((x >> 4) & 15) ^ ((x >> 3) & 8)); }
 
 // table slot of entry i: one spare slot per 8 entries, so strided gathers
 // spread over the banks
@@ -102,6 +104,106 @@ struct Dft<8, INV> {
     }
 };
 
+// x W16^e for the chosen direction (forward e^{-j 2 pi e/16}, inverse
+// e^{+j 2 pi e/16}), e a compile-time constant.
+template <int E, bool INV>
+__device__ __forceinline__ float2 tw16(float2 x) {
+    constexpr float kC[16] = {1.f, 0.92387953251128675613f, 0.70710678118654752440f, 0.38268343236508977173f,
+                              0.f, -0.38268343236508977173f, -0.70710678118654752440f, -0.92387953251128675613f,
+                              -1.f, -0.92387953251128675613f, -0.70710678118654752440f, -0.38268343236508977173f,
+                              0.f, 0.38268343236508977173f, 0.70710678118654752440f, 0.92387953251128675613f};
+    constexpr int e = E & 15;
+    if constexpr (e == 0) {
+        return x;
+    } else if constexpr (e == 4) {
+        return mulj<INV>(x);
+    } else if constexpr (e == 8) {
+        return make_float2(-x.x, -x.y);
+    } else if constexpr (e == 12) {
+        return mulj<!INV>(x);
+    } else {
+        const float c = kC[e], sn = kC[(e + 12) & 15];  // sin(2 pi e / 16) = cos(2 pi (e - 4) / 16)
+        const float si = INV ? sn : -sn;
+        return make_float2(fmaf(x.x, c, -x.y * si), fmaf(x.x, si, x.y * c));
+    }
+}
+
+// Radix-16 DFT as 4 x 4: DFT-4 over v[n2 + 4 n1], twiddles W16^{n2 k1},
+// DFT-4 over n2; X[k1 + 4 k2].
+template <bool INV>
+struct Dft<16, INV> {
+    __device__ __forceinline__ static void run(float2 *v) {
+        float2 a[4][4];
+#pragma unroll
+        for (int n2 = 0; n2 < 4; ++n2) {
+            a[n2][0] = v[n2];
+            a[n2][1] = v[n2 + 4];
+            a[n2][2] = v[n2 + 8];
+            a[n2][3] = v[n2 + 12];
+            Dft<4, INV>::run(a[n2]);
+        }
+        a[1][1] = tw16<1, INV>(a[1][1]);
+        a[1][2] = tw16<2, INV>(a[1][2]);
+        a[1][3] = tw16<3, INV>(a[1][3]);
+        a[2][1] = tw16<2, INV>(a[2][1]);
+        a[2][2] = tw16<4, INV>(a[2][2]);
+        a[2][3] = tw16<6, INV>(a[2][3]);
+        a[3][1] = tw16<3, INV>(a[3][1]);
+        a[3][2] = tw16<6, INV>(a[3][2]);
+        a[3][3] = tw16<9, INV>(a[3][3]);
+#pragma unroll
+        for (int k1 = 0; k1 < 4; ++k1) {
+            float2 b[4] = {a[0][k1], a[1][k1], a[2][k1], a[3][k1]};
+            Dft<4, INV>::run(b);
+            v[k1] = b[0];
+            v[k1 + 4] = b[1];
+            v[k1 + 8] = b[2];
+            v[k1 + 12] = b[3];
+        }
+    }
+};
+
+// Radix-16 stage twiddles W^{m r}, r = 1..15, applied to v[1..15] as products
+// of the four table powers w, w^2, w^4, w^8 (at most four factors), so only
+// the powers and four partial products are live.
+struct Tw16 {
+    float2 b1, b2, b4, b8;
+};
+template <bool INV, bool HOISTED_LO>
+__device__ __forceinline__ Tw16 tw16_bases(const Etab &E, int m, const float2 *lo) {
+    Tw16 t;
+    t.b1 = HOISTED_LO ? cmul(E.whi[m >> 7], lo[0]) : E.w(m);
+    t.b2 = HOISTED_LO ? cmul(E.whi[(2 * m) >> 7], lo[1]) : E.w(2 * m);
+    t.b4 = HOISTED_LO ? cmul(E.whi[(4 * m) >> 7], lo[2]) : E.w(4 * m);
+    t.b8 = HOISTED_LO ? cmul(E.whi[(8 * m) >> 7], lo[3]) : E.w(8 * m);
+    if (!INV) {
+        t.b1.y = -t.b1.y;
+        t.b2.y = -t.b2.y;
+        t.b4.y = -t.b4.y;
+        t.b8.y = -t.b8.y;
+    }
+    return t;
+}
+__device__ __forceinline__ void tw16_apply(float2 *v, const Tw16 &t) {
+    const float2 w3 = cmul(t.b1, t.b2), w5 = cmul(t.b1, t.b4), w6 = cmul(t.b2, t.b4);
+    const float2 w7 = cmul(w3, t.b4);
+    v[1] = cmul(v[1], t.b1);
+    v[2] = cmul(v[2], t.b2);
+    v[3] = cmul(v[3], w3);
+    v[4] = cmul(v[4], t.b4);
+    v[5] = cmul(v[5], w5);
+    v[6] = cmul(v[6], w6);
+    v[7] = cmul(v[7], w7);
+    v[8] = cmul(v[8], t.b8);
+    v[9] = cmul(v[9], cmul(t.b1, t.b8));
+    v[10] = cmul(v[10], cmul(t.b2, t.b8));
+    v[11] = cmul(v[11], cmul(w3, t.b8));
+    v[12] = cmul(v[12], cmul(t.b4, t.b8));
+    v[13] = cmul(v[13], cmul(w5, t.b8));
+    v[14] = cmul(v[14], cmul(w6, t.b8));
+    v[15] = cmul(v[15], cmul(w7, t.b8));
+}
+
 // Twiddles W^{m r}, r = 1..R-1 (forward: conjugated) for a butterfly whose
 // base exponent is m: w, w^2, w^4 from the table, the others as products.
 // lo1/lo2/lo4 are the low-level table entries when the caller hoisted them.
@@ -126,7 +228,7 @@ __device__ __forceinline__ void twiddles(const Etab &E, int m, float2 lo1, float
 // One Stockham stage: butterfly j reads s[j + r*N/R], applies twiddles
 // W_N^{k r N/(Ns R)} (k = j mod Ns), runs a radix-R DFT and writes
 // s[(j - k) R + k + r Ns] (slots through sw()).  Ns is a compile-time
-// constant: offsets that are multiples of 128 points pass through sw()
+// constant: offsets that are multiples of 256 points pass through sw()
 // unchanged and become immediates.  When T is a multiple of Ns every
 // butterfly of a thread has the same k and the twiddles are computed once.
 template <int N, int R, int T, bool INV, int Ns>
@@ -139,7 +241,7 @@ __device__ __forceinline__ void stage(float2 *s, const Etab &E) {
     for (int b = 0; b < PER; ++b) {
         const int j = threadIdx.x + b * T;
         if (PER * T == NB || j < NB) {
-            if constexpr (NB % 128 == 0) {
+            if constexpr (NB % 256 == 0) {
                 const float2 *src = s + sw(j);
 #pragma unroll
                 for (int r = 0; r < R; ++r) v[b][r] = src[r * NB];
@@ -150,18 +252,29 @@ __device__ __forceinline__ void stage(float2 *s, const Etab &E) {
         }
     }
     __syncthreads();
-    float2 w[R];
+    float2 w[R <= 8 ? R : 1];
+    Tw16 t16;
     constexpr bool kSameK = Ns > 1 && T % Ns == 0;
     // k = j when Ns >= NB (last stage); the low table level is then fixed per thread
     constexpr bool kHoistLo = Ns > 1 && !kSameK && Ns >= NB && N >= kWlo && (C * T) % kWlo == 0;
     float2 lo1 = make_float2(1.f, 0.f), lo2 = lo1, lo4 = lo1;
+    float2 lo[4] = {lo1, lo1, lo1, lo1};
     if constexpr (kSameK) {
-        twiddles<R, INV, false>(E, C * (int)(threadIdx.x & (Ns - 1)), lo1, lo2, lo4, w);
+        if constexpr (R == 16)
+            t16 = tw16_bases<INV, false>(E, C * (int)(threadIdx.x & (Ns - 1)), lo);
+        else
+            twiddles<R, INV, false>(E, C * (int)(threadIdx.x & (Ns - 1)), lo1, lo2, lo4, w);
     } else if constexpr (kHoistLo) {
         const int m = C * (int)threadIdx.x;
         lo1 = E.wlo[m & (kWlo - 1)];
         if (R >= 4) lo2 = E.wlo[(2 * m) & (kWlo - 1)];
         if (R >= 8) lo4 = E.wlo[(4 * m) & (kWlo - 1)];
+        if constexpr (R == 16) {
+            lo[0] = lo1;
+            lo[1] = lo2;
+            lo[2] = lo4;
+            lo[3] = E.wlo[(8 * m) & (kWlo - 1)];
+        }
     }
 #pragma unroll
     for (int b = 0; b < PER; ++b) {
@@ -169,13 +282,18 @@ __device__ __forceinline__ void stage(float2 *s, const Etab &E) {
         if (PER * T == NB || j < NB) {
             const int k = j & (Ns - 1);
             if constexpr (Ns > 1) {
-                if constexpr (!kSameK) twiddles<R, INV, kHoistLo>(E, C * k, lo1, lo2, lo4, w);
+                if constexpr (R == 16) {
+                    if constexpr (!kSameK) t16 = tw16_bases<INV, kHoistLo>(E, C * k, lo);
+                    tw16_apply(v[b], t16);
+                } else {
+                    if constexpr (!kSameK) twiddles<R, INV, kHoistLo>(E, C * k, lo1, lo2, lo4, w);
 #pragma unroll
-                for (int r = 1; r < R; ++r) v[b][r] = cmul(v[b][r], w[r]);
+                    for (int r = 1; r < R; ++r) v[b][r] = cmul(v[b][r], w[r]);
+                }
             }
             Dft<R, INV>::run(v[b]);
             const int x0 = (j - k) * R + k;
-            if constexpr (Ns % 128 == 0) {
+            if constexpr (Ns % 256 == 0) {
                 float2 *dst = s + sw(x0);
 #pragma unroll
                 for (int r = 0; r < R; ++r) dst[r * Ns] = v[b][r];
@@ -188,11 +306,19 @@ __device__ __forceinline__ void stage(float2 *s, const Etab &E) {
     __syncthreads();
 }
 
-// radix-8 stages while 8 * Ns <= N, then one radix-4 or radix-2 stage
+#ifndef SARBP_FFT_RADIX16
+#define SARBP_FFT_RADIX16 1
+#endif
+// radix-16 stages while 16 * Ns <= N and the stage keeps all T threads busy
+// (N / 16 >= T), then radix-8 stages while 8 * Ns <= N, then one radix-4 or
+// radix-2 stage
 template <int N, int T, bool INV, int Ns>
 struct Stages {
     __device__ __forceinline__ static void run(float2 *s, const Etab &E) {
-        if constexpr (Ns * 8 <= N) {
+        if constexpr (SARBP_FFT_RADIX16 && Ns * 16 <= N && N / 16 >= T) {
+            stage<N, 16, T, INV, Ns>(s, E);
+            Stages<N, T, INV, Ns * 16>::run(s, E);
+        } else if constexpr (Ns * 8 <= N) {
             stage<N, 8, T, INV, Ns>(s, E);
             Stages<N, T, INV, Ns * 8>::run(s, E);
         } else if constexpr (Ns * 4 == N) {
