@@ -38,9 +38,12 @@ namespace {
 #ifndef SARBP_DFT_T8192
 #define SARBP_DFT_T8192 512
 #endif
+#ifndef SARBP_DFT_T4096
+#define SARBP_DFT_T4096 512
+#endif
 template <int N>
 constexpr int dft_threads() {
-    return N >= 16384 ? 1024 : (N >= 8192 ? SARBP_DFT_T8192 : (N >= 4096 ? 512 : (N >= 512 ? N / 8 : 64)));
+    return N >= 16384 ? 1024 : (N >= 8192 ? SARBP_DFT_T8192 : (N >= 4096 ? SARBP_DFT_T4096 : (N >= 512 ? N / 8 : 64)));
 }
 
 // Element i of the transformed row b: the row itself, or (fused padding and
