@@ -51,6 +51,19 @@ constexpr int kTileX = 32;  // pixels along x (columns); tile height is 8 * PIX 
 #ifndef SARBP_BP_MINBLOCKS
 #define SARBP_BP_MINBLOCKS 2
 #endif
+// Per-update phase: phi_T + dR k_hi (k_hi = float(4 pi fc / c)); the
+// compensated form adds dR k_lo.  The omitted term is at most
+// |dR| ulp(k)/2 (7e-5 rad at config 2's tile corners) and is of the size of the
+// FP32 rounding of dR itself and of the sin/cos argument, so the image does
+// not change measurably (-81.68 dB against FP64 either way) and the update is
+// one packed FMA shorter.
+#ifndef SARBP_BP_PHASE_COMPENSATED
+#define SARBP_BP_PHASE_COMPENSATED 0
+#endif
+#ifndef SARBP_BP_PULSE_UNROLL
+#define SARBP_BP_PULSE_UNROLL 2
+#endif
+constexpr int kPulseUnroll = SARBP_BP_PULSE_UNROLL;  // pulses per loop body (SPLIT)
 constexpr int kChunk = SARBP_BP_CHUNK;  // pulses per staged chunk (a multiple of 8)
 constexpr int kPerWarp = kChunk / kWarps;  // pulses each warp prepares
 static_assert(kChunk % kWarps == 0 && kPerWarp <= 32, "chunk must split evenly over the warps");
@@ -510,7 +523,7 @@ __global__ void __launch_bounds__(kThreads, SARBP_BP_MINBLOCKS)
             // interpolation and the complex accumulate per pixel
             f2 MP = pk2(kMagic + (float)cen, kMagic + (float)cen);
             const f2 WIN2 = pk2((float)win, (float)win);
-#pragma unroll 1
+#pragma unroll kPulseUnroll
             for (int pl = 0; pl < count; ++pl) {
                 const Prm &q = S.prm[stage * kChunk + pl];
                 f2 C1, C2, C3, C4, BT, PHT, AA, BB;
@@ -527,7 +540,11 @@ __global__ void __launch_bounds__(kThreads, SARBP_BP_MINBLOCKS)
                     poly = ffma2(n, poly, C1);
                     const f2 dR = fmul2(n, poly);
                     f2 b2 = ffma2(dR, BPM2, BT);  // bin positions relative to the window middle
+#if SARBP_BP_PHASE_COMPENSATED
                     const f2 ph2 = ffma2(dR, KL2, ffma2(dR, KH2, PHT));
+#else
+                    const f2 ph2 = ffma2(dR, KH2, PHT);
+#endif
                     float bb[2], ph[2];
                     upk2(b2, bb[0], bb[1]);
                     upk2(ph2, ph[0], ph[1]);
