@@ -178,17 +178,21 @@ __device__ __forceinline__ void lds2x2(const void *p, f2 &a, f2 &b) {
 
 struct Smem {
     float4 *staged;      // [2][kChunk][win]
-    unsigned char *raw;  // [kStages][kChunk][win] * 8 bytes
+    unsigned char *raw;  // [kStages][kChunk][win] stored elements (8 or 4 bytes)
     Prm *prm;            // [kStages][kChunk]
     uint64_t *bar;       // [kStages]
     float2 *red;         // [2][kWarps][kChunk] per-warp pulse sums (weighted projection)
 };
 
+// Bytes of one stored range bin in the raw ring: complex64 rows 8, complex16 4.
+__host__ __device__ constexpr int raw_esize(int storage) { return storage == SARBP_STORE_C64 ? 8 : 4; }
+
+template <int STORE>
 __device__ __forceinline__ Smem carve(unsigned char *base, int win) {
     Smem s;
     s.staged = reinterpret_cast<float4 *>(base);
     s.raw = base + (size_t)2 * kChunk * win * 16;
-    s.prm = reinterpret_cast<Prm *>(s.raw + (size_t)kStages * kChunk * win * 8);
+    s.prm = reinterpret_cast<Prm *>(s.raw + (size_t)kStages * kChunk * win * raw_esize(STORE));
     s.bar = reinterpret_cast<uint64_t *>(s.prm + kStages * kChunk);
     s.red = reinterpret_cast<float2 *>(s.bar + kStages);
     return s;
@@ -328,7 +332,7 @@ __device__ __forceinline__ void produce(const BpPlan &P, const Smem &S, int stag
         if (hi > lo) {
             bytes = (unsigned)((hi - lo) * esize);
             src = reinterpret_cast<const char *>(P.rc) + ((size_t)p * P.nbins + (size_t)lo) * esize;
-            dst = smem_addr(S.raw + ((size_t)stage * kChunk + (size_t)slot) * win * 8 + (size_t)(lo - ws) * esize);
+            dst = smem_addr(S.raw + ((size_t)stage * kChunk + (size_t)slot) * win * esize + (size_t)(lo - ws) * esize);
         }
     }
     unsigned total = bytes;
@@ -350,7 +354,7 @@ __device__ __forceinline__ void convert(const Smem &S, int stage, int sbuf, int 
         const int i = e - pl * win;
         const Prm &q = S.prm[stage * kChunk + pl];
         const int lo = q.lo, hi = q.hi;
-        const unsigned char *rw = S.raw + ((size_t)stage * kChunk + pl) * win * 8;
+        const unsigned char *rw = S.raw + ((size_t)stage * kChunk + pl) * win * raw_esize(STORE);
         float2 a = make_float2(0.f, 0.f), b = make_float2(0.f, 0.f);
         if (STORE == SARBP_STORE_C64) {
             const float2 *r = reinterpret_cast<const float2 *>(rw);
@@ -398,7 +402,7 @@ __global__ void __launch_bounds__(kThreads, SARBP_BP_MINBLOCKS)
     constexpr int kTileY = 8 * PIX;
     extern __shared__ __align__(128) unsigned char smem_raw[];
     const int win = P.win;
-    const Smem S = carve(smem_raw, win);
+    const Smem S = carve<STORE>(smem_raw, win);
     const unsigned win_magic = (unsigned)((0xFFFFFFFFull + (unsigned long long)win) / (unsigned long long)win);
 
     const int tile = blockIdx.x;
@@ -704,7 +708,7 @@ __global__ void reduce_segments_kernel(const float2 *__restrict__ partial, int s
 template <int MODE, int STORE, int NTERMS, bool CHECKED, int PIX, bool ADJ = false>
 cudaError_t launch_variant(const BpPlan &p, cudaStream_t s, int tiles, int tiles_y, int pps, float qq_max) {
     auto k = bp_kernel<MODE, STORE, NTERMS, CHECKED, PIX, ADJ>;
-    const size_t smem = bp_smem_bytes(MODE, p.win);
+    const size_t smem = bp_smem_bytes(STORE, p.win);
     cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     dim3 grid(tiles, p.segments);
@@ -817,8 +821,9 @@ void bp_tile_dims(int pix, int *tile_x, int *tile_y) {
 
 int bp_pulses_per_chunk(int) { return kChunk; }
 
-size_t bp_smem_bytes(int, int win) {
-    return (size_t)2 * kChunk * win * 16 + (size_t)kStages * kChunk * win * 8 + kStages * kChunk * sizeof(Prm) +
+size_t bp_smem_bytes(int storage, int win) {
+    return (size_t)2 * kChunk * win * 16 + (size_t)kStages * kChunk * win * raw_esize(storage) +
+           kStages * kChunk * sizeof(Prm) +
            kStages * sizeof(uint64_t) + 2 * kWarps * kChunk * sizeof(float2);
 }
 

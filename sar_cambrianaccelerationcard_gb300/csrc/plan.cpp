@@ -121,7 +121,7 @@ bool plan_bp(int sms, const sarbp_radar &r, const sarbp_rc_view &rc, const doubl
         }
         int win = (int)std::ceil(2 * half) + 8;
         win = (win + 3) & ~3;
-        if (bp_smem_bytes(mode, win) > (size_t)(227u << 10)) {
+        if (bp_smem_bytes(p.storage, win) > (size_t)(227u << 10)) {
             why = "tile spans too many range bins for shared memory";
             continue;
         }
@@ -143,7 +143,7 @@ bool plan_bp(int sms, const sarbp_radar &r, const sarbp_rc_view &rc, const doubl
     // pulse segments: fill at least ~2 waves of CTAs
     const int tiles = ((g.nx + tx - 1) / tx) * ((g.ny + ty - 1) / ty);
     const int chunk = bp_pulses_per_chunk(mode);
-    const size_t smem = bp_smem_bytes(mode, p.win);
+    const size_t smem = bp_smem_bytes(p.storage, p.win);
     const int cta_per_sm = std::max<int>(1, std::min<int>(3, (int)((227u << 10) / (smem + 1024))));
     const int want = 2 * sms * cta_per_sm;
     const int npl = pulses_per_launch > 0 ? pulses_per_launch : np;

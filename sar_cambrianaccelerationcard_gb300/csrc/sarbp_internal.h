@@ -100,7 +100,7 @@ void rc_tables_host(const sarbp_radar &r, const sarbp_rc_layout &lay, std::vecto
                     std::vector<float2> &etab);
 // Tile geometry the planner needs to size the staging window.
 void bp_tile_dims(int pix, int *tile_x, int *tile_y);
-size_t bp_smem_bytes(int mode, int win);
+size_t bp_smem_bytes(int storage, int win);
 int bp_pulses_per_chunk(int mode);
 
 // ---------------------------------------------------------------- echo synthesis
