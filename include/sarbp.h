@@ -182,6 +182,29 @@ sarbp_status sarbp_backproject(sarbp_ctx *ctx, const sarbp_radar *radar,
                                const sarbp_grid *grid, int32_t mode,
                                sarbp_complex64 *image, int32_t accumulate, void *stream);
 
+/* How sarbp_backproject would run a call with these arguments (no launch of
+ * the back-projection itself).  The planner sizes tiles and staging windows from
+ * geometry extremes over a 9 x 9 lattice of grid points and every pulse; a
+ * squinted or long aperture widens the windows, and windows past the two-CTA
+ * shared-memory limit halve the resident CTAs, which this reports so callers can
+ * choose sub-aperture sizes.  host_reduction != 0 reduces the extremes on the
+ * host (apc must then be host memory), else on the device as sarbp_backproject
+ * does; both give identical bits.  No reference counterpart (the reference
+ * launches one thread per pixel with no staging, BPA_CUDA_kernels.cu:91-98). */
+typedef struct sarbp_bp_plan_info {
+    int32_t tile_x, tile_y;  /* pixels per tile (one CTA) */
+    int32_t window;          /* staged range bins per (tile, pulse) */
+    int32_t series_terms;    /* differential-range series terms (SPLIT / FP16STORE) */
+    int32_t segments;        /* pulse segments the launch is split into */
+    int32_t ctas_per_sm;     /* resident CTAs per SM of the chosen kernel */
+    uint64_t smem_bytes;     /* dynamic shared memory per CTA */
+    double rmin, rmax;       /* nearest and farthest range, lattice x pulses (m) */
+    double cos_x, cos_y;     /* largest |cosine| between line of sight and grid axis x, y */
+} sarbp_bp_plan_info;
+sarbp_status sarbp_bp_plan(sarbp_ctx *ctx, const sarbp_radar *radar, const sarbp_rc_view *rc,
+                           const double *apc, const sarbp_grid *grid, int32_t mode,
+                           int32_t host_reduction, sarbp_bp_plan_info *out);
+
 /* Per-pulse corrections applied inside back-projection: the motion-compensation
  * / autofocus hook on the APC track.  Pulse p's slant range becomes
  * |apc_p - pix| + drange[p] (metres; shifts the range bin and the carrier

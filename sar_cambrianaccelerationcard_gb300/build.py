@@ -28,7 +28,7 @@ def nvcc() -> str:
 
 
 def _flags(extra=()):
-    return ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-O2",
+    return ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-O2,-ffp-contract=off",
                    "-I", os.path.join(ROOT, "include"), "-I", CSRC, *extra]
 
 

@@ -55,6 +55,11 @@ struct DftCache {
     int n = 0, m = 0;
     uint64_t used = 0;
     DevBuf etab, chirp, kf, ki;
+    void release() {
+        for (DevBuf *b : {&etab, &chirp, &kf, &ki}) b->release();
+        n = m = 0;
+        used = 0;
+    }
 };
 
 struct RcTables {
@@ -78,6 +83,23 @@ struct sarbp_ctx {
     DftCache dft[4];
     uint64_t dft_clock = 0;
     RcTables tables;
+    DevBuf ext;                              // planning extremes [5] (FP64 bits, nonfinite flag)
+    unsigned long long *ext_host = nullptr;  // pinned host copy of ext
+    cudaEvent_t ev_ext = nullptr;
+    // Buffers sized by the calls (released by sarbp_trim and sarbp_destroy).
+    std::vector<DevBuf *> scratch() {
+        std::vector<DevBuf *> v = {&echo, &spec, &rc,     &scale,   &apc,   &image, &partial, &targets, &pref,
+                                   &corr, &weight, &proj, &projout, &sharp, &wk0,   &wk1,     &wkrow,   &wktab};
+        for (DftCache &d : dft)
+            for (DevBuf *b : {&d.etab, &d.chirp, &d.kf, &d.ki}) v.push_back(b);
+        return v;
+    }
+    // Buffers held for the context's lifetime.
+    std::vector<DevBuf *> persistent() { return {&errword, &power, &ext, &tables.filt, &tables.etab}; }
+    void release_scratch() {
+        for (DevBuf *b : scratch()) b->release();
+        for (DftCache &d : dft) d.release();  // also forgets the cached sizes
+    }
     int64_t launches = 0;
     int checked = 0;  // SARBP_BOUNDS_CHECK=1 at creation: clamped, self-reporting BP kernels
     float rc_ms = 0.f, bp_ms = 0.f;
@@ -262,9 +284,32 @@ sarbp_status check_grid(sarbp_ctx *ctx, const sarbp_grid *g) {
     return SARBP_OK;
 }
 
+// Geometry extremes for planning from a device-resident APC: a reduction on the
+// stream (after the work already queued there, which may produce the APC), then
+// a wait for its 40-byte result only.  Fails on a non-finite APC coordinate.
+sarbp_status extremes_device(sarbp_ctx *ctx, const double *apc_dev, int np, const sarbp_grid *g, cudaStream_t s,
+                             sarbp::BpExtremes &e) {
+    SARBP_CUDA(ctx, sarbp::launch_bp_extremes(apc_dev, np, *g, ctx->ext.as<unsigned long long>(), s),
+               "planning extremes");
+    ctx->launches += np > 0 ? 2 : 1;
+    SARBP_CUDA(ctx, cudaMemcpyAsync(ctx->ext_host, ctx->ext.ptr, 5 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, s),
+               "read planning extremes");
+    SARBP_CUDA(ctx, cudaEventRecord(ctx->ev_ext, s), "read planning extremes");
+    SARBP_CUDA(ctx, cudaEventSynchronize(ctx->ev_ext), "read planning extremes");
+    double v[4];
+    std::memcpy(v, ctx->ext_host, sizeof v);
+    e.rmin = v[0];
+    e.rmax = v[1];
+    e.cx = v[2];
+    e.sy = v[3];
+    e.nonfinite = ctx->ext_host[4] ? 1u : 0u;
+    if (e.nonfinite) return fail(ctx, SARBP_ERR_INVALID_ARGUMENT, "apc must be finite");
+    return SARBP_OK;
+}
+
 // Back-projection of device-resident rc + apc into a device image.
 sarbp_status bp_device(sarbp_ctx *ctx, const sarbp_radar *r, const sarbp_rc_view &rc, const double *apc_dev,
-                       const double *apc_host, const sarbp_grid *g, int mode, float2 *image, int accumulate,
+                       const sarbp::BpExtremes &ex, const sarbp_grid *g, int mode, float2 *image, int accumulate,
                        cudaStream_t s, const double *dr_dev = nullptr, const double *dph_dev = nullptr) {
     const int np = rc.np;
     if (g->nx == 0 || g->ny == 0) return SARBP_OK;
@@ -277,7 +322,7 @@ sarbp_status bp_device(sarbp_ctx *ctx, const sarbp_radar *r, const sarbp_rc_view
     if (((uintptr_t)rc.data & 15) != 0) return fail(ctx, SARBP_ERR_INVALID_ARGUMENT, "rc data must be 16-byte aligned");
     BpPlan p;
     std::string why;
-    if (!sarbp::plan_bp(ctx->sms, *r, rc, apc_host, np, *g, mode, 0, p, why))
+    if (!sarbp::plan_bp(ctx->sms, *r, rc, ex, np, *g, mode, 0, p, why))
         return fail(ctx, SARBP_ERR_UNSUPPORTED, "%s", why.c_str());
     p.rc = rc.data;
     p.scale = rc.scale;
@@ -308,7 +353,7 @@ sarbp_status bp_device(sarbp_ctx *ctx, const sarbp_radar *r, const sarbp_rc_view
 // Weighted projection of device-resident rc + apc against a device weight
 // image into out[np] (device, complex128).
 sarbp_status project_device(sarbp_ctx *ctx, const sarbp_radar *r, const sarbp_rc_view &rc, const double *apc_dev,
-                            const double *apc_host, const sarbp_grid *g, int mode, const float2 *weight,
+                            const sarbp::BpExtremes &ex, const sarbp_grid *g, int mode, const float2 *weight,
                             double2 *out, cudaStream_t s, const double *dr_dev, const double *dph_dev) {
     const int np = rc.np;
     if (np == 0) return SARBP_OK;
@@ -316,7 +361,7 @@ sarbp_status project_device(sarbp_ctx *ctx, const sarbp_radar *r, const sarbp_rc
     if (((uintptr_t)rc.data & 15) != 0) return fail(ctx, SARBP_ERR_INVALID_ARGUMENT, "rc data must be 16-byte aligned");
     BpPlan p;
     std::string why;
-    if (!sarbp::plan_bp(ctx->sms, *r, rc, apc_host, np, *g, mode, 0, p, why))
+    if (!sarbp::plan_bp(ctx->sms, *r, rc, ex, np, *g, mode, 0, p, why))
         return fail(ctx, SARBP_ERR_UNSUPPORTED, "%s", why.c_str());
     p.rc = rc.data;
     p.scale = rc.scale;
@@ -341,8 +386,8 @@ sarbp_status project_device(sarbp_ctx *ctx, const sarbp_radar *r, const sarbp_rc
 // into the context's buffers) after validation.
 struct BpInputs {
     sarbp_rc_view v{};
-    const double *apc_dev = nullptr, *apc_host = nullptr;
-    std::vector<double> apc_h;
+    const double *apc_dev = nullptr;
+    sarbp::BpExtremes ex{};
     const double *dr_dev = nullptr, *dph_dev = nullptr;
     bool any_host = false;
 };
@@ -371,25 +416,18 @@ sarbp_status stage_bp_inputs(sarbp_ctx *ctx, const sarbp_radar *radar, const sar
     const size_t esize = rc->storage == SARBP_STORE_C64 ? 8 : 4;
     const int np = rc->np;
     in.v = *rc;
-    in.apc_host = apc;
     in.apc_dev = apc;
     if (np == 0) return SARBP_OK;
-    // APC: always needed on the host for planning, and on the device for the kernel
-    if (is_device_ptr(apc)) {
-        in.apc_h.resize((size_t)3 * np);
-        SARBP_CUDA(ctx, cudaMemcpyAsync(in.apc_h.data(), apc, sizeof(double) * 3 * np, cudaMemcpyDeviceToHost, s),
-                   "read apc");
-        SARBP_CUDA(ctx, cudaStreamSynchronize(s), "read apc");
-        in.apc_host = in.apc_h.data();
-    } else {
+    // APC on the device for the kernel; the planner's extremes are reduced there
+    if (!is_device_ptr(apc)) {
         SARBP_CUDA(ctx, ctx->apc.ensure(sizeof(double) * 3 * np), "alloc apc");
         SARBP_CUDA(ctx, cudaMemcpyAsync(ctx->apc.ptr, apc, sizeof(double) * 3 * np, cudaMemcpyHostToDevice, s),
                    "upload apc");
         in.apc_dev = ctx->apc.as<double>();
         in.any_host = true;
     }
-    for (size_t i = 0; i < (size_t)3 * np; ++i)
-        if (!std::isfinite(in.apc_host[i])) return fail(ctx, SARBP_ERR_INVALID_ARGUMENT, "apc must be finite");
+    st = extremes_device(ctx, in.apc_dev, np, grid, s, in.ex);
+    if (st != SARBP_OK) return st;
     if (!is_device_ptr(rc->data)) {
         SARBP_CUDA(ctx, ctx->rc.ensure(esize * (size_t)np * rc->nbins), "alloc rc");
         SARBP_CUDA(ctx, cudaMemcpyAsync(ctx->rc.ptr, rc->data, esize * (size_t)np * rc->nbins, cudaMemcpyHostToDevice, s),
@@ -522,6 +560,9 @@ sarbp_status sarbp_create(sarbp_ctx **out, int device) {
     ctx->checked = (chk && chk[0] == '1') ? 1 : 0;
     bool ok = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) == cudaSuccess;
     for (int i = 0; i < 4 && ok; ++i) ok = cudaEventCreate(&ctx->ev[i]) == cudaSuccess;
+    ok = ok && cudaEventCreateWithFlags(&ctx->ev_ext, cudaEventDisableTiming) == cudaSuccess;
+    ok = ok && cudaMallocHost(reinterpret_cast<void **>(&ctx->ext_host), 8 * sizeof(unsigned long long)) == cudaSuccess;
+    ok = ok && ctx->ext.ensure(8 * sizeof(unsigned long long)) == cudaSuccess;
     ok = ok && ctx->errword.ensure(sizeof(unsigned)) == cudaSuccess && ctx->power.ensure(sizeof(double)) == cudaSuccess;
     ok = ok && cudaMemset(ctx->errword.ptr, 0, sizeof(unsigned)) == cudaSuccess;
     if (!ok) {
@@ -537,11 +578,12 @@ sarbp_status sarbp_destroy(sarbp_ctx *ctx) {
     if (!ctx) return SARBP_ERR_INVALID_ARGUMENT;
     cudaSetDevice(ctx->device);
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
-    for (DevBuf *b : {&ctx->echo, &ctx->spec, &ctx->rc, &ctx->scale, &ctx->apc, &ctx->image, &ctx->partial,
-                      &ctx->errword, &ctx->power, &ctx->targets, &ctx->pref, &ctx->tables.filt, &ctx->tables.etab})
-        b->release();
+    ctx->release_scratch();
+    for (DevBuf *b : ctx->persistent()) b->release();
+    if (ctx->ext_host) cudaFreeHost(ctx->ext_host);
     for (cudaEvent_t &e : ctx->ev)
         if (e) cudaEventDestroy(e);
+    if (ctx->ev_ext) cudaEventDestroy(ctx->ev_ext);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
     return SARBP_OK;
@@ -562,18 +604,16 @@ sarbp_status sarbp_trim(sarbp_ctx *ctx) {
     if (!ctx) return SARBP_ERR_INVALID_ARGUMENT;
     cudaSetDevice(ctx->device);
     cudaStreamSynchronize(ctx->stream);
-    for (DevBuf *b : {&ctx->echo, &ctx->spec, &ctx->rc, &ctx->scale, &ctx->apc, &ctx->image, &ctx->partial,
-                      &ctx->targets, &ctx->pref})
-        b->release();
+    ctx->release_scratch();
     return SARBP_OK;
 }
 
 size_t sarbp_device_bytes(const sarbp_ctx *ctx) {
     if (!ctx) return 0;
     size_t t = 0;
-    for (const DevBuf *b : {&ctx->echo, &ctx->spec, &ctx->rc, &ctx->scale, &ctx->apc, &ctx->image, &ctx->partial,
-                            &ctx->errword, &ctx->power, &ctx->targets, &ctx->pref, &ctx->tables.filt, &ctx->tables.etab})
-        t += b->bytes;
+    sarbp_ctx *c = const_cast<sarbp_ctx *>(ctx);
+    for (const DevBuf *b : c->scratch()) t += b->bytes;
+    for (const DevBuf *b : c->persistent()) t += b->bytes;
     return t;
 }
 
@@ -657,11 +697,72 @@ sarbp_status sarbp_backproject_ex(sarbp_ctx *ctx, const sarbp_radar *radar, cons
         any_host = true;
     }
     ctx->timed_rc = false;
-    st = bp_device(ctx, radar, in.v, in.apc_dev, in.apc_host, grid, mode, d_img, accumulate, s, in.dr_dev, in.dph_dev);
+    st = bp_device(ctx, radar, in.v, in.apc_dev, in.ex, grid, mode, d_img, accumulate, s, in.dr_dev, in.dph_dev);
     if (st != SARBP_OK) return st;
     if (!dev_img)
         SARBP_CUDA(ctx, cudaMemcpyAsync(image, d_img, sizeof(float2) * npix, cudaMemcpyDeviceToHost, s), "download image");
     return finish(ctx, s, any_host);
+}
+
+sarbp_status sarbp_bp_plan(sarbp_ctx *ctx, const sarbp_radar *radar, const sarbp_rc_view *rc, const double *apc,
+                           const sarbp_grid *grid, int32_t mode, int32_t host_reduction, sarbp_bp_plan_info *out) {
+    if (!ctx) return SARBP_ERR_INVALID_ARGUMENT;
+    ctx->err.clear();
+    cudaSetDevice(ctx->device);
+    if (!out) return fail(ctx, SARBP_ERR_INVALID_ARGUMENT, "out is null");
+    std::memset(out, 0, sizeof *out);
+    sarbp_status st = check_radar(ctx, radar);
+    if (st != SARBP_OK) return st;
+    if (!rc) return fail(ctx, SARBP_ERR_INVALID_ARGUMENT, "rc view is null");
+    st = check_grid(ctx, grid);
+    if (st != SARBP_OK) return st;
+    if (grid->nx < 1 || grid->ny < 1) return fail(ctx, SARBP_ERR_INVALID_ARGUMENT, "grid must have pixels");
+    if (mode < SARBP_MODE_FP64 || mode > SARBP_MODE_FP16STORE)
+        return fail(ctx, SARBP_ERR_INVALID_ARGUMENT, "unknown mode %d", mode);
+    if (rc->storage != SARBP_STORE_C64 && rc->storage != SARBP_STORE_C32H)
+        return fail(ctx, SARBP_ERR_INVALID_ARGUMENT, "unknown storage %d", rc->storage);
+    if (mode == SARBP_MODE_FP16STORE && rc->storage != SARBP_STORE_C32H)
+        return fail(ctx, SARBP_ERR_INVALID_ARGUMENT, "FP16STORE mode needs SARBP_STORE_C32H data");
+    if (rc->np < 1 || rc->nbins < 2 || rc->nbins % 4 != 0)
+        return fail(ctx, SARBP_ERR_INVALID_ARGUMENT, "rc needs np >= 1 and nbins >= 2, a multiple of 4");
+    if (!(rc->bin_rate > 0) || !std::isfinite(rc->t0_bins))
+        return fail(ctx, SARBP_ERR_INVALID_ARGUMENT, "rc bin_rate must be > 0 and t0_bins finite");
+    if (!apc) return fail(ctx, SARBP_ERR_INVALID_ARGUMENT, "apc is null");
+    const int np = rc->np;
+    sarbp::BpExtremes ex{};
+    if (host_reduction) {
+        if (is_device_ptr(apc)) return fail(ctx, SARBP_ERR_INVALID_ARGUMENT, "host_reduction needs a host apc");
+        sarbp::bp_extremes_host(apc, np, *grid, ex);
+        if (ex.nonfinite) return fail(ctx, SARBP_ERR_INVALID_ARGUMENT, "apc must be finite");
+    } else {
+        const double *apc_dev = apc;
+        if (!is_device_ptr(apc)) {
+            SARBP_CUDA(ctx, ctx->apc.ensure(sizeof(double) * 3 * np), "alloc apc");
+            SARBP_CUDA(ctx, cudaMemcpyAsync(ctx->apc.ptr, apc, sizeof(double) * 3 * np, cudaMemcpyHostToDevice, ctx->stream),
+                       "upload apc");
+            apc_dev = ctx->apc.as<double>();
+        }
+        st = extremes_device(ctx, apc_dev, np, grid, ctx->stream, ex);
+        if (st != SARBP_OK) return st;
+    }
+    sarbp::BpPlan p;
+    std::string why;
+    if (!sarbp::plan_bp(ctx->sms, *radar, *rc, ex, np, *grid, mode, 0, p, why))
+        return fail(ctx, SARBP_ERR_UNSUPPORTED, "%s", why.c_str());
+    p.checked = ctx->checked;
+    int occ = 0;
+    SARBP_CUDA(ctx, sarbp::bp_occupancy(p, &occ), "occupancy");
+    sarbp::bp_tile_dims(p.pix, &out->tile_x, &out->tile_y);
+    out->window = p.win;
+    out->series_terms = p.nterms;
+    out->segments = p.segments;
+    out->ctas_per_sm = occ;
+    out->smem_bytes = sarbp::bp_smem_bytes(p.storage, p.win);
+    out->rmin = ex.rmin;
+    out->rmax = ex.rmax;
+    out->cos_x = ex.cx;
+    out->cos_y = ex.sy;
+    return SARBP_OK;
 }
 
 sarbp_status sarbp_backproject(sarbp_ctx *ctx, const sarbp_radar *radar, const sarbp_rc_view *rc,
@@ -707,7 +808,7 @@ sarbp_status sarbp_project_weighted(sarbp_ctx *ctx, const sarbp_radar *radar, co
             d_w = ctx->weight.as<float2>();
             any_host = true;
         }
-        st = project_device(ctx, radar, in.v, in.apc_dev, in.apc_host, grid, mode, d_w, d_out, s, in.dr_dev,
+        st = project_device(ctx, radar, in.v, in.apc_dev, in.ex, grid, mode, d_w, d_out, s, in.dr_dev,
                             in.dph_dev);
         if (st != SARBP_OK) return st;
     }
@@ -758,14 +859,14 @@ sarbp_status sarbp_autofocus(sarbp_ctx *ctx, const sarbp_radar *radar, const sar
     float2 *d_w = ctx->weight.as<float2>();
     for (int it = 0; it <= iterations; ++it) {
         SARBP_CUDA(ctx, cudaMemcpyAsync(d_ph, ph.data(), sizeof(double) * np, cudaMemcpyHostToDevice, s), "upload phases");
-        st = bp_device(ctx, radar, in.v, in.apc_dev, in.apc_host, grid, mode, d_img, 0, s, in.dr_dev, d_ph);
+        st = bp_device(ctx, radar, in.v, in.apc_dev, in.ex, grid, mode, d_img, 0, s, in.dr_dev, d_ph);
         if (st != SARBP_OK) return st;
         const bool last = it == iterations;
         SARBP_CUDA(ctx, sarbp::launch_sharpness_weight(d_img, npix, last ? nullptr : d_w, ctx->sharp.as<double>(), s),
                    "sharpness");
         ctx->launches += 1;
         if (!last) {
-            st = project_device(ctx, radar, in.v, in.apc_dev, in.apc_host, grid, mode, d_w, ctx->projout.as<double2>(),
+            st = project_device(ctx, radar, in.v, in.apc_dev, in.ex, grid, mode, d_w, ctx->projout.as<double2>(),
                                 s, in.dr_dev, d_ph);
             if (st != SARBP_OK) return st;
             SARBP_CUDA(ctx, cudaMemcpyAsync(cp.data(), ctx->projout.ptr, sizeof(double2) * np, cudaMemcpyDeviceToHost, s),
@@ -1069,6 +1170,21 @@ sarbp_status sarbp_image(sarbp_ctx *ctx, const sarbp_radar *radar, const sarbp_c
     const int storage = mode == SARBP_MODE_FP16STORE ? SARBP_STORE_C32H : SARBP_STORE_C64;
     const size_t esize = storage == SARBP_STORE_C64 ? 8 : 4;
     bool any_host = false;
+    // APC first: the planner's extremes are reduced on the device and waited
+    // for before the echo upload and range compression are queued
+    const double *apc_dev = apc;
+    sarbp::BpExtremes ex{};
+    if (np > 0) {
+        if (!is_device_ptr(apc)) {
+            SARBP_CUDA(ctx, ctx->apc.ensure(sizeof(double) * 3 * np), "alloc apc");
+            SARBP_CUDA(ctx, cudaMemcpyAsync(ctx->apc.ptr, apc, sizeof(double) * 3 * np, cudaMemcpyHostToDevice, s),
+                       "upload apc");
+            apc_dev = ctx->apc.as<double>();
+            any_host = true;
+        }
+        st = extremes_device(ctx, apc_dev, np, grid, s, ex);
+        if (st != SARBP_OK) return st;
+    }
     const float2 *d_echo = reinterpret_cast<const float2 *>(echo);
     if (np > 0 && !is_device_ptr(echo)) {
         SARBP_CUDA(ctx, ctx->echo.ensure(sizeof(float2) * (size_t)np * ns), "alloc echo");
@@ -1076,23 +1192,6 @@ sarbp_status sarbp_image(sarbp_ctx *ctx, const sarbp_radar *radar, const sarbp_c
                    "upload echo");
         d_echo = ctx->echo.as<float2>();
         any_host = true;
-    }
-    std::vector<double> apc_h;
-    const double *apc_host = apc, *apc_dev = apc;
-    if (np > 0) {
-        if (is_device_ptr(apc)) {
-            apc_h.resize((size_t)3 * np);
-            SARBP_CUDA(ctx, cudaMemcpy(apc_h.data(), apc, sizeof(double) * 3 * np, cudaMemcpyDeviceToHost), "read apc");
-            apc_host = apc_h.data();
-        } else {
-            SARBP_CUDA(ctx, ctx->apc.ensure(sizeof(double) * 3 * np), "alloc apc");
-            SARBP_CUDA(ctx, cudaMemcpyAsync(ctx->apc.ptr, apc, sizeof(double) * 3 * np, cudaMemcpyHostToDevice, s),
-                       "upload apc");
-            apc_dev = ctx->apc.as<double>();
-            any_host = true;
-        }
-        for (size_t i = 0; i < (size_t)3 * np; ++i)
-            if (!std::isfinite(apc_host[i])) return fail(ctx, SARBP_ERR_INVALID_ARGUMENT, "apc must be finite");
     }
     float2 *d_img = reinterpret_cast<float2 *>(image);
     const bool dev_img = is_device_ptr(image);
@@ -1118,7 +1217,7 @@ sarbp_status sarbp_image(sarbp_ctx *ctx, const sarbp_radar *radar, const sarbp_c
         v.data = ctx->rc.ptr;
         v.scale = storage == SARBP_STORE_C32H ? ctx->scale.as<float>() : nullptr;
     }
-    st = bp_device(ctx, radar, v, apc_dev, apc_host, grid, mode, d_img, 0, s);
+    st = bp_device(ctx, radar, v, apc_dev, ex, grid, mode, d_img, 0, s);
     if (st != SARBP_OK) return st;
     if (!dev_img)
         SARBP_CUDA(ctx, cudaMemcpyAsync(image, d_img, sizeof(float2) * npix, cudaMemcpyDeviceToHost, s), "download image");

@@ -705,12 +705,17 @@ __global__ void reduce_segments_kernel(const float2 *__restrict__ partial, int s
     }
 }
 
+// When set (bp_occupancy), the dispatch below reports the chosen variant's
+// resident CTAs per SM there instead of launching it.
+thread_local int *t_occupancy = nullptr;
+
 template <int MODE, int STORE, int NTERMS, bool CHECKED, int PIX, bool ADJ = false>
 cudaError_t launch_variant(const BpPlan &p, cudaStream_t s, int tiles, int tiles_y, int pps, float qq_max) {
     auto k = bp_kernel<MODE, STORE, NTERMS, CHECKED, PIX, ADJ>;
     const size_t smem = bp_smem_bytes(STORE, p.win);
     cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
+    if (t_occupancy) return cudaOccupancyMaxActiveBlocksPerMultiprocessor(t_occupancy, k, kThreads, smem);
     dim3 grid(tiles, p.segments);
     k<<<grid, kThreads, smem, s>>>(p, tiles_y, pps, qq_max);
     return cudaGetLastError();
@@ -814,6 +819,20 @@ cudaError_t launch_project(const BpPlan &p, double2 *out, cudaStream_t s, int *l
     return e;
 }
 
+cudaError_t bp_occupancy(const BpPlan &p, int *ctas_per_sm) {
+    *ctas_per_sm = 0;
+    if (p.pix != 8 && p.pix != 4 && p.pix != 2) return cudaErrorInvalidValue;
+    int tiles, tiles_y, pps;
+    float qq_max;
+    launch_geometry(p, &tiles, &tiles_y, &pps, &qq_max);
+    t_occupancy = ctas_per_sm;
+    cudaError_t e = p.pix == 8 ? launch_pix<8>(p, nullptr, tiles, tiles_y, pps, qq_max)
+                  : p.pix == 4 ? launch_pix<4>(p, nullptr, tiles, tiles_y, pps, qq_max)
+                               : launch_pix<2>(p, nullptr, tiles, tiles_y, pps, qq_max);
+    t_occupancy = nullptr;
+    return e;
+}
+
 void bp_tile_dims(int pix, int *tile_x, int *tile_y) {
     *tile_x = kTileX;
     *tile_y = 8 * pix;
@@ -825,6 +844,67 @@ size_t bp_smem_bytes(int storage, int win) {
     return (size_t)2 * kChunk * win * 16 + (size_t)kStages * kChunk * win * raw_esize(storage) +
            kStages * kChunk * sizeof(Prm) +
            kStages * sizeof(uint64_t) + 2 * kWarps * kChunk * sizeof(float2);
+}
+
+// ---------------------------------------------------------------- planning extremes
+// One thread per (pulse, lattice point); warp min / max, then one atomic per
+// warp on the FP64 bit patterns (all four quantities are >= 0, where the
+// unsigned order of the bits is the numeric order).
+__global__ void bp_extremes_init_kernel(unsigned long long *out) {
+    if (threadIdx.x == 0) {
+        out[0] = (unsigned long long)__double_as_longlong(1e300);
+        out[1] = out[2] = out[3] = 0ull;
+        out[4] = 0ull;
+    }
+}
+
+__global__ void __launch_bounds__(256) bp_extremes_kernel(const double *apc, int np, const sarbp_grid g, double lux,
+                                                          double luy, unsigned long long *out) {
+    constexpr int kPts = kLattice * kLattice;
+    double rmin = 1e300, rmax = 0.0, cx = 0.0, sy = 0.0;
+    bool bad = false;
+    const long long total = (long long)np * kPts;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total; i += (long long)gridDim.x * blockDim.x) {
+        const int p = (int)(i / kPts), k = (int)(i - (long long)p * kPts);
+        const double a[3] = {apc[3 * (size_t)p], apc[3 * (size_t)p + 1], apc[3 * (size_t)p + 2]};
+        if (!isfinite(a[0]) || !isfinite(a[1]) || !isfinite(a[2])) {
+            bad = true;
+            continue;
+        }
+        double R, c, sv;
+        ext_point(g, lux, luy, a, k / kLattice, k % kLattice, &R, &c, &sv);
+        rmin = fmin(rmin, R);
+        rmax = fmax(rmax, R);
+        cx = fmax(cx, c);
+        sy = fmax(sy, sv);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        rmin = fmin(rmin, __shfl_xor_sync(0xffffffffu, rmin, o));
+        rmax = fmax(rmax, __shfl_xor_sync(0xffffffffu, rmax, o));
+        cx = fmax(cx, __shfl_xor_sync(0xffffffffu, cx, o));
+        sy = fmax(sy, __shfl_xor_sync(0xffffffffu, sy, o));
+    }
+    const bool any_bad = __any_sync(0xffffffffu, bad);
+    if ((threadIdx.x & 31) == 0) {
+        atomicMin(&out[0], (unsigned long long)__double_as_longlong(rmin));
+        atomicMax(&out[1], (unsigned long long)__double_as_longlong(rmax));
+        atomicMax(&out[2], (unsigned long long)__double_as_longlong(cx));
+        atomicMax(&out[3], (unsigned long long)__double_as_longlong(sy));
+        if (any_bad) atomicOr(&out[4], 1ull);
+    }
+}
+
+cudaError_t launch_bp_extremes(const double *apc, int np, const sarbp_grid &g, unsigned long long *out,
+                               cudaStream_t s) {
+    bp_extremes_init_kernel<<<1, 32, 0, s>>>(out);
+    if (np <= 0) return cudaGetLastError();
+    double lux, luy;
+    ext_axes(g, &lux, &luy);
+    const long long total = (long long)np * kLattice * kLattice;
+    const int blocks = (int)std::min<long long>((total + 255) / 256, 2048);
+    bp_extremes_kernel<<<blocks, 256, 0, s>>>(apc, np, g, lux, luy, out);
+    return cudaGetLastError();
 }
 
 cudaError_t launch_bp(const BpPlan &p, cudaStream_t s, int *launches) {

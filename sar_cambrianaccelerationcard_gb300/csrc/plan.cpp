@@ -40,7 +40,36 @@ void fft_pow2_host(std::vector<std::complex<double>> &h) {
 }
 }  // namespace
 
-bool plan_bp(int sms, const sarbp_radar &r, const sarbp_rc_view &rc, const double *apc_host, int np,
+void ext_axes(const sarbp_grid &g, double *lux, double *luy) {
+    *lux = std::sqrt(ext_dot(g.ux, g.ux));
+    *luy = std::sqrt(ext_dot(g.uy, g.uy));
+}
+
+void bp_extremes_host(const double *apc, int np, const sarbp_grid &g, BpExtremes &e) {
+    double lux, luy;
+    ext_axes(g, &lux, &luy);
+    e.rmin = 1e300;
+    e.rmax = e.cx = e.sy = 0.0;
+    e.nonfinite = 0;
+    for (int i = 0; i < np; ++i) {
+        const double *a = apc + 3 * (size_t)i;
+        if (!std::isfinite(a[0]) || !std::isfinite(a[1]) || !std::isfinite(a[2])) {
+            e.nonfinite = 1;
+            continue;
+        }
+        for (int u = 0; u < kLattice; ++u)
+            for (int v = 0; v < kLattice; ++v) {
+                double R, cx, sy;
+                ext_point(g, lux, luy, a, u, v, &R, &cx, &sy);
+                e.rmin = std::min(e.rmin, R);
+                e.rmax = std::max(e.rmax, R);
+                e.cx = std::max(e.cx, cx);
+                e.sy = std::max(e.sy, sy);
+            }
+    }
+}
+
+bool plan_bp(int sms, const sarbp_radar &r, const sarbp_rc_view &rc, const BpExtremes &ex, int np,
              const sarbp_grid &g, int mode, int pulses_per_launch, BpPlan &p, std::string &why) {
     std::memset(&p, 0, sizeof p);
     p.storage = rc.storage;
@@ -68,26 +97,9 @@ bool plan_bp(int sms, const sarbp_radar &r, const sarbp_rc_view &rc, const doubl
     split2(rc.t0_bins * rc.bin_rate, &p.tb_h, &p.tb_l);
     split2(2.0 * r.fc / r.c, &p.kc_h, &p.kc_l);
 
-    // Line-of-sight extremes over the grid (9x9 lattice of grid points, all pulses).
     const double lux = std::sqrt(p.g.g11), luy = std::sqrt(p.g.g22);
-    double cx = 0, sy = 0, rmin = 1e300, rmax = 0;
-    for (int i = 0; i < np; ++i) {
-        const double *a = apc_host + 3 * (size_t)i;
-        for (int u = 0; u <= 8; ++u) {
-            for (int v = 0; v <= 8; ++v) {
-                const double fx = (g.nx - 1) * u / 8.0, fy = (g.ny - 1) * v / 8.0;
-                double w[3];
-                for (int k = 0; k < 3; ++k) w[k] = g.origin[k] + fx * g.ux[k] + fy * g.uy[k] - a[k];
-                const double R = std::sqrt(dot3(w, w));
-                rmin = std::min(rmin, R);
-                rmax = std::max(rmax, R);
-                if (R > 0) {
-                    if (lux > 0) cx = std::max(cx, std::fabs(dot3(g.ux, w)) / (R * lux));
-                    if (luy > 0) sy = std::max(sy, std::fabs(dot3(g.uy, w)) / (R * luy));
-                }
-            }
-        }
-    }
+    double cx = ex.cx, sy = ex.sy;
+    const double rmin = ex.rmin, rmax = ex.rmax;
     cx = std::min(1.0, cx * 1.05 + 0.01);
     sy = std::min(1.0, sy * 1.05 + 0.01);
     const double bpm = 2.0 / r.c * rc.bin_rate;

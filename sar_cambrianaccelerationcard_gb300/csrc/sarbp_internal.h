@@ -5,6 +5,8 @@
 #include <cuda_fp16.h>
 #include <stdint.h>
 
+#include <cmath>
+
 #include <string>
 #include <vector>
 
@@ -82,16 +84,82 @@ struct BpPlan {
 };
 
 cudaError_t launch_bp(const BpPlan &p, cudaStream_t s, int *launches);
+// Resident CTAs per SM of the kernel variant launch_bp would run for `p`.
+cudaError_t bp_occupancy(const BpPlan &p, int *ctas_per_sm);
 // Weighted projection (adjoint of back-projection, SPLIT / FP16STORE arithmetic):
 // out[p] = sum over pixels of conj(weight) * pulse p's term, via p.proj
 // ([bp_tiles(p)][np] float2 scratch) and a fixed-order reduction in FP64.
 cudaError_t launch_project(const BpPlan &p, double2 *out, cudaStream_t s, int *launches);
 size_t bp_tiles(const BpPlan &p);
+// Geometry extremes the planner sizes tiles and windows from, over a 9 x 9
+// lattice of grid points (corners and edges included) and every pulse: the
+// nearest and farthest range and the largest |cosine| between the line of sight
+// and each grid axis.  The host (plan.cpp) and device (bp.cu) reductions give
+// identical bits: FP64 in one fixed operation order without fused multiply-adds,
+// correctly rounded square root and division, order-free min / max.
+struct BpExtremes {
+    double rmin, rmax, cx, sy;
+    unsigned nonfinite;  // 1 if an APC coordinate was not finite
+};
+constexpr int kLattice = 9;  // lattice points per grid axis
+
+__host__ __device__ inline double ext_mul(double a, double b) {
+#ifdef __CUDA_ARCH__
+    return __dmul_rn(a, b);
+#else
+    return a * b;
+#endif
+}
+__host__ __device__ inline double ext_add(double a, double b) {
+#ifdef __CUDA_ARCH__
+    return __dadd_rn(a, b);
+#else
+    return a + b;
+#endif
+}
+__host__ __device__ inline double ext_dot(const double *a, const double *b) {
+    return ext_add(ext_add(ext_mul(a[0], b[0]), ext_mul(a[1], b[1])), ext_mul(a[2], b[2]));
+}
+// Lattice point (u, v) against antenna position a: range R and the two direction
+// cosines |ux.w| / (R lux), |uy.w| / (R luy) (zero when R or the axis length is 0).
+__host__ __device__ inline void ext_point(const sarbp_grid &g, double lux, double luy, const double *a, int u, int v,
+                                          double *R, double *cx, double *sy) {
+    const double fx = (double)((g.nx - 1) * u) / (double)(kLattice - 1);
+    const double fy = (double)((g.ny - 1) * v) / (double)(kLattice - 1);
+    double w[3];
+    for (int k = 0; k < 3; ++k) w[k] = ext_add(ext_add(ext_add(g.origin[k], ext_mul(fx, g.ux[k])), ext_mul(fy, g.uy[k])), -a[k]);
+#ifdef __CUDA_ARCH__
+    const double r = __dsqrt_rn(ext_dot(w, w));
+#else
+    const double r = std::sqrt(ext_dot(w, w));
+#endif
+    *R = r;
+    *cx = *sy = 0.0;
+    if (r > 0) {
+#ifdef __CUDA_ARCH__
+        if (lux > 0) *cx = __ddiv_rn(fabs(ext_dot(g.ux, w)), ext_mul(r, lux));
+        if (luy > 0) *sy = __ddiv_rn(fabs(ext_dot(g.uy, w)), ext_mul(r, luy));
+#else
+        if (lux > 0) *cx = std::fabs(ext_dot(g.ux, w)) / ext_mul(r, lux);
+        if (luy > 0) *sy = std::fabs(ext_dot(g.uy, w)) / ext_mul(r, luy);
+#endif
+    }
+}
+// Axis lengths |ux|, |uy| as both reductions use them.
+void ext_axes(const sarbp_grid &g, double *lux, double *luy);
+// Host reduction over apc [np][3] (host memory).
+void bp_extremes_host(const double *apc, int np, const sarbp_grid &g, BpExtremes &e);
+// Device reduction over apc [np][3] (device memory) into out[0..3] (the four
+// extremes as FP64 bit patterns) and out[4] (nonfinite flag): launches the
+// initialisation and the reduction on `s`.
+cudaError_t launch_bp_extremes(const double *apc, int np, const sarbp_grid &g, unsigned long long *out,
+                               cudaStream_t s);
+
 // Host planning (plan.cpp): fills every BpPlan field that does not depend on
 // buffers (geometry, constants, tile height, window, series terms, segments
-// for launches of `pulses_per_launch` pulses; 0 = all np).  On failure returns
-// false with the reason in `why`.
-bool plan_bp(int sms, const sarbp_radar &r, const sarbp_rc_view &rc, const double *apc_host, int np,
+// for launches of `pulses_per_launch` pulses; 0 = all np) from the geometry
+// extremes.  On failure returns false with the reason in `why`.
+bool plan_bp(int sms, const sarbp_radar &r, const sarbp_rc_view &rc, const BpExtremes &ex, int np,
              const sarbp_grid &g, int mode, int pulses_per_launch, BpPlan &p, std::string &why);
 // Two-level table of E^m = e^{+j 2 pi m / (L N)} ([rc_etab_size(L, N)] entries, plan.cpp).
 void fft_etab_host(int L, int N, std::vector<float2> &etab);

@@ -522,7 +522,9 @@ sarbp_status sarbp_server_submit(sarbp_server *S, const sarbp_job *job, uint64_t
     v.t0_bins = j->lay.t0_bins;
     v.bin_rate = j->lay.bin_rate;
     std::string why;
-    if (!sarbp::plan_bp(S->sms, d.radar, v, d.apc, d.np, d.grid, d.mode, S->cfg.pulses_per_step, j->plan, why)) {
+    sarbp::BpExtremes ex;
+    sarbp::bp_extremes_host(d.apc, d.np, d.grid, ex);  // same bits as the one-shot calls' device reduction
+    if (!sarbp::plan_bp(S->sms, d.radar, v, ex, d.np, d.grid, d.mode, S->cfg.pulses_per_step, j->plan, why)) {
         delete j;
         return SARBP_ERR_UNSUPPORTED;
     }

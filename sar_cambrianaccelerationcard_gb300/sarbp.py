@@ -103,6 +103,13 @@ class RcView(ctypes.Structure):
                 ("t0_bins", ctypes.c_double), ("bin_rate", ctypes.c_double)]
 
 
+class BpPlanInfo(ctypes.Structure):
+    _fields_ = [("tile_x", ctypes.c_int32), ("tile_y", ctypes.c_int32), ("window", ctypes.c_int32),
+                ("series_terms", ctypes.c_int32), ("segments", ctypes.c_int32), ("ctas_per_sm", ctypes.c_int32),
+                ("smem_bytes", ctypes.c_uint64), ("rmin", ctypes.c_double), ("rmax", ctypes.c_double),
+                ("cos_x", ctypes.c_double), ("cos_y", ctypes.c_double)]
+
+
 class Target(ctypes.Structure):
     _fields_ = [("x", ctypes.c_double), ("y", ctypes.c_double), ("z", ctypes.c_double), ("amp", ctypes.c_double)]
 
@@ -173,6 +180,8 @@ SIGNATURES = {
     "sarbp_backproject_ex": ([ctypes.c_void_p, ctypes.POINTER(Radar), ctypes.POINTER(RcView), ctypes.c_void_p,
                               ctypes.POINTER(Grid), ctypes.c_int32, ctypes.POINTER(PulseCorr), ctypes.c_void_p,
                               ctypes.c_int32, ctypes.c_void_p], ctypes.c_int),
+    "sarbp_bp_plan": ([ctypes.c_void_p, ctypes.POINTER(Radar), ctypes.POINTER(RcView), ctypes.c_void_p,
+                       ctypes.POINTER(Grid), ctypes.c_int32, ctypes.c_int32, ctypes.POINTER(BpPlanInfo)], ctypes.c_int),
     "sarbp_project_weighted": ([ctypes.c_void_p, ctypes.POINTER(Radar), ctypes.POINTER(RcView), ctypes.c_void_p,
                                 ctypes.POINTER(Grid), ctypes.c_int32, ctypes.POINTER(PulseCorr), ctypes.c_void_p,
                                 ctypes.c_void_p, ctypes.c_void_p], ctypes.c_int),
@@ -371,6 +380,15 @@ class Context:
                                                      ctypes.byref(grid), mode, ctypes.byref(corr), _ptr(image),
                                                      int(accumulate), stream), "backproject_ex")
         return image
+
+    def bp_plan(self, radar: Radar, rc_view: RcView, apc, grid: Grid, mode: int, host_reduction: bool = False):
+        """The tile, staging window, series terms, segments, shared memory and
+        resident CTAs per SM sarbp_backproject would use (BpPlanInfo)."""
+        info = BpPlanInfo()
+        self.check(self.lib.sarbp_bp_plan(self.h, ctypes.byref(radar), ctypes.byref(rc_view), _ptr(apc),
+                                          ctypes.byref(grid), mode, int(host_reduction), ctypes.byref(info)),
+                   "bp_plan")
+        return info
 
     def project_weighted(self, radar: Radar, rc, apc, grid: Grid, mode: int, t0_bins: float, bin_rate: float,
                          weight, scale=None, drange=None, dphase=None, out=None, stream=None):

@@ -1,0 +1,111 @@
+"""Back-projection planning (sarbp_bp_plan): the geometry extremes the planner
+sizes tiles and staging windows from are reduced on the device for the
+one-shot calls and on the host for the serving loop; both must give the same
+bits, so that a job plans (and rounds) the same either way.  Also: the
+config-5 sub-aperture x tile launches keep two CTAs per SM with FP16 rows, and
+a non-finite APC is rejected by both reductions."""
+import numpy as np
+import pytest
+
+from sar_cambrianaccelerationcard_gb300 import sarbp, scenes
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def ctx():
+    c = sarbp.Context(0)
+    yield c
+    c.close()
+
+
+def view(s, storage=sarbp.STORE_C64, np_=None):
+    _, _, lay = sarbp.scene_args(s)
+    v = sarbp.RcView()
+    v.storage, v.np, v.nbins = storage, s.np_ if np_ is None else np_, lay.nbins
+    v.t0_bins, v.bin_rate = lay.t0_bins, lay.bin_rate
+    return v
+
+
+def sub_grid(g, x0, y0, nx, ny):
+    gs = sarbp.Grid()
+    for i in range(3):
+        gs.origin[i] = g.origin[i] + x0 * g.ux[i] + y0 * g.uy[i]
+        gs.ux[i], gs.uy[i] = g.ux[i], g.uy[i]
+    gs.nx, gs.ny = nx, ny
+    return gs
+
+
+def skewed_scene():
+    s = scenes.config1(np_=512, ns=2048, n_img=300, spacing=0.5)
+    g = s.grid
+    g.uy = g.uy + 0.2 * g.ux  # non-orthogonal axes
+    g.nx, g.ny = 301, 157
+    return s
+
+
+FIELDS = ("tile_x", "tile_y", "window", "series_terms", "segments", "ctas_per_sm", "smem_bytes",
+          "rmin", "rmax", "cos_x", "cos_y")
+
+
+@pytest.mark.parametrize("case", ["config2", "ground", "skewed", "config5_corner"])
+def test_host_and_device_extremes_agree(ctx, case):
+    if case == "config2":
+        s = scenes.config2()
+        r, g, _ = sarbp.scene_args(s)
+        apc, v = s.apc, view(s)
+    elif case == "ground":
+        s = scenes.ground_scene()
+        r, g, _ = sarbp.scene_args(s)
+        apc, v = s.apc, view(s)
+    elif case == "skewed":
+        s = skewed_scene()
+        r, g, _ = sarbp.scene_args(s)
+        apc, v = s.apc, view(s)
+    else:
+        s = scenes.config5()
+        r, g0, _ = sarbp.scene_args(s)
+        g = sub_grid(g0, 0, 0, 4096, 4096)
+        apc, v = np.ascontiguousarray(s.apc[12288:]), view(s, sarbp.STORE_C32H, 4096)
+    mode = sarbp.MODE_FP16STORE if v.storage == sarbp.STORE_C32H else sarbp.MODE_SPLIT
+    dev = ctx.bp_plan(r, v, apc, g, mode)
+    host = ctx.bp_plan(r, v, apc, g, mode, host_reduction=True)
+    for f in FIELDS:
+        assert getattr(dev, f) == getattr(host, f), f
+    # device-resident APC: the same plan
+    torch = pytest.importorskip("torch")
+    d_apc = torch.from_numpy(np.ascontiguousarray(apc)).cuda()
+    dev2 = ctx.bp_plan(r, v, d_apc, g, mode)
+    for f in FIELDS:
+        assert getattr(dev2, f) == getattr(dev, f), f
+    assert dev.rmin < dev.rmax and 0 < dev.cos_x <= 1 and 0 <= dev.cos_y <= 1
+    assert dev.window % 4 == 0 and dev.ctas_per_sm >= 1
+    print(case, {f: getattr(dev, f) for f in FIELDS})
+
+
+def test_config5_batches_keep_two_ctas(ctx):
+    """The 16 sub-aperture (4096 pulses) x tile (4096^2) launches of config 5:
+    windows of 92-140 bins, all at two resident CTAs per SM with FP16 rows."""
+    s = scenes.config5()
+    r, g, _ = sarbp.scene_args(s)
+    wins = []
+    for ty in (0, 4096):
+        for tx in (0, 4096):
+            gs = sub_grid(g, tx, ty, 4096, 4096)
+            for p0 in range(0, s.np_, 4096):
+                info = ctx.bp_plan(r, view(s, sarbp.STORE_C32H, 4096), np.ascontiguousarray(s.apc[p0:p0 + 4096]), gs,
+                                   sarbp.MODE_FP16STORE)
+                wins.append(info.window)
+                assert info.ctas_per_sm >= 2, (tx, ty, p0, info.window, info.smem_bytes)
+    assert max(wins) > 116  # wider than two complex64 CTAs would allow
+    print("config 5 windows", sorted(wins))
+
+
+def test_nonfinite_apc_rejected(ctx):
+    s = scenes.config1(np_=64, ns=1024, n_img=32)
+    r, g, _ = sarbp.scene_args(s)
+    apc = s.apc.copy()
+    apc[17, 1] = np.nan
+    for host in (False, True):
+        with pytest.raises(sarbp.SarbpError):
+            ctx.bp_plan(r, view(s), apc, g, sarbp.MODE_SPLIT, host_reduction=host)
