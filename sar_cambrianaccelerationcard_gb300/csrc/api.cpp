@@ -86,6 +86,8 @@ struct sarbp_ctx {
     DevBuf ext;                              // planning extremes [5] (FP64 bits, nonfinite flag)
     unsigned long long *ext_host = nullptr;  // pinned host copy of ext
     cudaEvent_t ev_ext = nullptr;
+    cudaStream_t copy_stream = nullptr;      // chunked echo uploads beside range compression
+    cudaEvent_t ev_copy = nullptr;
     // Buffers sized by the calls (released by sarbp_trim and sarbp_destroy).
     std::vector<DevBuf *> scratch() {
         std::vector<DevBuf *> v = {&echo, &spec, &rc,     &scale,   &apc,   &image, &partial, &targets, &pref,
@@ -235,7 +237,8 @@ sarbp_status finish(sarbp_ctx *ctx, cudaStream_t s, bool sync) {
 
 // Range compression of a device-resident echo into a device rc buffer.
 sarbp_status rc_device(sarbp_ctx *ctx, const sarbp_radar *r, const sarbp_rc_layout &lay, const float2 *echo,
-                       int np, int ns, int storage, void *rc_out, float *scale_out, cudaStream_t s) {
+                       int np, int ns, int storage, void *rc_out, float *scale_out, cudaStream_t s,
+                       bool record_events = true) {
     if (!sarbp::rc_size_supported(lay.nfft))
         return fail(ctx, SARBP_ERR_UNSUPPORTED, "range FFT size %d not supported (max 32768: ns + tp*fs - 1 <= 32768)",
                     lay.nfft);
@@ -249,7 +252,7 @@ sarbp_status rc_device(sarbp_ctx *ctx, const sarbp_radar *r, const sarbp_rc_layo
     float *scale = scale_out;
     if (storage == SARBP_STORE_C32H && !scale) return fail(ctx, SARBP_ERR_INVALID_ARGUMENT, "fp16 storage needs a scale array");
     const size_t esize = storage == SARBP_STORE_C64 ? 8 : 4;
-    cudaEventRecord(ctx->ev[0], s);
+    if (record_events) cudaEventRecord(ctx->ev[0], s);
     for (int p0 = 0; p0 < np; p0 += batch) {
         RcPlan plan{};
         plan.bound2 = bound2;
@@ -268,6 +271,41 @@ sarbp_status rc_device(sarbp_ctx *ctx, const sarbp_radar *r, const sarbp_rc_layo
                                                  static_cast<char *>(rc_out) + (size_t)p0 * lay.nbins * esize, s),
                    "range compression (inverse)");
         ctx->launches += 2;
+    }
+    if (record_events) {
+        cudaEventRecord(ctx->ev[1], s);
+        ctx->timed_rc = true;
+    }
+    return SARBP_OK;
+}
+
+// Range compression of a host echo: the upload runs in pulse chunks on the
+// context's copy stream and each chunk is range-compressed on `s` as soon as
+// its copy lands, so only the first chunk's copy is not hidden.  The copy
+// stream first waits for the work already on `s` (earlier users of the
+// context's echo buffer).
+sarbp_status rc_host_echo(sarbp_ctx *ctx, const sarbp_radar *r, const sarbp_rc_layout &lay, const sarbp_complex64 *echo,
+                          int np, int ns, int storage, void *rc_out, float *scale_out, cudaStream_t s) {
+    SARBP_CUDA(ctx, ctx->echo.ensure(sizeof(float2) * (size_t)np * ns), "alloc echo");
+    float2 *d_echo = ctx->echo.as<float2>();
+    const size_t row = sizeof(float2) * (size_t)ns;
+    const int chunk = std::max(256, (np + 7) / 8);
+    const size_t esize = storage == SARBP_STORE_C64 ? 8 : 4;
+    SARBP_CUDA(ctx, cudaEventRecord(ctx->ev_copy, s), "order echo upload");
+    SARBP_CUDA(ctx, cudaStreamWaitEvent(ctx->copy_stream, ctx->ev_copy, 0), "order echo upload");
+    cudaEventRecord(ctx->ev[0], s);
+    for (int p0 = 0; p0 < np; p0 += chunk) {
+        const int n = std::min(chunk, np - p0);
+        SARBP_CUDA(ctx, cudaMemcpyAsync(d_echo + (size_t)p0 * ns, echo + (size_t)p0 * ns, row * n, cudaMemcpyHostToDevice,
+                                        ctx->copy_stream),
+                   "upload echo");
+        // the wait binds to this record, so one event serves every chunk
+        SARBP_CUDA(ctx, cudaEventRecord(ctx->ev_copy, ctx->copy_stream), "upload echo");
+        SARBP_CUDA(ctx, cudaStreamWaitEvent(s, ctx->ev_copy, 0), "upload echo");
+        sarbp_status st = rc_device(ctx, r, lay, d_echo + (size_t)p0 * ns, n, ns, storage,
+                                    static_cast<char *>(rc_out) + (size_t)p0 * lay.nbins * esize,
+                                    scale_out ? scale_out + p0 : nullptr, s, false);
+        if (st != SARBP_OK) return st;
     }
     cudaEventRecord(ctx->ev[1], s);
     ctx->timed_rc = true;
@@ -561,6 +599,8 @@ sarbp_status sarbp_create(sarbp_ctx **out, int device) {
     bool ok = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) == cudaSuccess;
     for (int i = 0; i < 4 && ok; ++i) ok = cudaEventCreate(&ctx->ev[i]) == cudaSuccess;
     ok = ok && cudaEventCreateWithFlags(&ctx->ev_ext, cudaEventDisableTiming) == cudaSuccess;
+    ok = ok && cudaEventCreateWithFlags(&ctx->ev_copy, cudaEventDisableTiming) == cudaSuccess;
+    ok = ok && cudaStreamCreateWithFlags(&ctx->copy_stream, cudaStreamNonBlocking) == cudaSuccess;
     ok = ok && cudaMallocHost(reinterpret_cast<void **>(&ctx->ext_host), 8 * sizeof(unsigned long long)) == cudaSuccess;
     ok = ok && ctx->ext.ensure(8 * sizeof(unsigned long long)) == cudaSuccess;
     ok = ok && ctx->errword.ensure(sizeof(unsigned)) == cudaSuccess && ctx->power.ensure(sizeof(double)) == cudaSuccess;
@@ -584,6 +624,8 @@ sarbp_status sarbp_destroy(sarbp_ctx *ctx) {
     for (cudaEvent_t &e : ctx->ev)
         if (e) cudaEventDestroy(e);
     if (ctx->ev_ext) cudaEventDestroy(ctx->ev_ext);
+    if (ctx->ev_copy) cudaEventDestroy(ctx->ev_copy);
+    if (ctx->copy_stream) cudaStreamDestroy(ctx->copy_stream);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
     return SARBP_OK;
@@ -643,12 +685,6 @@ sarbp_status sarbp_range_compress(sarbp_ctx *ctx, const sarbp_radar *radar, cons
     const bool dev_in = is_device_ptr(echo), dev_out = is_device_ptr(rc_out);
     const bool dev_sc = storage == SARBP_STORE_C64 || is_device_ptr(rc_scale_out);
     const float2 *d_echo = reinterpret_cast<const float2 *>(echo);
-    if (!dev_in) {
-        SARBP_CUDA(ctx, ctx->echo.ensure(sizeof(float2) * (size_t)np * ns), "alloc echo");
-        SARBP_CUDA(ctx, cudaMemcpyAsync(ctx->echo.ptr, echo, sizeof(float2) * (size_t)np * ns, cudaMemcpyHostToDevice, s),
-                   "upload echo");
-        d_echo = ctx->echo.as<float2>();
-    }
     void *d_rc = rc_out;
     if (!dev_out) {
         SARBP_CUDA(ctx, ctx->rc.ensure(esize * (size_t)np * lay.nbins), "alloc rc");
@@ -660,7 +696,8 @@ sarbp_status sarbp_range_compress(sarbp_ctx *ctx, const sarbp_radar *radar, cons
         d_scale = ctx->scale.as<float>();
     }
     ctx->timed_bp = false;
-    st = rc_device(ctx, radar, lay, d_echo, np, ns, storage, d_rc, storage == SARBP_STORE_C32H ? d_scale : nullptr, s);
+    st = dev_in ? rc_device(ctx, radar, lay, d_echo, np, ns, storage, d_rc, storage == SARBP_STORE_C32H ? d_scale : nullptr, s)
+                : rc_host_echo(ctx, radar, lay, echo, np, ns, storage, d_rc, storage == SARBP_STORE_C32H ? d_scale : nullptr, s);
     if (st != SARBP_OK) return st;
     if (!dev_out)
         SARBP_CUDA(ctx, cudaMemcpyAsync(rc_out, d_rc, esize * (size_t)np * lay.nbins, cudaMemcpyDeviceToHost, s),
@@ -1185,14 +1222,8 @@ sarbp_status sarbp_image(sarbp_ctx *ctx, const sarbp_radar *radar, const sarbp_c
         st = extremes_device(ctx, apc_dev, np, grid, s, ex);
         if (st != SARBP_OK) return st;
     }
-    const float2 *d_echo = reinterpret_cast<const float2 *>(echo);
-    if (np > 0 && !is_device_ptr(echo)) {
-        SARBP_CUDA(ctx, ctx->echo.ensure(sizeof(float2) * (size_t)np * ns), "alloc echo");
-        SARBP_CUDA(ctx, cudaMemcpyAsync(ctx->echo.ptr, echo, sizeof(float2) * (size_t)np * ns, cudaMemcpyHostToDevice, s),
-                   "upload echo");
-        d_echo = ctx->echo.as<float2>();
-        any_host = true;
-    }
+    const bool host_echo = np > 0 && !is_device_ptr(echo);
+    any_host = any_host || host_echo;
     float2 *d_img = reinterpret_cast<float2 *>(image);
     const bool dev_img = is_device_ptr(image);
     if (!dev_img) {
@@ -1211,8 +1242,10 @@ sarbp_status sarbp_image(sarbp_ctx *ctx, const sarbp_radar *radar, const sarbp_c
     if (np > 0) {
         SARBP_CUDA(ctx, ctx->rc.ensure(esize * (size_t)np * lay.nbins), "alloc rc");
         if (storage == SARBP_STORE_C32H) SARBP_CUDA(ctx, ctx->scale.ensure(sizeof(float) * np), "alloc scale");
-        st = rc_device(ctx, radar, lay, d_echo, np, ns, storage, ctx->rc.ptr,
-                       storage == SARBP_STORE_C32H ? ctx->scale.as<float>() : nullptr, s);
+        float *d_scale = storage == SARBP_STORE_C32H ? ctx->scale.as<float>() : nullptr;
+        st = host_echo ? rc_host_echo(ctx, radar, lay, echo, np, ns, storage, ctx->rc.ptr, d_scale, s)
+                       : rc_device(ctx, radar, lay, reinterpret_cast<const float2 *>(echo), np, ns, storage, ctx->rc.ptr,
+                                   d_scale, s);
         if (st != SARBP_OK) return st;
         v.data = ctx->rc.ptr;
         v.scale = storage == SARBP_STORE_C32H ? ctx->scale.as<float>() : nullptr;

@@ -227,3 +227,38 @@ def test_ground_geometry_coarse_pixels(ctx, orc):
         err = metrics.rel_l2_db(img, ref)
         print("ground", mode, err)
         assert err <= -60.0
+
+
+@pytest.mark.parametrize("storage", [sarbp.STORE_C64, sarbp.STORE_C32H])
+def test_chunked_host_upload_is_bit_exact(ctx, storage):
+    """A host echo is uploaded in pulse chunks (2500 pulses: 8 chunks of 313,
+    the last 309) overlapped with range compression; rows and FP16 scales equal
+    those from a device-resident echo, and so does the image."""
+    torch = pytest.importorskip("torch")
+    s = scenes.config1(np_=2500, ns=1024, n_img=128)
+    r, g, lay = sarbp.scene_args(s)
+    rng = np.random.default_rng(9)
+    echo = (rng.standard_normal((s.np_, s.ns)) + 1j * rng.standard_normal((s.np_, s.ns))).astype(np.complex64)
+    host = ctx.range_compress(r, echo, storage=storage)
+    d_echo = torch.from_numpy(echo.view(np.float32)).cuda()
+    esize = 8 if storage == sarbp.STORE_C64 else 4
+    d_rc = torch.empty((s.np_, lay.nbins * esize // 4), dtype=torch.float32, device="cuda")
+    d_scale = torch.empty(s.np_, dtype=torch.float32, device="cuda")
+    ctx.check(ctx.lib.sarbp_range_compress(ctx.h, sarbp.ctypes.byref(r), d_echo.data_ptr(), s.np_, s.ns, storage,
+                                           d_rc.data_ptr(), d_scale.data_ptr() if storage == sarbp.STORE_C32H else None,
+                                           None), "rc device")
+    ctx.synchronize()
+    if storage == sarbp.STORE_C64:
+        assert np.array_equal(d_rc.cpu().numpy().view(np.complex64), host)
+    else:
+        h, scale = host
+        assert np.array_equal(d_rc.cpu().numpy().view(np.float16).reshape(h.shape), h)
+        assert np.array_equal(d_scale.cpu().numpy(), scale)
+    mode = sarbp.MODE_SPLIT if storage == sarbp.STORE_C64 else sarbp.MODE_FP16STORE
+    img_host = sarbp.image_scene(ctx, s, echo, mode)
+    img_dev = torch.zeros((g.ny, g.nx * 2), dtype=torch.float32, device="cuda")
+    apc = torch.from_numpy(s.apc).cuda()
+    ctx.check(ctx.lib.sarbp_image(ctx.h, sarbp.ctypes.byref(r), d_echo.data_ptr(), s.np_, s.ns, apc.data_ptr(),
+                                  sarbp.ctypes.byref(g), mode, img_dev.data_ptr(), None), "image device")
+    ctx.synchronize()
+    assert np.array_equal(img_dev.cpu().numpy().view(np.complex64), img_host)
