@@ -197,6 +197,8 @@ typedef struct sarbp_bp_plan_info {
     int32_t series_terms;    /* differential-range series terms (SPLIT / FP16STORE) */
     int32_t segments;        /* pulse segments the launch is split into */
     int32_t ctas_per_sm;     /* resident CTAs per SM of the chosen kernel */
+    int32_t pulse_chunk;     /* pulses staged per chunk (16, 8 or 4: two CTAs per SM where it can) */
+    int32_t reserved;
     uint64_t smem_bytes;     /* dynamic shared memory per CTA */
     double rmin, rmax;       /* nearest and farthest range, lattice x pulses (m) */
     double cos_x, cos_y;     /* largest |cosine| between line of sight and grid axis x, y */

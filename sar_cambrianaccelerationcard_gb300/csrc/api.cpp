@@ -794,7 +794,8 @@ sarbp_status sarbp_bp_plan(sarbp_ctx *ctx, const sarbp_radar *radar, const sarbp
     out->series_terms = p.nterms;
     out->segments = p.segments;
     out->ctas_per_sm = occ;
-    out->smem_bytes = sarbp::bp_smem_bytes(p.storage, p.win);
+    out->pulse_chunk = p.chunk;
+    out->smem_bytes = sarbp::bp_smem_bytes(p.storage, p.win, p.chunk);
     out->rmin = ex.rmin;
     out->rmax = ex.rmax;
     out->cos_x = ex.cx;

@@ -177,9 +177,9 @@ __device__ __forceinline__ void lds2x2(const void *p, f2 &a, f2 &b) {
 }
 
 struct Smem {
-    float4 *staged;      // [2][kChunk][win]
-    unsigned char *raw;  // [kStages][kChunk][win] stored elements (8 or 4 bytes)
-    Prm *prm;            // [kStages][kChunk]
+    float4 *staged;      // [2][chunk][win]
+    unsigned char *raw;  // [kStages][chunk][win] stored elements (8 or 4 bytes)
+    Prm *prm;            // [kStages][kChunk] (chunk <= kChunk pulses used per stage)
     uint64_t *bar;       // [kStages]
     float2 *red;         // [2][kWarps][kChunk] per-warp pulse sums (weighted projection)
 };
@@ -188,11 +188,11 @@ struct Smem {
 __host__ __device__ constexpr int raw_esize(int storage) { return storage == SARBP_STORE_C64 ? 8 : 4; }
 
 template <int STORE>
-__device__ __forceinline__ Smem carve(unsigned char *base, int win) {
+__device__ __forceinline__ Smem carve(unsigned char *base, int win, int chunk) {
     Smem s;
     s.staged = reinterpret_cast<float4 *>(base);
-    s.raw = base + (size_t)2 * kChunk * win * 16;
-    s.prm = reinterpret_cast<Prm *>(s.raw + (size_t)kStages * kChunk * win * raw_esize(STORE));
+    s.raw = base + (size_t)2 * chunk * win * 16;
+    s.prm = reinterpret_cast<Prm *>(s.raw + (size_t)kStages * chunk * win * raw_esize(STORE));
     s.bar = reinterpret_cast<uint64_t *>(s.prm + kStages * kChunk);
     s.red = reinterpret_cast<float2 *>(s.bar + kStages);
     return s;
@@ -332,7 +332,7 @@ __device__ __forceinline__ void produce(const BpPlan &P, const Smem &S, int stag
         if (hi > lo) {
             bytes = (unsigned)((hi - lo) * esize);
             src = reinterpret_cast<const char *>(P.rc) + ((size_t)p * P.nbins + (size_t)lo) * esize;
-            dst = smem_addr(S.raw + ((size_t)stage * kChunk + (size_t)slot) * win * esize + (size_t)(lo - ws) * esize);
+            dst = smem_addr(S.raw + ((size_t)stage * P.chunk + (size_t)slot) * win * esize + (size_t)(lo - ws) * esize);
         }
     }
     unsigned total = bytes;
@@ -346,15 +346,16 @@ __device__ __forceinline__ void produce(const BpPlan &P, const Smem &S, int stag
 
 // raw window -> (mid, diff) pairs; bins outside [lo, hi) read as zero.
 template <int MODE, int STORE>
-__device__ __forceinline__ void convert(const Smem &S, int stage, int sbuf, int count, int win, unsigned win_magic) {
+__device__ __forceinline__ void convert(const Smem &S, int stage, int sbuf, int count, int win, unsigned win_magic,
+                                        int chunk) {
     const int total = count * win;
-    float4 *st = S.staged + (size_t)sbuf * kChunk * win;
+    float4 *st = S.staged + (size_t)sbuf * chunk * win;
     for (int e = threadIdx.x; e < total; e += kThreads) {
         const int pl = (int)__umulhi((unsigned)e, win_magic);
         const int i = e - pl * win;
         const Prm &q = S.prm[stage * kChunk + pl];
         const int lo = q.lo, hi = q.hi;
-        const unsigned char *rw = S.raw + ((size_t)stage * kChunk + pl) * win * raw_esize(STORE);
+        const unsigned char *rw = S.raw + ((size_t)stage * chunk + pl) * win * raw_esize(STORE);
         float2 a = make_float2(0.f, 0.f), b = make_float2(0.f, 0.f);
         if (STORE == SARBP_STORE_C64) {
             const float2 *r = reinterpret_cast<const float2 *>(rw);
@@ -394,7 +395,9 @@ __device__ __forceinline__ void flush_projection(const BpPlan &P, const Smem &S,
 // ADJ: weighted projection (the adjoint) instead of back-projection: every
 // pixel's term of pulse p is multiplied by conj(weight[pixel]) and summed over
 // the tile into proj[tile][p] (SPLIT / FP16STORE arithmetic).
-template <int MODE, int STORE, int NTERMS, bool CHECKED, int PIX, bool ADJ = false>
+// CHUNK: pulses per staged chunk fixed at compile time (the hot unchecked
+// SPLIT / FP16STORE case at 16), or 0 to take the planner's P.chunk.
+template <int MODE, int STORE, int NTERMS, bool CHECKED, int PIX, bool ADJ = false, int CHUNK = 0>
 __global__ void __launch_bounds__(kThreads, SARBP_BP_MINBLOCKS)
     bp_kernel(const __grid_constant__ BpPlan P, int tiles_y, int pulses_per_seg, float qq_max) {
     static_assert(!ADJ || MODE == SARBP_MODE_SPLIT || MODE == SARBP_MODE_FP16STORE, "projection: split arithmetic");
@@ -402,7 +405,8 @@ __global__ void __launch_bounds__(kThreads, SARBP_BP_MINBLOCKS)
     constexpr int kTileY = 8 * PIX;
     extern __shared__ __align__(128) unsigned char smem_raw[];
     const int win = P.win;
-    const Smem S = carve<STORE>(smem_raw, win);
+    const int chunk = CHUNK ? CHUNK : P.chunk;  // pulses per staged chunk: 16, 8 or 4 (two CTAs per SM)
+    const Smem S = carve<STORE>(smem_raw, win, chunk);
     const unsigned win_magic = (unsigned)((0xFFFFFFFFull + (unsigned long long)win) / (unsigned long long)win);
 
     const int tile = blockIdx.x;
@@ -411,7 +415,7 @@ __global__ void __launch_bounds__(kThreads, SARBP_BP_MINBLOCKS)
     const int seg = blockIdx.y;
     const int p_begin = seg * pulses_per_seg;
     const int p_end = min(P.np, p_begin + pulses_per_seg);
-    const int nchunks = p_end > p_begin ? (p_end - p_begin + kChunk - 1) / kChunk : 0;
+    const int nchunks = p_end > p_begin ? (p_end - p_begin + chunk - 1) / chunk : 0;
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int lx = lane >> 2, ly = lane & 3;
@@ -497,7 +501,7 @@ __global__ void __launch_bounds__(kThreads, SARBP_BP_MINBLOCKS)
         QQ2[h] = pk2(qq[2 * h], qq[2 * h + 1]);
     }
 
-    if (nchunks > 0) produce<MODE, STORE, PIX>(P, S, 0, p_begin, min(kChunk, p_end - p_begin), T);
+    if (nchunks > 0) produce<MODE, STORE, PIX>(P, S, 0, p_begin, min(chunk, p_end - p_begin), T);
 
     bool failed = false;
     bool clamped = false;
@@ -505,22 +509,22 @@ __global__ void __launch_bounds__(kThreads, SARBP_BP_MINBLOCKS)
     for (int c = 0; c < nchunks; ++c) {
         const int stage = c % kStages;
         const int sbuf = c & 1;
-        const int pc0 = p_begin + c * kChunk;
-        const int count = min(kChunk, p_end - pc0);
+        const int pc0 = p_begin + c * chunk;
+        const int count = min(chunk, p_end - pc0);
         if (c + 1 < nchunks) {
-            const int pn = pc0 + kChunk;
-            produce<MODE, STORE, PIX>(P, S, (c + 1) % kStages, pn, min(kChunk, p_end - pn), T);
+            const int pn = pc0 + chunk;
+            produce<MODE, STORE, PIX>(P, S, (c + 1) % kStages, pn, min(chunk, p_end - pn), T);
         }
         const bool ok = mbar_wait_bounded(smem_addr(&S.bar[stage]), (c / kStages) & 1, 2000000000ull);
         if (!ok) { failed = true; }
         if (__syncthreads_or(failed)) { failed = true; break; }
-        convert<MODE, STORE>(S, stage, sbuf, count, win, win_magic);
+        convert<MODE, STORE>(S, stage, sbuf, count, win, win_magic, chunk);
         __syncthreads();
         if constexpr (ADJ) {  // every warp has finished chunk c-1: combine its pulse sums
-            if (c > 0) flush_projection(P, S, (c - 1) & 1, pc0 - kChunk, kChunk);
+            if (c > 0) flush_projection(P, S, (c - 1) & 1, pc0 - chunk, chunk);
         }
 
-        const float4 *stg = S.staged + (size_t)sbuf * kChunk * win;
+        const float4 *stg = S.staged + (size_t)sbuf * chunk * win;
         const unsigned sbase = smem_addr(stg) - kMagicBitsShift4;
         if (MODE == SARBP_MODE_SPLIT || MODE == SARBP_MODE_FP16STORE) {
             // geometry, bin and phase for pixel pairs (2j, 2j+1) in packed FP32x2;
@@ -664,7 +668,7 @@ __global__ void __launch_bounds__(kThreads, SARBP_BP_MINBLOCKS)
         if (nchunks > 0) {
             __syncthreads();
             const int last = nchunks - 1;
-            flush_projection(P, S, last & 1, p_begin + last * kChunk, min(kChunk, p_end - p_begin - last * kChunk));
+            flush_projection(P, S, last & 1, p_begin + last * chunk, min(chunk, p_end - p_begin - last * chunk));
         }
         return;
     }
@@ -709,10 +713,11 @@ __global__ void reduce_segments_kernel(const float2 *__restrict__ partial, int s
 // resident CTAs per SM there instead of launching it.
 thread_local int *t_occupancy = nullptr;
 
-template <int MODE, int STORE, int NTERMS, bool CHECKED, int PIX, bool ADJ = false>
+template <int MODE, int STORE, int NTERMS, bool CHECKED, int PIX, bool ADJ = false, int CHUNK = 0>
 cudaError_t launch_variant(const BpPlan &p, cudaStream_t s, int tiles, int tiles_y, int pps, float qq_max) {
-    auto k = bp_kernel<MODE, STORE, NTERMS, CHECKED, PIX, ADJ>;
-    const size_t smem = bp_smem_bytes(STORE, p.win);
+    if (CHUNK && p.chunk != CHUNK) return cudaErrorInvalidValue;
+    auto k = bp_kernel<MODE, STORE, NTERMS, CHECKED, PIX, ADJ, CHUNK>;
+    const size_t smem = bp_smem_bytes(STORE, p.win, p.chunk);
     cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     if (t_occupancy) return cudaOccupancyMaxActiveBlocksPerMultiprocessor(t_occupancy, k, kThreads, smem);
@@ -726,6 +731,9 @@ cudaError_t launch_split(const BpPlan &p, cudaStream_t s, int tiles, int tiles_y
     if (p.checked)
         return p.nterms == 3 ? launch_variant<MODE, STORE, 3, true, PIX>(p, s, tiles, tiles_y, pps, qq_max)
                              : launch_variant<MODE, STORE, 4, true, PIX>(p, s, tiles, tiles_y, pps, qq_max);
+    if (p.chunk == kChunk)
+        return p.nterms == 3 ? launch_variant<MODE, STORE, 3, false, PIX, false, kChunk>(p, s, tiles, tiles_y, pps, qq_max)
+                             : launch_variant<MODE, STORE, 4, false, PIX, false, kChunk>(p, s, tiles, tiles_y, pps, qq_max);
     return p.nterms == 3 ? launch_variant<MODE, STORE, 3, false, PIX>(p, s, tiles, tiles_y, pps, qq_max)
                          : launch_variant<MODE, STORE, 4, false, PIX>(p, s, tiles, tiles_y, pps, qq_max);
 }
@@ -838,10 +846,10 @@ void bp_tile_dims(int pix, int *tile_x, int *tile_y) {
     *tile_y = 8 * pix;
 }
 
-int bp_pulses_per_chunk(int) { return kChunk; }
+int bp_max_chunk() { return kChunk; }
 
-size_t bp_smem_bytes(int storage, int win) {
-    return (size_t)2 * kChunk * win * 16 + (size_t)kStages * kChunk * win * raw_esize(storage) +
+size_t bp_smem_bytes(int storage, int win, int chunk) {
+    return (size_t)2 * chunk * win * 16 + (size_t)kStages * chunk * win * raw_esize(storage) +
            kStages * kChunk * sizeof(Prm) +
            kStages * sizeof(uint64_t) + 2 * kWarps * kChunk * sizeof(float2);
 }

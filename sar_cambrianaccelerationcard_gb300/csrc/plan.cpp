@@ -7,6 +7,7 @@
 // height (32 x 64, 32 x 32 or 32 x 16 pixels), the staging window per
 // (tile, pulse), the number of series terms and the pulse segmentation.
 #include <cmath>
+#include <cstdlib>
 #include <complex>
 #include <cstring>
 #include <string>
@@ -39,6 +40,25 @@ void fft_pow2_host(std::vector<std::complex<double>> &h) {
             }
 }
 }  // namespace
+
+// Pulse chunk for a staging window: the largest (16, 8, 4) whose CTA still fits
+// twice in an SM's 228 KB of shared memory (1 KB reserved per CTA), else the
+// largest that fits once (227 KB per CTA); 0 if none.  SARBP_BP_CHUNK=16|8|4
+// forces a chunk where it fits (tuning and tests: results do not depend on it).
+int bp_choose_chunk(int storage, int win) {
+    constexpr size_t kSmemPerSm = 228u << 10, kSmemPerCta = 227u << 10, kReserve = 1u << 10;
+    const char *env = std::getenv("SARBP_BP_CHUNK");
+    if (env && env[0]) {
+        const int c = std::atoi(env);
+        if ((c == 16 || c == 8 || c == 4) && c <= bp_max_chunk() && bp_smem_bytes(storage, win, c) <= kSmemPerCta)
+            return c;
+    }
+    for (int c = bp_max_chunk(); c >= 4; c /= 2)
+        if (2 * (bp_smem_bytes(storage, win, c) + kReserve) <= kSmemPerSm) return c;
+    for (int c = bp_max_chunk(); c >= 4; c /= 2)
+        if (bp_smem_bytes(storage, win, c) <= kSmemPerCta) return c;
+    return 0;
+}
 
 void ext_axes(const sarbp_grid &g, double *lux, double *luy) {
     *lux = std::sqrt(ext_dot(g.ux, g.ux));
@@ -99,15 +119,17 @@ bool plan_bp(int sms, const sarbp_radar &r, const sarbp_rc_view &rc, const BpExt
 
     const double lux = std::sqrt(p.g.g11), luy = std::sqrt(p.g.g22);
     double cx = ex.cx, sy = ex.sy;
-    const double rmin = ex.rmin, rmax = ex.rmax;
+    const double rmin = ex.rmin;
     cx = std::min(1.0, cx * 1.05 + 0.01);
     sy = std::min(1.0, sy * 1.05 + 0.01);
     const double bpm = 2.0 / r.c * rc.bin_rate;
     // Tile choice: the tallest tile (32 x 64, 32 x 32, 32 x 16 pixels) whose
     // differential-range series truncation stays below kSeriesTol metres and
     // whose staging window fits shared memory.  Series remainder after k terms
-    // of sqrt(1+e)-1 times R: R (5/128) e^4 (k = 3), R (7/256) e^5 (k = 4), with
-    // e = |n|/R^2 <= (2 diag R + diag^2)/R^2 over the tile.
+    // of sqrt(1+e)-1 times R_T: R_T (5/128) e^4 (k = 3), R_T (7/256) e^5 (k = 4),
+    // with e = |n|/R_T^2 <= 2 diag/R_T + diag^2/R_T^2 over the tile.  R_T e^k
+    // falls as R_T grows, so the remainder is largest at the nearest tile centre
+    // (rmin_tile); x1.1 covers the terms past the first omitted one (|e| < 0.09).
     constexpr double kSeriesTol = 5e-7;  // 1.1e-4 rad of C-band phase at the tile corners
     why = "no tile size fits";
     bool chosen = false;
@@ -133,19 +155,22 @@ bool plan_bp(int sms, const sarbp_radar &r, const sarbp_rc_view &rc, const BpExt
         }
         int win = (int)std::ceil(2 * half) + 8;
         win = (win + 3) & ~3;
-        if (bp_smem_bytes(p.storage, win) > (size_t)(227u << 10)) {
+        const int chunk = bp_choose_chunk(p.storage, win);
+        if (!chunk) {
             why = "tile spans too many range bins for shared memory";
             continue;
         }
-        const double e = (2 * tile_diag * rmax + qq_max) / (rmin_tile * rmin_tile);
+        const double rt = rmin_tile;
+        const double e = (2 * tile_diag * rt + qq_max) / (rt * rt);
         const bool split = mode == SARBP_MODE_SPLIT || mode == SARBP_MODE_FP16STORE;
-        if (split && rmax * 0.02734375 * std::pow(e, 5) > kSeriesTol) {
+        if (split && (e >= 0.09 || 1.1 * rt * 0.02734375 * std::pow(e, 5) > kSeriesTol)) {
             why = "tiles too large for the differential-range series";
             continue;
         }
         p.pix = pix;
         p.win = win;
-        p.nterms = (rmax * 0.0390625 * e * e * e * e < kSeriesTol) ? 3 : 4;
+        p.chunk = chunk;
+        p.nterms = (1.1 * rt * 0.0390625 * e * e * e * e < kSeriesTol) ? 3 : 4;
         chosen = true;
         break;
     }
@@ -154,13 +179,14 @@ bool plan_bp(int sms, const sarbp_radar &r, const sarbp_rc_view &rc, const BpExt
     bp_tile_dims(p.pix, &tx, &ty);
     // pulse segments: fill at least ~2 waves of CTAs
     const int tiles = ((g.nx + tx - 1) / tx) * ((g.ny + ty - 1) / ty);
-    const int chunk = bp_pulses_per_chunk(mode);
-    const size_t smem = bp_smem_bytes(p.storage, p.win);
-    const int cta_per_sm = std::max<int>(1, std::min<int>(3, (int)((227u << 10) / (smem + 1024))));
-    const int want = 2 * sms * cta_per_sm;
+    // The segment count depends on the geometry only (not on the staging chunk,
+    // which the planner or SARBP_BP_CHUNK picks): partial images are summed per
+    // segment, so the same call gives the same bits whatever the chunk.  Two
+    // CTAs per SM (the SPLIT kernels' register bound).
+    const int want = 2 * sms * 2;
     const int npl = pulses_per_launch > 0 ? pulses_per_launch : np;
     int segments = 1;
-    while (tiles * segments < want && npl / (segments * 2) >= 4 * chunk) segments *= 2;
+    while (tiles * segments < want && npl / (segments * 2) >= 4 * bp_max_chunk()) segments *= 2;
     p.segments = segments;
     return true;
 }

@@ -76,6 +76,7 @@ struct BpPlan {
     int nterms;              // polynomial terms for the differential range (3 or 4)
     int checked;             // 1: clamp every interpolation index and report clamps
     int pix;                 // pixels per thread (8, 4 or 2): tiles of 32 x (8 pix) pixels
+    int chunk;               // pulses per staged chunk (16, 8 or 4)
     unsigned *err;           // device error word
     const double *drange;    // [np] device, per-pulse range corrections (m), or null
     const double *dphase;    // [np] device, per-pulse phase corrections (rad), or null
@@ -168,8 +169,9 @@ void rc_tables_host(const sarbp_radar &r, const sarbp_rc_layout &lay, std::vecto
                     std::vector<float2> &etab);
 // Tile geometry the planner needs to size the staging window.
 void bp_tile_dims(int pix, int *tile_x, int *tile_y);
-size_t bp_smem_bytes(int storage, int win);
-int bp_pulses_per_chunk(int mode);
+// Dynamic shared memory of a BP CTA for a staging window and pulse chunk.
+size_t bp_smem_bytes(int storage, int win, int chunk);
+int bp_max_chunk();  // largest pulse chunk (16); the planner may choose 8 or 4
 
 // ---------------------------------------------------------------- echo synthesis
 cudaError_t launch_echo_synth(const double *apc, int np, int ns, const sarbp_target *tg, int nt,

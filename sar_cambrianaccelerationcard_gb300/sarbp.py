@@ -106,7 +106,7 @@ class RcView(ctypes.Structure):
 class BpPlanInfo(ctypes.Structure):
     _fields_ = [("tile_x", ctypes.c_int32), ("tile_y", ctypes.c_int32), ("window", ctypes.c_int32),
                 ("series_terms", ctypes.c_int32), ("segments", ctypes.c_int32), ("ctas_per_sm", ctypes.c_int32),
-                ("smem_bytes", ctypes.c_uint64), ("rmin", ctypes.c_double), ("rmax", ctypes.c_double),
+                ("pulse_chunk", ctypes.c_int32), ("reserved", ctypes.c_int32), ("smem_bytes", ctypes.c_uint64), ("rmin", ctypes.c_double), ("rmax", ctypes.c_double),
                 ("cos_x", ctypes.c_double), ("cos_y", ctypes.c_double)]
 
 

@@ -44,7 +44,7 @@ def skewed_scene():
     return s
 
 
-FIELDS = ("tile_x", "tile_y", "window", "series_terms", "segments", "ctas_per_sm", "smem_bytes",
+FIELDS = ("tile_x", "tile_y", "window", "series_terms", "segments", "ctas_per_sm", "pulse_chunk", "smem_bytes",
           "rmin", "rmax", "cos_x", "cos_y")
 
 
@@ -109,3 +109,67 @@ def test_nonfinite_apc_rejected(ctx):
     for host in (False, True):
         with pytest.raises(sarbp.SarbpError):
             ctx.bp_plan(r, view(s), apc, g, sarbp.MODE_SPLIT, host_reduction=host)
+
+
+@pytest.mark.parametrize("case,storage,chunk", [("config1", sarbp.STORE_C64, 8), ("config1", sarbp.STORE_C32H, 16),
+                                                 ("ground", sarbp.STORE_C64, 8), ("config2", sarbp.STORE_C64, 16)])
+def test_wide_windows_keep_two_ctas(ctx, case, storage, chunk):
+    """Windows past the two-CTA limit of 16-pulse chunks (config 1: 128 bins of
+    complex64 at 0.5 m; the ground scene: 220 bins at 1 m) stage 8-pulse chunks."""
+    s = {"config1": scenes.config1, "ground": scenes.ground_scene, "config2": scenes.config2}[case]()
+    r, g, _ = sarbp.scene_args(s)
+    mode = sarbp.MODE_FP16STORE if storage == sarbp.STORE_C32H else sarbp.MODE_SPLIT
+    info = ctx.bp_plan(r, view(s, storage), s.apc, g, mode)
+    print(case, info.window, info.pulse_chunk, info.ctas_per_sm, info.smem_bytes)
+    assert info.pulse_chunk == chunk
+    assert info.ctas_per_sm == 2
+
+
+@pytest.mark.parametrize("storage", [sarbp.STORE_C64, sarbp.STORE_C32H])
+def test_chunk_size_does_not_change_results(ctx, monkeypatch, storage):
+    """Pixels accumulate pulses in the same order whatever the staging chunk, so
+    16-, 8- and 4-pulse chunks give the same bits (back-projection and the
+    weighted projection; 300 pulses: ragged last chunks)."""
+    s = scenes.config1(np_=300, ns=1024, n_img=96)
+    r, g, lay = sarbp.scene_args(s)
+    echo = sarbp.synthesize(ctx, s)
+    rc = ctx.range_compress(r, echo, storage=storage)
+    data, scale = rc if storage == sarbp.STORE_C32H else (rc, None)
+    mode = sarbp.MODE_FP16STORE if storage == sarbp.STORE_C32H else sarbp.MODE_SPLIT
+    w = (np.random.default_rng(4).standard_normal((g.ny, g.nx)) + 0j).astype(np.complex64)
+    imgs, projs = {}, {}
+    for c in ("16", "8", "4"):
+        monkeypatch.setenv("SARBP_BP_CHUNK", c)
+        assert ctx.bp_plan(r, view(s, storage), s.apc, g, mode).pulse_chunk == int(c)
+        imgs[c] = ctx.backproject(r, data, s.apc, g, mode, lay.t0_bins, lay.bin_rate, scale=scale)
+        projs[c] = ctx.project_weighted(r, data, s.apc, g, mode, lay.t0_bins, lay.bin_rate, w, scale=scale)
+    for c in ("8", "4"):
+        assert np.array_equal(imgs[c], imgs["16"])
+        assert np.array_equal(projs[c], projs["16"])
+    assert np.abs(imgs["16"]).max() > 0
+
+
+def test_wide_coarse_grid_plans_and_matches_fp64(ctx):
+    """A 4 km-wide range extent at 1 m pixels from 5 km range: the series bound
+    taken at the nearest tile centre admits 32 x 32 tiles with 4 terms (the
+    bound at the farthest range rejected every tile), the window (236 bins, past
+    the 116-bin two-CTA limit of 16-pulse chunks) stages 8-pulse chunks at two
+    CTAs per SM, and the near-range corner (largest
+    relative tile size) matches the FP64 mode within -65 dB."""
+    radar = scenes.Radar()
+    grid = scenes.centred_grid(radar, 4096, 256, 1.0)
+    s = scenes.Scene(name="coarse", radar=radar, np_=512, ns=8192, apc=scenes.straight_track(radar, 512), grid=grid,
+                     targets=scenes.random_targets(grid, 50, 3), t_rec0=scenes.centred_record_start(radar, 8192),
+                     snr_db=None, seed=3)
+    r, g, lay = sarbp.scene_args(s)
+    info = ctx.bp_plan(r, view(s), s.apc, g, sarbp.MODE_SPLIT)
+    assert (info.tile_x, info.tile_y, info.series_terms) == (32, 32, 4)
+    print("coarse grid plan", info.window, info.pulse_chunk, info.ctas_per_sm)
+    assert info.window > 116 and info.pulse_chunk in (8, 4) and info.ctas_per_sm == 2
+    rc = ctx.range_compress(r, sarbp.synthesize(ctx, s))
+    img = ctx.backproject(r, rc, s.apc, g, sarbp.MODE_SPLIT, lay.t0_bins, lay.bin_rate)
+    corner = sub_grid(g, 0, 0, 256, 256)
+    ref = ctx.backproject(r, rc, s.apc, corner, sarbp.MODE_FP64, lay.t0_bins, lay.bin_rate)
+    err = 20 * np.log10(np.linalg.norm(img[:256, :256] - ref) / np.linalg.norm(ref))
+    print("coarse grid near-range corner rel-L2 dB", err)
+    assert err <= -65.0
