@@ -8,6 +8,8 @@
 // tables held in shared memory (see Etab / load_etab).
 #pragma once
 
+#include <type_traits>
+
 #include "sarbp_internal.h"
 
 namespace sarbp {
@@ -231,8 +233,14 @@ __device__ __forceinline__ void twiddles(const Etab &E, int m, float2 lo1, float
 // constant: offsets that are multiples of 256 points pass through sw()
 // unchanged and become immediates.  When T is a multiple of Ns every
 // butterfly of a thread has the same k and the twiddles are computed once.
-template <int N, int R, int T, bool INV, int Ns>
-__device__ __forceinline__ void stage(float2 *s, const Etab &E) {
+// Destination of a stage's outputs: back to shared memory (every stage but
+// the last of an I/O-fused transform), or a caller's functor sink(x, value)
+// receiving output point x in natural order.
+struct SmemSink {};
+
+template <int N, int R, int T, bool INV, int Ns, class Sink = SmemSink>
+__device__ __forceinline__ void stage(float2 *s, const Etab &E, Sink sink = Sink{}) {
+    constexpr bool kToSmem = std::is_same<Sink, SmemSink>::value;
     constexpr int NB = N / R;
     constexpr int PER = (NB + T - 1) / T;
     constexpr int C = N / (Ns * R);  // k -> twiddle exponent step
@@ -251,7 +259,7 @@ __device__ __forceinline__ void stage(float2 *s, const Etab &E) {
             }
         }
     }
-    __syncthreads();
+    if constexpr (kToSmem) __syncthreads();  // loads done before the in-place stores
     float2 w[R <= 8 ? R : 1];
     Tw16 t16;
     constexpr bool kSameK = Ns > 1 && T % Ns == 0;
@@ -293,7 +301,10 @@ __device__ __forceinline__ void stage(float2 *s, const Etab &E) {
             }
             Dft<R, INV>::run(v[b]);
             const int x0 = (j - k) * R + k;
-            if constexpr (Ns % 256 == 0) {
+            if constexpr (!kToSmem) {
+#pragma unroll
+                for (int r = 0; r < R; ++r) sink(x0 + r * Ns, v[b][r]);
+            } else if constexpr (Ns % 256 == 0) {
                 float2 *dst = s + sw(x0);
 #pragma unroll
                 for (int r = 0; r < R; ++r) dst[r * Ns] = v[b][r];
@@ -303,7 +314,7 @@ __device__ __forceinline__ void stage(float2 *s, const Etab &E) {
             }
         }
     }
-    __syncthreads();
+    if constexpr (kToSmem) __syncthreads();
 }
 
 #ifndef SARBP_FFT_RADIX16
@@ -334,6 +345,61 @@ struct Stages {
 template <int N, int T, bool INV>
 __device__ void fft_smem(float2 *s, const Etab &E) {
     Stages<N, T, INV, 1>::run(s, E);
+}
+
+// Radix of the stage with stride Ns (the same sequence as Stages).
+template <int N, int T, int Ns>
+__host__ __device__ constexpr int stage_radix() {
+    return (SARBP_FFT_RADIX16 && Ns * 16 <= N && N / 16 >= T) ? 16 : (Ns * 8 <= N ? 8 : N / Ns);
+}
+
+// I/O-fused transform.  The first stage (stride 1) takes its inputs from
+// registers: butterfly j = threadIdx.x + b T (j < N / R) holds points
+// j + r N / R, r < R, in v[b][r] (FirstIn<N, T> gives R, the butterfly count
+// and the per-thread array shape), so the caller loads them straight from
+// global memory and shared memory is never filled in a pass of its own.  The
+// last stage hands its outputs to sink(x, value) instead of writing shared
+// memory back.  Two shared-memory passes and two barriers fewer than filling
+// s, fft_smem and reading s out.  s must not be in use by other threads'
+// reads when called (the first stage writes it without a barrier first).
+template <int N, int T>
+struct FirstIn {
+    static constexpr int R = stage_radix<N, T, 1>();
+    static constexpr int NB = N / R;
+    static constexpr int PER = (NB + T - 1) / T;
+    static_assert(R < N, "I/O-fused transforms need at least two stages");
+    __device__ __forceinline__ static bool live(int b) { return PER * T == NB || (int)threadIdx.x + b * T < NB; }
+    __device__ __forceinline__ static int point(int b, int r) { return (int)threadIdx.x + b * T + r * NB; }
+};
+
+template <int N, int T, bool INV, int Ns, class Sink>
+struct StagesTo {
+    __device__ __forceinline__ static void run(float2 *s, const Etab &E, Sink sink) {
+        constexpr int R = stage_radix<N, T, Ns>();
+        if constexpr (Ns * R == N) {
+            stage<N, R, T, INV, Ns, Sink>(s, E, sink);
+        } else {
+            stage<N, R, T, INV, Ns>(s, E);
+            StagesTo<N, T, INV, Ns * R, Sink>::run(s, E, sink);
+        }
+    }
+};
+
+template <int N, int T, bool INV, class Sink>
+__device__ void fft_io(float2 *s, const Etab &E, float2 (&v)[FirstIn<N, T>::PER][FirstIn<N, T>::R], Sink sink) {
+    using F = FirstIn<N, T>;
+    constexpr int R = F::R;
+#pragma unroll
+    for (int b = 0; b < F::PER; ++b) {
+        if (F::live(b)) {
+            const int j = (int)threadIdx.x + b * T;
+            Dft<R, INV>::run(v[b]);
+#pragma unroll
+            for (int r = 0; r < R; ++r) s[sw(j * R + r)] = v[b][r];  // stride 1: x0 = j R
+        }
+    }
+    __syncthreads();
+    StagesTo<N, T, INV, R, Sink>::run(s, E, sink);
 }
 
 // Shared memory after the N points: E low/high levels (slots through

@@ -63,18 +63,26 @@ __global__ void __launch_bounds__(T, (fft_min_blocks<N, T>())) rc_forward_kernel
     extern __shared__ float2 sm[];
     __shared__ float red[32];
     const int p = blockIdx.x;
-    const Etab E = load_etab<N, T>(sm, etab, L);
+    // first-stage inputs straight from the echo row (zero padding past ns),
+    // issued before the table loads so both latencies overlap
+    using F = FirstIn<N, T>;
+    float2 v[F::PER][F::R];
     const float2 *row = echo + (size_t)p * ns;
-    for (int i = threadIdx.x; i < N; i += T) sm[sw(i)] = i < ns ? __ldg(&row[i]) : make_float2(0.f, 0.f);
-    __syncthreads();
-    fft_smem<N, T, false>(sm, E);
+#pragma unroll
+    for (int b = 0; b < F::PER; ++b)
+#pragma unroll
+        for (int r = 0; r < F::R; ++r) {
+            const int i = F::point(b, r);
+            v[b][r] = (F::live(b) && i < ns) ? __ldg(&row[i]) : make_float2(0.f, 0.f);
+        }
+    const Etab E = load_etab<N, T>(sm, etab, L);  // the first stage's barrier publishes the W tables
     float2 *out = spec + (size_t)p * N;
     float acc = 0.f;
-    for (int k = threadIdx.x; k < N; k += T) {
-        float2 y = cmul(sm[sw(k)], __ldg(&filt[k]));
+    fft_io<N, T, false>(sm, E, v, [&](int k, float2 x) {
+        const float2 y = cmul(x, __ldg(&filt[k]));
         out[k] = y;
         acc += sqrtf(fmaf(y.x, y.x, y.y * y.y));
-    }
+    });
     const float bound = block_sum<T>(acc, red);
     if (threadIdx.x == 0 && scale) {
         // power-of-two scale so that stored FP16 magnitudes stay <= 2^14
@@ -95,48 +103,58 @@ __global__ void __launch_bounds__(T, (fft_min_blocks<N, T>())) rc_inverse_kernel
     const int r = blockIdx.x - p * L;
     const float2 *in = spec + (size_t)p * N;
     const int LN = L * N;
+    // first-stage inputs straight from the spectrum, issued before the tables
+    using F = FirstIn<N, T>;
+    float2 v[F::PER][F::R];
+#pragma unroll
+    for (int b = 0; b < F::PER; ++b)
+#pragma unroll
+        for (int q = 0; q < F::R; ++q)
+            v[b][q] = F::live(b) ? __ldg(&in[F::point(b, q)]) : make_float2(0.f, 0.f);
     const Etab E = load_etab<N, T>(sm, etab, L);
     // Ramp E^{kappa r}, kappa the signed frequency (MATLAB split floor((N+1)/2)
-    // = N/2 for even N).  With k = tid + T i and N/2 a multiple of T it factors
-    // into a per-thread E^{tid r} and a per-CTA table over i that also carries
-    // the E^{-N r} of the negative half (one broadcast read per point).
-    constexpr bool kTwoLevel = (N / 2) % T == 0 && N / T <= kRampMax;
+    // = N/2 for even N).  With k = tid + T i (every first-stage point of a
+    // thread is congruent to tid mod T when N / R is a multiple of T) and N/2 a
+    // multiple of T it factors into a per-thread E^{tid r} and a per-CTA table
+    // over i that also carries the E^{-N r} of the negative half.
+    constexpr bool kTwoLevel = (N / 2) % T == 0 && N / T <= kRampMax && F::NB % T == 0;
     float2 *rt = ramp_slots<N>(sm);
     float2 base = make_float2(1.f, 0.f);
     if (kTwoLevel && r != 0) {
         if (threadIdx.x < N / T) {
             const int i = threadIdx.x;
-            float2 v = E((T * i * r) & (LN - 1));
-            if (T * i >= N / 2) v = cmul(v, E((LN - N * r) & (LN - 1)));
-            rt[i] = v;
+            float2 w = E((T * i * r) & (LN - 1));
+            if (T * i >= N / 2) w = cmul(w, E((LN - N * r) & (LN - 1)));
+            rt[i] = w;
         }
         base = E((int)(threadIdx.x * r) & (LN - 1));
     }
     __syncthreads();
-    for (int k = threadIdx.x, i = 0; k < N; k += T, ++i) {
-        float2 y = __ldg(&in[k]);
-        if (r != 0) {
-            if (kTwoLevel) {
-                y = cmul(cmul(y, base), rt[i]);
-            } else {
-                const int kap = k < N / 2 ? k : k - N;
-                y = cmul(y, E((kap * r) & (LN - 1)));  // LN is a power of two
+    if (r != 0) {
+#pragma unroll
+        for (int b = 0; b < F::PER; ++b)
+#pragma unroll
+            for (int q = 0; q < F::R; ++q) {
+                const int k = F::point(b, q);
+                if (kTwoLevel) {
+                    v[b][q] = cmul(cmul(v[b][q], base), rt[k / T]);
+                } else {
+                    const int kap = k < N / 2 ? k : k - N;
+                    v[b][q] = cmul(v[b][q], E((kap * r) & (LN - 1)));  // LN is a power of two
+                }
             }
-        }
-        sm[sw(k)] = y;
     }
-    __syncthreads();
-    fft_smem<N, T, true>(sm, E);
     if (STORE == SARBP_STORE_C64) {
         float2 *o = reinterpret_cast<float2 *>(out) + (size_t)p * nbins + r;
-        for (int i = threadIdx.x; i < ns; i += T) o[(size_t)L * i] = sm[sw(i)];
+        fft_io<N, T, true>(sm, E, v, [&](int i, float2 x) {
+            if (i < ns) o[(size_t)L * i] = x;
+        });
     } else {
         const float inv = 1.f / __ldg(&scale[p]);  // exact: scale is a power of two
         __half2 *o = reinterpret_cast<__half2 *>(out) + (size_t)p * nbins + r;
-        for (int i = threadIdx.x; i < ns; i += T) {
-            float2 v = sm[sw(i)];
-            o[(size_t)L * i] = __floats2half2_rn(v.x * inv, v.y * inv);
-        }
+        fft_io<N, T, true>(sm, E, v, [&](int i, float2 x) {
+            if (i < ns) o[(size_t)L * i] = __floats2half2_rn(x.x * inv, x.y * inv);
+        });
     }
 }
 
