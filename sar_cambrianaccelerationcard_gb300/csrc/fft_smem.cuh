@@ -386,7 +386,7 @@ struct StagesTo {
 };
 
 template <int N, int T, bool INV, class Sink>
-__device__ void fft_io(float2 *s, const Etab &E, float2 (&v)[FirstIn<N, T>::PER][FirstIn<N, T>::R], Sink sink) {
+__device__ __forceinline__ void fft_io(float2 *s, const Etab &E, float2 (&v)[FirstIn<N, T>::PER][FirstIn<N, T>::R], Sink sink) {
     using F = FirstIn<N, T>;
     constexpr int R = F::R;
 #pragma unroll

@@ -170,31 +170,33 @@ __global__ void __launch_bounds__(T) rc_forward2_kernel(int ns, int L, const flo
     extern __shared__ float2 sm[];
     __shared__ float red[32];
     const int h = blockIdx.x & 1, p = blockIdx.x >> 1;
-    const Etab E = load_etab<M, T>(sm, etab, 2 * L);
+    const Etab E = load_etab<M, T>(sm, etab, 2 * L);  // E tables published by its barrier
     const float2 *row = echo + (size_t)p * ns;
-    for (int i = threadIdx.x; i < M; i += T) {
-        const float2 a = i < ns ? __ldg(&row[i]) : make_float2(0.f, 0.f);
-        const float2 b = i + M < ns ? __ldg(&row[i + M]) : make_float2(0.f, 0.f);
-        float2 v;
-        if (h == 0) {
-            v = cadd(a, b);
-        } else {
-            float2 w = E(L * i);  // W_N^i = conj(E^{L i})
-            w.y = -w.y;
-            v = cmul(csub(a, b), w);
+    using F = FirstIn<M, T>;
+    float2 v[F::PER][F::R];
+#pragma unroll
+    for (int b = 0; b < F::PER; ++b)
+#pragma unroll
+        for (int q = 0; q < F::R; ++q) {
+            const int i = F::point(b, q);
+            const float2 x0 = (F::live(b) && i < ns) ? __ldg(&row[i]) : make_float2(0.f, 0.f);
+            const float2 x1 = (F::live(b) && i + M < ns) ? __ldg(&row[i + M]) : make_float2(0.f, 0.f);
+            if (h == 0) {
+                v[b][q] = cadd(x0, x1);
+            } else {
+                float2 w = E(L * i);  // W_N^i = conj(E^{L i})
+                w.y = -w.y;
+                v[b][q] = cmul(csub(x0, x1), w);
+            }
         }
-        sm[sw(i)] = v;
-    }
-    __syncthreads();
-    fft_smem<M, T, false>(sm, E);
     float2 *out = spec + (size_t)p * (2 * M);
     float acc = 0.f;
-    for (int k = threadIdx.x; k < M; k += T) {
+    fft_io<M, T, false>(sm, E, v, [&](int k, float2 x) {
         const int idx = 2 * k + h;
-        const float2 y = cmul(sm[sw(k)], __ldg(&filt[idx]));
+        const float2 y = cmul(x, __ldg(&filt[idx]));
         out[idx] = y;
         acc += sqrtf(fmaf(y.x, y.x, y.y * y.y));
-    }
+    });
     const float bound = block_sum<T>(acc, red);
     if (threadIdx.x == 0) bound2[2 * p + h] = bound;
 }
@@ -212,19 +214,28 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(T)
     const int p = pr / L, r = pr - p * L;
     constexpr int N = 2 * M;
     const int LN = L * N;
-    const Etab E = load_etab<M, T>(sm, etab, 2 * L);
     const float2 *in = spec + (size_t)p * N;
-    for (int k = threadIdx.x; k < M; k += T) {
-        const int idx = 2 * k + h;
-        float2 y = __ldg(&in[idx]);
-        if (r != 0) {
-            const int kap = idx < N / 2 ? idx : idx - N;
-            y = cmul(y, E((kap * r) & (LN - 1)));  // LN is a power of two
-        }
-        sm[sw(k)] = y;
+    // first-stage inputs (bins 2k + h) straight into registers, issued before
+    // the table loads; the ramp needs the tables
+    using F = FirstIn<M, T>;
+    float2 v[F::PER][F::R];
+#pragma unroll
+    for (int b = 0; b < F::PER; ++b)
+#pragma unroll
+        for (int q = 0; q < F::R; ++q)
+            v[b][q] = F::live(b) ? __ldg(&in[2 * F::point(b, q) + h]) : make_float2(0.f, 0.f);
+    const Etab E = load_etab<M, T>(sm, etab, 2 * L);
+    if (r != 0) {  // the ramp reads only the E tables, published by load_etab's barrier
+#pragma unroll
+        for (int b = 0; b < F::PER; ++b)
+#pragma unroll
+            for (int q = 0; q < F::R; ++q) {
+                const int idx = 2 * F::point(b, q) + h;
+                const int kap = idx < N / 2 ? idx : idx - N;
+                v[b][q] = cmul(v[b][q], E((kap * r) & (LN - 1)));  // LN is a power of two
+            }
     }
-    __syncthreads();
-    fft_smem<M, T, true>(sm, E);
+    fft_io<M, T, true>(sm, E, v, SmemSink{});  // the partner reads the result from shared memory
     cluster.sync();  // both halves transformed
     const float2 *A = cluster.map_shared_rank(sm, 0);
     const float2 *B = cluster.map_shared_rank(sm, 1);

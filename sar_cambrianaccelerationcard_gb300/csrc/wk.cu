@@ -61,14 +61,29 @@ template <int N, int T, bool INV>
 __global__ void __launch_bounds__(T, (fft_min_blocks<N, T>())) dft_pow2_kernel(float2 *__restrict__ data, long long ld, float scale,
                                                      const float2 *__restrict__ etab, DftIo io) {
     extern __shared__ float2 sm[];
-    const Etab E = load_etab<N, T>(sm, etab, 1);
     float2 *row = data + (size_t)blockIdx.x * ld;
-    for (int i = threadIdx.x; i < N; i += T) sm[sw(i)] = dft_input(io, row, blockIdx.x, i);
-    __syncthreads();
-    fft_smem<N, T, INV>(sm, E);
-    for (int i = threadIdx.x; i < N; i += T) {
-        const float2 v = sm[sw(i)];
-        row[i] = make_float2(v.x * scale, v.y * scale);
+    if constexpr (stage_radix<N, T, 1>() == N) {  // one stage: through shared memory
+        const Etab E = load_etab<N, T>(sm, etab, 1);
+        for (int i = threadIdx.x; i < N; i += T) sm[sw(i)] = dft_input(io, row, blockIdx.x, i);
+        __syncthreads();
+        fft_smem<N, T, INV>(sm, E);
+        for (int i = threadIdx.x; i < N; i += T) {
+            const float2 v = sm[sw(i)];
+            row[i] = make_float2(v.x * scale, v.y * scale);
+        }
+        return;
+    } else {
+    // first-stage inputs straight from the row (read before any output is
+    // written: the last stage runs after every thread's loads)
+    using F = FirstIn<N, T>;
+    float2 v[F::PER][F::R];
+#pragma unroll
+    for (int b = 0; b < F::PER; ++b)
+#pragma unroll
+        for (int r = 0; r < F::R; ++r)
+            v[b][r] = F::live(b) ? dft_input(io, row, blockIdx.x, F::point(b, r)) : make_float2(0.f, 0.f);
+    const Etab E = load_etab<N, T>(sm, etab, 1);
+    fft_io<N, T, INV>(sm, E, v, [&](int i, float2 x) { row[i] = make_float2(x.x * scale, x.y * scale); });
     }
 }
 
@@ -83,27 +98,71 @@ __global__ void __launch_bounds__(T, (fft_min_blocks<M, T>())) dft_bluestein_ker
                                                           const float2 *__restrict__ chirp,
                                                           const float2 *__restrict__ kspec, DftIo io) {
     extern __shared__ float2 sm[];
-    const Etab E = load_etab<M, T>(sm, etab, 1);
     float2 *row = data + (size_t)blockIdx.x * ld;
-    for (int i = threadIdx.x; i < M; i += T) {
-        float2 v = make_float2(0.f, 0.f);
+    if constexpr (stage_radix<M, T, 1>() == M) {  // one stage: through shared memory
+        const Etab E = load_etab<M, T>(sm, etab, 1);
+        for (int i = threadIdx.x; i < M; i += T) {
+            float2 x = make_float2(0.f, 0.f);
+            if (i < n) {
+                float2 w = __ldg(&chirp[i]);
+                if (!INV) w.y = -w.y;
+                x = cmul(dft_input(io, row, blockIdx.x, i), w);
+            }
+            sm[sw(i)] = x;
+        }
+        __syncthreads();
+        fft_smem<M, T, false>(sm, E);
+        for (int i = threadIdx.x; i < M; i += T) sm[sw(i)] = cmul(sm[sw(i)], __ldg(&kspec[i]));
+        __syncthreads();
+        fft_smem<M, T, true>(sm, E);
+        for (int i = threadIdx.x; i < n; i += T) {
+            float2 w = __ldg(&chirp[i]);
+            if (!INV) w.y = -w.y;
+            const float2 y = cmul(sm[sw(i)], w);
+            row[i] = make_float2(y.x * scale, y.y * scale);
+        }
+        return;
+    } else {
+    using F = FirstIn<M, T>;
+    // tables first: with the chirped inputs live through the table loads the
+    // two-CTA register budget (64) spills
+    const Etab E = load_etab<M, T>(sm, etab, 1);
+    float2 v[F::PER][F::R];
+    // forward transform of the chirped row: inputs straight into registers
+#pragma unroll
+    for (int b = 0; b < F::PER; ++b)
+#pragma unroll
+        for (int r = 0; r < F::R; ++r) {
+            const int i = F::point(b, r);
+            float2 x = make_float2(0.f, 0.f);
+            if (F::live(b) && i < n) {
+                float2 w = __ldg(&chirp[i]);
+                if (!INV) w.y = -w.y;
+                x = cmul(dft_input(io, row, blockIdx.x, i), w);
+            }
+            v[b][r] = x;
+        }
+    fft_io<M, T, false>(sm, E, v, SmemSink{});
+    // times the kernel spectrum on the way into the inverse's first stage.
+    // At the two-CTA budget of 64 registers this keeps about 120 bytes per
+    // thread in (L1-resident) local memory; still faster than a separate
+    // multiply pass through shared memory: 1.080 vs 1.129 ms per omega-K image.
+#pragma unroll
+    for (int b = 0; b < F::PER; ++b)
+#pragma unroll
+        for (int r = 0; r < F::R; ++r) {
+            const int i = F::point(b, r);
+            v[b][r] = F::live(b) ? cmul(sm[sw(i)], __ldg(&kspec[i])) : make_float2(0.f, 0.f);
+        }
+    __syncthreads();  // every point read before the first stage overwrites it
+    fft_io<M, T, true>(sm, E, v, [&](int i, float2 x) {
         if (i < n) {
             float2 w = __ldg(&chirp[i]);
             if (!INV) w.y = -w.y;
-            v = cmul(dft_input(io, row, blockIdx.x, i), w);
+            const float2 y = cmul(x, w);
+            row[i] = make_float2(y.x * scale, y.y * scale);
         }
-        sm[sw(i)] = v;
-    }
-    __syncthreads();
-    fft_smem<M, T, false>(sm, E);
-    for (int i = threadIdx.x; i < M; i += T) sm[sw(i)] = cmul(sm[sw(i)], __ldg(&kspec[i]));
-    __syncthreads();
-    fft_smem<M, T, true>(sm, E);
-    for (int i = threadIdx.x; i < n; i += T) {
-        float2 w = __ldg(&chirp[i]);
-        if (!INV) w.y = -w.y;
-        const float2 v = cmul(sm[sw(i)], w);
-        row[i] = make_float2(v.x * scale, v.y * scale);
+    });
     }
 }
 
