@@ -266,11 +266,21 @@ def run_ours(args):
         ctx.check(ctx.lib.sarbp_backproject(ctx.h, sarbp.ctypes.byref(r), sarbp.ctypes.byref(view), apc_d.data_ptr(),
                                             sarbp.ctypes.byref(g), mode, img_d.data_ptr(), 0, sptr), "bp")
 
-    with torch.cuda.stream(stream):
+    # range compression: warm-up calls, then the mean of timed calls (events on
+    # the launching stream)
+    for _ in range(max(1, args.warmup)):
         rc_step()
     stream.synchronize()
     ctx.synchronize()
-    rc_ms = ctx.timings()[0]
+    rc_ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+    rc_reps = 5
+    rc_ev[0].record(stream)
+    for _ in range(rc_reps):
+        rc_step()
+    rc_ev[1].record(stream)
+    stream.synchronize()
+    ctx.synchronize()
+    rc_ms = rc_ev[0].elapsed_time(rc_ev[1]) / rc_reps
 
     # --- device-resident timing of back-projection
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -380,6 +390,14 @@ def run_ours(args):
                    "unit": "GB/s", "frac": (rc_bytes / (rc_ms * 1e-3) / 1e9 / hbm) if (rc_ms and hbm) else None,
                    "traffic": MEASURED_TRAFFIC.get((args.size, args.mode), {}).get("rc"),
                    "kernel": "rc_forward + rc_inverse", "ms": rc_ms}
+    # the transforms themselves: 1 forward + L inverse nfft-point FFTs per pulse at
+    # 5 N log2 N flops each, against the live FP32 FMA rate (2 flops per lane)
+    fft_flops = scene.np_ * (1 + scene.radar.upsample) * 5.0 * lay.nfft * math.log2(lay.nfft)
+    if rc_ms:
+        roofline_rc["fft_flops"] = fft_flops
+        roofline_rc["fft_tflops"] = fft_flops / (rc_ms * 1e-3) / 1e12
+        if not args.no_probe:
+            roofline_rc["fft_frac_of_fp32"] = roofline_rc["fft_tflops"] * 1e12 / (2.0 * fp32_rate)
 
     cpu = None
     if rank == 0 and not args.no_cpu:
