@@ -363,6 +363,11 @@ typedef struct sarbp_server_config {
     uint64_t hbm_budget_bytes;  /* device memory the server may hold for jobs */
     int32_t pulses_per_step;    /* pulses per job per step (multiple of 16); 0: 512 */
     int32_t use_graphs;         /* 1: capture each step's launches in a CUDA graph; 0: plain streams */
+    uint64_t step_updates;      /* 0: every job advances pulses_per_step pulses per step.  Else each
+                                   job advances about step_updates / (nx ny) pulses per step (a
+                                   multiple of 16, at least 16, at most all of them), so a step
+                                   costs every job about the same and small jobs finish in few
+                                   steps instead of waiting out a large neighbour's cadence */
 } sarbp_server_config;
 
 typedef struct sarbp_job {

@@ -13,9 +13,10 @@
 //     the echo and APC track are uploaded and the echo is range-compressed
 //     into the job's resident buffer; the job joins the steps once that work
 //     has completed;
-//   * steps (worker): each step back-projects the next pulses_per_step pulses
-//     of every admitted job into its resident image (accumulate after the
-//     first step).  The step's launches are captured into one CUDA graph with
+//   * steps (worker): each step back-projects the next pulses of every
+//     admitted job into its resident image (accumulate after the first step):
+//     pulses_per_step for every job, or with step_updates set a per-job count
+//     of about step_updates / (nx ny), fixed at submit.  The step's launches are captured into one CUDA graph with
 //     a branch per job on its own lane stream, so jobs overlap on the device;
 //     at most two steps are in flight;
 //   * completion: after a job's last step its image is copied back on a
@@ -70,6 +71,7 @@ struct Job {
     unsigned *d_err = nullptr;
     unsigned *h_err = nullptr;     // pinned copy of the job's device check word
     int lane = -1;
+    int pps = 0;                   // pulses this job advances per step
     int next_pulse = 0;
     int steps = 0;
     cudaEvent_t done_ev = nullptr;
@@ -301,7 +303,6 @@ void worker_main(sarbp_server *S) {
                 lk.lock();
                 S->step_pending[par] = false;
             }
-            const int pps = S->cfg.pulses_per_step;
             cudaError_t e = cudaSuccess;
             const bool graph = S->cfg.use_graphs != 0;
             cudaGraph_t g = nullptr;
@@ -310,7 +311,7 @@ void worker_main(sarbp_server *S) {
             for (Job *j : step) {
                 if (e != cudaSuccess) break;
                 cudaStream_t ls = S->lanes[j->lane];
-                const int p0 = j->next_pulse, p1 = std::min(j->desc.np, p0 + pps);
+                const int p0 = j->next_pulse, p1 = std::min(j->desc.np, p0 + j->pps);
                 e = cudaStreamWaitEvent(ls, S->fork, 0);
                 if (e == cudaSuccess) e = launch_step(j, p0, p1, ls);
                 if (e == cudaSuccess) e = cudaEventRecord(S->join[j->lane], ls);
@@ -346,7 +347,7 @@ void worker_main(sarbp_server *S) {
                     continue;
                 }
                 j->steps++;
-                j->next_pulse = std::min(j->desc.np, j->next_pulse + pps);
+                j->next_pulse = std::min(j->desc.np, j->next_pulse + j->pps);
                 if (j->next_pulse >= j->desc.np) {  // last step: copy the image back on the download stream
                     const size_t npix = (size_t)j->desc.grid.nx * j->desc.grid.ny;
                     cudaError_t ce = waited ? cudaSuccess : cudaStreamWaitEvent(S->sd, S->step_ev[par], 0);
@@ -524,7 +525,14 @@ sarbp_status sarbp_server_submit(sarbp_server *S, const sarbp_job *job, uint64_t
     std::string why;
     sarbp::BpExtremes ex;
     sarbp::bp_extremes_host(d.apc, d.np, d.grid, ex);  // same bits as the one-shot calls' device reduction
-    if (!sarbp::plan_bp(S->sms, d.radar, v, ex, d.np, d.grid, d.mode, S->cfg.pulses_per_step, j->plan, why)) {
+    j->pps = S->cfg.pulses_per_step;
+    if (S->cfg.step_updates > 0) {  // about step_updates pixel*pulse updates per step
+        const double px = (double)d.grid.nx * d.grid.ny;
+        const double want = std::floor((double)S->cfg.step_updates / px / 16.0) * 16.0;
+        const int all = (d.np + 15) / 16 * 16;
+        j->pps = (int)std::max(16.0, std::min((double)all, want));
+    }
+    if (!sarbp::plan_bp(S->sms, d.radar, v, ex, d.np, d.grid, d.mode, j->pps, j->plan, why)) {
         delete j;
         return SARBP_ERR_UNSUPPORTED;
     }

@@ -116,7 +116,8 @@ class Target(ctypes.Structure):
 
 class ServerConfig(ctypes.Structure):
     _fields_ = [("device", ctypes.c_int32), ("max_jobs", ctypes.c_int32), ("hbm_budget_bytes", ctypes.c_uint64),
-                ("pulses_per_step", ctypes.c_int32), ("use_graphs", ctypes.c_int32)]
+                ("pulses_per_step", ctypes.c_int32), ("use_graphs", ctypes.c_int32),
+                ("step_updates", ctypes.c_uint64)]
 
 
 class Job(ctypes.Structure):
@@ -518,9 +519,9 @@ class Server:
     """Continuous-batching imaging service (sarbp_server_* in include/sarbp.h)."""
 
     def __init__(self, device: int = 0, max_jobs: int = 16, hbm_budget_bytes: int = 64 << 30,
-                 pulses_per_step: int = 512, use_graphs: bool = True):
+                 pulses_per_step: int = 512, use_graphs: bool = True, step_updates: int = 0):
         self.lib = load()
-        cfg = ServerConfig(device, max_jobs, hbm_budget_bytes, pulses_per_step, int(use_graphs))
+        cfg = ServerConfig(device, max_jobs, hbm_budget_bytes, pulses_per_step, int(use_graphs), int(step_updates))
         h = ctypes.c_void_p()
         st = self.lib.sarbp_server_create(ctypes.byref(h), ctypes.byref(cfg))
         if st != OK:

@@ -114,3 +114,23 @@ def test_cancel_and_poll(jobs):
         assert st_a == sarbp.OK
         assert st_b in (sarbp.OK, sarbp.ERR_CANCELLED)
         assert srv.poll(a) == sarbp.ERR_INVALID_ARGUMENT  # released by wait
+
+
+def test_work_proportional_steps(jobs):
+    """step_updates = 2^31: a 512^2 job of 1024 pulses takes one step, a
+    2048^2 job of 2048 pulses advances 512 pulses per step (four steps); each
+    image is the same alone and in the mix and matches its one-shot image."""
+    s4, e4, ref4 = jobs[4]  # 1024 pulses, 512^2
+    s1, e1, ref1 = jobs[1]  # 2048 pulses, 2048^2
+    with sarbp.Server(0, max_jobs=8, hbm_budget_bytes=8 << 30, step_updates=1 << 31) as srv:
+        st, stats, alone = wait(srv, submit(srv, s4, e4))
+        assert st == sarbp.OK and stats.steps == 1
+        t1 = submit(srv, s1, e1)
+        t4 = submit(srv, s4, e4)
+        st1, stats1, img1 = wait(srv, t1)
+        st4, stats4, mixed = wait(srv, t4)
+        assert st1 == sarbp.OK and st4 == sarbp.OK
+        assert stats1.steps == 4 and stats4.steps == 1
+    assert np.array_equal(alone, mixed)
+    assert metrics.rel_l2_db(alone, ref4) <= -100.0
+    assert metrics.rel_l2_db(img1, ref1) <= -100.0
