@@ -263,7 +263,9 @@ __device__ __forceinline__ void stolt_taps(const float2 *sm, const float *sdelta
                 w = 1.f;
             } else {
                 const float s = (idx == t) ? (((fl - idx) & 1) ? -s0 : s0) : sinpif(u);
-                w = s / (3.14159265358979323846f * u);
+                // |pi u| is in [1e-7, 10): the reciprocal-based quotient (<= 2 ulp)
+                // is far inside the stage's FP32 error
+                w = __fdividef(s, 3.14159265358979323846f * u);
             }
             const float2 v = sm[idx];
             acc.x = fmaf(w, v.x, acc.x);
