@@ -256,7 +256,11 @@ sarbp_status sarbp_autofocus(sarbp_ctx *ctx, const sarbp_radar *radar,
 
 /* The SAR_BP entry point: echo + APC track + radar + grid in, complex image out.
  * Range compression (storage chosen by mode) followed by back-projection
- * (SAR_Processor::processImage + applyBPAlgorithm, BPA_CUDA.cpp:70-90). */
+ * (SAR_Processor::processImage + applyBPAlgorithm, BPA_CUDA.cpp:70-90).
+ * Each buffer may be host or device memory.  A host echo is uploaded in pulse
+ * chunks overlapped with range compression; a pinned host image (cudaHostAlloc,
+ * cudaMallocHost) is written by the kernels directly, pageable images are
+ * downloaded at the end.  Host buffers make the call synchronous. */
 sarbp_status sarbp_image(sarbp_ctx *ctx, const sarbp_radar *radar,
                          const sarbp_complex64 *echo, int32_t np, int32_t ns,
                          const double *apc, const sarbp_grid *grid, int32_t mode,

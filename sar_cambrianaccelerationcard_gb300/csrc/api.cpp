@@ -145,6 +145,19 @@ bool is_device_ptr(const void *p) {
     return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
 }
 
+// Device address of pinned, mapped host memory (cudaHostAlloc / cudaMallocHost,
+// torch pin_memory), or nullptr for pageable or device memory.  Kernels can
+// write results there directly (NVLink-C2C on GB300), so no download follows.
+void *mapped_host_ptr(const void *p) {
+    if (!p) return nullptr;
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    return a.type == cudaMemoryTypeHost ? a.devicePointer : nullptr;
+}
+
 bool is_pow2(long long n) { return n > 0 && (n & (n - 1)) == 0; }
 
 long long next_pow2(long long n) {
@@ -1227,7 +1240,12 @@ sarbp_status sarbp_image(sarbp_ctx *ctx, const sarbp_radar *radar, const sarbp_c
     any_host = any_host || host_echo;
     float2 *d_img = reinterpret_cast<float2 *>(image);
     const bool dev_img = is_device_ptr(image);
-    if (!dev_img) {
+    // a pinned host image is written by the back-projection itself (no download)
+    float2 *mapped_img = dev_img ? nullptr : static_cast<float2 *>(mapped_host_ptr(image));
+    if (mapped_img) {
+        d_img = mapped_img;
+        any_host = true;
+    } else if (!dev_img) {
         SARBP_CUDA(ctx, ctx->image.ensure(sizeof(float2) * npix), "alloc image");
         d_img = ctx->image.as<float2>();
         any_host = true;
@@ -1253,7 +1271,7 @@ sarbp_status sarbp_image(sarbp_ctx *ctx, const sarbp_radar *radar, const sarbp_c
     }
     st = bp_device(ctx, radar, v, apc_dev, ex, grid, mode, d_img, 0, s);
     if (st != SARBP_OK) return st;
-    if (!dev_img)
+    if (!dev_img && !mapped_img)
         SARBP_CUDA(ctx, cudaMemcpyAsync(image, d_img, sizeof(float2) * npix, cudaMemcpyDeviceToHost, s), "download image");
     return finish(ctx, s, any_host);
 }

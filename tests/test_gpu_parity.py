@@ -262,3 +262,21 @@ def test_chunked_host_upload_is_bit_exact(ctx, storage):
                                   sarbp.ctypes.byref(g), mode, img_dev.data_ptr(), None), "image device")
     ctx.synchronize()
     assert np.array_equal(img_dev.cpu().numpy().view(np.complex64), img_host)
+
+
+def test_pinned_host_image_written_in_place(ctx, c1):
+    """A pinned (device-mapped) host image is written by the back-projection
+    itself, with no download: same bits as the device-buffer path; with no
+    pulses the image is cleared."""
+    torch = pytest.importorskip("torch")
+    s = c1["scene"]
+    r, g, lay = sarbp.scene_args(s)
+    ref = sarbp.image_scene(ctx, s, c1["echo"], sarbp.MODE_SPLIT)  # pageable: downloaded
+    pinned = torch.full((g.ny, g.nx * 2), 7.0, dtype=torch.float32, pin_memory=True)
+    echo = torch.from_numpy(c1["echo"].view(np.float32)).pin_memory()
+    ctx.check(ctx.lib.sarbp_image(ctx.h, sarbp.ctypes.byref(r), echo.data_ptr(), s.np_, s.ns, s.apc.ctypes.data,
+                                  sarbp.ctypes.byref(g), sarbp.MODE_SPLIT, pinned.data_ptr(), None), "image pinned")
+    assert np.array_equal(pinned.numpy().view(np.complex64), ref)
+    ctx.check(ctx.lib.sarbp_image(ctx.h, sarbp.ctypes.byref(r), echo.data_ptr(), 0, s.ns, s.apc.ctypes.data,
+                                  sarbp.ctypes.byref(g), sarbp.MODE_SPLIT, pinned.data_ptr(), None), "image np=0")
+    assert not pinned.numpy().any()
