@@ -345,8 +345,9 @@ __device__ __forceinline__ void produce(const BpPlan &P, const Smem &S, int stag
 }
 
 // raw window -> (mid, diff) pairs; bins outside [lo, hi) read as zero.
+// Flat over (pulse, bin), used for complex64 rows.
 template <int MODE, int STORE>
-__device__ __forceinline__ void convert(const Smem &S, int stage, int sbuf, int count, int win, unsigned win_magic,
+__device__ __forceinline__ void convert_flat(const Smem &S, int stage, int sbuf, int count, int win, unsigned win_magic,
                                         int chunk) {
     const int total = count * win;
     float4 *st = S.staged + (size_t)sbuf * chunk * win;
@@ -374,6 +375,57 @@ __device__ __forceinline__ void convert(const Smem &S, int stage, int sbuf, int 
         const float o = MODE == SARBP_MODE_FP64 ? 0.f : (float)(i - (win >> 1));
         st[e] = make_float4(fmaf(-o, dx, 0.5f * (a.x + b.x)), fmaf(-o, dy, 0.5f * (a.y + b.y)), dx, dy);
     }
+}
+
+// The same with one warp per pulse (pulse-uniform bounds and scale, lane =
+// bin) and an unconditional path when the whole window was copied (every pulse
+// but those at the swath edges), used for complex16 rows.
+template <int MODE, int STORE>
+__device__ __forceinline__ void convert_warp(const Smem &S, int stage, int sbuf, int count, int win, int chunk) {
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int cen = win >> 1;
+    float4 *stb = S.staged + (size_t)sbuf * chunk * win;
+    for (int pl = warp; pl < count; pl += kWarps) {
+        const Prm &q = S.prm[stage * kChunk + pl];
+        const int lo = q.lo, hi = q.hi;
+        const float sc = STORE == SARBP_STORE_C32H ? q.scale : 1.f;
+        const unsigned char *rw = S.raw + ((size_t)stage * chunk + pl) * win * raw_esize(STORE);
+        float4 *st = stb + (size_t)pl * win;
+        const bool whole = lo == 0 && hi == win;
+        for (int i = lane; i < win; i += 32) {
+            float2 a = make_float2(0.f, 0.f), b = make_float2(0.f, 0.f);
+            const bool ina = whole || (i >= lo && i < hi);
+            const bool inb = whole ? i + 1 < win : (i + 1 >= lo && i + 1 < hi);
+            if (STORE == SARBP_STORE_C64) {
+                const float2 *r = reinterpret_cast<const float2 *>(rw);
+                if (ina) a = r[i];
+                if (inb) b = r[i + 1];
+            } else {
+                const __half2 *r = reinterpret_cast<const __half2 *>(rw);
+                if (ina) a = __half22float2(r[i]);
+                if (inb) b = __half22float2(r[i + 1]);
+                a.x *= sc; a.y *= sc; b.x *= sc; b.y *= sc;
+            }
+            const float dx = b.x - a.x, dy = b.y - a.y;
+            // FP32 arithmetic: pairs centred on the window middle, so that s = M + b d
+            // takes the centred position b directly; FP64 keeps (mid, diff).
+            const float o = MODE == SARBP_MODE_FP64 ? 0.f : (float)(i - cen);
+            st[i] = make_float4(fmaf(-o, dx, 0.5f * (a.x + b.x)), fmaf(-o, dy, 0.5f * (a.y + b.y)), dx, dy);
+        }
+    }
+}
+
+// Measured per storage on config 2 (Gupd/s, flat / warp-per-pulse): complex64
+// 1275.7 / 1241.5, complex16 1231.5 / 1244.8.  The pass itself is ~6% of the
+// kernel (3.1 ms of 53.9 without it), but its code shape moves the schedule
+// of the main loop more than its own cost.
+template <int MODE, int STORE>
+__device__ __forceinline__ void convert(const Smem &S, int stage, int sbuf, int count, int win, unsigned win_magic,
+                                        int chunk) {
+    if constexpr (STORE == SARBP_STORE_C32H)
+        convert_warp<MODE, STORE>(S, stage, sbuf, count, win, chunk);
+    else
+        convert_flat<MODE, STORE>(S, stage, sbuf, count, win, win_magic, chunk);
 }
 
 // Sum of the warps' projections for the pulses of one chunk into
