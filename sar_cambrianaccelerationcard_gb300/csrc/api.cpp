@@ -19,6 +19,8 @@
 #include <string>
 #include <vector>
 
+#include <nvtx3/nvToolsExt.h>
+
 #include "sarbp_internal.h"
 
 using sarbp::BpPlan;
@@ -158,6 +160,15 @@ void *mapped_host_ptr(const void *p) {
     return a.type == cudaMemoryTypeHost ? a.devicePointer : nullptr;
 }
 
+// NVTX range for the duration of a scope (header-only NVTX v3: a no-op
+// unless a profiler is attached), naming each stage of a call on the timeline.
+struct Range {
+    explicit Range(const char *name) { nvtxRangePushA(name); }
+    ~Range() { nvtxRangePop(); }
+    Range(const Range &) = delete;
+    Range &operator=(const Range &) = delete;
+};
+
 bool is_pow2(long long n) { return n > 0 && (n & (n - 1)) == 0; }
 
 long long next_pow2(long long n) {
@@ -252,6 +263,7 @@ sarbp_status finish(sarbp_ctx *ctx, cudaStream_t s, bool sync) {
 sarbp_status rc_device(sarbp_ctx *ctx, const sarbp_radar *r, const sarbp_rc_layout &lay, const float2 *echo,
                        int np, int ns, int storage, void *rc_out, float *scale_out, cudaStream_t s,
                        bool record_events = true) {
+    Range range("sarbp: range compression");
     if (!sarbp::rc_size_supported(lay.nfft))
         return fail(ctx, SARBP_ERR_UNSUPPORTED, "range FFT size %d not supported (max 32768: ns + tp*fs - 1 <= 32768)",
                     lay.nfft);
@@ -299,6 +311,7 @@ sarbp_status rc_device(sarbp_ctx *ctx, const sarbp_radar *r, const sarbp_rc_layo
 // context's echo buffer).
 sarbp_status rc_host_echo(sarbp_ctx *ctx, const sarbp_radar *r, const sarbp_rc_layout &lay, const sarbp_complex64 *echo,
                           int np, int ns, int storage, void *rc_out, float *scale_out, cudaStream_t s) {
+    Range range("sarbp: chunked echo upload + range compression");
     SARBP_CUDA(ctx, ctx->echo.ensure(sizeof(float2) * (size_t)np * ns), "alloc echo");
     float2 *d_echo = ctx->echo.as<float2>();
     const size_t row = sizeof(float2) * (size_t)ns;
@@ -340,6 +353,7 @@ sarbp_status check_grid(sarbp_ctx *ctx, const sarbp_grid *g) {
 // a wait for its 40-byte result only.  Fails on a non-finite APC coordinate.
 sarbp_status extremes_device(sarbp_ctx *ctx, const double *apc_dev, int np, const sarbp_grid *g, cudaStream_t s,
                              sarbp::BpExtremes &e) {
+    Range range("sarbp: planning extremes");
     SARBP_CUDA(ctx, sarbp::launch_bp_extremes(apc_dev, np, *g, ctx->ext.as<unsigned long long>(), s),
                "planning extremes");
     ctx->launches += np > 0 ? 2 : 1;
@@ -362,6 +376,7 @@ sarbp_status extremes_device(sarbp_ctx *ctx, const double *apc_dev, int np, cons
 sarbp_status bp_device(sarbp_ctx *ctx, const sarbp_radar *r, const sarbp_rc_view &rc, const double *apc_dev,
                        const sarbp::BpExtremes &ex, const sarbp_grid *g, int mode, float2 *image, int accumulate,
                        cudaStream_t s, const double *dr_dev = nullptr, const double *dph_dev = nullptr) {
+    Range range("sarbp: back-projection");
     const int np = rc.np;
     if (g->nx == 0 || g->ny == 0) return SARBP_OK;
     if (np == 0) {
@@ -406,6 +421,7 @@ sarbp_status bp_device(sarbp_ctx *ctx, const sarbp_radar *r, const sarbp_rc_view
 sarbp_status project_device(sarbp_ctx *ctx, const sarbp_radar *r, const sarbp_rc_view &rc, const double *apc_dev,
                             const sarbp::BpExtremes &ex, const sarbp_grid *g, int mode, const float2 *weight,
                             double2 *out, cudaStream_t s, const double *dr_dev, const double *dph_dev) {
+    Range range("sarbp: weighted projection");
     const int np = rc.np;
     if (np == 0) return SARBP_OK;
     if (rc.nbins % 4 != 0) return fail(ctx, SARBP_ERR_UNSUPPORTED, "nbins must be a multiple of 4");
@@ -872,6 +888,7 @@ sarbp_status sarbp_autofocus(sarbp_ctx *ctx, const sarbp_radar *radar, const sar
                              const sarbp_grid *grid, int32_t mode, int32_t iterations, const double *drange,
                              double *dphase, sarbp_complex64 *image, double *sharpness, void *stream) {
     if (!ctx) return SARBP_ERR_INVALID_ARGUMENT;
+    Range range("sarbp_autofocus");
     ctx->err.clear();
     cudaSetDevice(ctx->device);
     if (mode != SARBP_MODE_SPLIT && mode != SARBP_MODE_FP16STORE)
@@ -959,6 +976,7 @@ sarbp_status sarbp_wk_padded_size(int32_t na, int32_t nr, int32_t *na_pad, int32
 
 sarbp_status sarbp_dft(sarbp_ctx *ctx, sarbp_complex64 *data, int32_t rows, int32_t n, int32_t inverse, void *stream) {
     if (!ctx) return SARBP_ERR_INVALID_ARGUMENT;
+    Range range("sarbp_dft");
     ctx->err.clear();
     cudaSetDevice(ctx->device);
     if (rows < 0 || n < 1) return fail(ctx, SARBP_ERR_INVALID_ARGUMENT, "rows must be >= 0 and n >= 1");
@@ -987,6 +1005,7 @@ sarbp_status sarbp_wk_image(sarbp_ctx *ctx, const sarbp_wk_params *w, const sarb
                             int32_t nr, sarbp_complex64 *image, void *stream) {
     constexpr double kPi = 3.14159265358979323846;
     if (!ctx) return SARBP_ERR_INVALID_ARGUMENT;
+    Range range("sarbp_wk_image");
     ctx->err.clear();
     cudaSetDevice(ctx->device);
     if (!w) return fail(ctx, SARBP_ERR_INVALID_ARGUMENT, "params is null");
@@ -1117,6 +1136,7 @@ sarbp_status sarbp_ceos_decode(sarbp_ctx *ctx, const uint8_t *raw, uint64_t raw_
                                int32_t ncells, int32_t apply_agc, sarbp_complex64 *echo, int16_t *agc_db,
                                void *stream) {
     if (!ctx) return SARBP_ERR_INVALID_ARGUMENT;
+    Range range("sarbp_ceos_decode");
     ctx->err.clear();
     cudaSetDevice(ctx->device);
     if (!l) return fail(ctx, SARBP_ERR_INVALID_ARGUMENT, "layout is null");
@@ -1203,6 +1223,7 @@ sarbp_status sarbp_image(sarbp_ctx *ctx, const sarbp_radar *radar, const sarbp_c
                          int32_t ns, const double *apc, const sarbp_grid *grid, int32_t mode, sarbp_complex64 *image,
                          void *stream) {
     if (!ctx) return SARBP_ERR_INVALID_ARGUMENT;
+    Range range("sarbp_image");
     ctx->err.clear();
     cudaSetDevice(ctx->device);
     sarbp_rc_layout lay;

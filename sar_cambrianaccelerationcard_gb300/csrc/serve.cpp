@@ -30,6 +30,7 @@
 #include <chrono>
 #include <cmath>
 #include <condition_variable>
+#include <cstdlib>
 #include <cstring>
 #include <deque>
 #include <map>
@@ -112,6 +113,7 @@ struct sarbp_server {
     sarbp_server_stats st{};
     Clock::time_point busy_since;
     bool busy = false;
+    uint64_t fail_admit_ticket = 0;       // SARBP_SERVE_FAIL_ADMIT: host-side fault injection (tests)
 };
 
 namespace {
@@ -145,6 +147,8 @@ size_t job_bytes(const Job &j) {
 // Enqueue admission work for j on the admission stream: carve buffers, upload,
 // range-compress, then record the job's ready event.
 sarbp_status admit(sarbp_server *S, Job *j) {
+    // injected on the host, as a refused allocation would be: no device work
+    if (S->fail_admit_ticket != 0 && j->id == S->fail_admit_ticket) return SARBP_ERR_OUT_OF_MEMORY;
     cudaError_t e = cudaMallocAsync((void **)&j->dev, j->bytes, S->sa);
     if (e != cudaSuccess) {
         cudaGetLastError();
@@ -422,6 +426,7 @@ sarbp_status sarbp_server_create(sarbp_server **out, const sarbp_server_config *
     sarbp_server *S = new sarbp_server();
     S->cfg = *cfg;
     if (S->cfg.pulses_per_step == 0) S->cfg.pulses_per_step = 512;
+    if (const char *f = std::getenv("SARBP_SERVE_FAIL_ADMIT")) S->fail_admit_ticket = std::strtoull(f, nullptr, 10);
     S->sms = prop.multiProcessorCount;
     bool ok = cudaStreamCreateWithFlags(&S->s0, cudaStreamNonBlocking) == cudaSuccess &&
               cudaStreamCreateWithFlags(&S->sa, cudaStreamNonBlocking) == cudaSuccess &&
@@ -503,6 +508,10 @@ sarbp_status sarbp_server_submit(sarbp_server *S, const sarbp_job *job, uint64_t
         return SARBP_ERR_INVALID_ARGUMENT;
     for (size_t i = 0; i < (size_t)3 * d.np; ++i)
         if (!std::isfinite(d.apc[i])) return SARBP_ERR_INVALID_ARGUMENT;
+    for (int i = 0; i < 3; ++i)
+        if (!std::isfinite(d.grid.origin[i]) || !std::isfinite(d.grid.ux[i]) || !std::isfinite(d.grid.uy[i]))
+            return SARBP_ERR_INVALID_ARGUMENT;
+    if ((long long)d.grid.nx * d.grid.ny > (1LL << 31)) return SARBP_ERR_INVALID_ARGUMENT;
     Job *j = new Job();
     j->desc = d;
     sarbp_status st = sarbp_rc_layout_get(&d.radar, d.ns, &j->lay);

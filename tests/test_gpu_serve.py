@@ -134,3 +134,50 @@ def test_work_proportional_steps(jobs):
     assert np.array_equal(alone, mixed)
     assert metrics.rel_l2_db(alone, ref4) <= -100.0
     assert metrics.rel_l2_db(img1, ref1) <= -100.0
+
+
+def test_malformed_requests_rejected_at_submit(jobs):
+    """Requests the server cannot run are refused at submit with a status (no
+    device work); the server keeps serving."""
+    s0, e0, ref0 = jobs[4]
+    r, g, _ = sarbp.scene_args(s0)
+    with sarbp.Server(0, max_jobs=4, hbm_budget_bytes=4 << 30) as srv:
+        with pytest.raises(sarbp.SarbpError) as ex:
+            srv.submit(r, g, e0, s0.apc, sarbp.MODE_FP64)  # the server runs SPLIT / FP16STORE
+        assert ex.value.status == sarbp.ERR_UNSUPPORTED
+        bad = s0.apc.copy()
+        bad[3, 0] = np.nan
+        with pytest.raises(sarbp.SarbpError) as ex:
+            srv.submit(r, g, e0, bad)
+        assert ex.value.status == sarbp.ERR_INVALID_ARGUMENT
+        gb = sarbp.scene_args(s0)[1]
+        gb.origin[1] = float("inf")
+        with pytest.raises(sarbp.SarbpError) as ex:
+            srv.submit(r, gb, e0, s0.apc)
+        assert ex.value.status == sarbp.ERR_INVALID_ARGUMENT
+        long_echo = np.zeros((16, 40000), dtype=np.complex64)  # range FFT above 32768 points
+        with pytest.raises(sarbp.SarbpError) as ex:
+            srv.submit(r, g, long_echo, s0.apc[:16])
+        assert ex.value.status == sarbp.ERR_UNSUPPORTED
+        st, _, img = wait(srv, submit(srv, s0, e0))
+        assert st == sarbp.OK
+        assert metrics.rel_l2_db(img, ref0) <= -100.0
+        assert srv.stats().submitted == 1
+
+
+def test_injected_admission_failure(jobs, monkeypatch):
+    """A refused device allocation at admission (injected on the host for
+    ticket 2) fails that job with SARBP_ERR_OUT_OF_MEMORY; the jobs before and
+    after it complete with their one-shot images."""
+    monkeypatch.setenv("SARBP_SERVE_FAIL_ADMIT", "2")
+    s0, e0, ref0 = jobs[4]
+    with sarbp.Server(0, max_jobs=4, hbm_budget_bytes=4 << 30) as srv:
+        t = [submit(srv, s0, e0) for _ in range(3)]
+        assert t[1] == 2
+        res = [srv.wait(x, 120000) for x in t]
+        assert res[0][0] == sarbp.OK and res[2][0] == sarbp.OK
+        assert res[1][0] == sarbp.ERR_OUT_OF_MEMORY
+        for k in (0, 2):
+            assert metrics.rel_l2_db(res[k][2], ref0) <= -100.0
+        st = srv.stats()
+        assert st.failed == 1 and st.completed == 2
