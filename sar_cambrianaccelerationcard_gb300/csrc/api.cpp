@@ -1108,9 +1108,16 @@ sarbp_status sarbp_wk_image(sarbp_ctx *ctx, const sarbp_wk_params *w, const sarb
     io.col0 = pr;
     io.rowmul = d_rowphase + pa;
     SARBP_CUDA(ctx, sarbp::launch_dft_rows(pr_plan, A + (size_t)pa * NR, na, NR, false, 1.0f, s, io), "range FFT");
-    SARBP_CUDA(ctx, sarbp::launch_transpose(A, B, NA, NR, s), "transpose");
-    SARBP_CUDA(ctx, sarbp::launch_dft_rows(pa_plan, B, NR, NA, false, 1.0f, s), "azimuth FFT");
-    SARBP_CUDA(ctx, sarbp::launch_transpose(B, A, NR, NA, s), "transpose");
+    // azimuth transforms: down the columns in place (power-of-two lengths up to
+    // 4096), else through transposes
+    const bool cols = sarbp::dft_cols_supported(pa_plan);
+    if (cols) {
+        SARBP_CUDA(ctx, sarbp::launch_dft_cols(pa_plan, A, A, NR, false, 1.0f, s), "azimuth FFT");
+    } else {
+        SARBP_CUDA(ctx, sarbp::launch_transpose(A, B, NA, NR, s), "transpose");
+        SARBP_CUDA(ctx, sarbp::launch_dft_rows(pa_plan, B, NR, NA, false, 1.0f, s), "azimuth FFT");
+        SARBP_CUDA(ctx, sarbp::launch_transpose(B, A, NR, NA, s), "transpose");
+    }
     if (ff_stolt)
         SARBP_CUDA(ctx, sarbp::launch_wk_stolt_ff(A, B, NA, NR, d_colc, d_colip, d_rowq, a4r, NR / w->fr, w->taps, s),
                    "reference-function multiply and Stolt mapping");
@@ -1119,13 +1126,17 @@ sarbp_status sarbp_wk_image(sarbp_ctx *ctx, const sarbp_wk_params *w, const sarb
                                                 w->f0, NR / w->fr, w->taps, s),
                    "reference-function multiply and Stolt mapping");
     SARBP_CUDA(ctx, sarbp::launch_dft_rows(pr_plan, B, NA, NR, true, 1.0f / (float)NR, s), "range IFFT");
-    SARBP_CUDA(ctx, sarbp::launch_transpose(B, A, NA, NR, s), "transpose");
-    SARBP_CUDA(ctx, sarbp::launch_dft_rows(pa_plan, A, NR, NA, true, 1.0f / (float)NA, s), "azimuth IFFT");
-    SARBP_CUDA(ctx, sarbp::launch_transpose(A, out, NR, NA, s), "transpose");
+    if (cols) {
+        SARBP_CUDA(ctx, sarbp::launch_dft_cols(pa_plan, B, out, NR, true, 1.0f / (float)NA, s), "azimuth IFFT");
+    } else {
+        SARBP_CUDA(ctx, sarbp::launch_transpose(B, A, NA, NR, s), "transpose");
+        SARBP_CUDA(ctx, sarbp::launch_dft_rows(pa_plan, A, NR, NA, true, 1.0f / (float)NA, s), "azimuth IFFT");
+        SARBP_CUDA(ctx, sarbp::launch_transpose(A, out, NR, NA, s), "transpose");
+    }
     cudaEventRecord(ctx->ev[1], s);
     ctx->timed_rc = true;  // sarbp_last_timings reports the omega-K time in its rc slot
     ctx->timed_bp = false;
-    ctx->launches += 9;
+    ctx->launches += cols ? 5 : 9;
     if (!dev_img)
         SARBP_CUDA(ctx, cudaMemcpyAsync(image, out, sizeof(float2) * npix, cudaMemcpyDeviceToHost, s), "download image");
     return finish(ctx, s, any_host);

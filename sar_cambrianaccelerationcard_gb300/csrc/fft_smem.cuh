@@ -270,24 +270,32 @@ __device__ __forceinline__ void twiddles(const Etab &E, int m, float2 lo1, float
 // receiving output point x in natural order.
 struct SmemSink {};
 
-template <int N, int R, int T, bool INV, int Ns, class Sink = SmemSink>
+// BATCH > 1: the stage runs over BATCH independent N-point arrays CS points
+// apart (s + c CS), their butterflies spread over the threads and sharing the
+// stage's barriers.
+template <int N, int R, int T, bool INV, int Ns, class Sink = SmemSink, int BATCH = 1, int CS = N>
 __device__ __forceinline__ void stage(float2 *s, const Etab &E, Sink sink = Sink{}) {
     constexpr bool kToSmem = std::is_same<Sink, SmemSink>::value;
     constexpr int NB = N / R;
-    constexpr int PER = (NB + T - 1) / T;
+    constexpr int NBT = NB * BATCH;
+    constexpr int PER = (NBT + T - 1) / T;
     constexpr int C = N / (Ns * R);  // k -> twiddle exponent step
+    static_assert(BATCH == 1 || kToSmem, "batched stages write shared memory");
     float2 v[PER][R];
 #pragma unroll
     for (int b = 0; b < PER; ++b) {
-        const int j = threadIdx.x + b * T;
-        if (PER * T == NB || j < NB) {
+        const int jj = threadIdx.x + b * T;
+        if (PER * T == NBT || jj < NBT) {
+            const int col = BATCH == 1 ? 0 : jj / NB;
+            const int j = jj - col * NB;
+            const float2 *sc = s + col * CS;
             if constexpr (NB % 256 == 0) {
-                const float2 *src = s + sw(j);
+                const float2 *src = sc + sw(j);
 #pragma unroll
                 for (int r = 0; r < R; ++r) v[b][r] = src[r * NB];
             } else {
 #pragma unroll
-                for (int r = 0; r < R; ++r) v[b][r] = s[sw(j + r * NB)];
+                for (int r = 0; r < R; ++r) v[b][r] = sc[sw(j + r * NB)];
             }
         }
     }
@@ -296,7 +304,9 @@ __device__ __forceinline__ void stage(float2 *s, const Etab &E, Sink sink = Sink
     Tw16 t16;
     constexpr bool kSameK = Ns > 1 && T % Ns == 0;
     // k = j when Ns >= NB (last stage); the low table level is then fixed per thread
-    constexpr bool kHoistLo = Ns > 1 && !kSameK && Ns >= NB && N >= kWlo && (C * T) % kWlo == 0;
+    // (batched: also across the wrap from one array to the next)
+    constexpr bool kHoistLo = Ns > 1 && !kSameK && Ns >= NB && N >= kWlo && (C * T) % kWlo == 0 &&
+                              (BATCH == 1 || (C * NB) % kWlo == 0);
     float2 lo1 = make_float2(1.f, 0.f), lo2 = lo1, lo4 = lo1;
     float2 lo[4] = {lo1, lo1, lo1, lo1};
     if constexpr (kSameK) {
@@ -318,8 +328,11 @@ __device__ __forceinline__ void stage(float2 *s, const Etab &E, Sink sink = Sink
     }
 #pragma unroll
     for (int b = 0; b < PER; ++b) {
-        const int j = threadIdx.x + b * T;
-        if (PER * T == NB || j < NB) {
+        const int jj = threadIdx.x + b * T;
+        if (PER * T == NBT || jj < NBT) {
+            const int col = BATCH == 1 ? 0 : jj / NB;
+            const int j = jj - col * NB;
+            float2 *sc = s + col * CS;
             const int k = j & (Ns - 1);
             if constexpr (Ns > 1) {
                 if constexpr (R == 16) {
@@ -337,12 +350,12 @@ __device__ __forceinline__ void stage(float2 *s, const Etab &E, Sink sink = Sink
 #pragma unroll
                 for (int r = 0; r < R; ++r) sink(x0 + r * Ns, v[b][r]);
             } else if constexpr (Ns % 256 == 0) {
-                float2 *dst = s + sw(x0);
+                float2 *dst = sc + sw(x0);
 #pragma unroll
                 for (int r = 0; r < R; ++r) dst[r * Ns] = v[b][r];
             } else {
 #pragma unroll
-                for (int r = 0; r < R; ++r) s[sw(x0 + r * Ns)] = v[b][r];
+                for (int r = 0; r < R; ++r) sc[sw(x0 + r * Ns)] = v[b][r];
             }
         }
     }
@@ -378,6 +391,25 @@ template <int N, int T, bool INV>
 __device__ void fft_smem(float2 *s, const Etab &E) {
     Stages<N, T, INV, 1>::run(s, E);
 }
+
+// BATCH transforms of N points, array c at s + c CS, sharing each stage's
+// barriers (same radix sequence as Stages).
+template <int N, int T, bool INV, int Ns, int BATCH, int CS>
+struct StagesBatched {
+    __device__ __forceinline__ static void run(float2 *s, const Etab &E) {
+        if constexpr (SARBP_FFT_RADIX16 && Ns * 16 <= N && N / 16 >= T) {
+            stage<N, 16, T, INV, Ns, SmemSink, BATCH, CS>(s, E);
+            StagesBatched<N, T, INV, Ns * 16, BATCH, CS>::run(s, E);
+        } else if constexpr (Ns * 8 <= N) {
+            stage<N, 8, T, INV, Ns, SmemSink, BATCH, CS>(s, E);
+            StagesBatched<N, T, INV, Ns * 8, BATCH, CS>::run(s, E);
+        } else if constexpr (Ns * 4 == N) {
+            stage<N, 4, T, INV, Ns, SmemSink, BATCH, CS>(s, E);
+        } else if constexpr (Ns * 2 == N) {
+            stage<N, 2, T, INV, Ns, SmemSink, BATCH, CS>(s, E);
+        }
+    }
+};
 
 // Radix of the stage with stride Ns (the same sequence as Stages).
 template <int N, int T, int Ns>
@@ -447,12 +479,12 @@ __device__ __forceinline__ float2 *ramp_slots(float2 *sm) {
 // (W^m = E^{L m}).  Contains one block barrier; the caller synchronises again
 // before the W tables are read.
 template <int N, int T>
-__device__ __forceinline__ Etab load_etab(float2 *sm, const float2 *__restrict__ etab, int L) {
+__device__ __forceinline__ Etab load_etab_at(float2 *tables, const float2 *__restrict__ etab, int L) {
     static_assert(N / kWlo <= kWhiMax, "W table too small");
     const int LN = L * N;
     const int nlo = LN < 256 ? LN : 256;
     const int nhi = LN < 256 ? 1 : LN / 256;
-    float2 *lo = sm + N;
+    float2 *lo = tables;
     float2 *hi = lo + kEloSlots;
     float2 *wlo = hi + kEhiSlots;
     float2 *whi = wlo + kWlo;
@@ -469,6 +501,11 @@ __device__ __forceinline__ Etab load_etab(float2 *sm, const float2 *__restrict__
             whi[i - nwlo] = E((L * kWlo * (i - nwlo)) & (LN - 1));
     }
     return E;
+}
+// Tables right after the N points of a single transform at sm.
+template <int N, int T>
+__device__ __forceinline__ Etab load_etab(float2 *sm, const float2 *__restrict__ etab, int L) {
+    return load_etab_at<N, T>(sm + N, etab, L);
 }
 
 // CTAs per SM that a T-thread kernel holding an N-point transform (plus the

@@ -211,6 +211,11 @@ void dft_tables_host(int n, std::vector<float2> &etab, std::vector<float2> &chir
 cudaError_t launch_dft_rows(const DftPlan &p, float2 *data, int rows, long long ld, bool inverse, float scale,
                             cudaStream_t s, const DftIo &io = DftIo());
 cudaError_t launch_transpose(const float2 *in, float2 *out, int rows, int cols, cudaStream_t s);
+// Transforms of length p.n down the ncols columns of a row-major [p.n][ncols]
+// array (power-of-two p.n in [512, 4096]), out == in for in place.
+bool dft_cols_supported(const DftPlan &p);
+cudaError_t launch_dft_cols(const DftPlan &p, const float2 *in, float2 *out, int ncols, bool inverse, float scale,
+                            cudaStream_t s);
 size_t wk_stolt_smem(int NR);
 // FP32 / float-float form of the Stolt stage (eps = q / (f0 + fr)^2 <= 1e-2):
 // col_c = (A (f0 + fr) + pi fr^2 / kr) mod 2 pi, col_ip = 1 / (f0 + fr) and row_q as float pairs.

@@ -166,6 +166,52 @@ __global__ void __launch_bounds__(T, (fft_min_blocks<M, T>())) dft_bluestein_ker
     }
 }
 
+// Power-of-two transforms down C adjacent columns of a row-major [N][ncols]
+// array, times scale, written to out (out == in: in place).  Rows of C x 8
+// bytes are read and written whole (one 32-byte sector at C = 4), the C
+// columns are transformed together in shared memory (sharing each stage's
+// barriers; each column padded by 4 points so the columns start in different
+// banks).  Replaces transpose + row transform + transpose.
+#ifndef SARBP_WK_COLS
+#define SARBP_WK_COLS 4
+#endif
+#ifndef SARBP_WK_COL_THREADS
+#define SARBP_WK_COL_THREADS 512
+#endif
+constexpr int kColPad = 4;
+template <int N, int T, bool INV, int C>
+__global__ void __launch_bounds__(T, (C <= 2 ? 2 : 1)) dft_cols_kernel(const float2 *in, float2 *out, int ncols, float scale,
+                                                     const float2 *__restrict__ etab) {
+    extern __shared__ float2 sm[];
+    constexpr int CS = N + kColPad;
+    const Etab E = load_etab_at<N, T>(sm + C * CS, etab, 1);
+    const int c0 = blockIdx.x * C;
+    for (int e = threadIdx.x; e < N * C; e += T) {
+        const int c = e % C, i = e / C, col = c0 + c;
+        sm[c * CS + sw(i)] = col < ncols ? in[(size_t)i * ncols + col] : make_float2(0.f, 0.f);
+    }
+    __syncthreads();  // also publishes the W tables
+    StagesBatched<N, T, INV, 1, C, CS>::run(sm, E);
+    for (int e = threadIdx.x; e < N * C; e += T) {
+        const int c = e % C, i = e / C, col = c0 + c;
+        if (col < ncols) {
+            const float2 v = sm[c * CS + sw(i)];
+            out[(size_t)i * ncols + col] = make_float2(v.x * scale, v.y * scale);
+        }
+    }
+}
+
+template <int N, bool INV>
+cudaError_t cols_n(const DftPlan &p, const float2 *in, float2 *out, int ncols, float scale, cudaStream_t s) {
+    constexpr int C = SARBP_WK_COLS, T = SARBP_WK_COL_THREADS;
+    const size_t smem = sizeof(float2) * (size_t)C * (N + kColPad) + kTabSmem;
+    auto k = dft_cols_kernel<N, T, INV, C>;
+    cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    k<<<(ncols + C - 1) / C, T, smem, s>>>(in, out, ncols, scale, p.etab);
+    return cudaGetLastError();
+}
+
 template <int N, bool INV>
 cudaError_t pow2_n(const DftPlan &p, float2 *data, int rows, long long ld, float scale, const DftIo &io,
                    cudaStream_t s) {
@@ -370,6 +416,21 @@ cudaError_t launch_dft_rows(const DftPlan &p, float2 *data, int rows, long long 
     if (rows <= 0) return cudaSuccess;
     return inverse ? dft_dispatch<true>(p, data, rows, ld, scale, io, s)
                    : dft_dispatch<false>(p, data, rows, ld, scale, io, s);
+}
+
+bool dft_cols_supported(const DftPlan &p) { return p.m == 0 && p.n >= 512 && p.n <= 4096; }
+
+cudaError_t launch_dft_cols(const DftPlan &p, const float2 *in, float2 *out, int ncols, bool inverse, float scale,
+                            cudaStream_t s) {
+    if (ncols <= 0) return cudaSuccess;
+    if (!dft_cols_supported(p)) return cudaErrorInvalidValue;
+    switch (p.n) {
+        case 512: return inverse ? cols_n<512, true>(p, in, out, ncols, scale, s) : cols_n<512, false>(p, in, out, ncols, scale, s);
+        case 1024: return inverse ? cols_n<1024, true>(p, in, out, ncols, scale, s) : cols_n<1024, false>(p, in, out, ncols, scale, s);
+        case 2048: return inverse ? cols_n<2048, true>(p, in, out, ncols, scale, s) : cols_n<2048, false>(p, in, out, ncols, scale, s);
+        case 4096: return inverse ? cols_n<4096, true>(p, in, out, ncols, scale, s) : cols_n<4096, false>(p, in, out, ncols, scale, s);
+        default: return cudaErrorInvalidValue;
+    }
 }
 
 cudaError_t launch_transpose(const float2 *in, float2 *out, int rows, int cols, cudaStream_t s) {
