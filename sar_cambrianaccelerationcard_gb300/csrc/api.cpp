@@ -309,9 +309,9 @@ sarbp_status rc_device(sarbp_ctx *ctx, const sarbp_radar *r, const sarbp_rc_layo
 // its copy lands, so only the first chunk's copy is not hidden.  The copy
 // stream first waits for the work already on `s` (earlier users of the
 // context's echo buffer).
-sarbp_status rc_host_echo(sarbp_ctx *ctx, const sarbp_radar *r, const sarbp_rc_layout &lay, const sarbp_complex64 *echo,
-                          int np, int ns, int storage, void *rc_out, float *scale_out, cudaStream_t s) {
-    Range range("sarbp: chunked echo upload + range compression");
+sarbp_status rc_host_echo_enqueue(sarbp_ctx *ctx, const sarbp_radar *r, const sarbp_rc_layout &lay,
+                                  const sarbp_complex64 *echo, int np, int ns, int storage, void *rc_out,
+                                  float *scale_out, cudaStream_t s) {
     SARBP_CUDA(ctx, ctx->echo.ensure(sizeof(float2) * (size_t)np * ns), "alloc echo");
     float2 *d_echo = ctx->echo.as<float2>();
     const size_t row = sizeof(float2) * (size_t)ns;
@@ -336,6 +336,21 @@ sarbp_status rc_host_echo(sarbp_ctx *ctx, const sarbp_radar *r, const sarbp_rc_l
     cudaEventRecord(ctx->ev[1], s);
     ctx->timed_rc = true;
     return SARBP_OK;
+}
+
+// Waits for the echo uploads still reading the caller's host buffer: an error
+// return must not leave copies in flight from memory the caller may free.
+void drain_uploads(sarbp_ctx *ctx) {
+    cudaStreamSynchronize(ctx->copy_stream);
+    cudaGetLastError();
+}
+
+sarbp_status rc_host_echo(sarbp_ctx *ctx, const sarbp_radar *r, const sarbp_rc_layout &lay, const sarbp_complex64 *echo,
+                          int np, int ns, int storage, void *rc_out, float *scale_out, cudaStream_t s) {
+    Range range("sarbp: chunked echo upload + range compression");
+    const sarbp_status st = rc_host_echo_enqueue(ctx, r, lay, echo, np, ns, storage, rc_out, scale_out, s);
+    if (st != SARBP_OK) drain_uploads(ctx);
+    return st;
 }
 
 sarbp_status check_grid(sarbp_ctx *ctx, const sarbp_grid *g) {
@@ -1302,9 +1317,17 @@ sarbp_status sarbp_image(sarbp_ctx *ctx, const sarbp_radar *radar, const sarbp_c
         v.scale = storage == SARBP_STORE_C32H ? ctx->scale.as<float>() : nullptr;
     }
     st = bp_device(ctx, radar, v, apc_dev, ex, grid, mode, d_img, 0, s);
-    if (st != SARBP_OK) return st;
-    if (!dev_img && !mapped_img)
-        SARBP_CUDA(ctx, cudaMemcpyAsync(image, d_img, sizeof(float2) * npix, cudaMemcpyDeviceToHost, s), "download image");
+    if (st != SARBP_OK) {
+        if (host_echo) drain_uploads(ctx);
+        return st;
+    }
+    if (!dev_img && !mapped_img) {
+        const cudaError_t e = cudaMemcpyAsync(image, d_img, sizeof(float2) * npix, cudaMemcpyDeviceToHost, s);
+        if (e != cudaSuccess) {
+            if (host_echo) drain_uploads(ctx);
+            return cuda_fail(ctx, e, "download image");
+        }
+    }
     return finish(ctx, s, any_host);
 }
 

@@ -280,3 +280,25 @@ def test_pinned_host_image_written_in_place(ctx, c1):
     ctx.check(ctx.lib.sarbp_image(ctx.h, sarbp.ctypes.byref(r), echo.data_ptr(), 0, s.ns, s.apc.ctypes.data,
                                   sarbp.ctypes.byref(g), sarbp.MODE_SPLIT, pinned.data_ptr(), None), "image np=0")
     assert not pinned.numpy().any()
+
+
+def test_error_after_upload_leaves_nothing_in_flight(ctx, c1):
+    """A grid the planner cannot serve (on top of the flight track) fails after
+    the echo upload and range compression were queued; the call returns the
+    status with no copy left reading the caller's pinned echo, and the context
+    stays usable."""
+    torch = pytest.importorskip("torch")
+    s = c1["scene"]
+    r, g, lay = sarbp.scene_args(s)
+    echo = torch.from_numpy(c1["echo"].view(np.float32)).pin_memory()
+    bad = sarbp.scene_args(s)[1]
+    for i in range(3):
+        bad.origin[i] = float(s.apc[s.np_ // 2][i]) - 0.5 * (bad.nx * bad.ux[i] + bad.ny * bad.uy[i])
+    img = np.zeros((bad.ny, bad.nx), dtype=np.complex64)
+    with pytest.raises(sarbp.SarbpError) as ex:
+        ctx.check(ctx.lib.sarbp_image(ctx.h, sarbp.ctypes.byref(r), echo.data_ptr(), s.np_, s.ns, s.apc.ctypes.data,
+                                      sarbp.ctypes.byref(bad), sarbp.MODE_SPLIT, img.ctypes.data, None), "image")
+    assert ex.value.status == sarbp.ERR_UNSUPPORTED
+    del echo  # the caller may release its buffer right after the error
+    again = sarbp.image_scene(ctx, s, c1["echo"], sarbp.MODE_SPLIT)
+    assert np.array_equal(again, sarbp.image_scene(ctx, s, c1["echo"], sarbp.MODE_SPLIT))
