@@ -178,6 +178,10 @@ __global__ void __launch_bounds__(T, (fft_min_blocks<M, T>())) dft_bluestein_ker
 #ifndef SARBP_WK_COL_THREADS
 #define SARBP_WK_COL_THREADS 512
 #endif
+#ifndef SARBP_WK_COL_UNROLL
+#define SARBP_WK_COL_UNROLL 8
+#endif
+constexpr int kColUnroll = SARBP_WK_COL_UNROLL;
 constexpr int kColPad = 4;
 template <int N, int T, bool INV, int C>
 __global__ void __launch_bounds__(T, (C <= 2 ? 2 : 1)) dft_cols_kernel(const float2 *in, float2 *out, int ncols, float scale,
@@ -186,7 +190,12 @@ __global__ void __launch_bounds__(T, (C <= 2 ? 2 : 1)) dft_cols_kernel(const flo
     constexpr int CS = N + kColPad;
     const Etab E = load_etab_at<N, T>(sm + C * CS, etab, 1);
     const int c0 = blockIdx.x * C;
-    for (int e = threadIdx.x; e < N * C; e += T) {
+    // fill: kColUnroll loads in flight per thread (one CTA per SM: no other
+    // CTA hides a load's latency)
+    static_assert((N * C) % T == 0, "whole fill iterations");
+#pragma unroll kColUnroll
+    for (int it = 0; it < N * C / T; ++it) {
+        const int e = threadIdx.x + it * T;
         const int c = e % C, i = e / C, col = c0 + c;
         sm[c * CS + sw(i)] = col < ncols ? in[(size_t)i * ncols + col] : make_float2(0.f, 0.f);
     }
