@@ -304,6 +304,15 @@ sarbp_status sarbp_wk_image(sarbp_ctx *ctx, const sarbp_wk_params *params, const
 sarbp_status sarbp_dft(sarbp_ctx *ctx, sarbp_complex64 *data, int32_t rows, int32_t n, int32_t inverse,
                        void *stream);
 
+/* 2-D DFT of data [na][nr] (row-major), in place: along the rows (length nr)
+ * then down the columns (length na); the inverse scales by 1/nr and 1/na.
+ * Replaces perform2DFFT / perform2DIFFT (code/SAR_WK/wk_v5.2.3/task/fft.cc:18,200),
+ * which run the same two passes through CNNL FFT plans and a transpose.
+ * Power-of-two column lengths 512..4096 are transformed down the columns
+ * directly, others through two transposes (scratch in the context). */
+sarbp_status sarbp_dft2d(sarbp_ctx *ctx, sarbp_complex64 *data, int32_t na, int32_t nr, int32_t inverse,
+                         void *stream);
+
 /* ------------------------------------------------------ CEOS raw ingest -- */
 
 /* Layout of a RADARSAT-1 CEOS raw-data file as the reference's reader sees it

@@ -1016,6 +1016,53 @@ sarbp_status sarbp_dft(sarbp_ctx *ctx, sarbp_complex64 *data, int32_t rows, int3
     return finish(ctx, s, !dev);
 }
 
+sarbp_status sarbp_dft2d(sarbp_ctx *ctx, sarbp_complex64 *data, int32_t na, int32_t nr, int32_t inverse,
+                         void *stream) {
+    if (!ctx) return SARBP_ERR_INVALID_ARGUMENT;
+    Range range("sarbp_dft2d");
+    ctx->err.clear();
+    cudaSetDevice(ctx->device);
+    if (na < 1 || nr < 1) return fail(ctx, SARBP_ERR_INVALID_ARGUMENT, "na and nr must be >= 1");
+    if ((long long)na * nr > (1LL << 31)) return fail(ctx, SARBP_ERR_INVALID_ARGUMENT, "array too large");
+    if (!data) return fail(ctx, SARBP_ERR_INVALID_ARGUMENT, "data is null");
+    if (na == 1 && nr == 1) return SARBP_OK;
+    sarbp::DftPlan pr{}, pa{};
+    sarbp_status st;
+    if (nr > 1 && (st = get_dft(ctx, nr, pr)) != SARBP_OK) return st;
+    if (na > 1 && (st = get_dft(ctx, na, pa)) != SARBP_OK) return st;
+    if (nr > 1 && na > 1 && na != nr && (st = get_dft(ctx, nr, pr)) != SARBP_OK) return st;  // both still cached
+    cudaStream_t s = pick_stream(ctx, stream);
+    const size_t bytes = sizeof(float2) * (size_t)na * nr;
+    float2 *d = reinterpret_cast<float2 *>(data);
+    const bool dev = is_device_ptr(data);
+    if (!dev) {
+        SARBP_CUDA(ctx, ctx->wk0.ensure(bytes), "alloc DFT buffer");
+        d = ctx->wk0.as<float2>();
+        SARBP_CUDA(ctx, cudaMemcpyAsync(d, data, bytes, cudaMemcpyHostToDevice, s), "upload DFT array");
+    }
+    const bool inv = inverse != 0;
+    if (nr > 1) {  // range: along the rows
+        SARBP_CUDA(ctx, sarbp::launch_dft_rows(pr, d, na, nr, inv, inv ? 1.0f / (float)nr : 1.0f, s), "row DFT");
+        ctx->launches += 1;
+    }
+    if (na > 1) {  // azimuth: down the columns, through transposes where the column kernel does not apply
+        const float sc = inv ? 1.0f / (float)na : 1.0f;
+        if (sarbp::dft_cols_supported(pa)) {
+            SARBP_CUDA(ctx, sarbp::launch_dft_cols(pa, d, d, nr, inv, sc, s), "column DFT");
+            ctx->launches += 1;
+        } else {
+            SARBP_CUDA(ctx, ctx->wk1.ensure(bytes), "alloc transpose buffer");
+            float2 *t = ctx->wk1.as<float2>();
+            SARBP_CUDA(ctx, sarbp::launch_transpose(d, t, na, nr, s), "transpose");
+            SARBP_CUDA(ctx, sarbp::launch_dft_rows(pa, t, nr, na, inv, sc, s), "column DFT");
+            SARBP_CUDA(ctx, sarbp::launch_transpose(t, d, nr, na, s), "transpose");
+            ctx->launches += 3;
+        }
+    }
+    if (!dev) SARBP_CUDA(ctx, cudaMemcpyAsync(data, d, bytes, cudaMemcpyDeviceToHost, s), "download DFT array");
+    return finish(ctx, s, !dev);
+}
+
 sarbp_status sarbp_wk_image(sarbp_ctx *ctx, const sarbp_wk_params *w, const sarbp_complex64 *echo, int32_t na,
                             int32_t nr, sarbp_complex64 *image, void *stream) {
     constexpr double kPi = 3.14159265358979323846;

@@ -195,6 +195,8 @@ SIGNATURES = {
                         ctypes.c_void_p, ctypes.c_void_p], ctypes.c_int),
     "sarbp_dft": ([ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32, ctypes.c_void_p],
                   ctypes.c_int),
+    "sarbp_dft2d": ([ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32, ctypes.c_void_p],
+                  ctypes.c_int),
     "sarbp_ceos_decode": ([ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint64, ctypes.POINTER(CeosLayout),
                            ctypes.c_int32, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32,
                            ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p], ctypes.c_int),
@@ -450,6 +452,12 @@ class Context:
         """In-place batched DFT along the rows of data [rows][n] (complex64)."""
         rows, n = data.shape
         self.check(self.lib.sarbp_dft(self.h, _ptr(data), rows, n, int(inverse), stream), "dft")
+        return data
+
+    def dft2d(self, data, inverse: bool = False, stream=None):
+        """In-place 2-D DFT of data [na][nr] (complex64): rows, then columns."""
+        na, nr = data.shape
+        self.check(self.lib.sarbp_dft2d(self.h, _ptr(data), na, nr, int(inverse), stream), "dft2d")
         return data
 
     def image(self, radar: Radar, echo, apc, grid: Grid, mode: int, image=None, stream=None):

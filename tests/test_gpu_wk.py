@@ -111,3 +111,17 @@ def test_wk_rejects_bad_arguments(ctx):
         ctx.wk_image(q, rand((64, 64), 1))
     with pytest.raises(sarbp.SarbpError):  # padded range size 10924 > 8192 and not a power of two
         ctx.wk_image(p, rand((8, 6554), 1))
+
+
+@pytest.mark.parametrize("shape", [(1024, 854), (4096, 96), (512, 512), (300, 200), (100, 64), (64, 33), (1, 7), (7, 1)])
+def test_dft2d(ctx, shape):
+    """sarbp_dft2d (perform2DFFT / perform2DIFFT): against numpy fft2 / ifft2 in
+    FP64, both the column kernel (power-of-two column lengths 512..4096) and the
+    transpose path."""
+    x = rand(shape, shape[0] * 7 + shape[1])
+    ref = np.fft.fft2(x.astype(np.complex128))
+    got = ctx.dft2d(x.copy())
+    assert metrics.rel_l2_db(got, ref) <= -105.0
+    back = ctx.dft2d(got.copy(), inverse=True)
+    assert metrics.rel_l2_db(back, x.astype(np.complex128)) <= -105.0
+    assert metrics.rel_l2_db(ctx.dft2d(ref.astype(np.complex64), inverse=True), x.astype(np.complex128)) <= -105.0
