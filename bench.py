@@ -661,12 +661,14 @@ def run_wk(args):
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     clocks = ClockSampler(int(os.environ.get("LOCAL_RANK", "0")))
     clocks.start()
+    n0 = ctx.launches()
     ev0.record(stream)
     for _ in range(args.steps):
         step()
     ev1.record(stream)
     stream.synchronize()
     clk = clocks.stop()
+    launches = ctx.launches() - n0
     ms = ev0.elapsed_time(ev1) / args.steps
     npix = NA * NR
     # end to end: host echo in, host image out through the same call
@@ -702,7 +704,7 @@ def run_wk(args):
                      "traffic_algorithmic": alg, "kernel": "whole omega-K pipeline"},
         "cpu_baseline": {"value": npix / cpu_s / 1e6, "unit": "Mpix/s", "cores": 1, "kind": "port",
                          "sample": f"FP64 numpy restatement of the same {na} x {nr} image ({cpu_s:.1f} s)"},
-        "gpu_launches": 9 * args.steps,
+        "gpu_launches": launches,
         "clocks": clk,
     }
     if rank == 0:

@@ -299,6 +299,21 @@ sarbp_status sarbp_wk_padded_size(int32_t na, int32_t nr, int32_t *na_pad, int32
 sarbp_status sarbp_wk_image(sarbp_ctx *ctx, const sarbp_wk_params *params, const sarbp_complex64 *echo,
                             int32_t na, int32_t nr, sarbp_complex64 *image, void *stream);
 
+/* The omega-K stages one by one, for callers that drive process_wk's steps
+ * themselves: sarbp_wk_preprocess, sarbp_dft2d (forward), sarbp_wk_focus,
+ * sarbp_dft2d (inverse) give the same bits as sarbp_wk_image.
+ * sarbp_wk_preprocess replaces preprocess_wk (task/preprocess.cc:17-167): echo
+ * [na][nr] -> out [na_pad][nr_pad] (sarbp_wk_padded_size), zero padding and
+ * azimuth down-conversion exp(-j 2 pi f_nc ta).
+ * sarbp_wk_focus replaces the reference-function multiply and StoltInterp_sinc
+ * (task/compression.cc:17-73, task/stolt.cc:324+) on the 2-D spectrum
+ * [na_pad][nr_pad]: out = Stolt-mapped spectrum times exp(j theta); out may
+ * equal spectrum. */
+sarbp_status sarbp_wk_preprocess(sarbp_ctx *ctx, const sarbp_wk_params *params, const sarbp_complex64 *echo,
+                                 int32_t na, int32_t nr, sarbp_complex64 *out, void *stream);
+sarbp_status sarbp_wk_focus(sarbp_ctx *ctx, const sarbp_wk_params *params, const sarbp_complex64 *spectrum,
+                            int32_t na_pad, int32_t nr_pad, sarbp_complex64 *out, void *stream);
+
 /* Batched 1-D DFT along the rows of data [rows][n], in place: forward
  * (unnormalised) or inverse (times 1/n), any supported n (see above). */
 sarbp_status sarbp_dft(sarbp_ctx *ctx, sarbp_complex64 *data, int32_t rows, int32_t n, int32_t inverse,

@@ -1063,13 +1063,8 @@ sarbp_status sarbp_dft2d(sarbp_ctx *ctx, sarbp_complex64 *data, int32_t na, int3
     return finish(ctx, s, !dev);
 }
 
-sarbp_status sarbp_wk_image(sarbp_ctx *ctx, const sarbp_wk_params *w, const sarbp_complex64 *echo, int32_t na,
-                            int32_t nr, sarbp_complex64 *image, void *stream) {
-    constexpr double kPi = 3.14159265358979323846;
-    if (!ctx) return SARBP_ERR_INVALID_ARGUMENT;
-    Range range("sarbp_wk_image");
-    ctx->err.clear();
-    cudaSetDevice(ctx->device);
+// Omega-K parameter checks shared by the pipeline and its stage entry points.
+sarbp_status wk_check_params(sarbp_ctx *ctx, const sarbp_wk_params *w) {
     if (!w) return fail(ctx, SARBP_ERR_INVALID_ARGUMENT, "params is null");
     const double vals[8] = {w->fr, w->prf, w->f0, w->r0, w->kr, w->c, w->vr, w->f_nc};
     for (double v : vals)
@@ -1077,21 +1072,23 @@ sarbp_status sarbp_wk_image(sarbp_ctx *ctx, const sarbp_wk_params *w, const sarb
     if (!(w->fr > 0) || !(w->prf > 0) || !(w->f0 > 0) || !(w->c > 0) || !(w->vr > 0) || w->kr == 0.0)
         return fail(ctx, SARBP_ERR_INVALID_ARGUMENT, "fr, prf, f0, c, vr must be > 0 and kr != 0");
     if (w->taps < 1 || w->taps > 32) return fail(ctx, SARBP_ERR_INVALID_ARGUMENT, "taps must be in [1, 32]");
-    if (na <= 0 || nr <= 0) return fail(ctx, SARBP_ERR_INVALID_ARGUMENT, "echo size must be > 0");
-    if (!echo || !image) return fail(ctx, SARBP_ERR_INVALID_ARGUMENT, "echo and image must be non-null");
-    int32_t NA, NR;
-    if (sarbp_wk_padded_size(na, nr, &NA, &NR) != SARBP_OK)
-        return fail(ctx, SARBP_ERR_UNSUPPORTED, "padded size %d x %d not supported", NA, NR);
-    if (sarbp::wk_stolt_smem(NR) > (size_t)(227u << 10))
-        return fail(ctx, SARBP_ERR_UNSUPPORTED, "range size %d too large for the Stolt stage", NR);
-    int pa, pr;
-    wk_pads(na, nr, &pa, &pr);
-    sarbp::DftPlan pa_plan, pr_plan;
-    sarbp_status st = get_dft(ctx, NR, pr_plan);
-    if (st != SARBP_OK) return st;
-    st = get_dft(ctx, NA, pa_plan);
-    if (st != SARBP_OK) return st;
-    cudaStream_t s = pick_stream(ctx, stream);
+    return SARBP_OK;
+}
+
+// Device tables of the omega-K stages for a padded size NA x NR (built on the
+// host in FP64, uploaded on s): row phasors of the azimuth down-conversion, the
+// Stolt terms per row and column (float-float), and the FP64 tables of the
+// FP64 Stolt path.
+struct WkTables {
+    float2 *rowphase = nullptr, *rowq = nullptr, *colip = nullptr;
+    float *colc = nullptr;
+    const double *tab = nullptr;  // col_f2, col_ph, col_fr [NR] each, row_q [NA]
+    double a4r = 0.0;
+    bool ff = true;               // float-float Stolt (mapping a small correction)
+};
+
+sarbp_status wk_tables(sarbp_ctx *ctx, const sarbp_wk_params *w, int NA, int NR, cudaStream_t s, WkTables &t) {
+    constexpr double kPi = 3.14159265358979323846;
     // host tables (FP64): row phasors exp(-j 2 pi f_nc ta_m), ta_m = (m - NA/2) / prf;
     // frequency axes as the reference builds them (fftshifted index, wk.cc:181-205)
     const double a4r = 4.0 * kPi * w->r0 / w->c;
@@ -1128,9 +1125,6 @@ sarbp_status sarbp_wk_image(sarbp_ctx *ctx, const sarbp_wk_params *w, const sarb
     }
     // float-float Stolt stage when the mapping is a small correction (eps <= 1e-2), else FP64
     const bool ff_stolt = pmin > 0.0 && qmax / (pmin * pmin) <= 1e-2;
-    const size_t npix = (size_t)NA * NR;
-    SARBP_CUDA(ctx, ctx->wk0.ensure(sizeof(float2) * npix), "alloc omega-K buffer");
-    SARBP_CUDA(ctx, ctx->wk1.ensure(sizeof(float2) * npix), "alloc omega-K buffer");
     const size_t row_bytes = sizeof(float2) * 2 * NA, col_bytes = (sizeof(float) + sizeof(float2)) * NR;
     SARBP_CUDA(ctx, ctx->wkrow.ensure(row_bytes + col_bytes), "alloc omega-K tables");
     SARBP_CUDA(ctx, ctx->wktab.ensure(sizeof(double) * tab.size()), "alloc omega-K tables");
@@ -1146,7 +1140,61 @@ sarbp_status sarbp_wk_image(sarbp_ctx *ctx, const sarbp_wk_params *w, const sarb
                "upload omega-K tables");
     SARBP_CUDA(ctx, cudaMemcpyAsync(ctx->wktab.ptr, tab.data(), sizeof(double) * tab.size(), cudaMemcpyHostToDevice, s),
                "upload omega-K tables");
-    const double *d_tab = ctx->wktab.as<double>();
+    t.tab = ctx->wktab.as<double>();
+    t.rowphase = d_rowphase;
+    t.rowq = d_rowq;
+    t.colip = d_colip;
+    t.colc = d_colc;
+    t.a4r = a4r;
+    t.ff = ff_stolt;
+    return SARBP_OK;
+}
+
+// Reference-function multiply and Stolt mapping of a 2-D spectrum [NA][NR].
+sarbp_status wk_focus_launch(sarbp_ctx *ctx, const sarbp_wk_params *w, const WkTables &t, const float2 *in,
+                             float2 *out, int NA, int NR, cudaStream_t s) {
+    const double *d_tab = t.tab;
+    if (t.ff)
+        SARBP_CUDA(ctx, sarbp::launch_wk_stolt_ff(in, out, NA, NR, t.colc, t.colip, t.rowq, t.a4r, NR / w->fr, w->taps, s),
+                   "reference-function multiply and Stolt mapping");
+    else
+        SARBP_CUDA(ctx, sarbp::launch_wk_stolt(in, out, NA, NR, d_tab, d_tab + NR, d_tab + 2 * NR, d_tab + 3 * NR, t.a4r,
+                                                w->f0, NR / w->fr, w->taps, s),
+                   "reference-function multiply and Stolt mapping");
+    ctx->launches += 1;
+    return SARBP_OK;
+}
+
+sarbp_status sarbp_wk_image(sarbp_ctx *ctx, const sarbp_wk_params *w, const sarbp_complex64 *echo, int32_t na,
+                            int32_t nr, sarbp_complex64 *image, void *stream) {
+    if (!ctx) return SARBP_ERR_INVALID_ARGUMENT;
+    Range range("sarbp_wk_image");
+    ctx->err.clear();
+    cudaSetDevice(ctx->device);
+    sarbp_status st = wk_check_params(ctx, w);
+    if (st != SARBP_OK) return st;
+    if (na <= 0 || nr <= 0) return fail(ctx, SARBP_ERR_INVALID_ARGUMENT, "echo size must be > 0");
+    if (!echo || !image) return fail(ctx, SARBP_ERR_INVALID_ARGUMENT, "echo and image must be non-null");
+    int32_t NA, NR;
+    if (sarbp_wk_padded_size(na, nr, &NA, &NR) != SARBP_OK)
+        return fail(ctx, SARBP_ERR_UNSUPPORTED, "padded size %d x %d not supported", NA, NR);
+    if (sarbp::wk_stolt_smem(NR) > (size_t)(227u << 10))
+        return fail(ctx, SARBP_ERR_UNSUPPORTED, "range size %d too large for the Stolt stage", NR);
+    int pa, pr;
+    wk_pads(na, nr, &pa, &pr);
+    sarbp::DftPlan pa_plan, pr_plan;
+    st = get_dft(ctx, NR, pr_plan);
+    if (st != SARBP_OK) return st;
+    st = get_dft(ctx, NA, pa_plan);
+    if (st != SARBP_OK) return st;
+    cudaStream_t s = pick_stream(ctx, stream);
+    WkTables tb;
+    st = wk_tables(ctx, w, NA, NR, s, tb);
+    if (st != SARBP_OK) return st;
+    const size_t npix = (size_t)NA * NR;
+    SARBP_CUDA(ctx, ctx->wk0.ensure(sizeof(float2) * npix), "alloc omega-K buffer");
+    SARBP_CUDA(ctx, ctx->wk1.ensure(sizeof(float2) * npix), "alloc omega-K buffer");
+    float2 *d_rowphase = tb.rowphase;
     const float2 *d_echo = reinterpret_cast<const float2 *>(echo);
     bool any_host = true;  // the host tables above are staged through pageable memory
     if (!is_device_ptr(echo)) {
@@ -1180,13 +1228,8 @@ sarbp_status sarbp_wk_image(sarbp_ctx *ctx, const sarbp_wk_params *w, const sarb
         SARBP_CUDA(ctx, sarbp::launch_dft_rows(pa_plan, B, NR, NA, false, 1.0f, s), "azimuth FFT");
         SARBP_CUDA(ctx, sarbp::launch_transpose(B, A, NR, NA, s), "transpose");
     }
-    if (ff_stolt)
-        SARBP_CUDA(ctx, sarbp::launch_wk_stolt_ff(A, B, NA, NR, d_colc, d_colip, d_rowq, a4r, NR / w->fr, w->taps, s),
-                   "reference-function multiply and Stolt mapping");
-    else
-        SARBP_CUDA(ctx, sarbp::launch_wk_stolt(A, B, NA, NR, d_tab, d_tab + NR, d_tab + 2 * NR, d_tab + 3 * NR, a4r,
-                                                w->f0, NR / w->fr, w->taps, s),
-                   "reference-function multiply and Stolt mapping");
+    st = wk_focus_launch(ctx, w, tb, A, B, NA, NR, s);
+    if (st != SARBP_OK) return st;
     SARBP_CUDA(ctx, sarbp::launch_dft_rows(pr_plan, B, NA, NR, true, 1.0f / (float)NR, s), "range IFFT");
     if (cols) {
         SARBP_CUDA(ctx, sarbp::launch_dft_cols(pa_plan, B, out, NR, true, 1.0f / (float)NA, s), "azimuth IFFT");
@@ -1198,10 +1241,84 @@ sarbp_status sarbp_wk_image(sarbp_ctx *ctx, const sarbp_wk_params *w, const sarb
     cudaEventRecord(ctx->ev[1], s);
     ctx->timed_rc = true;  // sarbp_last_timings reports the omega-K time in its rc slot
     ctx->timed_bp = false;
-    ctx->launches += cols ? 5 : 9;
+    ctx->launches += cols ? 4 : 8;  // and the Stolt launch counted by wk_focus_launch
     if (!dev_img)
         SARBP_CUDA(ctx, cudaMemcpyAsync(image, out, sizeof(float2) * npix, cudaMemcpyDeviceToHost, s), "download image");
     return finish(ctx, s, any_host);
+}
+
+sarbp_status sarbp_wk_preprocess(sarbp_ctx *ctx, const sarbp_wk_params *w, const sarbp_complex64 *echo, int32_t na,
+                                 int32_t nr, sarbp_complex64 *out, void *stream) {
+    if (!ctx) return SARBP_ERR_INVALID_ARGUMENT;
+    Range range("sarbp_wk_preprocess");
+    ctx->err.clear();
+    cudaSetDevice(ctx->device);
+    sarbp_status st = wk_check_params(ctx, w);
+    if (st != SARBP_OK) return st;
+    if (na <= 0 || nr <= 0) return fail(ctx, SARBP_ERR_INVALID_ARGUMENT, "echo size must be > 0");
+    if (!echo || !out) return fail(ctx, SARBP_ERR_INVALID_ARGUMENT, "echo and out must be non-null");
+    int32_t NA, NR;
+    if (sarbp_wk_padded_size(na, nr, &NA, &NR) != SARBP_OK)
+        return fail(ctx, SARBP_ERR_UNSUPPORTED, "padded size %d x %d not supported", NA, NR);
+    int pa, pr;
+    wk_pads(na, nr, &pa, &pr);
+    cudaStream_t s = pick_stream(ctx, stream);
+    WkTables tb;
+    st = wk_tables(ctx, w, NA, NR, s, tb);
+    if (st != SARBP_OK) return st;
+    const float2 *d_echo = reinterpret_cast<const float2 *>(echo);
+    if (!is_device_ptr(echo)) {
+        SARBP_CUDA(ctx, ctx->echo.ensure(sizeof(float2) * (size_t)na * nr), "alloc echo");
+        SARBP_CUDA(ctx, cudaMemcpyAsync(ctx->echo.ptr, echo, sizeof(float2) * (size_t)na * nr, cudaMemcpyHostToDevice, s),
+                   "upload echo");
+        d_echo = ctx->echo.as<float2>();
+    }
+    const size_t bytes = sizeof(float2) * (size_t)NA * NR;
+    const bool dev_out = is_device_ptr(out);
+    float2 *d_out = reinterpret_cast<float2 *>(out);
+    if (!dev_out) {
+        SARBP_CUDA(ctx, ctx->wk0.ensure(bytes), "alloc omega-K buffer");
+        d_out = ctx->wk0.as<float2>();
+    }
+    SARBP_CUDA(ctx, sarbp::launch_wk_pad(d_echo, na, nr, tb.rowphase, pa, pr, NA, NR, d_out, s), "padding");
+    ctx->launches += 1;
+    if (!dev_out) SARBP_CUDA(ctx, cudaMemcpyAsync(out, d_out, bytes, cudaMemcpyDeviceToHost, s), "download");
+    return finish(ctx, s, true);  // the host tables are staged through pageable memory
+}
+
+sarbp_status sarbp_wk_focus(sarbp_ctx *ctx, const sarbp_wk_params *w, const sarbp_complex64 *spectrum, int32_t na_pad,
+                            int32_t nr_pad, sarbp_complex64 *out, void *stream) {
+    if (!ctx) return SARBP_ERR_INVALID_ARGUMENT;
+    Range range("sarbp_wk_focus");
+    ctx->err.clear();
+    cudaSetDevice(ctx->device);
+    sarbp_status st = wk_check_params(ctx, w);
+    if (st != SARBP_OK) return st;
+    if (na_pad <= 0 || nr_pad <= 0) return fail(ctx, SARBP_ERR_INVALID_ARGUMENT, "spectrum size must be > 0");
+    if (!spectrum || !out) return fail(ctx, SARBP_ERR_INVALID_ARGUMENT, "spectrum and out must be non-null");
+    if (sarbp::wk_stolt_smem(nr_pad) > (size_t)(227u << 10))
+        return fail(ctx, SARBP_ERR_UNSUPPORTED, "range size %d too large for the Stolt stage", nr_pad);
+    cudaStream_t s = pick_stream(ctx, stream);
+    WkTables tb;
+    st = wk_tables(ctx, w, na_pad, nr_pad, s, tb);
+    if (st != SARBP_OK) return st;
+    const size_t bytes = sizeof(float2) * (size_t)na_pad * nr_pad;
+    const float2 *d_in = reinterpret_cast<const float2 *>(spectrum);
+    if (!is_device_ptr(spectrum)) {
+        SARBP_CUDA(ctx, ctx->wk0.ensure(bytes), "alloc omega-K buffer");
+        SARBP_CUDA(ctx, cudaMemcpyAsync(ctx->wk0.ptr, spectrum, bytes, cudaMemcpyHostToDevice, s), "upload spectrum");
+        d_in = ctx->wk0.as<float2>();
+    }
+    const bool dev_out = is_device_ptr(out);
+    float2 *d_out = reinterpret_cast<float2 *>(out);
+    if (!dev_out) {
+        SARBP_CUDA(ctx, ctx->wk1.ensure(bytes), "alloc omega-K buffer");
+        d_out = ctx->wk1.as<float2>();
+    }
+    st = wk_focus_launch(ctx, w, tb, d_in, d_out, na_pad, nr_pad, s);
+    if (st != SARBP_OK) return st;
+    if (!dev_out) SARBP_CUDA(ctx, cudaMemcpyAsync(out, d_out, bytes, cudaMemcpyDeviceToHost, s), "download");
+    return finish(ctx, s, true);
 }
 
 sarbp_status sarbp_ceos_decode(sarbp_ctx *ctx, const uint8_t *raw, uint64_t raw_bytes,

@@ -214,6 +214,9 @@ cudaError_t launch_transpose(const float2 *in, float2 *out, int rows, int cols, 
 // Transforms of length p.n down the ncols columns of a row-major [p.n][ncols]
 // array (power-of-two p.n in [512, 4096]), out == in for in place.
 bool dft_cols_supported(const DftPlan &p);
+// out [NA][NR] = echo [na][nr] placed at (pa, pr) times rowmul[m] per row, zero elsewhere.
+cudaError_t launch_wk_pad(const float2 *echo, int na, int nr, const float2 *rowmul, int pa, int pr, int NA, int NR,
+                          float2 *out, cudaStream_t s);
 cudaError_t launch_dft_cols(const DftPlan &p, const float2 *in, float2 *out, int ncols, bool inverse, float scale,
                             cudaStream_t s);
 size_t wk_stolt_smem(int NR);

@@ -427,6 +427,29 @@ cudaError_t launch_dft_rows(const DftPlan &p, float2 *data, int rows, long long 
                    : dft_dispatch<false>(p, data, rows, ld, scale, io, s);
 }
 
+// Zero padding and azimuth down-conversion into [NA][NR]: echo row m - pa at
+// columns pr.., times rowmul[m] (task/preprocess.cc:17-167); HBM-bound.
+__global__ void __launch_bounds__(256) wk_pad_kernel(const float2 *__restrict__ echo, int na, int nr,
+                                                     const float2 *__restrict__ rowmul, int pa, int pr, int NA, int NR,
+                                                     float2 *__restrict__ out) {
+    const long long total = (long long)NA * NR;
+    for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < total; k += (long long)gridDim.x * blockDim.x) {
+        const int m = (int)(k / NR), n = (int)(k - (long long)m * NR);
+        const int a = m - pa, c = n - pr;
+        float2 v = make_float2(0.f, 0.f);
+        if (a >= 0 && a < na && c >= 0 && c < nr) v = cmul(__ldg(&echo[(size_t)a * nr + c]), __ldg(&rowmul[m]));
+        out[k] = v;
+    }
+}
+
+cudaError_t launch_wk_pad(const float2 *echo, int na, int nr, const float2 *rowmul, int pa, int pr, int NA, int NR,
+                          float2 *out, cudaStream_t s) {
+    const long long total = (long long)NA * NR;
+    const int blocks = (int)std::min<long long>((total + 255) / 256, 152LL * 16);
+    wk_pad_kernel<<<blocks, 256, 0, s>>>(echo, na, nr, rowmul, pa, pr, NA, NR, out);
+    return cudaGetLastError();
+}
+
 bool dft_cols_supported(const DftPlan &p) { return p.m == 0 && p.n >= 512 && p.n <= 4096; }
 
 cudaError_t launch_dft_cols(const DftPlan &p, const float2 *in, float2 *out, int ncols, bool inverse, float scale,

@@ -193,6 +193,10 @@ SIGNATURES = {
                               ctypes.POINTER(ctypes.c_int32)], ctypes.c_int),
     "sarbp_wk_image": ([ctypes.c_void_p, ctypes.POINTER(WkParams), ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32,
                         ctypes.c_void_p, ctypes.c_void_p], ctypes.c_int),
+    "sarbp_wk_preprocess": ([ctypes.c_void_p, ctypes.POINTER(WkParams), ctypes.c_void_p, ctypes.c_int32,
+                             ctypes.c_int32, ctypes.c_void_p, ctypes.c_void_p], ctypes.c_int),
+    "sarbp_wk_focus": ([ctypes.c_void_p, ctypes.POINTER(WkParams), ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32,
+                        ctypes.c_void_p, ctypes.c_void_p], ctypes.c_int),
     "sarbp_dft": ([ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32, ctypes.c_void_p],
                   ctypes.c_int),
     "sarbp_dft2d": ([ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32, ctypes.c_void_p],
@@ -435,6 +439,25 @@ class Context:
         self.check(self.lib.sarbp_wk_image(self.h, ctypes.byref(w), _ptr(echo), na, nr, _ptr(image), stream),
                    "wk_image")
         return image
+
+    def wk_preprocess(self, params, echo, stream=None):
+        """Zero-padded, azimuth down-converted echo [na_pad][nr_pad] complex64."""
+        w = params if isinstance(params, WkParams) else wk_params(params)
+        na, nr = echo.shape
+        NA, NR, _ = self.wk_padded_size(na, nr)
+        out = np.zeros((NA, NR), dtype=np.complex64)
+        self.check(self.lib.sarbp_wk_preprocess(self.h, ctypes.byref(w), _ptr(echo), na, nr, _ptr(out), stream),
+                   "wk_preprocess")
+        return out
+
+    def wk_focus(self, params, spectrum, stream=None):
+        """Reference-function multiply + Stolt mapping of a 2-D spectrum [na_pad][nr_pad]."""
+        w = params if isinstance(params, WkParams) else wk_params(params)
+        NA, NR = spectrum.shape
+        out = np.zeros((NA, NR), dtype=np.complex64)
+        self.check(self.lib.sarbp_wk_focus(self.h, ctypes.byref(w), _ptr(spectrum), NA, NR, _ptr(out), stream),
+                   "wk_focus")
+        return out
 
     def ceos_decode(self, raw, first_line: int, nlines: int, first_cell: int, ncells: int, layout=None,
                     apply_agc: bool = True, stream=None):
