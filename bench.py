@@ -73,6 +73,8 @@ def parse():
                     help="CEOS raw-data decode of the reference scene's size (3072 lines x 2048 cells)")
     ap.add_argument("--rates", default="10,20,30,40", help="arrival rates (jobs/s) for --serve")
     ap.add_argument("--jobs", type=int, default=60, help="jobs per rate for --serve")
+    ap.add_argument("--step-updates", default="2147483648,0",
+                    help="--serve schedules: comma list of step_updates (0: fixed 512 pulses per step)")
     return ap.parse_args()
 
 
@@ -471,49 +473,61 @@ def run_serve(args):
     ctx.close()
     torch.cuda.empty_cache()
     out = []
-    schedules = [("work-proportional steps (2^31 updates per job per step)", 1 << 31),
-                 ("fixed steps (512 pulses per job per step)", 0)]
-    for sched, step_updates in schedules:
-        for rate in [float(r) for r in args.rates.split(",")]:
-            srv = sarbp.Server(0, max_jobs=16, hbm_budget_bytes=96 << 30, pulses_per_step=512,
-                               step_updates=step_updates)
-            rng = np.random.default_rng(int(rate * 1000))
-            order = rng.integers(0, len(reqs), args.jobs)
-            gaps = rng.exponential(1.0 / rate, args.jobs)
-            tickets = []
-            t_first = time.perf_counter()
+    schedules = []
+    for u in (int(x) for x in args.step_updates.split(",")):
+        name = (f"work-proportional steps (2^{u.bit_length() - 1} updates per job per step)" if u > 0
+                else "fixed steps (512 pulses per job per step)")
+        schedules.append((name, u))
+    # rate-major, the schedules' order rotated per rate, so that a slow drift over
+    # the sweep (power, clocks) does not favour the schedule that runs first
+    rates = [float(r) for r in args.rates.split(",")]
+    runs = []
+    for k, rate in enumerate(rates):
+        for j in range(len(schedules)):
+            runs.append((schedules[(j + k) % len(schedules)], rate))
+    for (sched, step_updates), rate in runs:
+        clocks = ClockSampler(0)
+        clocks.start()
+        srv = sarbp.Server(0, max_jobs=16, hbm_budget_bytes=96 << 30, pulses_per_step=512,
+                           step_updates=step_updates)
+        rng = np.random.default_rng(int(rate * 1000))
+        order = rng.integers(0, len(reqs), args.jobs)
+        gaps = rng.exponential(1.0 / rate, args.jobs)
+        tickets = []
+        t_first = time.perf_counter()
 
-            def submitter():
-                t_next = time.perf_counter()
-                for k in range(args.jobs):
-                    t_next += gaps[k]
-                    d = t_next - time.perf_counter()
-                    if d > 0:
-                        time.sleep(d)
-                    sc, host, img = reqs[order[k]]
-                    r, g, _ = sarbp.scene_args(sc)
-                    tickets.append(srv.submit(r, g, host, sc.apc, sarbp.MODE_SPLIT, image=img))
+        def submitter():
+            t_next = time.perf_counter()
+            for k in range(args.jobs):
+                t_next += gaps[k]
+                d = t_next - time.perf_counter()
+                if d > 0:
+                    time.sleep(d)
+                sc, host, img = reqs[order[k]]
+                r, g, _ = sarbp.scene_args(sc)
+                tickets.append(srv.submit(r, g, host, sc.apc, sarbp.MODE_SPLIT, image=img))
 
-            th = threading.Thread(target=submitter)
-            th.start()
-            th.join()
-            lat, upd = [], 0.0
-            for t in tickets:
-                st, js, _ = srv.wait(t, 600000)
-                if st == sarbp.OK:
-                    lat.append(js.latency_ms)
-                    upd += js.updates
-            t_last = time.perf_counter()
-            stats = srv.stats()
-            srv.close()
-            lat.sort()
-            pct = lambda q: lat[min(len(lat) - 1, int(q * len(lat)))] if lat else None
-            out.append({"schedule": sched, "rate_jobs_s": rate, "jobs": len(lat), "p50_ms": pct(0.50), "p99_ms": pct(0.99),
-                        "mean_ms": sum(lat) / len(lat) if lat else None,
-                        "gpix_pulse_s": upd / (t_last - t_first) / 1e9,
-                        "busy_gpix_pulse_s": stats.updates / max(stats.busy_s, 1e-9) / 1e9,
-                        "peak_active": stats.peak_active, "graph_launches": stats.graph_launches,
-                        "peak_gb": stats.peak_bytes / 2**30})
+        th = threading.Thread(target=submitter)
+        th.start()
+        th.join()
+        lat, upd = [], 0.0
+        for t in tickets:
+            st, js, _ = srv.wait(t, 600000)
+            if st == sarbp.OK:
+                lat.append(js.latency_ms)
+                upd += js.updates
+        t_last = time.perf_counter()
+        stats = srv.stats()
+        srv.close()
+        clk = clocks.stop()
+        lat.sort()
+        pct = lambda q: lat[min(len(lat) - 1, int(q * len(lat)))] if lat else None
+        out.append({"schedule": sched, "rate_jobs_s": rate, "jobs": len(lat), "p50_ms": pct(0.50), "p99_ms": pct(0.99),
+                    "mean_ms": sum(lat) / len(lat) if lat else None,
+                    "gpix_pulse_s": upd / (t_last - t_first) / 1e9,
+                    "busy_gpix_pulse_s": stats.updates / max(stats.busy_s, 1e-9) / 1e9,
+                    "peak_active": stats.peak_active, "graph_launches": stats.graph_launches,
+                    "peak_gb": stats.peak_bytes / 2**30, "clocks": clk})
     line = {"metric": "serving p50/p99 latency and aggregate Gpix*pulse/s", "mode": "split",
             "workload": "config 4: Poisson arrivals, 256-8192 pulses x 2048-8192 samples, grids 256^2-4096^2 "
                         "log-uniform at 0.25 m, 9-200 targets, 20 dB SNR; 24 distinct requests drawn at random",
