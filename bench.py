@@ -170,13 +170,22 @@ def cpu_tile_side(orc, scene, rc, seconds: float) -> int:
     return max(32, min(side, g.nx, g.ny))
 
 
+def host_threads() -> int:
+    """Host threads this process may use (its CPU affinity).  The CPU arms run
+    on rank 0 alone, so they take all of them rather than the OMP_NUM_THREADS=1
+    that torchrun sets for every rank."""
+    try:
+        return len(os.sched_getaffinity(0))
+    except (AttributeError, OSError):
+        return os.cpu_count() or 1
+
+
 def cpu_sample(scene, threads=None, seconds: float = 12.0):
     """FP64 oracle back-projection of a centred square tile (all pulses) of the
     scene, sized for about `seconds` of host work, on range-compressed data
     computed by the oracle.  Returns (updates/s, cores, description, seconds)."""
     from oracle import oracle as orc
-    if threads:
-        orc.set_threads(threads)
+    orc.set_threads(threads or host_threads())
     cores = orc.threads()
     g = scene.grid
     # range-compress the pulses once (untimed setup): oracle FP64 chain
@@ -199,6 +208,7 @@ def run_reference(args):
     if rank != 0:
         return 0
     from oracle import oracle as orc
+    orc.set_threads(host_threads())
     scene = workload(args.size)
     echo = orc.echo(scene)
     rc = orc.range_compress(scene, echo)
