@@ -144,3 +144,34 @@ def test_wk_stages_match_oracle_and_pipeline(ctx, shape):
     img = ctx.dft2d(F.copy(), inverse=True)
     assert np.array_equal(img, ctx.wk_image(p, echo))
     assert metrics.rel_l2_db(img, wk.wk_image(echo.astype(np.complex128), p)) <= -80.0
+
+
+def test_stage_entry_points_device_pointers_and_errors(ctx):
+    """Device-resident buffers give the host path's bits (sarbp_dft2d in place,
+    sarbp_wk_focus in place as documented); invalid arguments return a status."""
+    torch = pytest.importorskip("torch")
+    p = wk.radarsat1()
+    echo = rand((192, 128), 5)
+    NA, NR, _ = ctx.wk_padded_size(192, 128)
+    host_x = ctx.wk_preprocess(p, echo)
+    w = sarbp.wk_params(p)
+    d_echo = torch.from_numpy(echo.view(np.float32)).cuda()
+    d_x = torch.empty((NA, NR * 2), dtype=torch.float32, device="cuda")
+    ctx.check(ctx.lib.sarbp_wk_preprocess(ctx.h, sarbp.ctypes.byref(w), d_echo.data_ptr(), 192, 128, d_x.data_ptr(),
+                                          None), "preprocess device")
+    ctx.check(ctx.lib.sarbp_dft2d(ctx.h, d_x.data_ptr(), NA, NR, 0, None), "dft2d device")
+    ctx.check(ctx.lib.sarbp_wk_focus(ctx.h, sarbp.ctypes.byref(w), d_x.data_ptr(), NA, NR, d_x.data_ptr(), None),
+              "focus in place")
+    ctx.synchronize()
+    host_f = ctx.wk_focus(p, ctx.dft2d(host_x.copy()))
+    assert np.array_equal(d_x.cpu().numpy().view(np.complex64), host_f)
+    with pytest.raises(sarbp.SarbpError):
+        ctx.dft2d(np.zeros((0, 8), dtype=np.complex64))
+    with pytest.raises(sarbp.SarbpError):
+        ctx.dft2d(np.zeros((4, 8193), dtype=np.complex64))  # 8193 is neither a power of two nor <= 8192
+    q = wk.radarsat1()
+    q.vr = float("nan")
+    with pytest.raises(sarbp.SarbpError):
+        ctx.wk_preprocess(q, echo)
+    with pytest.raises(sarbp.SarbpError):
+        ctx.wk_focus(p, np.zeros((8, 40000), dtype=np.complex64))  # Stolt row too large for shared memory
