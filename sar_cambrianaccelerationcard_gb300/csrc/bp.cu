@@ -444,6 +444,80 @@ __device__ __forceinline__ void flush_projection(const BpPlan &P, const Smem &S,
     }
 }
 
+// One chunk of the weighted projection: per pulse, this thread's sum over its
+// pixels of conj(w) * term, then the warp's sum into red[2 pulse + {re, im}].
+// conj(w) e^{i phi} = |w| e^{i (phi - arg w)}: the weight's phase joins the
+// packed phase (half an op per pixel) and its magnitude scales cos / sin, so
+// the weighted accumulate costs 6.5 FP32 ops instead of 8.
+// Pulses go in pairs through one shared butterfly: the xor-16 step splits the
+// pair's two pulses between the half-warps and the xor-8 step splits re / im,
+// so a pair costs 6 shuffles instead of 20 for two separate 32-lane sums.
+template <int NTERMS, int PIX>
+__device__ __forceinline__ void project_chunk(const Smem &S, int stage, int count, int win, unsigned sbase, int cen,
+                                              f2 XC2, const f2 (&YC2)[PIX / 2], const f2 (&QQ2)[PIX / 2], f2 BPM2,
+                                              f2 KH2, f2 KL2, const f2 (&TH2)[PIX / 2], const float (&wm)[PIX],
+                                              float *red) {
+    const int lane = threadIdx.x & 31;
+    const bool hi16 = (lane & 16) != 0, hi8 = (lane & 8) != 0;
+    f2 MP = pk2(kMagic + (float)cen, kMagic + (float)cen);
+    const f2 WIN2 = pk2((float)win, (float)win);
+#pragma unroll 1
+    for (int pl = 0; pl < count; pl += 2) {
+        float tr[2] = {0.f, 0.f}, ti[2] = {0.f, 0.f};
+#pragma unroll
+        for (int u2 = 0; u2 < 2; ++u2) {
+            if (u2 == 1 && pl + 1 >= count) break;  // odd tail: pulse-uniform
+            const Prm &q = S.prm[stage * kChunk + pl + u2];
+            f2 C1, C2, C3, C4, BT, PHT, AA, BB;
+            lds2x2(&q.k0, C1, C2);
+            lds2x2(&q.k1, C3, C4);
+            lds2x2(&q.k2, BT, PHT);
+            lds2x2(&q.k3, AA, BB);
+            const f2 XA = fmul2(XC2, AA);
+#pragma unroll
+            for (int h = 0; h < PIX / 2; ++h) {
+                const f2 n = ffma2(YC2[h], BB, fadd2(XA, QQ2[h]));
+                f2 poly = NTERMS == 4 ? ffma2(n, ffma2(n, C4, C3), C2) : ffma2(n, C3, C2);
+                poly = ffma2(n, poly, C1);
+                const f2 dR = fmul2(n, poly);
+                const f2 b2 = ffma2(dR, BPM2, BT);
+#if SARBP_BP_PHASE_COMPENSATED
+                const f2 ph2 = fadd2(ffma2(dR, KL2, ffma2(dR, KH2, PHT)), TH2[h]);
+#else
+                const f2 ph2 = fadd2(ffma2(dR, KH2, PHT), TH2[h]);
+#endif
+                float bb[2], ph[2], tt[2];
+                upk2(b2, bb[0], bb[1]);
+                upk2(ph2, ph[0], ph[1]);
+                upk2(fadd2(b2, MP), tt[0], tt[1]);
+#pragma unroll
+                for (int u = 0; u < 2; ++u) {
+                    const int j = 2 * h + u;
+                    const float4 v = lds128((__float_as_uint(tt[u]) << 4) + sbase);
+                    const float sr = fmaf(bb[u], v.z, v.x);
+                    const float si = fmaf(bb[u], v.w, v.y);
+                    float sn, cs;
+                    __sincosf(ph[u], &sn, &cs);
+                    const float zr = wm[j] * cs, zi = wm[j] * sn;
+                    tr[u2] = fmaf(sr, zr, fmaf(-si, zi, tr[u2]));
+                    ti[u2] = fmaf(sr, zi, fmaf(si, zr, ti[u2]));
+                }
+            }
+            MP = fadd2(MP, WIN2);
+        }
+        float k0 = hi16 ? tr[1] : tr[0], k1 = hi16 ? ti[1] : ti[0];
+        k0 += __shfl_xor_sync(0xffffffffu, hi16 ? tr[0] : tr[1], 16);
+        k1 += __shfl_xor_sync(0xffffffffu, hi16 ? ti[0] : ti[1], 16);
+        float k = hi8 ? k1 : k0;
+        k += __shfl_xor_sync(0xffffffffu, hi8 ? k0 : k1, 8);
+        k += __shfl_xor_sync(0xffffffffu, k, 4);
+        k += __shfl_xor_sync(0xffffffffu, k, 2);
+        k += __shfl_xor_sync(0xffffffffu, k, 1);
+        const int pp = pl + (hi16 ? 1 : 0);
+        if ((lane & 7) == 0 && pp < count) red[2 * pp + (hi8 ? 1 : 0)] = k;
+    }
+}
+
 // ADJ: weighted projection (the adjoint) instead of back-projection: every
 // pixel's term of pulse p is multiplied by conj(weight[pixel]) and summed over
 // the tile into proj[tile][p] (SPLIT / FP16STORE arithmetic).
@@ -520,16 +594,17 @@ __global__ void __launch_bounds__(kThreads, SARBP_BP_MINBLOCKS)
     const float kph_lo = (float)(kph_d - (double)kph_hi);
     const float wmax = (float)(win - 2);
 
-    // weighted projection: conj(weight) of this thread's pixels (zero outside the grid)
-    float wr[ADJ ? kPix : 1], wi[ADJ ? kPix : 1];
+    // weighted projection: |weight| and -arg(weight) of this thread's pixels
+    // (zero outside the grid)
+    float wm[ADJ ? kPix : 1], wth[ADJ ? kPix : 1];
     if constexpr (ADJ) {
 #pragma unroll
         for (int j = 0; j < kPix; ++j) {
             const int x = tx * kTileX + xl, y = ty * kTileY + ((warp >> 2) + 2 * j) * 4 + ly;
             float2 w = make_float2(0.f, 0.f);
             if (x < P.g.nx && y < P.g.ny) w = __ldg(&P.weight[(size_t)y * P.g.nx + x]);
-            wr[j] = w.x;
-            wi[j] = w.y;
+            wm[j] = hypotf(w.x, w.y);
+            wth[j] = -atan2f(w.y, w.x);
         }
     }
 
@@ -546,11 +621,12 @@ __global__ void __launch_bounds__(kThreads, SARBP_BP_MINBLOCKS)
 
     const f2 XC2 = pk2(xc, xc);
     const f2 BPM2 = pk2(bpm, bpm), KH2 = pk2(kph_hi, kph_hi), KL2 = pk2(kph_lo, kph_lo);
-    f2 YC2[kPix / 2], QQ2[kPix / 2];
+    f2 YC2[kPix / 2], QQ2[kPix / 2], TH2[ADJ ? kPix / 2 : 1];
 #pragma unroll
     for (int h = 0; h < kPix / 2; ++h) {
         YC2[h] = pk2(yc[2 * h], yc[2 * h + 1]);
         QQ2[h] = pk2(qq[2 * h], qq[2 * h + 1]);
+        if constexpr (ADJ) TH2[h] = pk2(wth[2 * h], wth[2 * h + 1]);
     }
 
     if (nchunks > 0) produce<MODE, STORE, PIX>(P, S, 0, p_begin, min(chunk, p_end - p_begin), T);
@@ -578,7 +654,10 @@ __global__ void __launch_bounds__(kThreads, SARBP_BP_MINBLOCKS)
 
         const float4 *stg = S.staged + (size_t)sbuf * chunk * win;
         const unsigned sbase = smem_addr(stg) - kMagicBitsShift4;
-        if (MODE == SARBP_MODE_SPLIT || MODE == SARBP_MODE_FP16STORE) {
+        if constexpr (ADJ) {
+            project_chunk<NTERMS, kPix>(S, stage, count, win, sbase, cen, XC2, YC2, QQ2, BPM2, KH2, KL2, TH2, wm,
+                                  reinterpret_cast<float *>(S.red + ((c & 1) * kWarps + warp) * kChunk));
+        } else if (MODE == SARBP_MODE_SPLIT || MODE == SARBP_MODE_FP16STORE) {
             // geometry, bin and phase for pixel pairs (2j, 2j+1) in packed FP32x2;
             // interpolation and the complex accumulate per pixel
             f2 MP = pk2(kMagic + (float)cen, kMagic + (float)cen);
@@ -592,7 +671,6 @@ __global__ void __launch_bounds__(kThreads, SARBP_BP_MINBLOCKS)
                 lds2x2(&q.k2, BT, PHT);
                 lds2x2(&q.k3, AA, BB);
                 const f2 XA = fmul2(XC2, AA);
-                float tr = 0.f, ti = 0.f;  // projection: this thread's sum for the pulse
 #pragma unroll
                 for (int h = 0; h < kPix / 2; ++h) {
                     const f2 n = ffma2(YC2[h], BB, fadd2(XA, QQ2[h]));
@@ -628,23 +706,9 @@ __global__ void __launch_bounds__(kThreads, SARBP_BP_MINBLOCKS)
                         const float si = fmaf(bb[u], v.w, v.y);
                         float sn, cs;
                         __sincosf(ph[u], &sn, &cs);
-                        if constexpr (ADJ) {
-                            const float ur = fmaf(sr, cs, -si * sn), ui = fmaf(sr, sn, si * cs);
-                            tr = fmaf(wr[j], ur, fmaf(wi[j], ui, tr));
-                            ti = fmaf(wr[j], ui, fmaf(-wi[j], ur, ti));
-                        } else {
-                            acc_r[j] = fmaf(sr, cs, fmaf(-si, sn, acc_r[j]));
-                            acc_i[j] = fmaf(sr, sn, fmaf(si, cs, acc_i[j]));
-                        }
+                        acc_r[j] = fmaf(sr, cs, fmaf(-si, sn, acc_r[j]));
+                        acc_i[j] = fmaf(sr, sn, fmaf(si, cs, acc_i[j]));
                     }
-                }
-                if constexpr (ADJ) {
-#pragma unroll
-                    for (int o = 16; o > 0; o >>= 1) {
-                        tr += __shfl_xor_sync(0xffffffffu, tr, o);
-                        ti += __shfl_xor_sync(0xffffffffu, ti, o);
-                    }
-                    if (lane == 0) S.red[((c & 1) * kWarps + warp) * kChunk + pl] = make_float2(tr, ti);
                 }
                 MP = fadd2(MP, WIN2);
             }
@@ -821,6 +885,12 @@ __global__ void proj_reduce_kernel(const float2 *__restrict__ proj, int tiles, i
 
 template <int STORE, int PIX>
 cudaError_t launch_proj_pix(const BpPlan &p, cudaStream_t s, int tiles, int tiles_y, int pps, float qq_max) {
+    if constexpr (PIX == 8) {  // the usual tile: pulse chunk fixed at compile time
+        if (p.chunk == kChunk)
+            return p.nterms == 3
+                       ? launch_variant<SARBP_MODE_SPLIT, STORE, 3, false, PIX, true, kChunk>(p, s, tiles, tiles_y, pps, qq_max)
+                       : launch_variant<SARBP_MODE_SPLIT, STORE, 4, false, PIX, true, kChunk>(p, s, tiles, tiles_y, pps, qq_max);
+    }
     return p.nterms == 3 ? launch_variant<SARBP_MODE_SPLIT, STORE, 3, false, PIX, true>(p, s, tiles, tiles_y, pps, qq_max)
                          : launch_variant<SARBP_MODE_SPLIT, STORE, 4, false, PIX, true>(p, s, tiles, tiles_y, pps, qq_max);
 }
@@ -945,13 +1015,34 @@ __global__ void __launch_bounds__(256) bp_extremes_kernel(const double *apc, int
         cx = fmax(cx, __shfl_xor_sync(0xffffffffu, cx, o));
         sy = fmax(sy, __shfl_xor_sync(0xffffffffu, sy, o));
     }
+    // the block's warps combine in shared memory, then one thread per block
+    // updates the result (order-free min / max: the same bits as the host's)
+    __shared__ double red[4][8];
+    __shared__ int red_bad;
+    const int warp = threadIdx.x >> 5;
+    if (threadIdx.x == 0) red_bad = 0;
+    __syncthreads();
     const bool any_bad = __any_sync(0xffffffffu, bad);
     if ((threadIdx.x & 31) == 0) {
+        red[0][warp] = rmin;
+        red[1][warp] = rmax;
+        red[2][warp] = cx;
+        red[3][warp] = sy;
+        if (any_bad) red_bad = 1;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {  // holds warp 0's values already
+        for (int w = 1; w < (int)(blockDim.x >> 5); ++w) {
+            rmin = fmin(rmin, red[0][w]);
+            rmax = fmax(rmax, red[1][w]);
+            cx = fmax(cx, red[2][w]);
+            sy = fmax(sy, red[3][w]);
+        }
         atomicMin(&out[0], (unsigned long long)__double_as_longlong(rmin));
         atomicMax(&out[1], (unsigned long long)__double_as_longlong(rmax));
         atomicMax(&out[2], (unsigned long long)__double_as_longlong(cx));
         atomicMax(&out[3], (unsigned long long)__double_as_longlong(sy));
-        if (any_bad) atomicOr(&out[4], 1ull);
+        if (red_bad) atomicOr(&out[4], 1ull);
     }
 }
 
@@ -962,7 +1053,8 @@ cudaError_t launch_bp_extremes(const double *apc, int np, const sarbp_grid &g, u
     double lux, luy;
     ext_axes(g, &lux, &luy);
     const long long total = (long long)np * kLattice * kLattice;
-    const int blocks = (int)std::min<long long>((total + 255) / 256, 2048);
+    // a few points per thread; one atomic update per block and quantity
+    const int blocks = (int)std::min<long long>((total + 255) / 256, 512);
     bp_extremes_kernel<<<blocks, 256, 0, s>>>(apc, np, g, lux, luy, out);
     return cudaGetLastError();
 }

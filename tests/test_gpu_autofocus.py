@@ -95,6 +95,23 @@ def test_weighted_projection(ctx, orc, case, mode):
     assert abs(lhs - out.sum()) <= 1e-3 * abs(lhs)
 
 
+@pytest.mark.parametrize("np_", [253, 17, 1])
+def test_weighted_projection_odd_pulse_counts(ctx, orc, np_):
+    """Pulses are summed in pairs: odd chunk tails (253 = 15 x 16 + 13 over
+    several segments, 17, a single pulse) against the oracle."""
+    s = scenes.config1(np_=np_, ns=1024, n_img=96)
+    rc = orc.range_compress(s, orc.echo(s)).astype(np.complex64)
+    r, g, lay = sarbp.scene_args(s)
+    rng = np.random.default_rng(np_)
+    w = (rng.standard_normal((g.ny, g.nx)) + 1j * rng.standard_normal((g.ny, g.nx))).astype(np.complex64)
+    ref = orc.project_weighted(s, rc, w, None, None)
+    out = ctx.project_weighted(r, rc, s.apc, g, sarbp.MODE_SPLIT, lay.t0_bins, lay.bin_rate, w)
+    assert out.shape == (np_,)
+    err = metrics.rel_l2_db(out, ref)
+    print("projection rel-L2 dB", np_, err)
+    assert err <= -60.0
+
+
 def test_projection_is_deterministic(ctx, case):
     s, rc, dr, ph = case
     r, g, lay = sarbp.scene_args(s)
