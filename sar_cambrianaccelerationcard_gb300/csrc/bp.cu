@@ -246,11 +246,11 @@ __device__ __forceinline__ void produce(const BpPlan &P, const Smem &S, int stag
     unsigned dst = 0;
     if (lane < kPerWarp && slot < count) {
         const int p = p0 + slot;
-        const float bpm = (float)(2.0 / P.c * P.bin_rate);  // bins per metre of range
+        const float bpm = P.kb_h;  // bins per metre of range
         const float hx = 0.5f * (kTileX - 1), hy = 0.5f * (kTileY - 1);
         const int cen = win >> 1;  // staged index origin
         Prm &q = S.prm[stage * kChunk + slot];
-        long long ws;
+        int ws;  // window start, clamped to +-1e9 bins: int arithmetic throughout
         bool sane;
         if (MODE == SARBP_MODE_SPLIT || MODE == SARBP_MODE_FP16STORE) {
             // R_T^2 = a0 + xT a1 + yT a2 + |q_T|^2 in float-float
@@ -272,12 +272,12 @@ __device__ __forceinline__ void produce(const BpPlan &P, const Smem &S, int stag
             const float fr = (cy - rintf(cy)) + cy_e;
             const float phT = fmaf(fr, 6.28318530717958647692f, r1v.w);
             const float iR = 1.0f / r;
-            const float A = r0v.z + 2.f * (T.xT * (float)P.g.g11 + T.yT * (float)P.g.g12);
-            const float B = r1v.x + 2.f * (T.xT * (float)P.g.g12 + T.yT * (float)P.g.g22);
+            const float A = r0v.z + 2.f * (T.xT * P.gf11 + T.yT * P.gf12);
+            const float B = r1v.x + 2.f * (T.xT * P.gf12 + T.yT * P.gf22);
             const float half = bpm * (fabsf(A) * hx + fabsf(B) * hy + T.qq_max) * 0.5f * iR * 1.03f + 2.f;
-            ws = (long long)floorf(fminf(fmaxf(bT.h - half, -1.0e9f), 1.0e9f));
-            ws &= ~3LL;
-            const long long need_end = (long long)ceilf(fminf(bT.h + half, 1.0e9f)) + 2;
+            ws = (int)floorf(fminf(fmaxf(bT.h - half, -1.0e9f), 1.0e9f));
+            ws &= ~3;
+            const int need_end = (int)ceilf(fminf(fmaxf(bT.h + half, -1.0e9f), 1.0e9f)) + 2;
             sane = isfinite(r) && r > 0.f && isfinite(half) && isfinite(phT) && need_end - ws <= win;
             const float i2 = iR * iR;
             if (sane) {
@@ -304,9 +304,9 @@ __device__ __forceinline__ void produce(const BpPlan &P, const Smem &S, int stag
             const double bT = fma(R, 2.0 / P.c * P.bin_rate, -P.t0_bins * P.bin_rate);
             const float half = bpm * (fabsf(A) * hx + fabsf(B) * hy + T.qq_max) * 0.5f * iR * 1.03f + 2.f;
             const float bTf = (float)bT;
-            ws = (long long)floorf(fminf(fmaxf(bTf - half, -1.0e9f), 1.0e9f));
-            ws &= ~3LL;
-            const long long need_end = (long long)ceilf(fminf(bTf + half, 1.0e9f)) + 2;
+            ws = (int)floorf(fminf(fmaxf(bTf - half, -1.0e9f), 1.0e9f));
+            ws &= ~3;
+            const int need_end = (int)ceilf(fminf(fmaxf(bTf + half, -1.0e9f), 1.0e9f)) + 2;
             sane = isfinite(R) && R > 0.0 && isfinite(half) && need_end - ws <= win;
             if (MODE == SARBP_MODE_FP32) {
                 const double kph_d = 4.0 * CUDART_PI * P.fc / P.c;
@@ -322,12 +322,12 @@ __device__ __forceinline__ void produce(const BpPlan &P, const Smem &S, int stag
             q.az = az;
         }
         if (!sane) atomicOr(P.err, kErrWindow);
-        long long lo = ws < 0 ? 0 : ws;
-        long long hi = ws + win > P.nbins ? P.nbins : ws + win;
+        const int lo = ws < 0 ? 0 : ws;
+        int hi = ws + win > P.nbins ? P.nbins : ws + win;
         if (hi < lo || !sane) hi = lo;
-        q.ws = (int)ws;
-        q.lo = (int)(lo - ws);
-        q.hi = (int)(hi - ws);
+        q.ws = ws;
+        q.lo = lo - ws;
+        q.hi = hi - ws;
         q.scale = STORE == SARBP_STORE_C32H ? __ldg(&P.scale[p]) : 1.f;
         if (hi > lo) {
             bytes = (unsigned)((hi - lo) * esize);
@@ -548,7 +548,7 @@ __global__ void __launch_bounds__(kThreads, SARBP_BP_MINBLOCKS)
     const int xl = (warp & 3) * 8 + lx;
     const float xc = (float)xl - 0.5f * (kTileX - 1);
     float yc[kPix], qq[kPix];
-    const float g11 = (float)P.g.g11, g12 = (float)P.g.g12, g22 = (float)P.g.g22;
+    const float g11 = P.gf11, g12 = P.gf12, g22 = P.gf22;
 #pragma unroll
     for (int j = 0; j < kPix; ++j) {
         const int yl = ((warp >> 2) + 2 * j) * 4 + ly;
@@ -588,10 +588,8 @@ __global__ void __launch_bounds__(kThreads, SARBP_BP_MINBLOCKS)
 #pragma unroll
     for (int j = 0; j < (MODE == SARBP_MODE_FP64 ? kPix : 1); ++j) { dacc_r[j] = 0.0; dacc_i[j] = 0.0; }
 
-    const float bpm = (float)(2.0 / P.c * P.bin_rate);
-    const double kph_d = 4.0 * CUDART_PI * P.fc / P.c;
-    const float kph_hi = (float)kph_d;
-    const float kph_lo = (float)(kph_d - (double)kph_hi);
+    const float bpm = P.kb_h;
+    const float kph_hi = P.kp_h, kph_lo = P.kp_l;  // 4 pi fc / c as a float pair
     const float wmax = (float)(win - 2);
 
     // weighted projection: |weight| and -arg(weight) of this thread's pixels
@@ -719,7 +717,7 @@ __global__ void __launch_bounds__(kThreads, SARBP_BP_MINBLOCKS)
                 const float4 k0 = q.k0;
                 const float phc = q.k1.x;  // per-pulse phase correction
                 const float mp = kMagic + (float)(pl * win + cen);
-                const float kph = (float)kph_d;
+                const float kph = kph_hi;
 #pragma unroll
                 for (int j = 0; j < kPix; ++j) {
                     const float dx = k0.x - fpxx[j], dy = k0.y - fpy[j], dz = k0.z - fpz[j];

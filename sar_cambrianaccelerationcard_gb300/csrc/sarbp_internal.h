@@ -68,6 +68,11 @@ struct BpPlan {
     // float pairs of 2 bin_rate / c (bins per metre of range), t0_bins * bin_rate and
     // 2 fc / c (carrier cycles per metre of range) for the float-float tile references
     float kb_h, kb_l, tb_h, tb_l, kc_h, kc_l;
+    // float pair of 4 pi fc / c (carrier phase per metre) and the grid metric
+    // in FP32: constants of the launch, so the kernel's per-chunk code has no
+    // FP64 division or conversion
+    float kp_h, kp_l;
+    float gf11, gf12, gf22;
     float2 *image;           // [ny][nx] final image
     float2 *partial;         // [segments][ny][nx] scratch when segments > 1
     int segments;            // pulse segments (1: write image directly)
