@@ -181,18 +181,43 @@ bool plan_bp(int sms, const sarbp_radar &r, const sarbp_rc_view &rc, const BpExt
     if (!chosen) return false;
     int tx, ty;
     bp_tile_dims(p.pix, &tx, &ty);
-    // pulse segments: fill at least ~2 waves of CTAs
     const int tiles = ((g.nx + tx - 1) / tx) * ((g.ny + ty - 1) / ty);
-    // The segment count depends on the geometry only (not on the staging chunk,
-    // which the planner or SARBP_BP_CHUNK picks): partial images are summed per
-    // segment, so the same call gives the same bits whatever the chunk.  Two
-    // CTAs per SM (the SPLIT kernels' register bound).
-    const int want = 2 * sms * 2;
     const int npl = pulses_per_launch > 0 ? pulses_per_launch : np;
-    int segments = 1;
-    while (tiles * segments < want && npl / (segments * 2) >= 4 * bp_max_chunk()) segments *= 2;
-    p.segments = segments;
+    p.segments = bp_choose_segments(tiles, npl, (long long)g.nx * g.ny, sms);
     return true;
+}
+
+// Pulse segments: every (tile, segment) is one CTA, two resident per SM (the
+// SPLIT kernels' register bound).  Finer CTAs fill the last wave and balance
+// CTAs that end at different times; measured on GB300 (4096 pulses, config-2
+// geometry, ms per call for 1 / 2 / 4 / 8 segments): 1024^2 4.10 / 3.58 / 3.54
+// / 3.42, 1536^2 8.00 / 7.94 / 7.68 / 7.58 (5: 7.54), 2048^2 13.82 / 13.30 /
+// 13.27 / 13.32; config 1 (512 pulses, 512^2) 0.237 / 0.202 / 0.201 / 0.188.
+// Rule: the fewest segments that give at least 12 waves of CTAs, with at least
+// 4 chunks of pulses per segment, no empty segment and the partial images (one
+// per segment) within 1 GiB.  The count depends on the geometry only (not on
+// the staging chunk, which the planner or SARBP_BP_CHUNK picks), so a call
+// gives the same bits whatever the chunk.  SARBP_BP_SEGMENTS=n (1..64) forces
+// n, for sweeps.
+int bp_choose_segments(int tiles, int npl, long long npix, int sms) {
+    const int kc = bp_max_chunk();
+    const char *env = std::getenv("SARBP_BP_SEGMENTS");
+    if (env && env[0]) {
+        const int s = std::atoi(env);
+        if (s >= 1 && s <= 64) return s;
+    }
+    const long long target = 12LL * 2 * std::max(sms, 1);
+    const double max_partial = 1024.0 * 1024.0 * 1024.0;
+    int best = 1;
+    for (int s = 1; s <= 64; ++s) {
+        if (s > 1 && (npl / s < 4 * kc || (double)s * (double)npix * 8.0 > max_partial)) break;
+        const int n = (npl + s - 1) / s;
+        const int pps = (n + kc - 1) / kc * kc;  // as the launch rounds it
+        if (s > 1 && (long long)(s - 1) * pps >= npl) continue;  // an empty segment
+        best = s;
+        if ((long long)tiles * s >= target) break;
+    }
+    return best;
 }
 
 void rc_tables_host(const sarbp_radar &r, const sarbp_rc_layout &lay, std::vector<float2> &filt,

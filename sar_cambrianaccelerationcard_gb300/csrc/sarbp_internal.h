@@ -177,6 +177,10 @@ void bp_tile_dims(int pix, int *tile_x, int *tile_y);
 // Dynamic shared memory of a BP CTA for a staging window and pulse chunk.
 size_t bp_smem_bytes(int storage, int win, int chunk);
 int bp_max_chunk();  // largest pulse chunk (16); the planner may choose 8 or 4
+// Pulse segments for `tiles` tiles and `npl` pulses per launch on `sms` SMs
+// (at least 12 waves of CTAs where the pulses allow; at least 4 chunks per
+// segment; partial images within 1 GiB).
+int bp_choose_segments(int tiles, int npl, long long npix, int sms);
 
 // ---------------------------------------------------------------- echo synthesis
 cudaError_t launch_echo_synth(const double *apc, int np, int ns, const sarbp_target *tg, int nt,
