@@ -868,17 +868,36 @@ cudaError_t launch_pix(const BpPlan &p, cudaStream_t s, int tiles, int tiles_y, 
     }
 }
 
-// out[p] = sum over tiles of proj[tile][p], accumulated in FP64 in tile order.
-__global__ void proj_reduce_kernel(const float2 *__restrict__ proj, int tiles, int np, double2 *__restrict__ out) {
-    const int p = blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= np) return;
+// out[p] = sum over tiles of proj[tile][p] in FP64.  A CTA takes 32 pulses
+// (one per lane, coalesced rows); its 16 warps take tiles w, w + 16, ... and
+// their partial sums combine in warp order, so the order is fixed and the
+// result deterministic.  (One thread per pulse walking every tile kept only
+// np / 128 CTAs busy: 0.15 ms for 512 tiles x 4096 pulses.)
+constexpr int kProjWarps = 16;
+__global__ void __launch_bounds__(32 * kProjWarps)
+    proj_reduce_kernel(const float2 *__restrict__ proj, int tiles, int np, double2 *__restrict__ out) {
+    __shared__ double2 part[kProjWarps][32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int p = blockIdx.x * 32 + lane;
     double sr = 0.0, si = 0.0;
-    for (int t = 0; t < tiles; ++t) {
-        const float2 v = __ldg(&proj[(size_t)t * np + p]);
-        sr += v.x;
-        si += v.y;
+    if (p < np) {
+        for (int t = warp; t < tiles; t += kProjWarps) {
+            const float2 v = __ldg(&proj[(size_t)t * np + p]);
+            sr += v.x;
+            si += v.y;
+        }
     }
-    out[p] = make_double2(sr, si);
+    part[warp][lane] = make_double2(sr, si);
+    __syncthreads();
+    if (warp == 0 && p < np) {
+        double r = 0.0, i = 0.0;
+#pragma unroll
+        for (int w = 0; w < kProjWarps; ++w) {
+            r += part[w][lane].x;
+            i += part[w][lane].y;
+        }
+        out[p] = make_double2(r, i);
+    }
 }
 
 template <int STORE, int PIX>
@@ -941,7 +960,7 @@ cudaError_t launch_project(const BpPlan &p, double2 *out, cudaStream_t s, int *l
                   : launch_proj_pix<SARBP_STORE_C64, 2>(p, s, tiles, tiles_y, pps, qq_max);
     if (e != cudaSuccess) return e;
     if (launches) ++*launches;
-    proj_reduce_kernel<<<(p.np + 255) / 256, 256, 0, s>>>(p.proj, tiles, p.np, out);
+    proj_reduce_kernel<<<(p.np + 31) / 32, 32 * kProjWarps, 0, s>>>(p.proj, tiles, p.np, out);
     e = cudaGetLastError();
     if (launches) ++*launches;
     return e;
