@@ -173,3 +173,61 @@ def test_wide_coarse_grid_plans_and_matches_fp64(ctx):
     err = 20 * np.log10(np.linalg.norm(img[:256, :256] - ref) / np.linalg.norm(ref))
     print("coarse grid near-range corner rel-L2 dB", err)
     assert err <= -65.0
+
+
+def expected_segments(tiles, npl, npix, sms):
+    """The planner's rule restated: the fewest segments giving 12 waves of CTAs
+    (two per SM), at least 64 pulses per segment, no empty segment, partial
+    images within 1 GiB."""
+    best = 1
+    for s in range(1, 65):
+        if s > 1 and (npl // s < 64 or s * npix * 8 > 2 ** 30):
+            break
+        n = (npl + s - 1) // s
+        pps = (n + 15) // 16 * 16
+        if s > 1 and (s - 1) * pps >= npl:
+            continue
+        best = s
+        if tiles * s >= 12 * 2 * sms:
+            break
+    return best
+
+
+@pytest.mark.parametrize("n_img,np_", [(4096, 4096), (2048, 4096), (1024, 4096), (512, 512), (256, 100)])
+def test_segments_fill_waves(ctx, n_img, np_):
+    """Pulse segments follow the 12-wave rule: config 2 keeps one segment, a
+    1024^2 image of 4096 pulses on 152 SMs takes 8, short apertures stop at 64
+    pulses per segment."""
+    torch = pytest.importorskip("torch")
+    sms = torch.cuda.get_device_properties(0).multi_processor_count
+    s = scenes.config2(n_img=n_img) if np_ == 4096 else scenes.config1(np_=np_, ns=1024, n_img=n_img)
+    r, g, _ = sarbp.scene_args(s)
+    info = ctx.bp_plan(r, view(s), s.apc, g, sarbp.MODE_SPLIT)
+    tiles = ((g.nx + info.tile_x - 1) // info.tile_x) * ((g.ny + info.tile_y - 1) // info.tile_y)
+    assert info.segments == expected_segments(tiles, np_, g.nx * g.ny, sms)
+    if sms == 152:
+        assert info.segments == {4096: 1, 2048: 2, 1024: 8, 512: 8, 256: 1}[n_img]
+
+
+def test_forced_segments_agree(ctx, monkeypatch):
+    """Segment counts only regroup the per-pixel pulse sums: 1, 3 and 7
+    segments (uneven last segments) agree with the planner's choice to FP32
+    rounding.  The weighted projection sums each pulse inside one CTA per tile
+    whatever the segments, so it is bit-identical."""
+    s = scenes.config1(np_=700, ns=1024, n_img=128)
+    r, g, lay = sarbp.scene_args(s)
+    rc = ctx.range_compress(r, sarbp.synthesize(ctx, s))
+    w = (np.random.default_rng(9).standard_normal((g.ny, g.nx)) + 0j).astype(np.complex64)
+    monkeypatch.delenv("SARBP_BP_SEGMENTS", raising=False)
+    auto = ctx.bp_plan(r, view(s), s.apc, g, sarbp.MODE_SPLIT).segments
+    ref = ctx.backproject(r, rc, s.apc, g, sarbp.MODE_SPLIT, lay.t0_bins, lay.bin_rate)
+    pref = ctx.project_weighted(r, rc, s.apc, g, sarbp.MODE_SPLIT, lay.t0_bins, lay.bin_rate, w)
+    for n in ("1", "3", "7"):
+        monkeypatch.setenv("SARBP_BP_SEGMENTS", n)
+        assert ctx.bp_plan(r, view(s), s.apc, g, sarbp.MODE_SPLIT).segments == int(n)
+        img = ctx.backproject(r, rc, s.apc, g, sarbp.MODE_SPLIT, lay.t0_bins, lay.bin_rate)
+        prj = ctx.project_weighted(r, rc, s.apc, g, sarbp.MODE_SPLIT, lay.t0_bins, lay.bin_rate, w)
+        err = 20 * np.log10(np.linalg.norm(img - ref) / np.linalg.norm(ref))
+        print("segments", n, "vs", auto, "image rel-L2 dB", err)
+        assert err <= -110.0
+        assert np.array_equal(prj, pref)
