@@ -412,8 +412,8 @@ typedef struct sarbp_job {
 typedef struct sarbp_job_stats {
     int32_t status;          /* the job's sarbp_status */
     int32_t steps;           /* back-projection steps the job took */
-    double queued_ms;        /* submit -> admitted */
-    double latency_ms;       /* submit -> image in host memory */
+    double queued_ms;        /* entry into sarbp_server_submit -> admitted */
+    double latency_ms;       /* entry into sarbp_server_submit (validation and planning included) -> image in host memory */
     double updates;          /* nx * ny * np */
     uint64_t device_bytes;   /* admission footprint */
 } sarbp_job_stats;

@@ -376,10 +376,9 @@ sarbp_status extremes_device(sarbp_ctx *ctx, const double *apc_dev, int np, cons
                "read planning extremes");
     SARBP_CUDA(ctx, cudaEventRecord(ctx->ev_ext, s), "read planning extremes");
     SARBP_CUDA(ctx, cudaEventSynchronize(ctx->ev_ext), "read planning extremes");
-    double v[4];
+    double v[4];  // squared range extremes, cosines
     std::memcpy(v, ctx->ext_host, sizeof v);
-    e.rmin = v[0];
-    e.rmax = v[1];
+    sarbp::ext_ranges(v[0], v[1], e);
     e.cx = v[2];
     e.sy = v[3];
     e.nonfinite = ctx->ext_host[4] ? 1u : 0u;

@@ -1008,27 +1008,29 @@ __global__ void bp_extremes_init_kernel(unsigned long long *out) {
 __global__ void __launch_bounds__(256) bp_extremes_kernel(const double *apc, int np, const sarbp_grid g, double lux,
                                                           double luy, unsigned long long *out) {
     constexpr int kPts = kLattice * kLattice;
-    double rmin = 1e300, rmax = 0.0, cx = 0.0, sy = 0.0;
+    __shared__ double P[kPts][3];
+    for (int k = threadIdx.x; k < kPts; k += blockDim.x) ext_lattice(g, k / kLattice, k % kLattice, P[k]);
+    __syncthreads();
+    // one thread per (pulse, lattice row): nine points
+    ExtAcc acc;
+    ext_acc_init(acc);
     bool bad = false;
-    const long long total = (long long)np * kPts;
+    const long long total = (long long)np * kLattice;
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total; i += (long long)gridDim.x * blockDim.x) {
-        const int p = (int)(i / kPts), k = (int)(i - (long long)p * kPts);
+        const int p = (int)(i / kLattice), u = (int)(i - (long long)p * kLattice);
         const double a[3] = {apc[3 * (size_t)p], apc[3 * (size_t)p + 1], apc[3 * (size_t)p + 2]};
         if (!isfinite(a[0]) || !isfinite(a[1]) || !isfinite(a[2])) {
             bad = true;
             continue;
         }
-        double R, c, sv;
-        ext_point(g, lux, luy, a, k / kLattice, k % kLattice, &R, &c, &sv);
-        rmin = fmin(rmin, R);
-        rmax = fmax(rmax, R);
-        cx = fmax(cx, c);
-        sy = fmax(sy, sv);
+#pragma unroll 1
+        for (int v = 0; v < kLattice; ++v) ext_acc_point(acc, g, lux, luy, P[u * kLattice + v], a);
     }
+    double r2min = acc.r2min, r2max = acc.r2max, cx = acc.cx.best, sy = acc.sy.best;
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
-        rmin = fmin(rmin, __shfl_xor_sync(0xffffffffu, rmin, o));
-        rmax = fmax(rmax, __shfl_xor_sync(0xffffffffu, rmax, o));
+        r2min = fmin(r2min, __shfl_xor_sync(0xffffffffu, r2min, o));
+        r2max = fmax(r2max, __shfl_xor_sync(0xffffffffu, r2max, o));
         cx = fmax(cx, __shfl_xor_sync(0xffffffffu, cx, o));
         sy = fmax(sy, __shfl_xor_sync(0xffffffffu, sy, o));
     }
@@ -1041,8 +1043,8 @@ __global__ void __launch_bounds__(256) bp_extremes_kernel(const double *apc, int
     __syncthreads();
     const bool any_bad = __any_sync(0xffffffffu, bad);
     if ((threadIdx.x & 31) == 0) {
-        red[0][warp] = rmin;
-        red[1][warp] = rmax;
+        red[0][warp] = r2min;
+        red[1][warp] = r2max;
         red[2][warp] = cx;
         red[3][warp] = sy;
         if (any_bad) red_bad = 1;
@@ -1050,13 +1052,13 @@ __global__ void __launch_bounds__(256) bp_extremes_kernel(const double *apc, int
     __syncthreads();
     if (threadIdx.x == 0) {  // holds warp 0's values already
         for (int w = 1; w < (int)(blockDim.x >> 5); ++w) {
-            rmin = fmin(rmin, red[0][w]);
-            rmax = fmax(rmax, red[1][w]);
+            r2min = fmin(r2min, red[0][w]);
+            r2max = fmax(r2max, red[1][w]);
             cx = fmax(cx, red[2][w]);
             sy = fmax(sy, red[3][w]);
         }
-        atomicMin(&out[0], (unsigned long long)__double_as_longlong(rmin));
-        atomicMax(&out[1], (unsigned long long)__double_as_longlong(rmax));
+        atomicMin(&out[0], (unsigned long long)__double_as_longlong(r2min));
+        atomicMax(&out[1], (unsigned long long)__double_as_longlong(r2max));
         atomicMax(&out[2], (unsigned long long)__double_as_longlong(cx));
         atomicMax(&out[3], (unsigned long long)__double_as_longlong(sy));
         if (red_bad) atomicOr(&out[4], 1ull);
@@ -1069,8 +1071,7 @@ cudaError_t launch_bp_extremes(const double *apc, int np, const sarbp_grid &g, u
     if (np <= 0) return cudaGetLastError();
     double lux, luy;
     ext_axes(g, &lux, &luy);
-    const long long total = (long long)np * kLattice * kLattice;
-    // a few points per thread; one atomic update per block and quantity
+    const long long total = (long long)np * kLattice;  // threads: (pulse, lattice row)
     const int blocks = (int)std::min<long long>((total + 255) / 256, 512);
     bp_extremes_kernel<<<blocks, 256, 0, s>>>(apc, np, g, lux, luy, out);
     return cudaGetLastError();

@@ -126,30 +126,89 @@ __host__ __device__ inline double ext_add(double a, double b) {
 __host__ __device__ inline double ext_dot(const double *a, const double *b) {
     return ext_add(ext_add(ext_mul(a[0], b[0]), ext_mul(a[1], b[1])), ext_mul(a[2], b[2]));
 }
-// Lattice point (u, v) against antenna position a: range R and the two direction
-// cosines |ux.w| / (R lux), |uy.w| / (R luy) (zero when R or the axis length is 0).
-__host__ __device__ inline void ext_point(const sarbp_grid &g, double lux, double luy, const double *a, int u, int v,
-                                          double *R, double *cx, double *sy) {
+__host__ __device__ inline double ext_sqrt(double x) {
+#ifdef __CUDA_ARCH__
+    return __dsqrt_rn(x);
+#else
+    return std::sqrt(x);
+#endif
+}
+__host__ __device__ inline double ext_div(double a, double b) {
+#ifdef __CUDA_ARCH__
+    return __ddiv_rn(a, b);
+#else
+    return a / b;
+#endif
+}
+// Lattice point (u, v) of the grid: origin + fx ux + fy uy with
+// fx = (nx - 1) u / 8, fy = (ny - 1) v / 8 (corners and edges included).
+__host__ __device__ inline void ext_lattice(const sarbp_grid &g, int u, int v, double *P) {
     const double fx = (double)((g.nx - 1) * u) / (double)(kLattice - 1);
     const double fy = (double)((g.ny - 1) * v) / (double)(kLattice - 1);
-    double w[3];
-    for (int k = 0; k < 3; ++k) w[k] = ext_add(ext_add(ext_add(g.origin[k], ext_mul(fx, g.ux[k])), ext_mul(fy, g.uy[k])), -a[k]);
-#ifdef __CUDA_ARCH__
-    const double r = __dsqrt_rn(ext_dot(w, w));
-#else
-    const double r = std::sqrt(ext_dot(w, w));
-#endif
-    *R = r;
-    *cx = *sy = 0.0;
-    if (r > 0) {
-#ifdef __CUDA_ARCH__
-        if (lux > 0) *cx = __ddiv_rn(fabs(ext_dot(g.ux, w)), ext_mul(r, lux));
-        if (luy > 0) *sy = __ddiv_rn(fabs(ext_dot(g.uy, w)), ext_mul(r, luy));
-#else
-        if (lux > 0) *cx = std::fabs(ext_dot(g.ux, w)) / ext_mul(r, lux);
-        if (luy > 0) *sy = std::fabs(ext_dot(g.uy, w)) / ext_mul(r, luy);
-#endif
+    for (int k = 0; k < 3; ++k) P[k] = ext_add(ext_add(g.origin[k], ext_mul(fx, g.ux[k])), ext_mul(fy, g.uy[k]));
+}
+// Running maximum of the direction cosine q = |axis.w| / (R |axis|) over points.
+// q is evaluated (correctly rounded square root, product and quotient) only
+// where the division-free comparison n^2 R_b^2 >= n_b^2 R^2 (1 - 1e-9) against
+// the best point so far (n_b, R_b^2) cannot rule the point out: the margin is
+// far above the few ulps of rounding in that comparison and in q, so every
+// point skipped has a smaller q, and the maximum is the value that evaluating
+// q at every point gives.  Along a track that is about one evaluation per
+// pulse instead of one per point.
+struct ExtCos {
+    double best, n, r2;
+};
+__host__ __device__ inline void ext_cos(ExtCos &c, double n, double r2, double len) {
+    const double lhs = ext_mul(ext_mul(n, n), c.r2), rhs = ext_mul(ext_mul(c.n, c.n), r2);
+    if (lhs < ext_mul(rhs, 1.0 - 1e-9)) return;
+    const double q = ext_div(n, ext_mul(ext_sqrt(r2), len));
+    if (q > c.best) {
+        c.best = q;
+        c.n = n;
+        c.r2 = r2;
     }
+}
+// Reduction state over (pulse, lattice point): squared ranges (the range
+// extremes are their square roots: the square root is monotonic and correctly
+// rounded, so this equals the extremes of the ranges) and the two cosines
+// (zero where R or the axis length is 0).
+struct ExtAcc {
+    double r2min, r2max;
+    ExtCos cx, sy;
+};
+__host__ __device__ inline void ext_acc_init(ExtAcc &a) {
+    a.r2min = 1e300;
+    a.r2max = 0.0;
+    a.cx = ExtCos{0.0, 0.0, 0.0};
+    a.sy = ExtCos{0.0, 0.0, 0.0};
+}
+// Squared range and |axis . w| of lattice point P against antenna position a.
+__host__ __device__ inline void ext_terms(const sarbp_grid &g, const double *P, const double *apc, double &r2,
+                                          double &nx, double &ny) {
+    double w[3];
+    for (int k = 0; k < 3; ++k) w[k] = ext_add(P[k], -apc[k]);
+    r2 = ext_dot(w, w);
+    nx = fabs(ext_dot(g.ux, w));
+    ny = fabs(ext_dot(g.uy, w));
+}
+__host__ __device__ inline void ext_acc_terms(ExtAcc &a, double r2, double nx, double ny, double lux, double luy) {
+    a.r2min = fmin(a.r2min, r2);  // NaN-ignoring on host and device alike
+    a.r2max = fmax(a.r2max, r2);
+    if (r2 > 0) {
+        if (lux > 0) ext_cos(a.cx, nx, r2, lux);
+        if (luy > 0) ext_cos(a.sy, ny, r2, luy);
+    }
+}
+__host__ __device__ inline void ext_acc_point(ExtAcc &a, const sarbp_grid &g, double lux, double luy, const double *P,
+                                              const double *apc) {
+    double r2, nx, ny;
+    ext_terms(g, P, apc, r2, nx, ny);
+    ext_acc_terms(a, r2, nx, ny, lux, luy);
+}
+// Range extremes from the squared ones (1e300: no finite point).
+inline void ext_ranges(double r2min, double r2max, BpExtremes &e) {
+    e.rmin = r2min >= 1e300 ? 1e300 : std::sqrt(r2min);
+    e.rmax = std::sqrt(r2max);
 }
 // Axis lengths |ux|, |uy| as both reductions use them.
 void ext_axes(const sarbp_grid &g, double *lux, double *luy);

@@ -48,8 +48,7 @@ FIELDS = ("tile_x", "tile_y", "window", "series_terms", "segments", "ctas_per_sm
           "rmin", "rmax", "cos_x", "cos_y")
 
 
-@pytest.mark.parametrize("case", ["config2", "ground", "skewed", "config5_corner"])
-def test_host_and_device_extremes_agree(ctx, case):
+def plan_case(case):
     if case == "config2":
         s = scenes.config2()
         r, g, _ = sarbp.scene_args(s)
@@ -68,6 +67,45 @@ def test_host_and_device_extremes_agree(ctx, case):
         g = sub_grid(g0, 0, 0, 4096, 4096)
         apc, v = np.ascontiguousarray(s.apc[12288:]), view(s, sarbp.STORE_C32H, 4096)
     mode = sarbp.MODE_FP16STORE if v.storage == sarbp.STORE_C32H else sarbp.MODE_SPLIT
+    return r, g, np.ascontiguousarray(apc, dtype=np.float64), v, mode
+
+
+def brute_extremes(apc, g):
+    """Every (pulse, lattice point) of the planner's 9 x 9 lattice, one IEEE
+    operation at a time in the planner's order: range and the two direction
+    cosines |axis.w| / (R |axis|) (numpy ufuncs round each operation and do not
+    fuse multiply-adds)."""
+    o, ux, uy = (np.array(x, dtype=np.float64) for x in (g.origin, g.ux, g.uy))
+    dot = lambda a, b: (a[..., 0] * b[..., 0] + a[..., 1] * b[..., 1]) + a[..., 2] * b[..., 2]
+    lux, luy = np.sqrt(dot(ux, ux)), np.sqrt(dot(uy, uy))
+    k = np.arange(9)
+    fx = ((g.nx - 1) * k).astype(np.float64) / 8.0
+    fy = ((g.ny - 1) * k).astype(np.float64) / 8.0
+    P = (o[None, None, :] + fx[:, None, None] * ux[None, None, :]) + fy[None, :, None] * uy[None, None, :]
+    w = P[None, :, :, :] - apc[:, None, None, :]
+    R = np.sqrt(dot(w, w))
+    with np.errstate(divide="ignore", invalid="ignore"):
+        cx = np.where(R > 0, np.abs(dot(ux, w)) / (R * lux), 0.0) if lux > 0 else np.zeros_like(R)
+        cy = np.where(R > 0, np.abs(dot(uy, w)) / (R * luy), 0.0) if luy > 0 else np.zeros_like(R)
+    return R.min(), R.max(), cx.max(), cy.max()
+
+
+@pytest.mark.parametrize("case", ["config2", "ground", "skewed", "config5_corner"])
+def test_extremes_equal_brute_force(ctx, case):
+    """Both reductions skip the cosine divisions that a division-free
+    comparison rules out and take the square root of the squared-range
+    extremes; their results are the exact extremes of the per-point formula."""
+    r, g, apc, v, mode = plan_case(case)
+    want = brute_extremes(apc, g)
+    for host in (False, True):
+        info = ctx.bp_plan(r, v, apc, g, mode, host_reduction=host)
+        got = (info.rmin, info.rmax, info.cos_x, info.cos_y)
+        assert got == want, (host, got, want)
+
+
+@pytest.mark.parametrize("case", ["config2", "ground", "skewed", "config5_corner"])
+def test_host_and_device_extremes_agree(ctx, case):
+    r, g, apc, v, mode = plan_case(case)
     dev = ctx.bp_plan(r, v, apc, g, mode)
     host = ctx.bp_plan(r, v, apc, g, mode, host_reduction=True)
     for f in FIELDS:
