@@ -71,6 +71,25 @@ struct RcTables {
     DevBuf filt, etab;
 };
 
+// Omega-K tables on the device (row phasors, axes, Stolt terms) for one
+// (parameters, padded size): built on the host and uploaded only when these
+// change, then reused by every image; `ready` marks the upload on its stream.
+struct WkTables {
+    float2 *rowphase = nullptr, *rowq = nullptr, *colip = nullptr;
+    float *colc = nullptr;
+    const double *tab = nullptr;  // col_f2, col_ph, col_fr [NR] each, row_q [NA]
+    double a4r = 0.0;
+    bool ff = true;               // float-float Stolt (mapping a small correction)
+};
+struct WkCache {
+    bool valid = false;
+    int NA = 0, NR = 0;
+    double fr = 0, prf = 0, f0 = 0, r0 = 0, kr = 0, c = 0, vr = 0, f_nc = 0;
+    DevBuf row, tab;
+    WkTables t;
+    cudaEvent_t ready = nullptr;
+};
+
 }  // namespace
 
 struct sarbp_ctx {
@@ -81,7 +100,8 @@ struct sarbp_ctx {
     std::string err;
     DevBuf echo, spec, rc, scale, apc, image, partial, errword, power, targets, pref;
     DevBuf corr, weight, proj, projout, sharp;  // per-pulse corrections, projection and autofocus scratch
-    DevBuf wk0, wk1, wkrow, wktab;                // omega-K ping-pong buffers and tables
+    DevBuf wk0, wk1, wkrow;                       // omega-K ping-pong buffers, CEOS gain table
+    WkCache wkc;                                  // omega-K tables
     DftCache dft[4];
     uint64_t dft_clock = 0;
     RcTables tables;
@@ -92,8 +112,9 @@ struct sarbp_ctx {
     cudaEvent_t ev_copy = nullptr;
     // Buffers sized by the calls (released by sarbp_trim and sarbp_destroy).
     std::vector<DevBuf *> scratch() {
-        std::vector<DevBuf *> v = {&echo, &spec, &rc,     &scale,   &apc,   &image, &partial, &targets, &pref,
-                                   &corr, &weight, &proj, &projout, &sharp, &wk0,   &wk1,     &wkrow,   &wktab};
+        std::vector<DevBuf *> v = {&echo,   &spec,  &rc,      &scale,   &apc,     &image,   &partial,
+                                   &targets, &pref,  &corr,    &weight,  &proj,    &projout, &sharp,
+                                   &wk0,    &wk1,   &wkrow,   &wkc.row, &wkc.tab};
         for (DftCache &d : dft)
             for (DevBuf *b : {&d.etab, &d.chirp, &d.kf, &d.ki}) v.push_back(b);
         return v;
@@ -103,6 +124,7 @@ struct sarbp_ctx {
     void release_scratch() {
         for (DevBuf *b : scratch()) b->release();
         for (DftCache &d : dft) d.release();  // also forgets the cached sizes
+        wkc.valid = false;
     }
     int64_t launches = 0;
     int checked = 0;  // SARBP_BOUNDS_CHECK=1 at creation: clamped, self-reporting BP kernels
@@ -667,6 +689,7 @@ sarbp_status sarbp_destroy(sarbp_ctx *ctx) {
     for (cudaEvent_t &e : ctx->ev)
         if (e) cudaEventDestroy(e);
     if (ctx->ev_ext) cudaEventDestroy(ctx->ev_ext);
+    if (ctx->wkc.ready) cudaEventDestroy(ctx->wkc.ready);
     if (ctx->ev_copy) cudaEventDestroy(ctx->ev_copy);
     if (ctx->copy_stream) cudaStreamDestroy(ctx->copy_stream);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
@@ -1078,16 +1101,16 @@ sarbp_status wk_check_params(sarbp_ctx *ctx, const sarbp_wk_params *w) {
 // host in FP64, uploaded on s): row phasors of the azimuth down-conversion, the
 // Stolt terms per row and column (float-float), and the FP64 tables of the
 // FP64 Stolt path.
-struct WkTables {
-    float2 *rowphase = nullptr, *rowq = nullptr, *colip = nullptr;
-    float *colc = nullptr;
-    const double *tab = nullptr;  // col_f2, col_ph, col_fr [NR] each, row_q [NA]
-    double a4r = 0.0;
-    bool ff = true;               // float-float Stolt (mapping a small correction)
-};
-
 sarbp_status wk_tables(sarbp_ctx *ctx, const sarbp_wk_params *w, int NA, int NR, cudaStream_t s, WkTables &t) {
     constexpr double kPi = 3.14159265358979323846;
+    WkCache &k = ctx->wkc;
+    if (k.valid && k.NA == NA && k.NR == NR && k.fr == w->fr && k.prf == w->prf && k.f0 == w->f0 && k.r0 == w->r0 &&
+        k.kr == w->kr && k.c == w->c && k.vr == w->vr && k.f_nc == w->f_nc) {
+        SARBP_CUDA(ctx, cudaStreamWaitEvent(s, k.ready, 0), "omega-K tables");
+        t = k.t;
+        return SARBP_OK;
+    }
+    k.valid = false;
     // host tables (FP64): row phasors exp(-j 2 pi f_nc ta_m), ta_m = (m - NA/2) / prf;
     // frequency axes as the reference builds them (fftshifted index, wk.cc:181-205)
     const double a4r = 4.0 * kPi * w->r0 / w->c;
@@ -1125,9 +1148,9 @@ sarbp_status wk_tables(sarbp_ctx *ctx, const sarbp_wk_params *w, int NA, int NR,
     // float-float Stolt stage when the mapping is a small correction (eps <= 1e-2), else FP64
     const bool ff_stolt = pmin > 0.0 && qmax / (pmin * pmin) <= 1e-2;
     const size_t row_bytes = sizeof(float2) * 2 * NA, col_bytes = (sizeof(float) + sizeof(float2)) * NR;
-    SARBP_CUDA(ctx, ctx->wkrow.ensure(row_bytes + col_bytes), "alloc omega-K tables");
-    SARBP_CUDA(ctx, ctx->wktab.ensure(sizeof(double) * tab.size()), "alloc omega-K tables");
-    float2 *d_rowphase = ctx->wkrow.as<float2>(), *d_rowq = d_rowphase + NA, *d_colip = d_rowq + NA;
+    SARBP_CUDA(ctx, k.row.ensure(row_bytes + col_bytes), "alloc omega-K tables");
+    SARBP_CUDA(ctx, k.tab.ensure(sizeof(double) * tab.size()), "alloc omega-K tables");
+    float2 *d_rowphase = k.row.as<float2>(), *d_rowq = d_rowphase + NA, *d_colip = d_rowq + NA;
     float *d_colc = reinterpret_cast<float *>(d_colip + NR);
     SARBP_CUDA(ctx, cudaMemcpyAsync(d_rowphase, rowphase.data(), sizeof(float2) * NA, cudaMemcpyHostToDevice, s),
                "upload omega-K tables");
@@ -1137,15 +1160,29 @@ sarbp_status wk_tables(sarbp_ctx *ctx, const sarbp_wk_params *w, int NA, int NR,
                "upload omega-K tables");
     SARBP_CUDA(ctx, cudaMemcpyAsync(d_colc, col_c.data(), sizeof(float) * NR, cudaMemcpyHostToDevice, s),
                "upload omega-K tables");
-    SARBP_CUDA(ctx, cudaMemcpyAsync(ctx->wktab.ptr, tab.data(), sizeof(double) * tab.size(), cudaMemcpyHostToDevice, s),
+    SARBP_CUDA(ctx, cudaMemcpyAsync(k.tab.ptr, tab.data(), sizeof(double) * tab.size(), cudaMemcpyHostToDevice, s),
                "upload omega-K tables");
-    t.tab = ctx->wktab.as<double>();
+    if (!k.ready) SARBP_CUDA(ctx, cudaEventCreateWithFlags(&k.ready, cudaEventDisableTiming), "omega-K tables");
+    SARBP_CUDA(ctx, cudaEventRecord(k.ready, s), "omega-K tables");
+    t.tab = k.tab.as<double>();
     t.rowphase = d_rowphase;
     t.rowq = d_rowq;
     t.colip = d_colip;
     t.colc = d_colc;
     t.a4r = a4r;
     t.ff = ff_stolt;
+    k.t = t;
+    k.NA = NA;
+    k.NR = NR;
+    k.fr = w->fr;
+    k.prf = w->prf;
+    k.f0 = w->f0;
+    k.r0 = w->r0;
+    k.kr = w->kr;
+    k.c = w->c;
+    k.vr = w->vr;
+    k.f_nc = w->f_nc;
+    k.valid = true;
     return SARBP_OK;
 }
 

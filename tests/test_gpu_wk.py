@@ -83,6 +83,28 @@ def test_wk_fp64_stolt_path(ctx):
     assert err <= -80.0
 
 
+def test_wk_tables_follow_parameters(ctx):
+    """The omega-K tables are built once per (parameters, padded size) and
+    reused: alternating two parameter sets and two sizes on one context, and
+    trimming its buffers in between, gives each call the image a fresh
+    context gives."""
+    a = wk.radarsat1()
+    b = wk.WkParams(fr=100e6, prf=1000.0, f0=1.3e9, r0=3000.0, kr=5e12, vr=120.0, f_nc=0.0)
+    e1, e2 = rand((192, 128), 31), rand((160, 96), 32)
+    fresh = sarbp.Context(0)
+    try:
+        want = {(k, i): fresh.wk_image(p, e) for k, p in (("a", a), ("b", b)) for i, e in ((1, e1), (2, e2))}
+    finally:
+        fresh.close()
+    order = [("a", 1), ("a", 1), ("b", 1), ("a", 1), ("a", 2), ("b", 2), ("trim", 0), ("b", 2), ("a", 1)]
+    for k, i in order:
+        if k == "trim":
+            ctx.check(ctx.lib.sarbp_trim(ctx.h), "trim")
+            continue
+        img = ctx.wk_image(a if k == "a" else b, e1 if i == 1 else e2)
+        assert np.array_equal(img, want[(k, i)]), (k, i)
+
+
 def test_wk_device_pointers(ctx):
     torch = pytest.importorskip("torch")
     p = wk.radarsat1()
