@@ -102,6 +102,9 @@ struct sarbp_ctx {
     DevBuf corr, weight, proj, projout, sharp;  // per-pulse corrections, projection and autofocus scratch
     DevBuf wk0, wk1, wkrow;                       // omega-K ping-pong buffers, CEOS gain table
     WkCache wkc;                                  // omega-K tables
+    bool ceos_valid = false;                      // wkrow holds the CEOS gains of ceos_gain
+    float ceos_gain = 0.f;
+    cudaEvent_t ceos_ready = nullptr;             // their upload
     DftCache dft[4];
     uint64_t dft_clock = 0;
     RcTables tables;
@@ -125,6 +128,7 @@ struct sarbp_ctx {
         for (DevBuf *b : scratch()) b->release();
         for (DftCache &d : dft) d.release();  // also forgets the cached sizes
         wkc.valid = false;
+        ceos_valid = false;
     }
     int64_t launches = 0;
     int checked = 0;  // SARBP_BOUNDS_CHECK=1 at creation: clamped, self-reporting BP kernels
@@ -690,6 +694,7 @@ sarbp_status sarbp_destroy(sarbp_ctx *ctx) {
         if (e) cudaEventDestroy(e);
     if (ctx->ev_ext) cudaEventDestroy(ctx->ev_ext);
     if (ctx->wkc.ready) cudaEventDestroy(ctx->wkc.ready);
+    if (ctx->ceos_ready) cudaEventDestroy(ctx->ceos_ready);
     if (ctx->ev_copy) cudaEventDestroy(ctx->ev_copy);
     if (ctx->copy_stream) cudaStreamDestroy(ctx->copy_stream);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
@@ -1410,14 +1415,25 @@ sarbp_status sarbp_ceos_decode(sarbp_ctx *ctx, const uint8_t *raw, uint64_t raw_
         g.raw_offset = b0 * g.block_bytes;
         any_host = true;
     }
-    // gain per AGC code: float(gain) * float(10^(dB / 20)), the reader's float arithmetic
-    float gains[64];
-    for (int code = 0; code < 64; ++code) {
-        const int db = code - 24 * (code > 31);
-        gains[code] = l->gain * (float)std::pow(10.0, db / 20.0);
+    // gain per AGC code: float(gain) * float(10^(dB / 20)), the reader's float
+    // arithmetic; uploaded when the layout's gain changes, else reused
+    if (ctx->ceos_valid && ctx->ceos_gain == l->gain) {
+        SARBP_CUDA(ctx, cudaStreamWaitEvent(s, ctx->ceos_ready, 0), "gain table");
+    } else {
+        ctx->ceos_valid = false;
+        float gains[64];
+        for (int code = 0; code < 64; ++code) {
+            const int db = code - 24 * (code > 31);
+            gains[code] = l->gain * (float)std::pow(10.0, db / 20.0);
+        }
+        SARBP_CUDA(ctx, ctx->wkrow.ensure(sizeof gains), "alloc gain table");
+        SARBP_CUDA(ctx, cudaMemcpyAsync(ctx->wkrow.ptr, gains, sizeof gains, cudaMemcpyHostToDevice, s), "upload gains");
+        if (!ctx->ceos_ready)
+            SARBP_CUDA(ctx, cudaEventCreateWithFlags(&ctx->ceos_ready, cudaEventDisableTiming), "gain table");
+        SARBP_CUDA(ctx, cudaEventRecord(ctx->ceos_ready, s), "gain table");
+        ctx->ceos_gain = l->gain;
+        ctx->ceos_valid = true;
     }
-    SARBP_CUDA(ctx, ctx->wkrow.ensure(sizeof gains), "alloc gain table");
-    SARBP_CUDA(ctx, cudaMemcpyAsync(ctx->wkrow.ptr, gains, sizeof gains, cudaMemcpyHostToDevice, s), "upload gains");
     float2 *d_echo = reinterpret_cast<float2 *>(echo);
     const size_t out_bytes = sizeof(float2) * (size_t)nlines * ncells;
     const bool dev_echo = is_device_ptr(echo);

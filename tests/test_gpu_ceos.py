@@ -43,6 +43,18 @@ def test_decode_matches_reader(ctx, raw_file, first, cnt, c0, nc, agc):
     assert np.array_equal(got_a, ref_a)
 
 
+def test_gain_table_follows_layout(ctx, raw_file):
+    """The AGC gain table is uploaded when the layout's gain changes and reused
+    otherwise: alternating gains on one context match the reader each time."""
+    import dataclasses
+    lay, raw = raw_file
+    for g in (1.5, 2.25, 2.25, 1.5, 0.75):
+        lg = dataclasses.replace(lay, gain=g)
+        ref, _ = ceos.read(raw, lg, 2, 20, 1049, 2048, apply_agc=True)
+        got, _ = ctx.ceos_decode(raw, 2, 20, 1049, 2048, layout=lg, apply_agc=True)
+        assert np.array_equal(got, ref), g
+
+
 def test_decode_device_input(ctx, raw_file):
     torch = pytest.importorskip("torch")
     lay, raw = raw_file
