@@ -92,8 +92,13 @@ void bp_extremes_host(const double *apc, int np, const sarbp_grid &g, BpExtremes
     std::vector<unsigned> bad(nt);
     std::vector<std::thread> pool;
     const int per = (np + nt - 1) / nt;
-    for (int t = 1; t < nt; ++t)
-        pool.emplace_back(run, t * per, std::min(np, (t + 1) * per), std::ref(acc[t]), std::ref(bad[t]));
+    int t = 1;
+    try {
+        for (; t < nt; ++t)
+            pool.emplace_back(run, t * per, std::min(np, (t + 1) * per), std::ref(acc[t]), std::ref(bad[t]));
+    } catch (...) {  // no thread to be had: the rest on this thread (no exception crosses the C ABI)
+        for (int u = t; u < nt; ++u) run(u * per, std::min(np, (u + 1) * per), acc[u], bad[u]);
+    }
     run(0, std::min(np, per), acc[0], bad[0]);
     for (auto &th : pool) th.join();
     ExtAcc all = acc[0];
