@@ -667,7 +667,11 @@ sarbp_status sarbp_create(sarbp_ctx **out, int device) {
     ctx->checked = (chk && chk[0] == '1') ? 1 : 0;
     bool ok = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) == cudaSuccess;
     for (int i = 0; i < 4 && ok; ++i) ok = cudaEventCreate(&ctx->ev[i]) == cudaSuccess;
-    ok = ok && cudaEventCreateWithFlags(&ctx->ev_ext, cudaEventDisableTiming) == cudaSuccess;
+    // the planning read-back waits for the stream's earlier work (a whole
+    // back-projection when calls come back to back): a blocking wait sleeps
+    // and wakes on completion instead of spinning a core for that long, which
+    // a busy host may preempt for a scheduler slice
+    ok = ok && cudaEventCreateWithFlags(&ctx->ev_ext, cudaEventDisableTiming | cudaEventBlockingSync) == cudaSuccess;
     ok = ok && cudaEventCreateWithFlags(&ctx->ev_copy, cudaEventDisableTiming) == cudaSuccess;
     ok = ok && cudaStreamCreateWithFlags(&ctx->copy_stream, cudaStreamNonBlocking) == cudaSuccess;
     ok = ok && cudaMallocHost(reinterpret_cast<void **>(&ctx->ext_host), 8 * sizeof(unsigned long long)) == cudaSuccess;

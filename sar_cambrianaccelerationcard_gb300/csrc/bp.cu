@@ -82,6 +82,7 @@ struct __align__(16) Prm {
     int ws;        // first bin of the window
     int lo, hi;    // copied part of the window [lo, hi) relative to ws
     float scale;   // FP16 storage scale
+    int need;      // (M, d) pairs [0, need) any pixel of the tile reads (the rest are not converted)
 };
 
 __device__ __forceinline__ unsigned smem_addr(const void *p) {
@@ -251,6 +252,7 @@ __device__ __forceinline__ void produce(const BpPlan &P, const Smem &S, int stag
         const int cen = win >> 1;  // staged index origin
         Prm &q = S.prm[stage * kChunk + slot];
         int ws;  // window start, clamped to +-1e9 bins: int arithmetic throughout
+        int need = win;
         bool sane;
         if (MODE == SARBP_MODE_SPLIT || MODE == SARBP_MODE_FP16STORE) {
             // R_T^2 = a0 + xT a1 + yT a2 + |q_T|^2 in float-float
@@ -279,6 +281,10 @@ __device__ __forceinline__ void produce(const BpPlan &P, const Smem &S, int stag
             ws &= ~3;
             const int need_end = (int)ceilf(fminf(fmaxf(bT.h + half, -1.0e9f), 1.0e9f)) + 2;
             sane = isfinite(r) && r > 0.f && isfinite(half) && isfinite(phT) && need_end - ws <= win;
+            // the tile's bins lie in [bT - half, bT + half]: pair indices up to
+            // need_end - ws - 2, so pairs [0, need) cover every read (the checked
+            // build flags any read past need - 2)
+            if (sane) need = need_end - ws;
             const float i2 = iR * iR;
             if (sane) {
                 const float c1 = 0.5f * iR, c2 = -0.125f * iR * i2, c3 = 0.0625f * iR * i2 * i2;
@@ -328,6 +334,7 @@ __device__ __forceinline__ void produce(const BpPlan &P, const Smem &S, int stag
         q.ws = ws;
         q.lo = lo - ws;
         q.hi = hi - ws;
+        q.need = need;
         q.scale = STORE == SARBP_STORE_C32H ? __ldg(&P.scale[p]) : 1.f;
         if (hi > lo) {
             bytes = (unsigned)((hi - lo) * esize);
@@ -346,7 +353,7 @@ __device__ __forceinline__ void produce(const BpPlan &P, const Smem &S, int stag
 
 // raw window -> (mid, diff) pairs; bins outside [lo, hi) read as zero.
 // Flat over (pulse, bin), used for complex64 rows.
-template <int MODE, int STORE>
+template <int MODE, int STORE, bool TRIM>
 __device__ __forceinline__ void convert_flat(const Smem &S, int stage, int sbuf, int count, int win, unsigned win_magic,
                                         int chunk) {
     const int total = count * win;
@@ -355,6 +362,7 @@ __device__ __forceinline__ void convert_flat(const Smem &S, int stage, int sbuf,
         const int pl = (int)__umulhi((unsigned)e, win_magic);
         const int i = e - pl * win;
         const Prm &q = S.prm[stage * kChunk + pl];
+        if (TRIM && i >= q.need) continue;  // no pixel of the tile reads it
         const int lo = q.lo, hi = q.hi;
         const unsigned char *rw = S.raw + ((size_t)stage * chunk + pl) * win * raw_esize(STORE);
         float2 a = make_float2(0.f, 0.f), b = make_float2(0.f, 0.f);
@@ -380,7 +388,7 @@ __device__ __forceinline__ void convert_flat(const Smem &S, int stage, int sbuf,
 // The same with one warp per pulse (pulse-uniform bounds and scale, lane =
 // bin) and an unconditional path when the whole window was copied (every pulse
 // but those at the swath edges), used for complex16 rows.
-template <int MODE, int STORE>
+template <int MODE, int STORE, bool TRIM>
 __device__ __forceinline__ void convert_warp(const Smem &S, int stage, int sbuf, int count, int win, int chunk) {
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int cen = win >> 1;
@@ -392,7 +400,8 @@ __device__ __forceinline__ void convert_warp(const Smem &S, int stage, int sbuf,
         const unsigned char *rw = S.raw + ((size_t)stage * chunk + pl) * win * raw_esize(STORE);
         float4 *st = stb + (size_t)pl * win;
         const bool whole = lo == 0 && hi == win;
-        for (int i = lane; i < win; i += 32) {
+        const int n = TRIM ? q.need : win;  // pairs any pixel of the tile reads
+        for (int i = lane; i < n; i += 32) {
             float2 a = make_float2(0.f, 0.f), b = make_float2(0.f, 0.f);
             const bool ina = whole || (i >= lo && i < hi);
             const bool inb = whole ? i + 1 < win : (i + 1 >= lo && i + 1 < hi);
@@ -419,13 +428,16 @@ __device__ __forceinline__ void convert_warp(const Smem &S, int stage, int sbuf,
 // 1275.7 / 1241.5, complex16 1231.5 / 1244.8.  The pass itself is ~6% of the
 // kernel (3.1 ms of 53.9 without it), but its code shape moves the schedule
 // of the main loop more than its own cost.
-template <int MODE, int STORE>
+// TRIM: convert only the pairs [0, need) the tile reads (unchecked SPLIT /
+// FP16STORE kernels); the checked build and the FP32 / FP64 comparators clamp
+// reads anywhere in the window and convert all of it.
+template <int MODE, int STORE, bool TRIM>
 __device__ __forceinline__ void convert(const Smem &S, int stage, int sbuf, int count, int win, unsigned win_magic,
                                         int chunk) {
     if constexpr (STORE == SARBP_STORE_C32H)
-        convert_warp<MODE, STORE>(S, stage, sbuf, count, win, chunk);
+        convert_warp<MODE, STORE, TRIM>(S, stage, sbuf, count, win, chunk);
     else
-        convert_flat<MODE, STORE>(S, stage, sbuf, count, win, win_magic, chunk);
+        convert_flat<MODE, STORE, TRIM>(S, stage, sbuf, count, win, win_magic, chunk);
 }
 
 // Sum of the warps' projections for the pulses of one chunk into
@@ -644,7 +656,12 @@ __global__ void __launch_bounds__(kThreads, SARBP_BP_MINBLOCKS)
         const bool ok = mbar_wait_bounded(smem_addr(&S.bar[stage]), (c / kStages) & 1, 2000000000ull);
         if (!ok) { failed = true; }
         if (__syncthreads_or(failed)) { failed = true; break; }
-        convert<MODE, STORE>(S, stage, sbuf, count, win, win_magic, chunk);
+        // trimmed to the pairs the tile reads for complex16 rows (warp per pulse:
+        // config 5 892 -> 864 ms); the flat complex64 pass measured slower with
+        // the per-element test (config 2 1296 -> 1283 Gupd/s), so it converts all
+        convert<MODE, STORE,
+                !CHECKED && STORE == SARBP_STORE_C32H && (MODE == SARBP_MODE_SPLIT || MODE == SARBP_MODE_FP16STORE)>(
+            S, stage, sbuf, count, win, win_magic, chunk);
         __syncthreads();
         if constexpr (ADJ) {  // every warp has finished chunk c-1: combine its pulse sums
             if (c > 0) flush_projection(P, S, (c - 1) & 1, pc0 - chunk, chunk);
@@ -685,10 +702,12 @@ __global__ void __launch_bounds__(kThreads, SARBP_BP_MINBLOCKS)
                     upk2(b2, bb[0], bb[1]);
                     upk2(ph2, ph[0], ph[1]);
                     if (CHECKED) {
+                        // past the window, or past the pairs an unchecked kernel converts
+                        const float needf = (float)(q.need - 2) - cenf;
 #pragma unroll
                         for (int u = 0; u < 2; ++u) {
                             const float bc = fminf(fmaxf(bb[u], -cenf), wmax - cenf);
-                            clamped |= !(bc == bb[u]);
+                            clamped |= !(bc == bb[u]) || bb[u] > needf;
                             bb[u] = bc;
                         }
                         b2 = pk2(bb[0], bb[1]);
