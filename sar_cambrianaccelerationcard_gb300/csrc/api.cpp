@@ -392,8 +392,10 @@ sarbp_status check_grid(sarbp_ctx *ctx, const sarbp_grid *g) {
 // Geometry extremes for planning from a device-resident APC: a reduction on the
 // stream (after the work already queued there, which may produce the APC), then
 // a wait for its 40-byte result only.  Fails on a non-finite APC coordinate.
-sarbp_status extremes_device(sarbp_ctx *ctx, const double *apc_dev, int np, const sarbp_grid *g, cudaStream_t s,
-                             sarbp::BpExtremes &e) {
+// Planning extremes in two halves: queue the reduction and its 40-byte
+// read-back on s, then (after any work that does not need the plan has been
+// queued behind it) wait for the read-back alone.
+sarbp_status extremes_enqueue(sarbp_ctx *ctx, const double *apc_dev, int np, const sarbp_grid *g, cudaStream_t s) {
     Range range("sarbp: planning extremes");
     SARBP_CUDA(ctx, sarbp::launch_bp_extremes(apc_dev, np, *g, ctx->ext.as<unsigned long long>(), s),
                "planning extremes");
@@ -401,6 +403,10 @@ sarbp_status extremes_device(sarbp_ctx *ctx, const double *apc_dev, int np, cons
     SARBP_CUDA(ctx, cudaMemcpyAsync(ctx->ext_host, ctx->ext.ptr, 5 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, s),
                "read planning extremes");
     SARBP_CUDA(ctx, cudaEventRecord(ctx->ev_ext, s), "read planning extremes");
+    return SARBP_OK;
+}
+
+sarbp_status extremes_wait(sarbp_ctx *ctx, sarbp::BpExtremes &e) {
     SARBP_CUDA(ctx, cudaEventSynchronize(ctx->ev_ext), "read planning extremes");
     double v[4];  // squared range extremes, cosines
     std::memcpy(v, ctx->ext_host, sizeof v);
@@ -410,6 +416,12 @@ sarbp_status extremes_device(sarbp_ctx *ctx, const double *apc_dev, int np, cons
     e.nonfinite = ctx->ext_host[4] ? 1u : 0u;
     if (e.nonfinite) return fail(ctx, SARBP_ERR_INVALID_ARGUMENT, "apc must be finite");
     return SARBP_OK;
+}
+
+sarbp_status extremes_device(sarbp_ctx *ctx, const double *apc_dev, int np, const sarbp_grid *g, cudaStream_t s,
+                             sarbp::BpExtremes &e) {
+    sarbp_status st = extremes_enqueue(ctx, apc_dev, np, g, s);
+    return st != SARBP_OK ? st : extremes_wait(ctx, e);
 }
 
 // Back-projection of device-resident rc + apc into a device image.
@@ -1488,8 +1500,9 @@ sarbp_status sarbp_image(sarbp_ctx *ctx, const sarbp_radar *radar, const sarbp_c
     const int storage = mode == SARBP_MODE_FP16STORE ? SARBP_STORE_C32H : SARBP_STORE_C64;
     const size_t esize = storage == SARBP_STORE_C64 ? 8 : 4;
     bool any_host = false;
-    // APC first: the planner's extremes are reduced on the device and waited
-    // for before the echo upload and range compression are queued
+    // APC first: the planner's extremes are reduced on the device ahead of the
+    // echo upload and range compression, and waited for only once those are
+    // queued behind them (the plan is needed by the back-projection alone)
     const double *apc_dev = apc;
     sarbp::BpExtremes ex{};
     if (np > 0) {
@@ -1500,7 +1513,7 @@ sarbp_status sarbp_image(sarbp_ctx *ctx, const sarbp_radar *radar, const sarbp_c
             apc_dev = ctx->apc.as<double>();
             any_host = true;
         }
-        st = extremes_device(ctx, apc_dev, np, grid, s, ex);
+        st = extremes_enqueue(ctx, apc_dev, np, grid, s);
         if (st != SARBP_OK) return st;
     }
     const bool host_echo = np > 0 && !is_device_ptr(echo);
@@ -1535,6 +1548,11 @@ sarbp_status sarbp_image(sarbp_ctx *ctx, const sarbp_radar *radar, const sarbp_c
         if (st != SARBP_OK) return st;
         v.data = ctx->rc.ptr;
         v.scale = storage == SARBP_STORE_C32H ? ctx->scale.as<float>() : nullptr;
+        st = extremes_wait(ctx, ex);
+        if (st != SARBP_OK) {
+            if (host_echo) drain_uploads(ctx);
+            return st;
+        }
     }
     st = bp_device(ctx, radar, v, apc_dev, ex, grid, mode, d_img, 0, s);
     if (st != SARBP_OK) {

@@ -302,3 +302,24 @@ def test_error_after_upload_leaves_nothing_in_flight(ctx, c1):
     del echo  # the caller may release its buffer right after the error
     again = sarbp.image_scene(ctx, s, c1["echo"], sarbp.MODE_SPLIT)
     assert np.array_equal(again, sarbp.image_scene(ctx, s, c1["echo"], sarbp.MODE_SPLIT))
+
+
+def test_nonfinite_apc_fails_after_upload_is_queued(ctx, c1):
+    """sarbp_image queues the echo upload and range compression before it waits
+    for the planning extremes; a non-finite APC is found there and returns
+    SARBP_ERR_INVALID_ARGUMENT with no copy left reading the caller's pinned
+    echo, and the context stays usable."""
+    torch = pytest.importorskip("torch")
+    s = c1["scene"]
+    r, g, _ = sarbp.scene_args(s)
+    echo = torch.from_numpy(c1["echo"].view(np.float32)).pin_memory()
+    bad = s.apc.copy()
+    bad[s.np_ // 3, 0] = np.inf
+    img = np.zeros((g.ny, g.nx), dtype=np.complex64)
+    with pytest.raises(sarbp.SarbpError) as ex:
+        ctx.check(ctx.lib.sarbp_image(ctx.h, sarbp.ctypes.byref(r), echo.data_ptr(), s.np_, s.ns, bad.ctypes.data,
+                                      sarbp.ctypes.byref(g), sarbp.MODE_SPLIT, img.ctypes.data, None), "image")
+    assert ex.value.status == sarbp.ERR_INVALID_ARGUMENT
+    del echo
+    again = sarbp.image_scene(ctx, s, c1["echo"], sarbp.MODE_SPLIT)
+    assert np.isfinite(again).all() and np.abs(again).max() > 0
