@@ -658,7 +658,9 @@ __global__ void __launch_bounds__(kThreads, SARBP_BP_MINBLOCKS)
         if (__syncthreads_or(failed)) { failed = true; break; }
         // trimmed to the pairs the tile reads for complex16 rows (warp per pulse:
         // config 5 892 -> 864 ms); the flat complex64 pass measured slower with
-        // the per-element test (config 2 1296 -> 1283 Gupd/s), so it converts all
+        // the per-element test (config 2 1296 -> 1283 Gupd/s), and complex64 rows
+        // through the trimmed warp-per-pulse pass tied with it (1300.2 vs
+        // 1301-1303), so complex64 converts the whole window
         convert<MODE, STORE,
                 !CHECKED && STORE == SARBP_STORE_C32H && (MODE == SARBP_MODE_SPLIT || MODE == SARBP_MODE_FP16STORE)>(
             S, stage, sbuf, count, win, win_magic, chunk);
