@@ -492,6 +492,37 @@ sarbp_status sarbp_last_timings(sarbp_ctx *ctx, float *rc_ms, float *bp_ms);
 /* Number of this library's kernels launched through the context so far. */
 int64_t sarbp_kernel_launches(const sarbp_ctx *ctx);
 
+/* ---------------------------------------------------- tests and tuning -- */
+
+/* Switches of one context for tests and tuning sweeps, not for production
+ * use; no reference counterpart.  A value of 0 (for the wait fault, -1)
+ * restores the default.
+ *   SARBP_DEBUG_BP_CHUNK        pulses staged per chunk (16, 8 or 4) where it fits;
+ *                               images do not depend on it
+ *   SARBP_DEBUG_BP_SEGMENTS     pulse segments per launch (1..64); images agree to
+ *                               FP32 rounding
+ *   SARBP_DEBUG_BP_CHECKED      1: back-projection kernels that clamp every
+ *                               interpolation index and report any clamp
+ *                               (SARBP_ERR_DEVICE_CHECK)
+ *   SARBP_DEBUG_WAIT_LIMIT_NS   limit of the kernels' bounded staging waits (default 2 s)
+ *   SARBP_DEBUG_WAIT_FAULT_CHUNK  >= 0: that pulse chunk's staging barrier in every
+ *                               CTA expects 16 bytes more than its copies bring, so
+ *                               the wait runs out (SARBP_ERR_TIMEOUT); the kernel
+ *                               then lets every copy in flight land before it exits
+ *   SARBP_DEBUG_DEVICE_FLAGS    (get only) device check bits of the last call
+ *                               that reported any: 1 wait ran out, 2 index clamped,
+ *                               8 staging window, 16 a copy did not land in the drain */
+enum {
+    SARBP_DEBUG_BP_CHUNK = 1,
+    SARBP_DEBUG_BP_SEGMENTS = 2,
+    SARBP_DEBUG_BP_CHECKED = 3,
+    SARBP_DEBUG_WAIT_LIMIT_NS = 4,
+    SARBP_DEBUG_WAIT_FAULT_CHUNK = 5,
+    SARBP_DEBUG_DEVICE_FLAGS = 6
+};
+sarbp_status sarbp_debug_set(sarbp_ctx *ctx, int32_t key, int64_t value);
+sarbp_status sarbp_debug_get(sarbp_ctx *ctx, int32_t key, int64_t *value);
+
 #ifdef __cplusplus
 }
 #endif

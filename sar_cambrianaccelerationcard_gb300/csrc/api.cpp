@@ -131,7 +131,8 @@ struct sarbp_ctx {
         ceos_valid = false;
     }
     int64_t launches = 0;
-    int checked = 0;  // SARBP_BOUNDS_CHECK=1 at creation: clamped, self-reporting BP kernels
+    sarbp::Tuning tune;           // sarbp_debug_set: forced chunk / segments, checked kernels, wait faults
+    unsigned last_device_flags = 0;  // device check word of the last call that reported one
     float rc_ms = 0.f, bp_ms = 0.f;
     bool timed_rc = false, timed_bp = false;
 };
@@ -267,8 +268,12 @@ sarbp_status check_errword(sarbp_ctx *ctx) {
     unsigned w = 0;
     SARBP_CUDA(ctx, cudaMemcpy(&w, ctx->errword.ptr, sizeof w, cudaMemcpyDeviceToHost), "read device check word");
     if (w == 0) return SARBP_OK;
+    ctx->last_device_flags = w;
     SARBP_CUDA(ctx, cudaMemset(ctx->errword.ptr, 0, sizeof(unsigned)), "reset device check word");
-    if (w & sarbp::kErrWaitTimeout) return fail(ctx, SARBP_ERR_TIMEOUT, "a bounded device wait ran out (0x%x)", w);
+    if (w & sarbp::kErrDrainTimeout)
+        return fail(ctx, SARBP_ERR_TIMEOUT, "a bounded device wait ran out and a copy in flight did not land (0x%x)", w);
+    if (w & sarbp::kErrWaitTimeout)
+        return fail(ctx, SARBP_ERR_TIMEOUT, "a bounded device wait ran out; its copies landed (0x%x)", w);
     if (w & sarbp::kErrIndexClamp)
         return fail(ctx, SARBP_ERR_DEVICE_CHECK, "an interpolation index left its staging window (0x%x)", w);
     if (w & sarbp::kErrWindow)
@@ -440,7 +445,7 @@ sarbp_status bp_device(sarbp_ctx *ctx, const sarbp_radar *r, const sarbp_rc_view
     if (((uintptr_t)rc.data & 15) != 0) return fail(ctx, SARBP_ERR_INVALID_ARGUMENT, "rc data must be 16-byte aligned");
     BpPlan p;
     std::string why;
-    if (!sarbp::plan_bp(ctx->sms, *r, rc, ex, np, *g, mode, 0, p, why))
+    if (!sarbp::plan_bp(ctx->sms, *r, rc, ex, np, *g, mode, 0, p, why, &ctx->tune))
         return fail(ctx, SARBP_ERR_UNSUPPORTED, "%s", why.c_str());
     p.rc = rc.data;
     p.scale = rc.scale;
@@ -449,7 +454,6 @@ sarbp_status bp_device(sarbp_ctx *ctx, const sarbp_radar *r, const sarbp_rc_view
     p.image = image;
     p.accumulate = accumulate;
     p.err = ctx->errword.as<unsigned>();
-    p.checked = ctx->checked;
     p.drange = dr_dev;
     p.dphase = dph_dev;
     SARBP_CUDA(ctx, ctx->pref.ensure(sizeof(float) * 8 * (size_t)np), "alloc pulse references");
@@ -480,14 +484,14 @@ sarbp_status project_device(sarbp_ctx *ctx, const sarbp_radar *r, const sarbp_rc
     if (((uintptr_t)rc.data & 15) != 0) return fail(ctx, SARBP_ERR_INVALID_ARGUMENT, "rc data must be 16-byte aligned");
     BpPlan p;
     std::string why;
-    if (!sarbp::plan_bp(ctx->sms, *r, rc, ex, np, *g, mode, 0, p, why))
+    if (!sarbp::plan_bp(ctx->sms, *r, rc, ex, np, *g, mode, 0, p, why, &ctx->tune))
         return fail(ctx, SARBP_ERR_UNSUPPORTED, "%s", why.c_str());
     p.rc = rc.data;
     p.scale = rc.scale;
     p.np = np;
     p.apc = apc_dev;
     p.err = ctx->errword.as<unsigned>();
-    p.checked = 0;
+    p.checked = 0;  // the projection has no checked variant
     p.drange = dr_dev;
     p.dphase = dph_dev;
     p.weight = weight;
@@ -675,8 +679,6 @@ sarbp_status sarbp_create(sarbp_ctx **out, int device) {
     sarbp_ctx *ctx = new sarbp_ctx();
     ctx->device = device;
     ctx->sms = prop.multiProcessorCount;
-    const char *chk = std::getenv("SARBP_BOUNDS_CHECK");
-    ctx->checked = (chk && chk[0] == '1') ? 1 : 0;
     bool ok = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) == cudaSuccess;
     for (int i = 0; i < 4 && ok; ++i) ok = cudaEventCreate(&ctx->ev[i]) == cudaSuccess;
     // the planning read-back waits for the stream's earlier work (a whole
@@ -871,9 +873,8 @@ sarbp_status sarbp_bp_plan(sarbp_ctx *ctx, const sarbp_radar *radar, const sarbp
     }
     sarbp::BpPlan p;
     std::string why;
-    if (!sarbp::plan_bp(ctx->sms, *radar, *rc, ex, np, *grid, mode, 0, p, why))
+    if (!sarbp::plan_bp(ctx->sms, *radar, *rc, ex, np, *grid, mode, 0, p, why, &ctx->tune))
         return fail(ctx, SARBP_ERR_UNSUPPORTED, "%s", why.c_str());
-    p.checked = ctx->checked;
     int occ = 0;
     SARBP_CUDA(ctx, sarbp::bp_occupancy(p, &occ), "occupancy");
     sarbp::bp_tile_dims(p.pix, &out->tile_x, &out->tile_y);
@@ -1695,6 +1696,49 @@ sarbp_status sarbp_launch_generate_echo(sarbp_complex64 *Srnm, const float *Ptar
     ctx->launches += 1;
     SARBP_CUDA(ctx, cudaStreamSynchronize(ctx->stream), "reference echo sync");
     return SARBP_OK;
+}
+
+sarbp_status sarbp_debug_set(sarbp_ctx *ctx, int32_t key, int64_t value) {
+    if (!ctx) return SARBP_ERR_INVALID_ARGUMENT;
+    sarbp::Tuning &t = ctx->tune;
+    switch (key) {
+        case SARBP_DEBUG_BP_CHUNK:
+            if (value != 0 && value != 4 && value != 8 && value != 16)
+                return fail(ctx, SARBP_ERR_INVALID_ARGUMENT, "pulse chunk must be 0, 4, 8 or 16");
+            t.bp_chunk = (int)value;
+            return SARBP_OK;
+        case SARBP_DEBUG_BP_SEGMENTS:
+            if (value < 0 || value > 64) return fail(ctx, SARBP_ERR_INVALID_ARGUMENT, "segments must be in 0..64");
+            t.bp_segments = (int)value;
+            return SARBP_OK;
+        case SARBP_DEBUG_BP_CHECKED:
+            t.checked = value != 0;
+            return SARBP_OK;
+        case SARBP_DEBUG_WAIT_LIMIT_NS:
+            if (value < 0 || value > 60000000000LL)
+                return fail(ctx, SARBP_ERR_INVALID_ARGUMENT, "wait limit must be in 0..60 s");
+            t.wait_ns = value;
+            return SARBP_OK;
+        case SARBP_DEBUG_WAIT_FAULT_CHUNK:
+            t.wait_fault_chunk = value < 0 ? -1 : (int)std::min<int64_t>(value, 1 << 30);
+            return SARBP_OK;
+        default:
+            return fail(ctx, SARBP_ERR_INVALID_ARGUMENT, "unknown debug key %d", (int)key);
+    }
+}
+
+sarbp_status sarbp_debug_get(sarbp_ctx *ctx, int32_t key, int64_t *value) {
+    if (!ctx || !value) return SARBP_ERR_INVALID_ARGUMENT;
+    const sarbp::Tuning &t = ctx->tune;
+    switch (key) {
+        case SARBP_DEBUG_BP_CHUNK: *value = t.bp_chunk; return SARBP_OK;
+        case SARBP_DEBUG_BP_SEGMENTS: *value = t.bp_segments; return SARBP_OK;
+        case SARBP_DEBUG_BP_CHECKED: *value = t.checked; return SARBP_OK;
+        case SARBP_DEBUG_WAIT_LIMIT_NS: *value = t.wait_ns; return SARBP_OK;
+        case SARBP_DEBUG_WAIT_FAULT_CHUNK: *value = t.wait_fault_chunk; return SARBP_OK;
+        case SARBP_DEBUG_DEVICE_FLAGS: *value = ctx->last_device_flags; return SARBP_OK;
+        default: return fail(ctx, SARBP_ERR_INVALID_ARGUMENT, "unknown debug key %d", (int)key);
+    }
 }
 
 sarbp_status sarbp_probe_issue_rates(sarbp_ctx *ctx, double *fp32_lanes_per_s, double *mufu_lanes_per_s,

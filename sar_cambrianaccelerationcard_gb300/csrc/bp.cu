@@ -68,6 +68,7 @@ constexpr int kChunk = SARBP_BP_CHUNK;  // pulses per staged chunk (a multiple o
 constexpr int kPerWarp = kChunk / kWarps;  // pulses each warp prepares
 static_assert(kChunk % kWarps == 0 && kPerWarp <= 32, "chunk must split evenly over the warps");
 constexpr int kStages = 3;  // raw-window ring depth
+constexpr uint64_t kDrainWaitNs = 500000000ull;  // limit of each wait for copies in flight after a timeout
 constexpr float kMagic = 12582912.0f;  // 1.5 * 2^23: adding it rounds to an integer
 constexpr unsigned kMagicBitsShift4 = 0x4B400000u << 4;
 
@@ -98,6 +99,12 @@ __device__ __forceinline__ void mbar_expect_tx_arrive(unsigned bar, unsigned byt
                  : "memory");
 }
 
+// Delivers `bytes` of a phase's expected transaction count without a copy (the
+// late bytes of an injected fault).
+__device__ __forceinline__ void mbar_complete_tx(unsigned bar, unsigned bytes) {
+    asm volatile("mbarrier.complete_tx.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+}
+
 __device__ __forceinline__ bool mbar_try_wait(unsigned bar, unsigned parity) {
     unsigned ok;
     asm volatile(
@@ -122,7 +129,7 @@ __device__ __forceinline__ bool mbar_wait_bounded(unsigned bar, unsigned parity,
     const uint64_t t0 = globaltimer_ns();
     for (;;) {
 #pragma unroll 1
-        for (int i = 0; i < 256; ++i)
+        for (int i = 0; i < 32; ++i)
             if (mbar_try_wait(bar, parity)) return true;
         if (globaltimer_ns() - t0 > limit_ns) return false;
     }
@@ -232,11 +239,31 @@ __global__ void pulse_ref_kernel(const double *__restrict__ apc, int np, BpGeom 
     pref[2 * p + 1] = make_float4(a2h, (float)(a2 - (double)a2h), (float)(dr * bins_per_m), (float)dph);
 }
 
+// After the wait for chunk c ran out: raise the timeout bit and let the copies
+// still in flight land before the CTA's shared memory is released.  Every warp
+// has issued chunks c and (if it exists) c + 1 and waited for all before them,
+// so those two phases are the outstanding ones: wait for each on its own
+// parity (chunk k is phase k / kStages of ring stage k % kStages).  Out of line:
+// inlined, this cold path moved the main loop's schedule (config 2: 54.1 ms
+// against 53.1 ms per launch).
+template <bool TESTF>
+__device__ __noinline__ void drain_after_timeout(const BpPlan &P, uint64_t *bars, int c, int nchunks) {
+    atomicOr(P.err, kErrWaitTimeout);
+    for (int k = c; k <= c + 1 && k < nchunks; ++k) {
+        const unsigned bar = smem_addr(&bars[k % kStages]);
+        if (TESTF && k == P.fault_chunk) mbar_complete_tx(bar, kFaultBytes);
+        const uint64_t lim = TESTF && P.wait_ns > kDrainWaitNs ? P.wait_ns : kDrainWaitNs;
+        if (!mbar_wait_bounded(bar, (k / kStages) & 1, lim)) atomicOr(P.err, kErrDrainTimeout);
+    }
+}
+
 // Per-(tile, pulse) geometry, window and TMA issue for this warp's pulses of
-// one chunk.  Every warp arrives once on the stage's barrier.
+// one chunk.  Every warp arrives once on the stage's barrier.  `fault` (tests
+// only) arms warp 0's arrival with kFaultBytes that no copy delivers, so the
+// phase cannot complete and the consumers' bounded wait runs out.
 template <int MODE, int STORE, int PIX>
 __device__ __forceinline__ void produce(const BpPlan &P, const Smem &S, int stage, int p0, int count,
-                                        const TileGeo &T) {
+                                        const TileGeo &T, bool fault) {
     constexpr int kTileY = 8 * PIX;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int win = P.win;
@@ -346,6 +373,7 @@ __device__ __forceinline__ void produce(const BpPlan &P, const Smem &S, int stag
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) total += __shfl_xor_sync(0xffffffffu, total, o);
     const unsigned bar = smem_addr(&S.bar[stage]);
+    if (fault && warp == 0) total += kFaultBytes;
     if (lane == 0) mbar_expect_tx_arrive(bar, total);
     __syncwarp();
     if (bytes) tma_bulk_g2s(dst, src, bytes, bar);
@@ -535,7 +563,10 @@ __device__ __forceinline__ void project_chunk(const Smem &S, int stage, int coun
 // the tile into proj[tile][p] (SPLIT / FP16STORE arithmetic).
 // CHUNK: pulses per staged chunk fixed at compile time (the hot unchecked
 // SPLIT / FP16STORE case at 16), or 0 to take the planner's P.chunk.
-template <int MODE, int STORE, int NTERMS, bool CHECKED, int PIX, bool ADJ = false, int CHUNK = 0>
+// TESTF: the waits take their limit from P.wait_ns and P.fault_chunk arms one
+// chunk's barrier so that its wait runs out (tests of the timeout path, through
+// sarbp_debug_set); production variants wait 2 s and carry no injector.
+template <int MODE, int STORE, int NTERMS, bool CHECKED, int PIX, bool ADJ = false, int CHUNK = 0, bool TESTF = false>
 __global__ void __launch_bounds__(kThreads, SARBP_BP_MINBLOCKS)
     bp_kernel(const __grid_constant__ BpPlan P, int tiles_y, int pulses_per_seg, float qq_max) {
     static_assert(!ADJ || MODE == SARBP_MODE_SPLIT || MODE == SARBP_MODE_FP16STORE, "projection: split arithmetic");
@@ -639,21 +670,25 @@ __global__ void __launch_bounds__(kThreads, SARBP_BP_MINBLOCKS)
         if constexpr (ADJ) TH2[h] = pk2(wth[2 * h], wth[2 * h + 1]);
     }
 
-    if (nchunks > 0) produce<MODE, STORE, PIX>(P, S, 0, p_begin, min(chunk, p_end - p_begin), T);
+    if (nchunks > 0)
+        produce<MODE, STORE, PIX>(P, S, 0, p_begin, min(chunk, p_end - p_begin), T, TESTF && P.fault_chunk == 0);
 
     bool failed = false;
     bool clamped = false;
+    int c = 0;  // after a failed wait, the chunk it was for
 #pragma unroll 1
-    for (int c = 0; c < nchunks; ++c) {
+    for (; c < nchunks; ++c) {
         const int stage = c % kStages;
         const int sbuf = c & 1;
         const int pc0 = p_begin + c * chunk;
         const int count = min(chunk, p_end - pc0);
         if (c + 1 < nchunks) {
             const int pn = pc0 + chunk;
-            produce<MODE, STORE, PIX>(P, S, (c + 1) % kStages, pn, min(chunk, p_end - pn), T);
+            produce<MODE, STORE, PIX>(P, S, (c + 1) % kStages, pn, min(chunk, p_end - pn), T,
+                                      TESTF && P.fault_chunk == c + 1);
         }
-        const bool ok = mbar_wait_bounded(smem_addr(&S.bar[stage]), (c / kStages) & 1, 2000000000ull);
+        const bool ok =
+            mbar_wait_bounded(smem_addr(&S.bar[stage]), (c / kStages) & 1, TESTF ? P.wait_ns : kDefaultWaitNs);
         if (!ok) { failed = true; }
         if (__syncthreads_or(failed)) { failed = true; break; }
         // trimmed to the pairs the tile reads for complex16 rows (warp per pulse:
@@ -790,11 +825,7 @@ __global__ void __launch_bounds__(kThreads, SARBP_BP_MINBLOCKS)
 
     if (CHECKED && clamped) atomicOr(P.err, kErrIndexClamp);
     if (failed) {
-        if (threadIdx.x == 0) {
-            atomicOr(P.err, kErrWaitTimeout);
-            // let copies still in flight land before the CTA's shared memory is released
-            for (int s = 0; s < kStages; ++s) mbar_wait_bounded(smem_addr(&S.bar[s]), 0, 500000000ull);
-        }
+        if (threadIdx.x == 0) drain_after_timeout<TESTF>(P, S.bar, c, nchunks);
         __syncthreads();
         return;
     }
@@ -848,10 +879,10 @@ __global__ void reduce_segments_kernel(const float2 *__restrict__ partial, int s
 // resident CTAs per SM there instead of launching it.
 thread_local int *t_occupancy = nullptr;
 
-template <int MODE, int STORE, int NTERMS, bool CHECKED, int PIX, bool ADJ = false, int CHUNK = 0>
+template <int MODE, int STORE, int NTERMS, bool CHECKED, int PIX, bool ADJ = false, int CHUNK = 0, bool TESTF = false>
 cudaError_t launch_variant(const BpPlan &p, cudaStream_t s, int tiles, int tiles_y, int pps, float qq_max) {
     if (CHUNK && p.chunk != CHUNK) return cudaErrorInvalidValue;
-    auto k = bp_kernel<MODE, STORE, NTERMS, CHECKED, PIX, ADJ, CHUNK>;
+    auto k = bp_kernel<MODE, STORE, NTERMS, CHECKED, PIX, ADJ, CHUNK, TESTF>;
     const size_t smem = bp_smem_bytes(STORE, p.win, p.chunk);
     cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
@@ -871,6 +902,39 @@ cudaError_t launch_split(const BpPlan &p, cudaStream_t s, int tiles, int tiles_y
                              : launch_variant<MODE, STORE, 4, false, PIX, false, kChunk>(p, s, tiles, tiles_y, pps, qq_max);
     return p.nterms == 3 ? launch_variant<MODE, STORE, 3, false, PIX>(p, s, tiles, tiles_y, pps, qq_max)
                          : launch_variant<MODE, STORE, 4, false, PIX>(p, s, tiles, tiles_y, pps, qq_max);
+}
+
+// A plan asks for the test variants when it carries a fault or a wait limit
+// other than the default (sarbp_debug_set); they exist for 8-pixel columns.
+bool bp_testing(const BpPlan &p) { return p.fault_chunk >= 0 || p.wait_ns != kDefaultWaitNs; }
+
+template <int MODE, int STORE, bool ADJ>
+cudaError_t launch_testf_mode(const BpPlan &p, cudaStream_t s, int tiles, int tiles_y, int pps, float qq_max) {
+    if constexpr (MODE == SARBP_MODE_SPLIT || MODE == SARBP_MODE_FP16STORE)
+        return p.nterms == 3 ? launch_variant<MODE, STORE, 3, false, 8, ADJ, 0, true>(p, s, tiles, tiles_y, pps, qq_max)
+                             : launch_variant<MODE, STORE, 4, false, 8, ADJ, 0, true>(p, s, tiles, tiles_y, pps, qq_max);
+    else
+        return launch_variant<MODE, STORE, 4, false, 8, false, 0, true>(p, s, tiles, tiles_y, pps, qq_max);
+}
+
+template <bool ADJ>
+cudaError_t launch_testf(const BpPlan &p, cudaStream_t s, int tiles, int tiles_y, int pps, float qq_max) {
+    if (p.pix != 8) return cudaErrorNotSupported;
+    const bool fp16 = p.storage == SARBP_STORE_C32H;
+    if constexpr (ADJ)
+        return fp16 ? launch_testf_mode<SARBP_MODE_SPLIT, SARBP_STORE_C32H, true>(p, s, tiles, tiles_y, pps, qq_max)
+                    : launch_testf_mode<SARBP_MODE_SPLIT, SARBP_STORE_C64, true>(p, s, tiles, tiles_y, pps, qq_max);
+    switch (p.mode) {
+        case SARBP_MODE_FP64:
+            return fp16 ? launch_testf_mode<SARBP_MODE_FP64, SARBP_STORE_C32H, false>(p, s, tiles, tiles_y, pps, qq_max)
+                        : launch_testf_mode<SARBP_MODE_FP64, SARBP_STORE_C64, false>(p, s, tiles, tiles_y, pps, qq_max);
+        case SARBP_MODE_FP32:
+            return fp16 ? launch_testf_mode<SARBP_MODE_FP32, SARBP_STORE_C32H, false>(p, s, tiles, tiles_y, pps, qq_max)
+                        : launch_testf_mode<SARBP_MODE_FP32, SARBP_STORE_C64, false>(p, s, tiles, tiles_y, pps, qq_max);
+        default:
+            return fp16 ? launch_testf_mode<SARBP_MODE_SPLIT, SARBP_STORE_C32H, false>(p, s, tiles, tiles_y, pps, qq_max)
+                        : launch_testf_mode<SARBP_MODE_SPLIT, SARBP_STORE_C64, false>(p, s, tiles, tiles_y, pps, qq_max);
+    }
 }
 
 template <int PIX>
@@ -973,7 +1037,8 @@ cudaError_t launch_project(const BpPlan &p, double2 *out, cudaStream_t s, int *l
     if (e != cudaSuccess) return e;
     if (launches) ++*launches;
     const bool fp16 = p.storage == SARBP_STORE_C32H;
-    if (p.pix == 8) e = fp16 ? launch_proj_pix<SARBP_STORE_C32H, 8>(p, s, tiles, tiles_y, pps, qq_max)
+    if (bp_testing(p)) e = launch_testf<true>(p, s, tiles, tiles_y, pps, qq_max);
+    else if (p.pix == 8) e = fp16 ? launch_proj_pix<SARBP_STORE_C32H, 8>(p, s, tiles, tiles_y, pps, qq_max)
                              : launch_proj_pix<SARBP_STORE_C64, 8>(p, s, tiles, tiles_y, pps, qq_max);
     else if (p.pix == 4) e = fp16 ? launch_proj_pix<SARBP_STORE_C32H, 4>(p, s, tiles, tiles_y, pps, qq_max)
                                   : launch_proj_pix<SARBP_STORE_C64, 4>(p, s, tiles, tiles_y, pps, qq_max);
@@ -1110,7 +1175,8 @@ cudaError_t launch_bp(const BpPlan &p, cudaStream_t s, int *launches) {
         if (e != cudaSuccess) return e;
         if (launches) ++*launches;
     }
-    if (p.pix == 8) e = launch_pix<8>(p, s, tiles, tiles_y, pps, qq_max);
+    if (bp_testing(p)) e = launch_testf<false>(p, s, tiles, tiles_y, pps, qq_max);
+    else if (p.pix == 8) e = launch_pix<8>(p, s, tiles, tiles_y, pps, qq_max);
     else if (p.pix == 4) e = launch_pix<4>(p, s, tiles, tiles_y, pps, qq_max);
     else e = launch_pix<2>(p, s, tiles, tiles_y, pps, qq_max);
     if (e != cudaSuccess) return e;

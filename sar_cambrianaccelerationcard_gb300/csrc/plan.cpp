@@ -44,16 +44,14 @@ void fft_pow2_host(std::vector<std::complex<double>> &h) {
 
 // Pulse chunk for a staging window: the largest (16, 8, 4) whose CTA still fits
 // twice in an SM's 228 KB of shared memory (1 KB reserved per CTA), else the
-// largest that fits once (227 KB per CTA); 0 if none.  SARBP_BP_CHUNK=16|8|4
-// forces a chunk where it fits (tuning and tests: results do not depend on it).
-int bp_choose_chunk(int storage, int win) {
+// largest that fits once (227 KB per CTA); 0 if none.  `force` = 16, 8 or 4
+// takes that chunk where it fits (tuning and tests through sarbp_debug_set:
+// results do not depend on it).
+int bp_choose_chunk(int storage, int win, int force) {
     constexpr size_t kSmemPerSm = 228u << 10, kSmemPerCta = 227u << 10, kReserve = 1u << 10;
-    const char *env = std::getenv("SARBP_BP_CHUNK");
-    if (env && env[0]) {
-        const int c = std::atoi(env);
-        if ((c == 16 || c == 8 || c == 4) && c <= bp_max_chunk() && bp_smem_bytes(storage, win, c) <= kSmemPerCta)
-            return c;
-    }
+    if ((force == 16 || force == 8 || force == 4) && force <= bp_max_chunk() &&
+        bp_smem_bytes(storage, win, force) <= kSmemPerCta)
+        return force;
     for (int c = bp_max_chunk(); c >= 4; c /= 2)
         if (2 * (bp_smem_bytes(storage, win, c) + kReserve) <= kSmemPerSm) return c;
     for (int c = bp_max_chunk(); c >= 4; c /= 2)
@@ -116,8 +114,12 @@ void bp_extremes_host(const double *apc, int np, const sarbp_grid &g, BpExtremes
 }
 
 bool plan_bp(int sms, const sarbp_radar &r, const sarbp_rc_view &rc, const BpExtremes &ex, int np,
-             const sarbp_grid &g, int mode, int pulses_per_launch, BpPlan &p, std::string &why) {
+             const sarbp_grid &g, int mode, int pulses_per_launch, BpPlan &p, std::string &why,
+             const Tuning *tune) {
     std::memset(&p, 0, sizeof p);
+    p.wait_ns = tune && tune->wait_ns > 0 ? (unsigned long long)tune->wait_ns : kDefaultWaitNs;
+    p.fault_chunk = tune ? tune->wait_fault_chunk : -1;
+    p.checked = tune ? tune->checked : 0;
     p.storage = rc.storage;
     p.nbins = rc.nbins;
     p.mode = mode;
@@ -185,7 +187,7 @@ bool plan_bp(int sms, const sarbp_radar &r, const sarbp_rc_view &rc, const BpExt
         }
         int win = (int)std::ceil(2 * half) + 8;
         win = (win + 3) & ~3;
-        const int chunk = bp_choose_chunk(p.storage, win);
+        const int chunk = bp_choose_chunk(p.storage, win, tune ? tune->bp_chunk : 0);
         if (!chunk) {
             why = "tile spans too many range bins for shared memory";
             continue;
@@ -209,7 +211,7 @@ bool plan_bp(int sms, const sarbp_radar &r, const sarbp_rc_view &rc, const BpExt
     bp_tile_dims(p.pix, &tx, &ty);
     const int tiles = ((g.nx + tx - 1) / tx) * ((g.ny + ty - 1) / ty);
     const int npl = pulses_per_launch > 0 ? pulses_per_launch : np;
-    p.segments = bp_choose_segments(tiles, npl, (long long)g.nx * g.ny, sms);
+    p.segments = bp_choose_segments(tiles, npl, (long long)g.nx * g.ny, sms, tune ? tune->bp_segments : 0);
     return true;
 }
 
@@ -222,16 +224,12 @@ bool plan_bp(int sms, const sarbp_radar &r, const sarbp_rc_view &rc, const BpExt
 // Rule: the fewest segments that give at least 12 waves of CTAs, with at least
 // 4 chunks of pulses per segment, no empty segment and the partial images (one
 // per segment) within 1 GiB.  The count depends on the geometry only (not on
-// the staging chunk, which the planner or SARBP_BP_CHUNK picks), so a call
-// gives the same bits whatever the chunk.  SARBP_BP_SEGMENTS=n (1..64) forces
-// n, for sweeps.
-int bp_choose_segments(int tiles, int npl, long long npix, int sms) {
+// the staging chunk, which the planner or a forced chunk picks), so a call
+// gives the same bits whatever the chunk.  `force` = n (1..64) takes n, for
+// sweeps and tests.
+int bp_choose_segments(int tiles, int npl, long long npix, int sms, int force) {
     const int kc = bp_max_chunk();
-    const char *env = std::getenv("SARBP_BP_SEGMENTS");
-    if (env && env[0]) {
-        const int s = std::atoi(env);
-        if (s >= 1 && s <= 64) return s;
-    }
+    if (force >= 1 && force <= 64) return force;
     const long long target = 12LL * 2 * std::max(sms, 1);
     const double max_partial = 1024.0 * 1024.0 * 1024.0;
     int best = 1;

@@ -21,7 +21,22 @@ enum : unsigned {
     kErrIndexClamp = 1u << 1,    // (checked builds) an interpolation index was clamped
     kErrBadLaunch = 1u << 2,     // a kernel saw inconsistent launch parameters
     kErrWindow = 1u << 3,        // a (tile, pulse) needed more bins than the staging window
+    kErrDrainTimeout = 1u << 4,  // after a timed-out wait, a copy in flight did not land within the drain limit
 };
+
+// Test and tuning switches of a context (sarbp_debug_set).  Zero / negative
+// values leave the planner and the kernels their defaults.
+struct Tuning {
+    int bp_chunk = 0;              // staged pulse chunk (16, 8, 4) where it fits; 0: planner
+    int bp_segments = 0;           // pulse segments (1..64); 0: planner
+    int checked = 0;               // 1: clamped, self-reporting back-projection kernels
+    long long wait_ns = 0;         // limit of the staging waits; 0: 2 s
+    int wait_fault_chunk = -1;     // >= 0: that chunk's staging barrier of every CTA is armed with
+                                   // kFaultBytes more than its copies deliver (the wait runs out); the
+                                   // drain then delivers them, as a late copy would
+};
+constexpr unsigned kFaultBytes = 16;
+constexpr unsigned long long kDefaultWaitNs = 2000000000ull;
 
 // ---------------------------------------------------------------- range compression
 struct RcPlan {
@@ -87,6 +102,8 @@ struct BpPlan {
     const double *dphase;    // [np] device, per-pulse phase corrections (rad), or null
     const float2 *weight;    // [ny][nx] device, projection weights (launch_project only)
     float2 *proj;            // [tiles][np] device scratch of tile sums (launch_project only)
+    unsigned long long wait_ns;  // limit of each bounded staging wait
+    int fault_chunk;         // < 0: none; else that chunk's barrier is over-armed (tests, Tuning)
 };
 
 cudaError_t launch_bp(const BpPlan &p, cudaStream_t s, int *launches);
@@ -224,8 +241,11 @@ cudaError_t launch_bp_extremes(const double *apc, int np, const sarbp_grid &g, u
 // buffers (geometry, constants, tile height, window, series terms, segments
 // for launches of `pulses_per_launch` pulses; 0 = all np) from the geometry
 // extremes.  On failure returns false with the reason in `why`.
+// `tune` (may be null) forces the chunk or the segments and sets the waits'
+// limit and fault injection.
 bool plan_bp(int sms, const sarbp_radar &r, const sarbp_rc_view &rc, const BpExtremes &ex, int np,
-             const sarbp_grid &g, int mode, int pulses_per_launch, BpPlan &p, std::string &why);
+             const sarbp_grid &g, int mode, int pulses_per_launch, BpPlan &p, std::string &why,
+             const Tuning *tune = nullptr);
 // Two-level table of E^m = e^{+j 2 pi m / (L N)} ([rc_etab_size(L, N)] entries, plan.cpp).
 void fft_etab_host(int L, int N, std::vector<float2> &etab);
 // Matched-filter spectrum [nfft] and phase table [rc_etab_size] for a layout (plan.cpp).
@@ -238,8 +258,8 @@ size_t bp_smem_bytes(int storage, int win, int chunk);
 int bp_max_chunk();  // largest pulse chunk (16); the planner may choose 8 or 4
 // Pulse segments for `tiles` tiles and `npl` pulses per launch on `sms` SMs
 // (at least 12 waves of CTAs where the pulses allow; at least 4 chunks per
-// segment; partial images within 1 GiB).
-int bp_choose_segments(int tiles, int npl, long long npix, int sms);
+// segment; partial images within 1 GiB); `force` in 1..64 overrides.
+int bp_choose_segments(int tiles, int npl, long long npix, int sms, int force = 0);
 
 // ---------------------------------------------------------------- echo synthesis
 cudaError_t launch_echo_synth(const double *apc, int np, int ns, const sarbp_target *tg, int nt,

@@ -5,7 +5,8 @@ contour of the magnitude (code/SAR_BP/matlab/BPA_SAR.m:168-175, :213-220).
 These metrics make that quantitative and comparable between an image and the
 FP64 oracle's image of the same scene:
   * relative L2 error in dB, 20 log10(||a - b|| / ||b||);
-  * point-target peak position with sub-pixel accuracy (local FFT upsampling);
+  * point-target peak position with sub-pixel accuracy (band-limited cuts of a
+    patch around the target, parabolic refinement);
   * PSLR (peak side-lobe ratio) and ISLR (integrated side-lobe ratio) on the
     range and azimuth cuts through the peak;
   * -3 dB mainlobe widths (the reference's contour level) on both cuts.
@@ -42,18 +43,48 @@ class PointTarget:
     width_azimuth: float  # -3 dB width, pixels
 
 
-def _upsample_patch(patch: np.ndarray, up: int) -> np.ndarray:
-    ny, nx = patch.shape
-    F = np.fft.fftshift(np.fft.fft2(patch))
-    big = np.zeros((ny * up, nx * up), dtype=np.complex128)
-    y0 = (ny * up - ny) // 2
-    x0 = (nx * up - nx) // 2
-    big[y0:y0 + ny, x0:x0 + nx] = F
-    return np.fft.ifft2(np.fft.ifftshift(big)) * (up * up)
+def _band_limited_cut(F: np.ndarray, axis: int, pos: float, start: float, up: int) -> np.ndarray:
+    """Cut of a patch through a fractional position, from its 2-D spectrum F
+    (numpy fft2 order, ny x nx).  axis 1: the row at y = pos, sampled along x
+    at start + j / up; axis 0: the column at x = pos, sampled along y.  The
+    patch is treated as one period of a band-limited signal (zero-padded
+    spectrum), so the cut passes through the exact position instead of the
+    nearest row or column of an upsampled grid."""
+    ny, nx = F.shape
+    if axis == 1:
+        lf = np.fft.fftfreq(ny) * ny
+        g = (np.exp(2j * np.pi * lf * pos / ny) / ny) @ F
+        n = nx
+    else:
+        kf = np.fft.fftfreq(nx) * nx
+        g = F @ (np.exp(2j * np.pi * kf * pos / nx) / nx)
+        n = ny
+    g = g * np.exp(2j * np.pi * (np.fft.fftfreq(n) * n) * start / n)
+    G = np.zeros(n * up, dtype=np.complex128)
+    h = (n + 1) // 2
+    G[:h] = g[:h]
+    G[n * up - (n - h):] = g[h:]
+    if n % 2 == 0:  # the Nyquist bin splits between +n/2 and -n/2
+        G[n // 2] = g[n // 2] / 2
+        G[n * up - n // 2] = g[n // 2] / 2
+    return np.fft.ifft(G) * up
 
 
-def _cut_metrics(cut: np.ndarray, k: int, up: int):
-    m = np.abs(cut)
+def _parabolic_peak(m: np.ndarray) -> float:
+    """Fractional index of the maximum of m (3-point parabola through it)."""
+    k = int(np.argmax(m))
+    if k == 0 or k == len(m) - 1:
+        return float(k)
+    a, b, c = m[k - 1], m[k], m[k + 1]
+    d = a - 2.0 * b + c
+    return float(k) if d == 0 else k + 0.5 * (a - c) / d
+
+
+def _cut_metrics(m: np.ndarray, k: int, up: int):
+    """PSLR, ISLR and -3 dB width (pixels) of the magnitude cut m (samples
+    1/up pixel apart) whose peak is sample k.  The main lobe runs between the
+    first minima on either side; the width interpolates the 1/sqrt(2) crossings
+    linearly between samples."""
     pk = m[k]
     left = k
     while left > 0 and m[left - 1] < m[left]:
@@ -65,23 +96,33 @@ def _cut_metrics(cut: np.ndarray, k: int, up: int):
     main = m[left:right + 1]
     pslr = 20.0 * np.log10(side.max() / pk) if side.size and side.max() > 0 else float("-inf")
     islr = 10.0 * np.log10((side ** 2).sum() / (main ** 2).sum()) if side.size else float("-inf")
-    above = np.nonzero(m >= pk / np.sqrt(2.0))[0]
-    # contiguous -3 dB region around the peak
+    lvl = pk / np.sqrt(2.0)
     lo = k
-    while lo - 1 in set(above) and lo - 1 >= 0:
+    while lo > 0 and m[lo - 1] >= lvl:
         lo -= 1
     hi = k
-    while hi + 1 < len(m) and m[hi + 1] >= pk / np.sqrt(2.0):
+    while hi < len(m) - 1 and m[hi + 1] >= lvl:
         hi += 1
-    width = (hi - lo + 1) / up
-    return pslr, islr, width
+    xl = lo - (m[lo] - lvl) / (m[lo] - m[lo - 1]) if lo > 0 else float(lo)
+    xr = hi + (m[hi] - lvl) / (m[hi] - m[hi + 1]) if hi < len(m) - 1 else float(hi)
+    return pslr, islr, (xr - xl) / up
 
 
-def point_target(img: np.ndarray, x_guess: int, y_guess: int, half: int = 16, up: int = 16) -> PointTarget:
-    """Metrics of the point response nearest (x_guess, y_guess)."""
+def point_target(img: np.ndarray, x_guess: int, y_guess: int, half: int = 32, up: int = 16) -> PointTarget:
+    """Metrics of the point response nearest (x_guess, y_guess).
+
+    A patch of up to 2 half pixels square around the brightest pixel near the
+    guess is treated as band-limited.  The peak is located by alternating
+    row and column cuts through the current estimate, each upsampled `up`
+    times, with a parabola through the largest samples (three rounds).  The
+    range (x) and azimuth (y) cuts are then taken through that peak, sampled
+    so that the peak is a sample, and give PSLR, ISLR and the -3 dB widths.
+    On an analytic sinc of 2 to 6 pixels' resolution at sub-pixel offsets this
+    gives PSLR -13.26 dB, ISLR equal to the integral of sinc^2 over the cut,
+    widths of 0.886 resolution cells and the position to 1e-3 pixel
+    (tests/test_metrics.py)."""
     img = np.asarray(img, dtype=np.complex128)
     ny, nx = img.shape
-    # recentre on the brightest pixel of a small window
     y0, y1 = max(0, y_guess - 3), min(ny, y_guess + 4)
     x0, x1 = max(0, x_guess - 3), min(nx, x_guess + 4)
     w = np.abs(img[y0:y1, x0:x1])
@@ -89,12 +130,19 @@ def point_target(img: np.ndarray, x_guess: int, y_guess: int, half: int = 16, up
     yc, xc = y0 + dy, x0 + dx
     ya, yb = max(0, yc - half), min(ny, yc + half)
     xa, xb = max(0, xc - half), min(nx, xc + half)
-    patch = img[ya:yb, xa:xb]
-    U = _upsample_patch(patch, up)
-    ky, kx = np.unravel_index(np.argmax(np.abs(U)), U.shape)
-    pr, ir, wr = _cut_metrics(U[ky, :], kx, up)
-    pa, ia, wa = _cut_metrics(U[:, kx], ky, up)
-    return PointTarget(x=xa + kx / up, y=ya + ky / up, peak=float(np.abs(U[ky, kx])),
+    F = np.fft.fft2(img[ya:yb, xa:xb])
+    py, px = float(yc - ya), float(xc - xa)
+    for _ in range(3):
+        px = _parabolic_peak(np.abs(_band_limited_cut(F, 1, py, 0.0, up))) / up
+        py = _parabolic_peak(np.abs(_band_limited_cut(F, 0, px, 0.0, up))) / up
+    sx = px - np.floor(px * up) / up  # sample offsets that put the peak on a sample
+    sy = py - np.floor(py * up) / up
+    cx = _band_limited_cut(F, 1, py, sx, up)
+    cy = _band_limited_cut(F, 0, px, sy, up)
+    kx, ky = int(round((px - sx) * up)), int(round((py - sy) * up))
+    pr, ir, wr = _cut_metrics(np.abs(cx), kx, up)
+    pa, ia, wa = _cut_metrics(np.abs(cy), ky, up)
+    return PointTarget(x=xa + px, y=ya + py, peak=float(np.abs(cx[kx])),
                        pslr_range_db=float(pr), pslr_azimuth_db=float(pa),
                        islr_range_db=float(ir), islr_azimuth_db=float(ia),
                        width_range=float(wr), width_azimuth=float(wa))

@@ -227,7 +227,17 @@ SIGNATURES = {
     "sarbp_last_timings": ([ctypes.c_void_p, ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_float)],
                            ctypes.c_int),
     "sarbp_kernel_launches": ([ctypes.c_void_p], ctypes.c_int64),
+    "sarbp_debug_set": ([ctypes.c_void_p, ctypes.c_int32, ctypes.c_int64], ctypes.c_int),
+    "sarbp_debug_get": ([ctypes.c_void_p, ctypes.c_int32, ctypes.POINTER(ctypes.c_int64)], ctypes.c_int),
 }
+
+# sarbp_debug_set / sarbp_debug_get keys (tests and tuning sweeps)
+DEBUG_BP_CHUNK = 1
+DEBUG_BP_SEGMENTS = 2
+DEBUG_BP_CHECKED = 3
+DEBUG_WAIT_LIMIT_NS = 4
+DEBUG_WAIT_FAULT_CHUNK = 5
+DEBUG_DEVICE_FLAGS = 6
 
 _lib = None
 
@@ -515,6 +525,15 @@ class Context:
 
     def launches(self) -> int:
         return int(self.lib.sarbp_kernel_launches(self.h))
+
+    def debug_set(self, key: int, value: int):
+        """Test / tuning switch of this context (sarbp_debug_set)."""
+        self.check(self.lib.sarbp_debug_set(self.h, int(key), int(value)), "debug_set")
+
+    def debug_get(self, key: int) -> int:
+        v = ctypes.c_int64()
+        self.check(self.lib.sarbp_debug_get(self.h, int(key), ctypes.byref(v)), "debug_get")
+        return int(v.value)
 
     def probe_issue_rates(self):
         f, m, n = ctypes.c_double(), ctypes.c_double(), ctypes.c_int32()

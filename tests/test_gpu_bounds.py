@@ -3,13 +3,11 @@
 The production SPLIT / FP16STORE kernels index the staged range window
 without a per-update clamp: the window is sized (and checked per tile and
 pulse by the producer) so that every bin a pixel needs lies inside it.  The
-checked build (SARBP_BOUNDS_CHECK=1 when the context is created) keeps a clamp
-on every index and reports through the context if it ever changed one.  Over
-straight, curved and ragged geometries it must report nothing and produce the
+checked kernels (sarbp_debug_set(SARBP_DEBUG_BP_CHECKED, 1)) keep a clamp
+on every index and report through the context if they ever changed one.  Over
+straight, curved and ragged geometries they must report nothing and produce the
 same image bit for bit.
 """
-import os
-
 import numpy as np
 import pytest
 
@@ -31,15 +29,8 @@ def scenes_to_check():
 
 @pytest.mark.parametrize("mode", ["split", "fp16store"])
 def test_checked_kernel_never_clamps(mode):
-    old = os.environ.get("SARBP_BOUNDS_CHECK")
-    os.environ["SARBP_BOUNDS_CHECK"] = "1"
-    try:
-        checked = sarbp.Context(0)
-    finally:
-        if old is None:
-            del os.environ["SARBP_BOUNDS_CHECK"]
-        else:
-            os.environ["SARBP_BOUNDS_CHECK"] = old
+    checked = sarbp.Context(0)
+    checked.debug_set(sarbp.DEBUG_BP_CHECKED, 1)
     results = []
     for s in scenes_to_check():  # the clamped kernel runs first and must report nothing
         echo = sarbp.synthesize(checked, s)

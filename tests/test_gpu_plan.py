@@ -164,7 +164,7 @@ def test_wide_windows_keep_two_ctas(ctx, case, storage, chunk):
 
 
 @pytest.mark.parametrize("storage", [sarbp.STORE_C64, sarbp.STORE_C32H])
-def test_chunk_size_does_not_change_results(ctx, monkeypatch, storage):
+def test_chunk_size_does_not_change_results(ctx, storage):
     """Pixels accumulate pulses in the same order whatever the staging chunk, so
     16-, 8- and 4-pulse chunks give the same bits (back-projection and the
     weighted projection; 300 pulses: ragged last chunks)."""
@@ -176,11 +176,14 @@ def test_chunk_size_does_not_change_results(ctx, monkeypatch, storage):
     mode = sarbp.MODE_FP16STORE if storage == sarbp.STORE_C32H else sarbp.MODE_SPLIT
     w = (np.random.default_rng(4).standard_normal((g.ny, g.nx)) + 0j).astype(np.complex64)
     imgs, projs = {}, {}
-    for c in ("16", "8", "4"):
-        monkeypatch.setenv("SARBP_BP_CHUNK", c)
-        assert ctx.bp_plan(r, view(s, storage), s.apc, g, mode).pulse_chunk == int(c)
-        imgs[c] = ctx.backproject(r, data, s.apc, g, mode, lay.t0_bins, lay.bin_rate, scale=scale)
-        projs[c] = ctx.project_weighted(r, data, s.apc, g, mode, lay.t0_bins, lay.bin_rate, w, scale=scale)
+    try:
+        for c in ("16", "8", "4"):
+            ctx.debug_set(sarbp.DEBUG_BP_CHUNK, int(c))
+            assert ctx.bp_plan(r, view(s, storage), s.apc, g, mode).pulse_chunk == int(c)
+            imgs[c] = ctx.backproject(r, data, s.apc, g, mode, lay.t0_bins, lay.bin_rate, scale=scale)
+            projs[c] = ctx.project_weighted(r, data, s.apc, g, mode, lay.t0_bins, lay.bin_rate, w, scale=scale)
+    finally:
+        ctx.debug_set(sarbp.DEBUG_BP_CHUNK, 0)
     for c in ("8", "4"):
         assert np.array_equal(imgs[c], imgs["16"])
         assert np.array_equal(projs[c], projs["16"])
@@ -247,7 +250,7 @@ def test_segments_fill_waves(ctx, n_img, np_):
         assert info.segments == {4096: 1, 2048: 2, 1024: 8, 512: 8, 256: 1}[n_img]
 
 
-def test_forced_segments_agree(ctx, monkeypatch):
+def test_forced_segments_agree(ctx):
     """Segment counts only regroup the per-pixel pulse sums: 1, 3 and 7
     segments (uneven last segments) agree with the planner's choice to FP32
     rounding.  The weighted projection sums each pulse inside one CTA per tile
@@ -256,16 +259,18 @@ def test_forced_segments_agree(ctx, monkeypatch):
     r, g, lay = sarbp.scene_args(s)
     rc = ctx.range_compress(r, sarbp.synthesize(ctx, s))
     w = (np.random.default_rng(9).standard_normal((g.ny, g.nx)) + 0j).astype(np.complex64)
-    monkeypatch.delenv("SARBP_BP_SEGMENTS", raising=False)
     auto = ctx.bp_plan(r, view(s), s.apc, g, sarbp.MODE_SPLIT).segments
     ref = ctx.backproject(r, rc, s.apc, g, sarbp.MODE_SPLIT, lay.t0_bins, lay.bin_rate)
     pref = ctx.project_weighted(r, rc, s.apc, g, sarbp.MODE_SPLIT, lay.t0_bins, lay.bin_rate, w)
-    for n in ("1", "3", "7"):
-        monkeypatch.setenv("SARBP_BP_SEGMENTS", n)
-        assert ctx.bp_plan(r, view(s), s.apc, g, sarbp.MODE_SPLIT).segments == int(n)
-        img = ctx.backproject(r, rc, s.apc, g, sarbp.MODE_SPLIT, lay.t0_bins, lay.bin_rate)
-        prj = ctx.project_weighted(r, rc, s.apc, g, sarbp.MODE_SPLIT, lay.t0_bins, lay.bin_rate, w)
-        err = 20 * np.log10(np.linalg.norm(img - ref) / np.linalg.norm(ref))
-        print("segments", n, "vs", auto, "image rel-L2 dB", err)
-        assert err <= -110.0
-        assert np.array_equal(prj, pref)
+    try:
+        for n in ("1", "3", "7"):
+            ctx.debug_set(sarbp.DEBUG_BP_SEGMENTS, int(n))
+            assert ctx.bp_plan(r, view(s), s.apc, g, sarbp.MODE_SPLIT).segments == int(n)
+            img = ctx.backproject(r, rc, s.apc, g, sarbp.MODE_SPLIT, lay.t0_bins, lay.bin_rate)
+            prj = ctx.project_weighted(r, rc, s.apc, g, sarbp.MODE_SPLIT, lay.t0_bins, lay.bin_rate, w)
+            err = 20 * np.log10(np.linalg.norm(img - ref) / np.linalg.norm(ref))
+            print("segments", n, "vs", auto, "image rel-L2 dB", err)
+            assert err <= -110.0
+            assert np.array_equal(prj, pref)
+    finally:
+        ctx.debug_set(sarbp.DEBUG_BP_SEGMENTS, 0)
