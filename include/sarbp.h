@@ -156,18 +156,25 @@ sarbp_status sarbp_range_compress(sarbp_ctx *ctx, const sarbp_radar *radar,
 /* Range compression that allocates no device memory.  No counterpart in the
  * reference.  For callers that cannot call cudaMalloc while they run -- a host
  * program whose own allocator already reserved the GPU's memory, or a
- * latency-bound loop that must not stall on an allocation.  Same kernels and
- * results as sarbp_range_compress, but all scratch (filter spectrum, FFT
- * phase table for twiddles and upsampling ramp, a batch of pulse spectra) lives in one fixed
- * SARBP_NOALLOC_SCRATCH_BYTES device array that every GPU loading the library
- * holds until exit.  Pointers must be device memory; the call is asynchronous
- * on `stream` (NULL: the default stream) except when the radar/layout tables
- * change, which uploads them and waits.  The first call on a device (with that
- * device current) looks up the array's address; make it before any stream
- * capture.  Calls share the array: calls that overlap on the GPU race.
- * Returns SARBP_ERR_UNSUPPORTED when the tables and one pulse spectrum,
- * 8*(2*nfft + 256 + upsample*nfft/256) bytes, exceed the array (the FFT itself
- * is limited to nfft <= 32768, which always fits). */
+ * latency-bound loop that must not stall on an allocation.  Same kernels,
+ * tables and results as sarbp_range_compress, but all scratch (filter
+ * spectrum, FFT phase table for twiddles and upsampling ramp, a batch of pulse
+ * spectra) lives in one fixed SARBP_NOALLOC_SCRATCH_BYTES device array that
+ * every GPU loading the library holds until exit; every supported layout
+ * (range FFT up to 32768 points, upsampling up to 16) fits in it.  Pointers
+ * must be device memory; the call is asynchronous on `stream` (NULL: the
+ * default stream) except when the radar/layout differs from the previous
+ * call's on that device: it then uploads the tables and waits, so such calls
+ * must stay outside stream capture.
+ * Set-up: the first call on a device (with that device current) looks up the
+ * array's address, uploads the tables and loads the kernels; under CUDA's lazy
+ * module loading the array and the kernels' code reach the GPU only then.
+ * Make that call before the caller's allocator reserves the GPU's memory and
+ * before any capture: a call with np = 0 (valid radar and ns, echo and outputs
+ * may be NULL) does the set-up and nothing else.  Or run with
+ * CUDA_MODULE_LOADING=EAGER.  Calls share the array, which keeps the last
+ * call's contents: calls that overlap on the GPU race.
+ * SARBP_ERR_UNSUPPORTED: a range FFT beyond 32768 points or upsampling beyond 16. */
 #define SARBP_NOALLOC_SCRATCH_BYTES (4u << 20)
 sarbp_status sarbp_range_compress_noalloc(const sarbp_radar *radar, const sarbp_complex64 *echo,
                                           int32_t np, int32_t ns, int32_t storage, void *rc_out,

@@ -1183,7 +1183,7 @@ cudaError_t launch_bp(const BpPlan &p, cudaStream_t s, int *launches) {
     if (launches) ++*launches;
     if (p.segments > 1) {
         const size_t count = (size_t)p.g.nx * p.g.ny;
-        const int blocks = (int)std::min<size_t>((count + 255) / 256, 152 * 8);
+        const int blocks = (int)std::min<size_t>((count + 255) / 256, (size_t)current_sms() * 8);
         reduce_segments_kernel<<<blocks, 256, 0, s>>>(p.partial, p.segments, count, p.image, p.accumulate);
         e = cudaGetLastError();
         if (launches) ++*launches;

@@ -13,7 +13,14 @@
 //
 // Set-up: the first call on each device, with that device current, looks up
 // the array's device address with cudaGetSymbolAddress (the array's name in
-// host code is only a host-side stand-in).  Make that first call before any
+// host code is only a host-side stand-in), uploads the tables of its layout
+// and loads the kernels.  Under CUDA's default lazy module loading the array
+// and the kernels' code reach the GPU only then, so a caller whose allocator
+// later reserves the GPU's memory makes that first call before (a call with
+// np = 0 and a valid radar and layout does the set-up and nothing else), or
+// runs with CUDA_MODULE_LOADING=EAGER.  Every call whose radar or layout
+// differs from the previous one on that device rebuilds the tables and waits
+// for their upload, so those calls (the first included) must stay outside
 // stream capture.  All calls share the array and it keeps the last call's
 // contents; calls whose work overlaps on the GPU (different host threads or
 // streams) race on it and must be serialised by the caller.
@@ -32,7 +39,12 @@ namespace {
 constexpr size_t kScratchBytes = size_t(4) << 20;  // SARBP_NOALLOC_SCRATCH_BYTES
 constexpr int kMaxDevices = 64;
 constexpr int kMaxN = 32768;  // largest range FFT the kernels support
-constexpr int kMaxL = 16;
+constexpr int kMaxL = 16;     // largest upsampling factor
+constexpr size_t kMaxEtab = 256 + kMaxL * kMaxN / 256;
+// The largest tables (filter spectrum and phase table) plus one pulse spectrum
+// and its split-path bounds fit, so every supported layout runs here.
+static_assert(sizeof(float2) * (kMaxN + kMaxEtab) + 256 + sizeof(float2) * kMaxN + 2 * sizeof(float) <= kScratchBytes,
+              "scratch array too small for the largest layout");
 
 static __device__ __align__(256) unsigned char g_rc_scratch[kScratchBytes];
 
@@ -52,55 +64,7 @@ TableKey g_keys[kMaxDevices];
 
 // host staging for the tables: static storage, no heap
 std::complex<double> g_h[kMaxN];
-float2 g_filt[kMaxN], g_etab[256 + kMaxL * kMaxN / 256];
-
-constexpr double kPi = 3.14159265358979323846;
-
-void fft_inplace(std::complex<double> *x, int n) {
-    for (int i = 1, j = 0; i < n; ++i) {
-        int bit = n >> 1;
-        for (; j & bit; bit >>= 1) j ^= bit;
-        j ^= bit;
-        if (i < j) std::swap(x[i], x[j]);
-    }
-    for (int len = 2; len <= n; len <<= 1) {
-        for (int i = 0; i < n; i += len) {
-            for (int k = 0; k < len / 2; ++k) {
-                const double a = -2.0 * kPi * (double)k / (double)len;
-                const std::complex<double> w(std::cos(a), std::sin(a));
-                const std::complex<double> u = x[i + k], v = x[i + k + len / 2] * w;
-                x[i + k] = u + v;
-                x[i + k + len / 2] = u - v;
-            }
-        }
-    }
-}
-
-// Fills g_filt and g_etab for the layout (same tables as the allocating path).
-void build_tables(const sarbp_radar &r, const sarbp_rc_layout &lay) {
-    const int N = lay.nfft, L = r.upsample;
-    for (int i = 0; i < N; ++i) g_h[i] = 0.0;
-    for (int i = 0; i < lay.nc && i < N; ++i) {
-        const double u = (double)i / r.fs;
-        if (u >= 0.0 && u < r.tp) {
-            const double ph = kPi * r.kr * (u - r.tc) * (u - r.tc);
-            g_h[i] = std::complex<double>(std::cos(ph), std::sin(ph));
-        }
-    }
-    fft_inplace(g_h, N);
-    for (int k = 0; k < N; ++k) {
-        const long long m = ((long long)k * lay.shift) % N;
-        const double a = -2.0 * kPi * (double)m / (double)N;
-        const std::complex<double> v = std::conj(g_h[k]) * std::complex<double>(std::cos(a), std::sin(a)) / (double)N;
-        g_filt[k] = make_float2((float)v.real(), (float)v.imag());
-    }
-    const double LN = (double)L * N;
-    const int ne = sarbp::rc_etab_size(L, N);
-    for (int i = 0; i < ne; ++i) {
-        const double a = 2.0 * kPi * (double)(i < 256 ? i : 256 * (i - 256)) / LN;
-        g_etab[i] = make_float2((float)std::cos(a), (float)std::sin(a));
-    }
-}
+float2 g_filt[kMaxN], g_etab[kMaxEtab];
 
 bool on_device(const void *p) {
     cudaPointerAttributes a;
@@ -121,18 +85,16 @@ extern "C" sarbp_status sarbp_range_compress_noalloc(const sarbp_radar *radar, c
     if (st != SARBP_OK) return st;
     if (np < 0) return SARBP_ERR_INVALID_ARGUMENT;
     if (storage != SARBP_STORE_C64 && storage != SARBP_STORE_C32H) return SARBP_ERR_INVALID_ARGUMENT;
-    if (np == 0) return SARBP_OK;
-    if (!echo || !rc_out || (storage == SARBP_STORE_C32H && !rc_scale_out)) return SARBP_ERR_INVALID_ARGUMENT;
-    if (!sarbp::rc_size_supported(lay.nfft)) return SARBP_ERR_UNSUPPORTED;
-    // tables (filter spectrum, phase table) plus at least one pulse spectrum must fit
+    if (!sarbp::rc_size_supported(lay.nfft) || radar->upsample > kMaxL) return SARBP_ERR_UNSUPPORTED;
+    if (np > 0) {
+        if (!echo || !rc_out || (storage == SARBP_STORE_C32H && !rc_scale_out)) return SARBP_ERR_INVALID_ARGUMENT;
+        if (!on_device(echo) || !on_device(rc_out) || (storage == SARBP_STORE_C32H && !on_device(rc_scale_out)))
+            return SARBP_ERR_INVALID_ARGUMENT;  // device memory only: a host buffer would need a staging copy
+    }
     const size_t N = (size_t)lay.nfft, L = (size_t)radar->upsample;
     const size_t ne = (size_t)sarbp::rc_etab_size((int)L, (int)N);
     const size_t tables = sizeof(float2) * (N + ne);
     const size_t row = sizeof(float2) * N;
-    if (tables + row + 2 * sizeof(float) + 256 > kScratchBytes || N > (size_t)kMaxN || L > (size_t)kMaxL)
-        return SARBP_ERR_UNSUPPORTED;
-    if (!on_device(echo) || !on_device(rc_out) || (storage == SARBP_STORE_C32H && !on_device(rc_scale_out)))
-        return SARBP_ERR_INVALID_ARGUMENT;  // device memory only: a host buffer would need a staging copy
 
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) {
@@ -155,7 +117,8 @@ extern "C" sarbp_status sarbp_range_compress_noalloc(const sarbp_radar *radar, c
     float2 *d_spec = reinterpret_cast<float2 *>(base + ((tables + 255) & ~size_t(255)));
     const size_t spec_bytes = kScratchBytes - ((tables + 255) & ~size_t(255));
     // per pulse: one spectrum row and two split-path bounds
-    const int batch = (int)std::max<size_t>(1, std::min<size_t>((size_t)np, spec_bytes / (row + 2 * sizeof(float))));
+    const int batch =
+        (int)std::max<size_t>(1, std::min<size_t>((size_t)std::max(np, 1), spec_bytes / (row + 2 * sizeof(float))));
     float *d_bound2 = reinterpret_cast<float *>(reinterpret_cast<char *>(d_spec) + row * (size_t)batch);
 
     TableKey key;
@@ -168,7 +131,7 @@ extern "C" sarbp_status sarbp_range_compress_noalloc(const sarbp_radar *radar, c
     key.tc = radar->tc;
     key.tp = radar->tp;
     if (!g_have_tables[dev] || !(g_keys[dev] == key)) {
-        build_tables(*radar, lay);
+        sarbp::rc_tables_fill(*radar, lay, g_h, g_filt, g_etab);  // the allocating path's tables, bit for bit
         // the host staging arrays are reused by the next call: wait for the copies
         if (cudaMemcpyAsync(d_filt, g_filt, sizeof(float2) * N, cudaMemcpyHostToDevice, s) != cudaSuccess ||
             cudaMemcpyAsync(d_etab, g_etab, sizeof(float2) * ne, cudaMemcpyHostToDevice, s) != cudaSuccess ||
@@ -180,19 +143,26 @@ extern "C" sarbp_status sarbp_range_compress_noalloc(const sarbp_radar *radar, c
         g_keys[dev] = key;
         g_have_tables[dev] = true;
     }
+    sarbp::RcPlan plan{};
+    plan.bound2 = d_bound2;
+    plan.ns = ns;
+    plan.nfft = lay.nfft;
+    plan.L = radar->upsample;
+    plan.nbins = lay.nbins;
+    plan.storage = storage;
+    if (np == 0) {  // set-up only: load and configure this layout's kernels
+        if (sarbp::prepare_rc_kernels(plan) != cudaSuccess) {
+            cudaGetLastError();
+            return SARBP_ERR_CUDA;
+        }
+        return SARBP_OK;
+    }
     // No scratch byte needs clearing: every spectrum the inverse kernel reads
     // was written by the forward kernel of the same batch.
     const size_t esize = storage == SARBP_STORE_C64 ? 8 : 4;
     const float2 *e2 = reinterpret_cast<const float2 *>(echo);
     for (int p0 = 0; p0 < np; p0 += batch) {
-        sarbp::RcPlan plan{};
-        plan.bound2 = d_bound2;
         plan.np = std::min(batch, np - p0);
-        plan.ns = ns;
-        plan.nfft = lay.nfft;
-        plan.L = radar->upsample;
-        plan.nbins = lay.nbins;
-        plan.storage = storage;
         float *sc = storage == SARBP_STORE_C32H ? rc_scale_out + p0 : nullptr;
         if (sarbp::launch_rc_forward(plan, e2 + (size_t)p0 * ns, d_filt, d_etab, d_spec, sc, s) != cudaSuccess ||
             sarbp::launch_rc_inverse(plan, d_spec, d_etab, sc,

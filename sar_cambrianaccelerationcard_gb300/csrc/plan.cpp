@@ -17,13 +17,9 @@
 #include "sarbp_internal.h"
 
 namespace sarbp {
-namespace {
-double dot3(const double *a, const double *b) { return a[0] * b[0] + a[1] * b[1] + a[2] * b[2]; }
 
-// In-place radix-2 forward DFT (unnormalised) of a power-of-two length, FP64.
-void fft_pow2_host(std::vector<std::complex<double>> &h) {
+void fft_pow2_inplace(std::complex<double> *h, int N) {
     constexpr double kPi = 3.14159265358979323846;
-    const int N = (int)h.size();
     for (int i = 1, j = 0; i < N; ++i) {
         int bit = N >> 1;
         for (; j & bit; bit >>= 1) j ^= bit;
@@ -40,6 +36,12 @@ void fft_pow2_host(std::vector<std::complex<double>> &h) {
                 h[i + k + len / 2] = u - v;
             }
 }
+
+namespace {
+double dot3(const double *a, const double *b) { return a[0] * b[0] + a[1] * b[1] + a[2] * b[2]; }
+
+// In-place radix-2 forward DFT (unnormalised) of a power-of-two length, FP64.
+void fft_pow2_host(std::vector<std::complex<double>> &h) { fft_pow2_inplace(h.data(), (int)h.size()); }
 }  // namespace
 
 // Pulse chunk for a staging window: the largest (16, 8, 4) whose CTA still fits
@@ -244,11 +246,11 @@ int bp_choose_segments(int tiles, int npl, long long npix, int sms, int force) {
     return best;
 }
 
-void rc_tables_host(const sarbp_radar &r, const sarbp_rc_layout &lay, std::vector<float2> &filt,
-                    std::vector<float2> &etab) {
+void rc_tables_fill(const sarbp_radar &r, const sarbp_rc_layout &lay, std::complex<double> *h, float2 *filt,
+                    float2 *etab) {
     constexpr double kPi = 3.14159265358979323846;
     const int N = lay.nfft, L = r.upsample;
-    std::vector<std::complex<double>> h(N);
+    for (int i = 0; i < N; ++i) h[i] = 0.0;
     for (int i = 0; i < lay.nc && i < N; ++i) {
         const double u = (double)i / r.fs;
         if (u >= 0.0 && u < r.tp) {
@@ -256,15 +258,22 @@ void rc_tables_host(const sarbp_radar &r, const sarbp_rc_layout &lay, std::vecto
             h[i] = std::complex<double>(std::cos(ph), std::sin(ph));
         }
     }
-    fft_pow2_host(h);  // forward transform of the chirp (unnormalised)
-    filt.resize(N);
+    fft_pow2_inplace(h, N);
     for (int k = 0; k < N; ++k) {
         const long long m = ((long long)k * lay.shift) % N;
         const double a = -2.0 * kPi * (double)m / (double)N;
         const std::complex<double> v = std::conj(h[k]) * std::complex<double>(std::cos(a), std::sin(a)) / (double)N;
         filt[k] = make_float2((float)v.real(), (float)v.imag());
     }
-    fft_etab_host(L, N, etab);
+    fft_etab_fill(L, N, etab);
+}
+
+void rc_tables_host(const sarbp_radar &r, const sarbp_rc_layout &lay, std::vector<float2> &filt,
+                    std::vector<float2> &etab) {
+    std::vector<std::complex<double>> h(lay.nfft);
+    filt.resize(lay.nfft);
+    etab.resize(rc_etab_size(r.upsample, lay.nfft));
+    rc_tables_fill(r, lay, h.data(), filt.data(), etab.data());
 }
 
 void dft_tables_host(int n, std::vector<float2> &etab, std::vector<float2> &chirp, std::vector<float2> &kfwd,
@@ -300,14 +309,19 @@ void dft_tables_host(int n, std::vector<float2> &etab, std::vector<float2> &chir
     }
 }
 
-void fft_etab_host(int L, int N, std::vector<float2> &etab) {
+void fft_etab_fill(int L, int N, float2 *etab) {
     constexpr double kPi = 3.14159265358979323846;
-    etab.resize(rc_etab_size(L, N));
+    const int n = rc_etab_size(L, N);
     const double LN = (double)L * N;
-    for (size_t i = 0; i < etab.size(); ++i) {
+    for (int i = 0; i < n; ++i) {
         const double a = 2.0 * kPi * (double)(i < 256 ? i : 256 * (i - 256)) / LN;
         etab[i] = make_float2((float)std::cos(a), (float)std::sin(a));
     }
+}
+
+void fft_etab_host(int L, int N, std::vector<float2> &etab) {
+    etab.resize(rc_etab_size(L, N));
+    fft_etab_fill(L, N, etab.data());
 }
 
 }  // namespace sarbp

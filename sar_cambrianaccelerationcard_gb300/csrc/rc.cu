@@ -282,6 +282,10 @@ constexpr int threads_for() {
 }
 
 
+// With t_prepare set the launchers below configure their kernel and return
+// without launching it (prepare_rc_kernels).
+thread_local bool t_prepare = false;
+
 template <int N>
 cudaError_t fwd_n(const RcPlan &p, const float2 *echo, const float2 *filt, const float2 *etab,
                   float2 *spec, float *scale, cudaStream_t s) {
@@ -289,7 +293,7 @@ cudaError_t fwd_n(const RcPlan &p, const float2 *echo, const float2 *filt, const
     const size_t smem = sizeof(float2) * N + kTabSmem;
     auto k = rc_forward_kernel<N, T>;
     cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return e;
+    if (e != cudaSuccess || t_prepare) return e;
     k<<<p.np, T, smem, s>>>(p.ns, p.L, echo, filt, etab, spec, scale);
     return cudaGetLastError();
 }
@@ -303,12 +307,12 @@ cudaError_t inv_n(const RcPlan &p, const float2 *spec, const float2 *etab, const
     if (p.storage == SARBP_STORE_C64) {
         auto k = rc_inverse_kernel<N, T, SARBP_STORE_C64>;
         e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        if (e != cudaSuccess) return e;
+        if (e != cudaSuccess || t_prepare) return e;
         k<<<p.np * p.L, T, smem, s>>>(p.ns, p.L, p.nbins, spec, etab, scale, out);
     } else {
         auto k = rc_inverse_kernel<N, T, SARBP_STORE_C32H>;
         e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        if (e != cudaSuccess) return e;
+        if (e != cudaSuccess || t_prepare) return e;
         k<<<p.np * p.L, T, smem, s>>>(p.ns, p.L, p.nbins, spec, etab, scale, out);
     }
     return cudaGetLastError();
@@ -321,7 +325,7 @@ cudaError_t fwd2(const RcPlan &p, const float2 *echo, const float2 *filt, const 
     const size_t smem = sizeof(float2) * M + kTabSmem;
     auto k = rc_forward2_kernel<M, T>;
     cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return e;
+    if (e != cudaSuccess || t_prepare) return e;
     k<<<2 * p.np, T, smem, s>>>(p.ns, p.L, echo, filt, etab, spec, bound2);
     return cudaGetLastError();
 }
@@ -335,12 +339,12 @@ cudaError_t inv2(const RcPlan &p, const float2 *spec, const float2 *etab, const 
     if (p.storage == SARBP_STORE_C64) {
         auto k = rc_inverse2_kernel<M, T, SARBP_STORE_C64>;
         e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        if (e != cudaSuccess) return e;
+        if (e != cudaSuccess || t_prepare) return e;
         k<<<2 * p.np * p.L, T, smem, s>>>(p.ns, p.L, p.nbins, spec, etab, bound2, scale, out);
     } else {
         auto k = rc_inverse2_kernel<M, T, SARBP_STORE_C32H>;
         e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        if (e != cudaSuccess) return e;
+        if (e != cudaSuccess || t_prepare) return e;
         k<<<2 * p.np * p.L, T, smem, s>>>(p.ns, p.L, p.nbins, spec, etab, bound2, scale, out);
     }
     return cudaGetLastError();
@@ -371,7 +375,7 @@ cudaError_t launch_rc_forward(const RcPlan &p, const float2 *echo, const float2 
     if (p.np <= 0) return cudaSuccess;
     if (p.L < 1 || p.L > 16) return cudaErrorInvalidValue;
     if (p.nfft >= SARBP_RC_SPLIT_MIN && p.nfft >= 8192) {
-        if (!p.bound2) return cudaErrorInvalidValue;
+        if (!p.bound2 && !t_prepare) return cudaErrorInvalidValue;
         if (p.nfft == 32768) return fwd2<16384>(p, echo, filt, etab, spec, p.bound2, s);
         if (p.nfft == 16384) return fwd2<8192>(p, echo, filt, etab, spec, p.bound2, s);
         if (p.nfft == 8192) return fwd2<4096>(p, echo, filt, etab, spec, p.bound2, s);
@@ -386,7 +390,7 @@ cudaError_t launch_rc_inverse(const RcPlan &p, const float2 *spec, const float2 
     if (p.np <= 0) return cudaSuccess;
     if (p.L < 1 || p.L > 16) return cudaErrorInvalidValue;
     if (p.nfft >= SARBP_RC_SPLIT_MIN && p.nfft >= 8192) {
-        if (!p.bound2) return cudaErrorInvalidValue;
+        if (!p.bound2 && !t_prepare) return cudaErrorInvalidValue;
         float *sc = const_cast<float *>(scale);
         if (p.nfft == 32768) return inv2<16384>(p, spec, etab, p.bound2, sc, out, s);
         if (p.nfft == 16384) return inv2<8192>(p, spec, etab, p.bound2, sc, out, s);
@@ -395,6 +399,17 @@ cudaError_t launch_rc_inverse(const RcPlan &p, const float2 *spec, const float2 
 #define SARBP_INV(N) inv_n<N>(p, spec, etab, scale, out, s)
     SARBP_RC_SWITCH(p.nfft, SARBP_INV)
 #undef SARBP_INV
+}
+
+cudaError_t prepare_rc_kernels(const RcPlan &p) {
+    if (p.L < 1 || p.L > 16) return cudaErrorInvalidValue;
+    RcPlan q = p;
+    q.np = 1;  // the launchers return early for empty plans
+    t_prepare = true;
+    cudaError_t e = launch_rc_forward(q, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr);
+    if (e == cudaSuccess) e = launch_rc_inverse(q, nullptr, nullptr, nullptr, nullptr, nullptr);
+    t_prepare = false;
+    return e;
 }
 
 }  // namespace sarbp

@@ -5,7 +5,10 @@
 #include <cuda_fp16.h>
 #include <stdint.h>
 
+#include <atomic>
+
 #include <cmath>
+#include <complex>
 
 #include <string>
 #include <vector>
@@ -38,6 +41,25 @@ struct Tuning {
 constexpr unsigned kFaultBytes = 16;
 constexpr unsigned long long kDefaultWaitNs = 2000000000ull;
 
+// SMs of the current device, queried once per device: grid-stride launches
+// size their grids as a multiple of it.
+inline int current_sms() {
+    static std::atomic<int> cache[64];
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) {
+        cudaGetLastError();
+        return 1;
+    }
+    int n = cache[dev].load(std::memory_order_relaxed);
+    if (n > 0) return n;
+    if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n <= 0) {
+        cudaGetLastError();
+        return 1;
+    }
+    cache[dev].store(n, std::memory_order_relaxed);
+    return n;
+}
+
 // ---------------------------------------------------------------- range compression
 struct RcPlan {
     int np;          // pulses in this launch
@@ -59,6 +81,9 @@ cudaError_t launch_rc_inverse(const RcPlan &p, const float2 *spec, const float2 
                               const float *scale, void *out, cudaStream_t s);
 // The split path (nfft = 32768) writes the FP16 scale in the inverse, so the
 // scale pointer passed to launch_rc_inverse must be writable there.
+// Loads and configures the kernels a plan's launches use without launching
+// them (the module loads here under lazy loading, not at the first launch).
+cudaError_t prepare_rc_kernels(const RcPlan &p);
 inline int rc_etab_size(int L, int nfft) { return 256 + (L * nfft >= 256 ? L * nfft / 256 : 1); }
 bool rc_size_supported(int nfft);
 
@@ -248,9 +273,16 @@ bool plan_bp(int sms, const sarbp_radar &r, const sarbp_rc_view &rc, const BpExt
              const Tuning *tune = nullptr);
 // Two-level table of E^m = e^{+j 2 pi m / (L N)} ([rc_etab_size(L, N)] entries, plan.cpp).
 void fft_etab_host(int L, int N, std::vector<float2> &etab);
+void fft_etab_fill(int L, int N, float2 *etab);
 // Matched-filter spectrum [nfft] and phase table [rc_etab_size] for a layout (plan.cpp).
 void rc_tables_host(const sarbp_radar &r, const sarbp_rc_layout &lay, std::vector<float2> &filt,
                     std::vector<float2> &etab);
+// The same tables into caller buffers: work [nfft], filt [nfft], etab
+// [rc_etab_size] (the allocation-free entry point passes static arrays).
+void rc_tables_fill(const sarbp_radar &r, const sarbp_rc_layout &lay, std::complex<double> *work, float2 *filt,
+                    float2 *etab);
+// In-place unnormalised forward DFT of a power-of-two length N, FP64 (plan.cpp).
+void fft_pow2_inplace(std::complex<double> *x, int N);
 // Tile geometry the planner needs to size the staging window.
 void bp_tile_dims(int pix, int *tile_x, int *tile_y);
 // Dynamic shared memory of a BP CTA for a staging window and pulse chunk.

@@ -160,7 +160,7 @@ cudaError_t launch_echo_synth(const double *apc, int np, int ns, const sarbp_tar
 cudaError_t launch_echo_noise(float2 *echo, int64_t count, const double *power_acc, double snr_db,
                               uint64_t seed, cudaStream_t s) {
     if (count <= 0) return cudaSuccess;
-    const int blocks = (int)std::min<int64_t>((count + 255) / 256, 152 * 16);
+    const int blocks = (int)std::min<int64_t>((count + 255) / 256, (int64_t)current_sms() * 16);
     echo_noise_kernel<<<blocks, 256, 0, s>>>(echo, count, power_acc, snr_db, seed);
     return cudaGetLastError();
 }
@@ -169,7 +169,7 @@ cudaError_t launch_ref_echo(float2 *Srnm, const float *Ptarget, const float *ta,
                             const sarbp_ref_params &p, int Mslow, int Nfast, cudaStream_t s) {
     const int64_t total = (int64_t)Mslow * Nfast;
     if (total <= 0) return cudaSuccess;
-    const int blocks = (int)std::min<int64_t>((total + 255) / 256, 152 * 16);
+    const int blocks = (int)std::min<int64_t>((total + 255) / 256, (int64_t)current_sms() * 16);
     ref_echo_kernel<<<blocks, 256, 0, s>>>(Srnm, Ptarget, ta, tr, p, Mslow, Nfast);
     return cudaGetLastError();
 }

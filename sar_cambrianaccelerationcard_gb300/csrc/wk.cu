@@ -7,24 +7,31 @@
 // a P-tap sinc kernel (task/stolt.cc:324+) and 2-D IFFT.
 //
 // GPU design (data [Na][Nr] complex64 in HBM, ping-pong between two buffers):
-//   * 1-D DFTs run along rows, one CTA per row, in shared memory: the
+//   * 1-D DFTs along the rows, one CTA per row, in shared memory: the
 //     Stockham FFT of fft_smem.cuh for power-of-two lengths (<= 16384), and
 //     Bluestein's chirp-z form for other lengths n <= 8192: the row times the
 //     chirp conj(w), w_j = e^{j pi j^2 / n}, is convolved with w through one
 //     forward and one inverse power-of-two FFT of M >= 2n - 1 points held in
 //     the same shared memory, with the convolution kernel's spectrum
-//     precomputed in FP64 on the host.  Azimuth transforms run on transposed
-//     data (32 x 32-tile transposes through shared memory).
+//     precomputed in FP64 on the host.  The first range transform takes its
+//     input straight from the echo (zero padding and azimuth down-conversion
+//     fused into its load).
+//   * Azimuth transforms of power-of-two lengths 512..4096 run down the
+//     columns (dft_cols_kernel: 4 adjacent columns per CTA, whole 32-byte row
+//     segments, the columns' butterflies batched per stage); other lengths go
+//     through 32 x 32-tile transposes and the row transforms.
 //   * The reference-function multiply and the Stolt interpolation are one
-//     kernel per azimuth-frequency row: sqrt((f0+fr)^2 - c^2 fa^2 / (4 Vr^2))
-//     is evaluated once per sample in FP64 and gives both the phase
-//     theta = 4 pi R0 / c * root + pi fr^2 / kr (reduced modulo 2 pi in FP64,
-//     rotated in FP32) and the Stolt shift delta = (root - f0 - fr) Nr / Fr;
-//     the multiplied row is staged in shared memory and each output sums P
-//     taps at clip(floor(n - delta + k - P/2), 0, Nr - 1) weighted by
-//     sin(pi u) / (pi u), u = (n - delta) - tap, as the reference's gather /
-//     sinc / reduce chain does.  One sin per output: away from the row edges
-//     the taps' sines differ only in sign.
+//     kernel per azimuth-frequency row.  With P = f0 + fr, q = c^2 fa^2 /
+//     (4 Vr^2) and eps = q / P^2 <= 1e-2 (wk_stolt_ff_kernel), the phase
+//     theta = 4 pi R0 / c sqrt(P^2 - q) + pi fr^2 / kr is a per-column table
+//     reduced modulo 2 pi in FP64 on the host, minus a float-float term
+//     (ffloat.cuh) and an FP32 remainder, so no sample needs FP64; larger eps
+//     (wk_stolt_kernel) takes an FP64 square root per sample.  The Stolt shift
+//     is delta = (sqrt(P^2 - q) - P) Nr / Fr; the multiplied row is staged in
+//     shared memory and each output sums P taps at clip(floor(n - delta + k -
+//     P/2), 0, Nr - 1) weighted by sin(pi u) / (pi u), u = (n - delta) - tap, as
+//     the reference's gather / sinc / reduce chain does.  One sin per output:
+//     away from the row edges the taps' sines differ only in sign.
 #include <algorithm>
 
 #include "fft_smem.cuh"
@@ -445,7 +452,7 @@ __global__ void __launch_bounds__(256) wk_pad_kernel(const float2 *__restrict__ 
 cudaError_t launch_wk_pad(const float2 *echo, int na, int nr, const float2 *rowmul, int pa, int pr, int NA, int NR,
                           float2 *out, cudaStream_t s) {
     const long long total = (long long)NA * NR;
-    const int blocks = (int)std::min<long long>((total + 255) / 256, 152LL * 16);
+    const int blocks = (int)std::min<long long>((total + 255) / 256, (long long)current_sms() * 16);
     wk_pad_kernel<<<blocks, 256, 0, s>>>(echo, na, nr, rowmul, pa, pr, NA, NR, out);
     return cudaGetLastError();
 }

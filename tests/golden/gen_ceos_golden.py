@@ -5,7 +5,7 @@ code/data_process/CEOS/specify_parameters.m, CD_run_params.mat), taken from
 the reference's code/data_process/CEOS/AGC_attenuation_values.mat.  Run where
 the reference tree exists:
 
-    python tests/golden/gen_ceos_golden.py /root/reference
+    python tests/golden/gen_ceos_golden.py <reference checkout>
 """
 import os
 import sys
@@ -29,4 +29,7 @@ def main(ref_root: str):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    src = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("SARBP_REFERENCE_DIR")
+    if not src:
+        sys.exit(f"usage: {sys.argv[0]} <reference checkout> (or set SARBP_REFERENCE_DIR)")
+    main(src)

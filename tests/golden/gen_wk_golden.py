@@ -3,7 +3,7 @@ echo blocks (code/SAR_WK/wk_v5.2.3/data/CDdata1.mat, CDdata2.mat; 3072 x 2048)
 with the FP64 omega-K restatement (oracle/wk.py).  Run where the reference
 tree exists:
 
-    python tests/golden/gen_wk_golden.py /root/reference
+    python tests/golden/gen_wk_golden.py <reference checkout>
 
 Stores:
   echo      a 96 x 64 crop of the echo (rows 1500.., columns 1000..), complex64
@@ -43,4 +43,7 @@ def main(ref_root: str):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    src = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("SARBP_REFERENCE_DIR")
+    if not src:
+        sys.exit(f"usage: {sys.argv[0]} <reference checkout> (or set SARBP_REFERENCE_DIR)")
+    main(src)
