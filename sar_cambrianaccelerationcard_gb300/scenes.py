@@ -161,6 +161,21 @@ def random_targets(grid: Grid, n: int, seed: int, margin: float = 0.05) -> np.nd
     return np.column_stack([pos, amp]).astype(np.float64)
 
 
+def isolated_targets(grid: Grid, seed: int,
+                     fractions=((0.22, 0.26), (0.71, 0.21), (0.48, 0.52), (0.24, 0.77), (0.79, 0.74))) -> np.ndarray:
+    """Point targets far enough apart for point-target metrics (image
+    fractions of the grid, default five), each moved by a random sub-pixel
+    offset, with Rayleigh(sigma=1) amplitudes kept above 0.5."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for fx, fy in fractions:
+        x = fx * grid.nx + rng.uniform(-0.5, 0.5)
+        y = fy * grid.ny + rng.uniform(-0.5, 0.5)
+        pos = grid.origin + x * grid.ux + y * grid.uy
+        out.append((*pos, max(0.5, rng.rayleigh(1.0))))
+    return np.array(out, dtype=np.float64)
+
+
 def config1(np_: int = 512, ns: int = 1024, n_img: int = 512, spacing: float = 0.5,
             seed: int = 1, snr_db: float | None = 30.0) -> Scene:
     """Plain BP point-target scene: 512 pulses x 1024 samples, 3x3 targets

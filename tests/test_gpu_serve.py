@@ -181,3 +181,32 @@ def test_injected_admission_failure(jobs, monkeypatch):
             assert metrics.rel_l2_db(res[k][2], ref0) <= -100.0
         st = srv.stats()
         assert st.failed == 1 and st.completed == 2
+
+
+def test_served_jobs_match_the_oracle(orc):
+    """Served images against the FP64 CPU oracle directly (not only against the
+    one-shot path): two jobs of uneven size in one mix -- a config-1-sized
+    scene and a config-2-geometry tile with isolated targets -- each within
+    -60 dB of the oracle's image of the same echo, peaks within 0.05 pixel,
+    PSLR and ISLR within 0.1 dB, in split precision and FP16 storage."""
+    a = scenes.config1(np_=512, ns=1024, snr_db=20.0, seed=31)
+    b = scenes.config2(np_=768, n_img=256, seed=32)
+    b.targets = scenes.isolated_targets(b.grid, seed=33)
+    cases = []
+    for s in (a, b):
+        echo = orc.echo(s).astype(np.complex64)
+        ref = orc.image(s, echo.astype(np.complex128))
+        cases.append((s, echo, ref))
+    for mode in (sarbp.MODE_SPLIT, sarbp.MODE_FP16STORE):
+        with sarbp.Server(0, max_jobs=4, hbm_budget_bytes=8 << 30, pulses_per_step=128) as srv:
+            tickets = [submit(srv, s, e, mode) for (s, e, _) in cases]
+            results = [wait(srv, t) for t in tickets]
+            assert srv.stats().peak_active >= 1
+        for (s, _, ref), (st, _, img) in zip(cases, results):
+            assert st == sarbp.OK
+            err = metrics.rel_l2_db(img, ref)
+            cmp = metrics.compare_point_targets(img, ref, metrics.target_pixels(s))
+            print(s.name, mode, f"served vs oracle {err:.1f} dB, shift {cmp['peak_shift_px']:.4f} px, "
+                                f"PSLR {cmp['pslr_diff_db']:.4f} dB, ISLR {cmp['islr_diff_db']:.4f} dB")
+            assert err <= -60.0
+            assert cmp["peak_shift_px"] <= 0.05 and cmp["pslr_diff_db"] <= 0.1 and cmp["islr_diff_db"] <= 0.1
