@@ -518,6 +518,10 @@ class Context:
     def synchronize(self):
         self.check(self.lib.sarbp_synchronize(self.h), "synchronize")
 
+    def trim(self):
+        """Release the context's cached device buffers."""
+        self.check(self.lib.sarbp_trim(self.h), "trim")
+
     def timings(self):
         a, b = ctypes.c_float(), ctypes.c_float()
         self.check(self.lib.sarbp_last_timings(self.h, ctypes.byref(a), ctypes.byref(b)), "timings")
