@@ -37,18 +37,22 @@ sys.path.insert(0, ROOT)
 # and 3 MUFU operations (a square-root-class op, sin, cos).
 FP32_OPS_PER_UPDATE = 19
 MUFU_OPS_PER_UPDATE = 3
-# DRAM bytes (read + write) per launch measured by ncu (dram__bytes_read.sum +
-# dram__bytes_write.sum, one-pass capture of the full-size launch) on GB300 for
-# the default workload (4096 pulses x 8192 samples -> 4096^2, complex64 rows).
-# BP: 236.3 MB read + 115.6 MB written (part of the image is still in L2 when
-# the launch ends); the algorithmic bytes are each pulse's swath bins once
-# (227.9 MB) plus the image (134.2 MB).
-# Range compression (two 2048-pulse batches of forward + inverse): 2 x
-# (134.6 + 208.4 + 268.6 + 1014.2) MB.
+# DRAM bytes (read + write) and L2 bytes (lts__t_bytes.sum) per call, measured by
+# ncu on GB300 for the default workload (4096 pulses x 8192 samples -> 4096^2,
+# complex64 rows): profiles/traffic_bp_rc_config2.md (captured 2026-12-04, one-pass
+# full-size captures of bp_kernel<2,0,3,0,8,0,16,0>, rc_forward_kernel<16384,1024>
+# and rc_inverse_kernel<16384,1024,0>).  Back-projection: one launch; range
+# compression: two batches of forward + inverse.
 MEASURED_TRAFFIC = {
-    ("full", "split"): {"bp": 236301312 + 115647232,
-                        "rc": 2 * (134575872 + 208381184 + 268595200 + 1014241280)},
+    ("full", "split"): {"bp": 234726656 + 115588864,
+                        "rc": (134388736 + 209891072 + 269426176 + 1013657600) +
+                              (134387200 + 207002880 + 268637440 + 1013731584)},
 }
+L2_TRAFFIC = {
+    ("full", "split"): {"bp": 25964478848, "rc": 802581504 + 8414586688 + 804555200 + 8421029760},
+}
+# ncu's L2 peak for these launches: lts__t_bytes.sum / duration / pct_of_peak (same file)
+L2_PEAK_GBS = 25964478848 / 53.124512e-3 / 0.0134 / 1e9
 
 
 def parse():
@@ -454,6 +458,12 @@ def run_ours(args):
     hbm = None
     if os.path.exists(peaks_path):
         hbm = json.load(open(peaks_path)).get("hbm_gbs")
+    l2 = L2_TRAFFIC.get((args.size, args.mode), {})
+    if bp_ms_each and l2.get("bp"):
+        # L2 bytes of the profiled launch over this run's launch time, against ncu's L2 peak
+        bw = l2["bp"] / (bp_ms_each * 1e-3) / 1e9
+        roofline["l2"] = {"achieved": bw, "peak": L2_PEAK_GBS, "unit": "GB/s", "frac": bw / L2_PEAK_GBS,
+                          "traffic": l2["bp"], "source": "profiles/traffic_bp_rc_config2.md"}
     if bp_ms_each and hbm:
         # the same launch against HBM (of measured): algorithmic bytes / launch time
         bw = bp_alg_bytes / (bp_ms_each * 1e-3) / 1e9
@@ -464,6 +474,10 @@ def run_ours(args):
                    "unit": "GB/s", "frac": (rc_bytes / (rc_ms * 1e-3) / 1e9 / hbm) if (rc_ms and hbm) else None,
                    "traffic": MEASURED_TRAFFIC.get((args.size, args.mode), {}).get("rc"),
                    "kernel": "rc_forward + rc_inverse", "ms": rc_ms}
+    if rc_ms and l2.get("rc"):
+        bw = l2["rc"] / (rc_ms * 1e-3) / 1e9
+        roofline_rc["l2"] = {"achieved": bw, "peak": L2_PEAK_GBS, "unit": "GB/s", "frac": bw / L2_PEAK_GBS,
+                             "traffic": l2["rc"], "source": "profiles/traffic_bp_rc_config2.md"}
     # the transforms themselves: 1 forward + L inverse nfft-point FFTs per pulse at
     # 5 N log2 N flops each, against the live FP32 FMA rate (2 flops per lane)
     fft_flops = scene.np_ * (1 + scene.radar.upsample) * 5.0 * lay.nfft * math.log2(lay.nfft)
