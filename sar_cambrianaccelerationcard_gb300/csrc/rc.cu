@@ -270,17 +270,31 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(T)
 #ifndef SARBP_RC_SPLIT_MIN
 #define SARBP_RC_SPLIT_MIN 32768
 #endif
+// CTA sizes (threads) per transform length, measured on GB300 (ms for 4096
+// pulses, forward + eight inverse transforms each): 8192 points at 512 threads
+// (64 KB of points, two CTAs per SM) 1.295 against 1.886 at 1024 threads (one
+// CTA per SM: a CTA's barriers are then overlapped by nothing); 16384 points
+// (128 KB, one CTA per SM either way) 3.075 at 1024 against 3.12 at 512; the
+// 16384-point halves of the 32768-point split path 4.29 at 512 against 4.35
+// at 1024 (2048 pulses).
 #ifndef SARBP_RC_8K_THREADS
-#define SARBP_RC_8K_THREADS 1024
+#define SARBP_RC_8K_THREADS 512
 #endif
 #ifndef SARBP_RC_BIG_THREADS
 #define SARBP_RC_BIG_THREADS 1024
+#endif
+#ifndef SARBP_RC_HALF_THREADS
+#define SARBP_RC_HALF_THREADS 512
 #endif
 template <int N>
 constexpr int threads_for() {
     return N >= 16384 ? SARBP_RC_BIG_THREADS : (N >= 8192 ? SARBP_RC_8K_THREADS : (N >= 4096 ? 512 : (N >= 512 ? N / 8 : 64)));
 }
-
+// the half-size transforms of the split path (two CTAs / a 2-CTA cluster per transform)
+template <int M>
+constexpr int threads_for_half() {
+    return M >= 16384 ? SARBP_RC_HALF_THREADS : threads_for<M>();
+}
 
 // With t_prepare set the launchers below configure their kernel and return
 // without launching it (prepare_rc_kernels).
@@ -321,7 +335,7 @@ cudaError_t inv_n(const RcPlan &p, const float2 *spec, const float2 *etab, const
 template <int M>
 cudaError_t fwd2(const RcPlan &p, const float2 *echo, const float2 *filt, const float2 *etab, float2 *spec,
                  float *bound2, cudaStream_t s) {
-    constexpr int T = threads_for<M>();
+    constexpr int T = threads_for_half<M>();
     const size_t smem = sizeof(float2) * M + kTabSmem;
     auto k = rc_forward2_kernel<M, T>;
     cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
@@ -333,7 +347,7 @@ cudaError_t fwd2(const RcPlan &p, const float2 *echo, const float2 *filt, const 
 template <int M>
 cudaError_t inv2(const RcPlan &p, const float2 *spec, const float2 *etab, const float *bound2, float *scale,
                  void *out, cudaStream_t s) {
-    constexpr int T = threads_for<M>();
+    constexpr int T = threads_for_half<M>();
     const size_t smem = sizeof(float2) * M + kTabSmem;
     cudaError_t e;
     if (p.storage == SARBP_STORE_C64) {
