@@ -680,6 +680,12 @@ def serve_sweep(reqs, rates, jobs, schedules):
                     "mean_ms": sum(lat) / len(lat) if lat else None,
                     "gpix_pulse_s": upd / (t_last - t_first) / 1e9,
                     "busy_gpix_pulse_s": stats.updates / max(stats.busy_s, 1e-9) / 1e9,
+                    # where the busy time went (device time from CUDA events): the steps'
+                    # back-projection and the admissions' upload + range compression,
+                    # which run beside the steps on their own stream
+                    "busy_s": stats.busy_s, "step_device_s": stats.step_device_s,
+                    "admit_device_s": stats.admit_device_s,
+                    "bp_in_steps_gpix_pulse_s": stats.updates / max(stats.step_device_s, 1e-9) / 1e9,
                     "peak_active": stats.peak_active, "graph_launches": stats.graph_launches,
                     "peak_gb": stats.peak_bytes / 2**30, "clocks": clk})
     return out

@@ -432,6 +432,8 @@ typedef struct sarbp_server_stats {
     double busy_s;           /* wall time with at least one job admitted */
     uint64_t bytes_in_use, peak_bytes;
     int32_t active, queued, peak_active, reserved;
+    double step_device_s;    /* device time of the back-projection steps (CUDA events around each step) */
+    double admit_device_s;   /* device time of admissions: echo and APC upload, range compression */
 } sarbp_server_stats;
 
 sarbp_status sarbp_server_create(sarbp_server **out, const sarbp_server_config *cfg);

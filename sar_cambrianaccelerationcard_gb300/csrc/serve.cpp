@@ -10,9 +10,10 @@
 //   * admission (worker): in arrival order, every queued job that fits the
 //     free budget and a free slot is admitted -- on an admission stream that
 //     runs beside the steps, device buffers come from the stream-ordered pool,
-//     the echo and APC track are uploaded and the echo is range-compressed
-//     into the job's resident buffer; the job joins the steps once that work
-//     has completed;
+//     the APC track is uploaded, the echo goes up in pulse chunks on a copy
+//     stream and each chunk is range-compressed into the job's resident buffer
+//     as soon as it lands; the job joins the steps once that work has
+//     completed;
 //   * steps (worker): each step back-projects the next pulses of every
 //     admitted job into its resident image (accumulate after the first step):
 //     pulses_per_step for every job, or with step_updates set a per-job count
@@ -92,6 +93,7 @@ struct Job {
     int steps = 0;
     cudaEvent_t done_ev = nullptr;
     cudaEvent_t ready_ev = nullptr;  // echo uploaded and range-compressed
+    cudaEvent_t admit_ev = nullptr;  // start of the admission work (timing)
     JobState state = JobState::Queued;
     sarbp_status status = SARBP_OK;
     std::string msg;
@@ -119,10 +121,13 @@ struct sarbp_server {
     cudaStream_t s0 = nullptr;            // back-projection steps (graphs)
     cudaStream_t sa = nullptr;            // admission: allocation, upload, range compression
     cudaStream_t sd = nullptr;            // image downloads and frees
+    cudaStream_t sc = nullptr;            // admission echo uploads, in pulse chunks
+    cudaEvent_t chunk_ev = nullptr;       // a chunk's upload (re-recorded per chunk: each wait takes the latest)
     std::vector<cudaStream_t> lanes;
     std::vector<cudaEvent_t> join;        // one per lane
     cudaEvent_t fork = nullptr;
-    cudaEvent_t step_ev[2] = {nullptr, nullptr};
+    cudaEvent_t step_ev[2] = {nullptr, nullptr};   // end of a step (timing)
+    cudaEvent_t step_t0[2] = {nullptr, nullptr};   // start of a step (timing)
     int step_parity = 0;
     bool step_pending[2] = {false, false};
     cudaGraphExec_t exec = nullptr;
@@ -173,6 +178,7 @@ sarbp_status admit(sarbp_server *S, Job *j) {
         cudaGetLastError();
         return SARBP_ERR_OUT_OF_MEMORY;
     }
+    cudaEventRecord(j->admit_ev, S->sa);
     const size_t np = j->desc.np, ns = j->desc.ns, nb = j->lay.nbins;
     const size_t npix = (size_t)j->desc.grid.nx * j->desc.grid.ny;
     unsigned char *p = j->dev;
@@ -191,7 +197,12 @@ sarbp_status admit(sarbp_server *S, Job *j) {
     j->d_filt = (float2 *)take(j->tab->filt.size() * 8);
     j->d_etab = (float2 *)take(j->tab->etab.size() * 8);
     j->d_err = (unsigned *)take(sizeof(unsigned));
-    e = cudaMemcpyAsync(j->d_echo, j->desc.echo, np * ns * 8, cudaMemcpyHostToDevice, S->sa);
+    // The echo goes up in chunks of spec_rows pulses on the copy stream, and each
+    // chunk is range-compressed on the admission stream as soon as it lands, so
+    // only the first chunk's upload is exposed.  The copy stream first waits for
+    // the admission stream (the allocation above, and earlier admissions).
+    e = cudaEventRecord(S->chunk_ev, S->sa);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(S->sc, S->chunk_ev, 0);
     if (e == cudaSuccess) e = cudaMemcpyAsync(j->d_apc, j->desc.apc, np * 24, cudaMemcpyHostToDevice, S->sa);
     if (e == cudaSuccess)
         e = cudaMemcpyAsync(j->d_filt, j->tab->filt.data(), j->tab->filt.size() * 8, cudaMemcpyHostToDevice, S->sa);
@@ -199,6 +210,12 @@ sarbp_status admit(sarbp_server *S, Job *j) {
         e = cudaMemcpyAsync(j->d_etab, j->tab->etab.data(), j->tab->etab.size() * 8, cudaMemcpyHostToDevice, S->sa);
     if (e == cudaSuccess) e = cudaMemsetAsync(j->d_err, 0, sizeof(unsigned), S->sa);
     for (size_t p0 = 0; e == cudaSuccess && p0 < np; p0 += S->spec_rows) {
+        const size_t rows = std::min(S->spec_rows, np - p0);
+        e = cudaMemcpyAsync(j->d_echo + p0 * ns, reinterpret_cast<const float2 *>(j->desc.echo) + p0 * ns,
+                            rows * ns * 8, cudaMemcpyHostToDevice, S->sc);
+        if (e == cudaSuccess) e = cudaEventRecord(S->chunk_ev, S->sc);
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(S->sa, S->chunk_ev, 0);
+        if (e != cudaSuccess) break;
         sarbp::RcPlan rp{};
         rp.bound2 = S->d_bound2;
         rp.np = (int)std::min(S->spec_rows, np - p0);
@@ -215,6 +232,10 @@ sarbp_status admit(sarbp_server *S, Job *j) {
     }
     if (e == cudaSuccess) e = cudaEventRecord(j->ready_ev, S->sa);
     if (e != cudaSuccess) {
+        cudaGetLastError();
+        // chunk copies may still be reading the caller's echo and writing the
+        // job's buffer, which the caller frees next: let them finish first
+        cudaStreamSynchronize(S->sc);
         cudaGetLastError();
         return SARBP_ERR_CUDA;
     }
@@ -248,6 +269,15 @@ void release(sarbp_server *S, Job *j) {
     if (j->lane >= 0) j->lane = -1;
 }
 
+// Device time of step `par` once it has completed (caller holds S->mu).
+void fold_step(sarbp_server *S, int par) {
+    if (!S->step_pending[par] || cudaEventQuery(S->step_ev[par]) != cudaSuccess) return;
+    float ms = 0.f;
+    if (cudaEventElapsedTime(&ms, S->step_t0[par], S->step_ev[par]) == cudaSuccess) S->st.step_device_s += ms * 1e-3;
+    cudaGetLastError();
+    S->step_pending[par] = false;
+}
+
 void worker_main(sarbp_server *S) {
     cudaSetDevice(S->cfg.device);
     std::vector<bool> lane_busy(S->cfg.max_jobs, false);
@@ -275,7 +305,14 @@ void worker_main(sarbp_server *S) {
             }
         }
         for (Job *j : S->active)
-            if (j->state == JobState::Loading && cudaEventQuery(j->ready_ev) == cudaSuccess) j->state = JobState::Active;
+            if (j->state == JobState::Loading && cudaEventQuery(j->ready_ev) == cudaSuccess) {
+                j->state = JobState::Active;
+                float ms = 0.f;
+                if (cudaEventElapsedTime(&ms, j->admit_ev, j->ready_ev) == cudaSuccess) S->st.admit_device_s += ms * 1e-3;
+                cudaGetLastError();
+            }
+        fold_step(S, 0);
+        fold_step(S, 1);
         if (S->active.empty() && S->busy) {
             S->st.busy_s += std::chrono::duration<double>(Clock::now() - S->busy_since).count();
             S->busy = false;
@@ -324,12 +361,12 @@ void worker_main(sarbp_server *S) {
                 lk.unlock();
                 cudaEventSynchronize(S->step_ev[par]);
                 lk.lock();
-                S->step_pending[par] = false;
+                fold_step(S, par);
             }
-            cudaError_t e = cudaSuccess;
+            cudaError_t e = cudaEventRecord(S->step_t0[par], S->s0);
             const bool graph = S->cfg.use_graphs != 0;
             cudaGraph_t g = nullptr;
-            if (graph) e = cudaStreamBeginCapture(S->s0, cudaStreamCaptureModeRelaxed);
+            if (graph && e == cudaSuccess) e = cudaStreamBeginCapture(S->s0, cudaStreamCaptureModeRelaxed);
             if (e == cudaSuccess) e = cudaEventRecord(S->fork, S->s0);
             for (Job *j : step) {
                 if (e != cudaSuccess) break;
@@ -457,8 +494,10 @@ sarbp_status sarbp_server_create(sarbp_server **out, const sarbp_server_config *
              cudaEventCreateWithFlags(&S->join[i], cudaEventDisableTiming) == cudaSuccess;
     }
     ok = ok && cudaEventCreateWithFlags(&S->fork, cudaEventDisableTiming) == cudaSuccess &&
-         cudaEventCreateWithFlags(&S->step_ev[0], cudaEventDisableTiming) == cudaSuccess &&
-         cudaEventCreateWithFlags(&S->step_ev[1], cudaEventDisableTiming) == cudaSuccess;
+         cudaEventCreate(&S->step_ev[0]) == cudaSuccess && cudaEventCreate(&S->step_ev[1]) == cudaSuccess &&
+         cudaEventCreate(&S->step_t0[0]) == cudaSuccess && cudaEventCreate(&S->step_t0[1]) == cudaSuccess;
+    ok = ok && cudaStreamCreateWithFlags(&S->sc, cudaStreamNonBlocking) == cudaSuccess &&
+         cudaEventCreateWithFlags(&S->chunk_ev, cudaEventDisableTiming) == cudaSuccess;
     S->spec_rows = kSpecRows;
     ok = ok && cudaMalloc(&S->d_spec, sizeof(float2) * kSpecRows * kMaxN + sizeof(float) * 2 * kSpecRows) == cudaSuccess;
     if (ok) S->d_bound2 = reinterpret_cast<float *>(S->d_spec + kSpecRows * kMaxN);
@@ -494,12 +533,13 @@ sarbp_status sarbp_server_destroy(sarbp_server *S) {
     S->cv_work.notify_all();
     if (S->worker.joinable()) S->worker.join();
     cudaSetDevice(S->cfg.device);
-    for (cudaStream_t st : {S->sa, S->s0, S->sd})
+    for (cudaStream_t st : {S->sc, S->sa, S->s0, S->sd})
         if (st) cudaStreamSynchronize(st);
     for (auto &kv : S->jobs) {
         Job *j = kv.second;
         if (j->done_ev) cudaEventDestroy(j->done_ev);
         if (j->ready_ev) cudaEventDestroy(j->ready_ev);
+        if (j->admit_ev) cudaEventDestroy(j->admit_ev);
         if (j->h_err) cudaFreeHost(j->h_err);
         delete j;
     }
@@ -512,8 +552,11 @@ sarbp_status sarbp_server_destroy(sarbp_server *S) {
     if (S->fork) cudaEventDestroy(S->fork);
     for (cudaEvent_t e : S->step_ev)
         if (e) cudaEventDestroy(e);
-    for (cudaStream_t st : {S->s0, S->sa, S->sd})
+    for (cudaEvent_t e : S->step_t0)
+        if (e) cudaEventDestroy(e);
+    for (cudaStream_t st : {S->s0, S->sa, S->sd, S->sc})
         if (st) cudaStreamDestroy(st);
+    if (S->chunk_ev) cudaEventDestroy(S->chunk_ev);
     delete S;
     return SARBP_OK;
 }
@@ -592,11 +635,12 @@ sarbp_status sarbp_server_submit(sarbp_server *S, const sarbp_job *job, uint64_t
     }
     cudaSetDevice(S->cfg.device);
     if (cudaEventCreateWithFlags(&j->done_ev, cudaEventDisableTiming) != cudaSuccess ||
-        cudaEventCreateWithFlags(&j->ready_ev, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreate(&j->ready_ev) != cudaSuccess || cudaEventCreate(&j->admit_ev) != cudaSuccess ||
         cudaMallocHost(&j->h_err, sizeof(unsigned)) != cudaSuccess) {
         cudaGetLastError();
         if (j->done_ev) cudaEventDestroy(j->done_ev);
         if (j->ready_ev) cudaEventDestroy(j->ready_ev);
+        if (j->admit_ev) cudaEventDestroy(j->admit_ev);
         delete j;
         return SARBP_ERR_CUDA;
     }
@@ -607,6 +651,7 @@ sarbp_status sarbp_server_submit(sarbp_server *S, const sarbp_job *job, uint64_t
         if (S->stop) {
             cudaEventDestroy(j->done_ev);
             cudaEventDestroy(j->ready_ev);
+            cudaEventDestroy(j->admit_ev);
             cudaFreeHost(j->h_err);
             delete j;
             return SARBP_ERR_CANCELLED;
@@ -663,6 +708,7 @@ sarbp_status sarbp_server_wait(sarbp_server *S, uint64_t ticket, int32_t timeout
     lk.unlock();
     if (j->done_ev) cudaEventDestroy(j->done_ev);
     if (j->ready_ev) cudaEventDestroy(j->ready_ev);
+    if (j->admit_ev) cudaEventDestroy(j->admit_ev);
     if (j->h_err) cudaFreeHost(j->h_err);
     delete j;
     return st;
@@ -686,6 +732,8 @@ sarbp_status sarbp_server_cancel(sarbp_server *S, uint64_t ticket) {
 sarbp_status sarbp_server_get_stats(sarbp_server *S, sarbp_server_stats *out) {
     if (!S || !out) return SARBP_ERR_INVALID_ARGUMENT;
     std::lock_guard<std::mutex> lk(S->mu);
+    fold_step(S, 0);
+    fold_step(S, 1);
     *out = S->st;
     out->bytes_in_use = S->in_use;
     out->active = (int32_t)S->active.size();

@@ -136,7 +136,8 @@ class ServerStats(ctypes.Structure):
                                                "steps", "graph_launches")] + \
                [("updates", ctypes.c_double), ("busy_s", ctypes.c_double), ("bytes_in_use", ctypes.c_uint64),
                 ("peak_bytes", ctypes.c_uint64), ("active", ctypes.c_int32), ("queued", ctypes.c_int32),
-                ("peak_active", ctypes.c_int32), ("reserved", ctypes.c_int32)]
+                ("peak_active", ctypes.c_int32), ("reserved", ctypes.c_int32),
+                ("step_device_s", ctypes.c_double), ("admit_device_s", ctypes.c_double)]
 
 
 class RefParams(ctypes.Structure):

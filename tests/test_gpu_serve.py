@@ -65,6 +65,9 @@ def test_alone_equals_in_mix(jobs):
         stat = srv.stats()
         assert stat.peak_active >= 2, "jobs overlapped on the device"
         assert stat.graph_launches > 0
+        # device time is accounted per step and per admission (CUDA events)
+        assert stat.step_device_s > 0 and stat.admit_device_s > 0
+        assert stat.step_device_s <= stat.busy_s * 1.05
     assert np.array_equal(alone, mixed)
     assert metrics.rel_l2_db(alone, one_shot) <= -100.0
     # every job in the mix matches its one-shot image
