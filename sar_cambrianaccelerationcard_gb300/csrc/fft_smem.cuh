@@ -1,8 +1,8 @@
 // fft_smem.cuh -- shared-memory Stockham FFT used by range compression
 // (rc.cu) and the omega-K imager (wk.cu).
 //
-// Stockham autosort transform with radix-8 stages (one radix-4 or radix-2
-// stage when log2 N is not a multiple of 3), in place in shared memory
+// Stockham autosort transform with radix-32, radix-16 and radix-8 stages (one
+// radix-4 or radix-2 stage for the remaining factor), in place in shared memory
 // (XOR-swizzled so every stage's accesses are free of bank conflicts) with a
 // barrier between each stage's loads and stores.  Twiddles come from two-level
 // tables held in shared memory (see Etab / load_etab).
@@ -197,6 +197,61 @@ struct Dft<16, INV> {
     }
 };
 
+// x W32^e for the chosen direction, e a compile-time constant (odd e; the even
+// ones are W16 powers).
+template <int E, bool INV>
+__device__ __forceinline__ float2 tw32(float2 x) {
+    constexpr int e = E & 31;
+    if constexpr ((e & 1) == 0) {
+        return tw16<e / 2, INV>(x);
+    } else {
+        // cos and sin of 2 pi e / 32 for the odd e (first quadrant values, then signs)
+        constexpr float kC[8] = {0.98078528040323044913f, 0.83146961230254523708f, 0.55557023301960222474f,
+                                 0.19509032201612826785f, -0.19509032201612826785f, -0.55557023301960222474f,
+                                 -0.83146961230254523708f, -0.98078528040323044913f};
+        // e = 2 i + 1: cos(2 pi e/32) = kC[i] for e < 16; e >= 16: cos(2 pi e/32) = -cos(2 pi (e-16)/32)
+        constexpr int i = (e & 15) >> 1;
+        constexpr float c0 = kC[i];
+        // sin(2 pi e/32) = cos(2 pi (e - 8)/32): e - 8 is odd and in [-7, 7] for e < 16
+        constexpr int es = (e & 15) - 8;  // odd, -7..7
+        constexpr float s0 = es >= 0 ? kC[es >> 1] : kC[(-es) >> 1];  // cos is even
+        constexpr float c = e >= 16 ? -c0 : c0, sn = e >= 16 ? -s0 : s0;
+        const float si = INV ? sn : -sn;
+        return make_float2(fmaf(x.x, c, -x.y * si), fmaf(x.x, si, x.y * c));
+    }
+}
+
+template <int... K>
+struct Seq {};
+
+// Radix-32 DFT as 2 x 16 (decimation in time): X[k] = E[k] + W32^k O[k],
+// X[k + 16] = E[k] - W32^k O[k], E and O the 16-point DFTs of the even and
+// odd points.
+template <bool INV>
+struct Dft<32, INV> {
+    template <int K>
+    __device__ __forceinline__ static void out(float2 *v, const float2 *e, const float2 *o) {
+        const float2 t = tw32<K, INV>(o[K]);
+        v[K] = cadd(e[K], t);
+        v[K + 16] = csub(e[K], t);
+    }
+    template <int... K>
+    __device__ __forceinline__ static void outs(float2 *v, const float2 *e, const float2 *o, Seq<K...>) {
+        (out<K>(v, e, o), ...);
+    }
+    __device__ __forceinline__ static void run(float2 *v) {
+        float2 e[16], o[16];
+#pragma unroll
+        for (int i = 0; i < 16; ++i) {
+            e[i] = v[2 * i];
+            o[i] = v[2 * i + 1];
+        }
+        Dft<16, INV>::run(e);
+        Dft<16, INV>::run(o);
+        outs(v, e, o, Seq<0, 1, 2, 3, 4, 5, 6, 7, 8, 9, 10, 11, 12, 13, 14, 15>{});
+    }
+};
+
 // Radix-16 stage twiddles W^{m r}, r = 1..15, applied to v[1..15] as products
 // of the four table powers w, w^2, w^4, w^8 (at most four factors), so only
 // the powers and four partial products are live.
@@ -236,6 +291,27 @@ __device__ __forceinline__ void tw16_apply(float2 *v, const Tw16 &t) {
     v[13] = cmul(v[13], cmul(w5, t.b8));
     v[14] = cmul(v[14], cmul(w6, t.b8));
     v[15] = cmul(v[15], cmul(w7, t.b8));
+}
+
+// Radix-32 stage twiddles: v[r] W^{m r}, r = 1..31, as v[16 + r] times w^16
+// and then the radix-16 pattern on both halves.
+struct Tw32 {
+    Tw16 t16;
+    float2 b16;
+};
+template <bool INV, bool HOISTED_LO>
+__device__ __forceinline__ Tw32 tw32_bases(const Etab &E, int m, const float2 *lo) {
+    Tw32 t;
+    t.t16 = tw16_bases<INV, HOISTED_LO>(E, m, lo);
+    t.b16 = HOISTED_LO ? cmul(E.whi[(16 * m) >> 7], lo[4]) : E.w(16 * m);
+    if (!INV) t.b16.y = -t.b16.y;
+    return t;
+}
+__device__ __forceinline__ void tw32_apply(float2 *v, const Tw32 &t) {
+#pragma unroll
+    for (int r = 16; r < 32; ++r) v[r] = cmul(v[r], t.b16);
+    tw16_apply(v, t.t16);
+    tw16_apply(v + 16, t.t16);
 }
 
 // Twiddles W^{m r}, r = 1..R-1 (forward: conjugated) for a butterfly whose
@@ -302,15 +378,18 @@ __device__ __forceinline__ void stage(float2 *s, const Etab &E, Sink sink = Sink
     if constexpr (kToSmem) __syncthreads();  // loads done before the in-place stores
     float2 w[R <= 8 ? R : 1];
     Tw16 t16;
+    Tw32 t32;
     constexpr bool kSameK = Ns > 1 && T % Ns == 0;
     // k = j when Ns >= NB (last stage); the low table level is then fixed per thread
     // (batched: also across the wrap from one array to the next)
     constexpr bool kHoistLo = Ns > 1 && !kSameK && Ns >= NB && N >= kWlo && (C * T) % kWlo == 0 &&
                               (BATCH == 1 || (C * NB) % kWlo == 0);
     float2 lo1 = make_float2(1.f, 0.f), lo2 = lo1, lo4 = lo1;
-    float2 lo[4] = {lo1, lo1, lo1, lo1};
+    float2 lo[5] = {lo1, lo1, lo1, lo1, lo1};
     if constexpr (kSameK) {
-        if constexpr (R == 16)
+        if constexpr (R == 32)
+            t32 = tw32_bases<INV, false>(E, C * (int)(threadIdx.x & (Ns - 1)), lo);
+        else if constexpr (R == 16)
             t16 = tw16_bases<INV, false>(E, C * (int)(threadIdx.x & (Ns - 1)), lo);
         else
             twiddles<R, INV, false>(E, C * (int)(threadIdx.x & (Ns - 1)), lo1, lo2, lo4, w);
@@ -319,12 +398,13 @@ __device__ __forceinline__ void stage(float2 *s, const Etab &E, Sink sink = Sink
         lo1 = E.wlo[m & (kWlo - 1)];
         if (R >= 4) lo2 = E.wlo[(2 * m) & (kWlo - 1)];
         if (R >= 8) lo4 = E.wlo[(4 * m) & (kWlo - 1)];
-        if constexpr (R == 16) {
+        if constexpr (R >= 16) {
             lo[0] = lo1;
             lo[1] = lo2;
             lo[2] = lo4;
             lo[3] = E.wlo[(8 * m) & (kWlo - 1)];
         }
+        if constexpr (R == 32) lo[4] = E.wlo[(16 * m) & (kWlo - 1)];
     }
 #pragma unroll
     for (int b = 0; b < PER; ++b) {
@@ -335,7 +415,10 @@ __device__ __forceinline__ void stage(float2 *s, const Etab &E, Sink sink = Sink
             float2 *sc = s + col * CS;
             const int k = j & (Ns - 1);
             if constexpr (Ns > 1) {
-                if constexpr (R == 16) {
+                if constexpr (R == 32) {
+                    if constexpr (!kSameK) t32 = tw32_bases<INV, kHoistLo>(E, C * k, lo);
+                    tw32_apply(v[b], t32);
+                } else if constexpr (R == 16) {
                     if constexpr (!kSameK) t16 = tw16_bases<INV, kHoistLo>(E, C * k, lo);
                     tw16_apply(v[b], t16);
                 } else {
@@ -365,13 +448,26 @@ __device__ __forceinline__ void stage(float2 *s, const Etab &E, Sink sink = Sink
 #ifndef SARBP_FFT_RADIX16
 #define SARBP_FFT_RADIX16 1
 #endif
+// radix-32 stages where every thread holds at least one 32-point butterfly
+// (N / 32 >= T: transforms with at least 32 points per thread): two
+// shared-memory passes instead of three for 16384 points at 512 threads
+// (32-32-16) and 8192 at 256 (32-32-8).  Range compression on GB300, 4096
+// pulses: 16384 points 3.077 -> 2.986 ms, 8192 points 1.295 -> 1.123 ms; 32768
+// (2048 pulses) 4.289 -> 4.170 ms.  Shapes with fewer points per thread (the
+// omega-K transforms) keep their radix-16/8 stages.
+#ifndef SARBP_FFT_RADIX32
+#define SARBP_FFT_RADIX32 1
+#endif
 // radix-16 stages while 16 * Ns <= N and the stage keeps all T threads busy
 // (N / 16 >= T), then radix-8 stages while 8 * Ns <= N, then one radix-4 or
 // radix-2 stage
 template <int N, int T, bool INV, int Ns>
 struct Stages {
     __device__ __forceinline__ static void run(float2 *s, const Etab &E) {
-        if constexpr (SARBP_FFT_RADIX16 && Ns * 16 <= N && N / 16 >= T) {
+        if constexpr (SARBP_FFT_RADIX32 && Ns * 32 <= N && N / 32 >= T) {
+            stage<N, 32, T, INV, Ns>(s, E);
+            Stages<N, T, INV, Ns * 32>::run(s, E);
+        } else if constexpr (SARBP_FFT_RADIX16 && Ns * 16 <= N && N / 16 >= T) {
             stage<N, 16, T, INV, Ns>(s, E);
             Stages<N, T, INV, Ns * 16>::run(s, E);
         } else if constexpr (Ns * 8 <= N) {
@@ -397,7 +493,10 @@ __device__ void fft_smem(float2 *s, const Etab &E) {
 template <int N, int T, bool INV, int Ns, int BATCH, int CS>
 struct StagesBatched {
     __device__ __forceinline__ static void run(float2 *s, const Etab &E) {
-        if constexpr (SARBP_FFT_RADIX16 && Ns * 16 <= N && N / 16 >= T) {
+        if constexpr (SARBP_FFT_RADIX32 && Ns * 32 <= N && N / 32 >= T) {
+            stage<N, 32, T, INV, Ns, SmemSink, BATCH, CS>(s, E);
+            StagesBatched<N, T, INV, Ns * 32, BATCH, CS>::run(s, E);
+        } else if constexpr (SARBP_FFT_RADIX16 && Ns * 16 <= N && N / 16 >= T) {
             stage<N, 16, T, INV, Ns, SmemSink, BATCH, CS>(s, E);
             StagesBatched<N, T, INV, Ns * 16, BATCH, CS>::run(s, E);
         } else if constexpr (Ns * 8 <= N) {
@@ -414,7 +513,9 @@ struct StagesBatched {
 // Radix of the stage with stride Ns (the same sequence as Stages).
 template <int N, int T, int Ns>
 __host__ __device__ constexpr int stage_radix() {
-    return (SARBP_FFT_RADIX16 && Ns * 16 <= N && N / 16 >= T) ? 16 : (Ns * 8 <= N ? 8 : N / Ns);
+    return (SARBP_FFT_RADIX32 && Ns * 32 <= N && N / 32 >= T)   ? 32
+           : (SARBP_FFT_RADIX16 && Ns * 16 <= N && N / 16 >= T) ? 16
+           : (Ns * 8 <= N ? 8 : N / Ns);
 }
 
 // I/O-fused transform.  The first stage (stride 1) takes its inputs from

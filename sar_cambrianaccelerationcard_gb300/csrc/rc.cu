@@ -15,8 +15,8 @@
 //               (kappa = signed frequency), so each CTA runs one N-point
 //               inverse FFT and writes every L-th output bin.
 //
-// The FFT is a Stockham autosort transform with radix-8 stages (one radix-4
-// or radix-2 stage when log2 N is not a multiple of 3), in place in shared
+// The FFT is a Stockham autosort transform with radix-32/16/8 stages (one
+// radix-4 or radix-2 stage for the remaining factor), in place in shared
 // memory (XOR-swizzled so every stage's accesses are free of bank conflicts)
 // with a barrier between each stage's loads and stores.  The upsampling ramp
 // is a power of E = e^{j 2 pi / (L N)}, read from a two-level table in shared
@@ -271,17 +271,18 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(T)
 #define SARBP_RC_SPLIT_MIN 32768
 #endif
 // CTA sizes (threads) per transform length, measured on GB300 (ms for 4096
-// pulses, forward + eight inverse transforms each): 8192 points at 512 threads
-// (64 KB of points, two CTAs per SM) 1.295 against 1.886 at 1024 threads (one
-// CTA per SM: a CTA's barriers are then overlapped by nothing); 16384 points
-// (128 KB, one CTA per SM either way) 3.075 at 1024 against 3.12 at 512; the
-// 16384-point halves of the 32768-point split path 4.29 at 512 against 4.35
-// at 1024 (2048 pulses).
+// pulses, forward + eight inverse transforms each).  8192 points: 1.886 at
+// 1024 threads (one CTA per SM: its barriers are overlapped by nothing), 1.295
+// at 512 (two CTAs per SM), 1.123 at 256 (two per SM, 32 points per thread:
+// radix-32 stages 32-32-8).  16384 points (128 KB, one CTA per SM whatever the
+// size): 3.077 at 1024 (16-16-16-4), 2.986 at 512 (32-32-16).  The 16384-point
+// halves of the 32768-point split path: 4.35 at 1024, 4.29 at 512 (radix-16),
+// 4.17 at 512 with radix-32 stages (2048 pulses).
 #ifndef SARBP_RC_8K_THREADS
-#define SARBP_RC_8K_THREADS 512
+#define SARBP_RC_8K_THREADS 256
 #endif
 #ifndef SARBP_RC_BIG_THREADS
-#define SARBP_RC_BIG_THREADS 1024
+#define SARBP_RC_BIG_THREADS 512
 #endif
 #ifndef SARBP_RC_HALF_THREADS
 #define SARBP_RC_HALF_THREADS 512
