@@ -40,16 +40,16 @@ MUFU_OPS_PER_UPDATE = 3
 # DRAM bytes (read + write) and L2 bytes (lts__t_bytes.sum) per call, measured by
 # ncu on GB300 for the default workload (4096 pulses x 8192 samples -> 4096^2,
 # complex64 rows): profiles/traffic_bp_rc_config2.md (captured 2026-12-04, one-pass
-# full-size captures of bp_kernel<2,0,3,0,8,0,16,0>, rc_forward_kernel<16384,1024>
-# and rc_inverse_kernel<16384,1024,0>).  Back-projection: one launch; range
+# full-size captures of bp_kernel<2,0,3,0,8,0,16,0>, rc_forward_kernel<16384,512>
+# and rc_inverse_kernel<16384,512,0>).  Back-projection: one launch; range
 # compression: two batches of forward + inverse.
 MEASURED_TRAFFIC = {
     ("full", "split"): {"bp": 234726656 + 115588864,
-                        "rc": (134388736 + 209891072 + 269426176 + 1013657600) +
-                              (134387200 + 207002880 + 268637440 + 1013731584)},
+                        "rc": (134409984 + 209805824 + 268619008 + 1013745408) +
+                              (134468864 + 207117824 + 268857344 + 1014054912)},
 }
 L2_TRAFFIC = {
-    ("full", "split"): {"bp": 25964478848, "rc": 802581504 + 8414586688 + 804555200 + 8421029760},
+    ("full", "split"): {"bp": 25964478848, "rc": 784757152 + 8282912800 + 791771840 + 8362595552},
 }
 # ncu's L2 peak for these launches: lts__t_bytes.sum / duration / pct_of_peak (same file)
 L2_PEAK_GBS = 25964478848 / 53.124512e-3 / 0.0134 / 1e9
@@ -473,7 +473,7 @@ def run_ours(args):
     roofline_rc = {"bound": "hbm", "achieved": rc_bytes / (rc_ms * 1e-3) / 1e9 if rc_ms else None, "peak": hbm,
                    "unit": "GB/s", "frac": (rc_bytes / (rc_ms * 1e-3) / 1e9 / hbm) if (rc_ms and hbm) else None,
                    "traffic": MEASURED_TRAFFIC.get((args.size, args.mode), {}).get("rc"),
-                   "kernel": "rc_forward + rc_inverse", "ms": rc_ms}
+                   "kernel": "rc_forward_kernel<16384,512> + rc_inverse_kernel<16384,512,0>", "ms": rc_ms}
     if rc_ms and l2.get("rc"):
         bw = l2["rc"] / (rc_ms * 1e-3) / 1e9
         roofline_rc["l2"] = {"achieved": bw, "peak": L2_PEAK_GBS, "unit": "GB/s", "frac": bw / L2_PEAK_GBS,

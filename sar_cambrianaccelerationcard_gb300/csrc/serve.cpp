@@ -94,6 +94,8 @@ struct Job {
     cudaEvent_t done_ev = nullptr;
     cudaEvent_t ready_ev = nullptr;  // echo uploaded and range-compressed
     cudaEvent_t admit_ev = nullptr;  // start of the admission work (timing)
+    std::vector<cudaEvent_t> chunk_done;  // range compression of pulses [b spec_rows, (b + 1) spec_rows) complete
+    bool admit_counted = false;      // admission device time added to the stats
     JobState state = JobState::Queued;
     sarbp_status status = SARBP_OK;
     std::string msg;
@@ -229,6 +231,7 @@ sarbp_status admit(sarbp_server *S, Job *j) {
         if (e == cudaSuccess)
             e = sarbp::launch_rc_inverse(rp, S->d_spec, j->d_etab, sc,
                                          static_cast<char *>(j->d_rc) + p0 * nb * j->esize, S->sa);
+        if (e == cudaSuccess) e = cudaEventRecord(j->chunk_done[p0 / S->spec_rows], S->sa);
     }
     if (e == cudaSuccess) e = cudaEventRecord(j->ready_ev, S->sa);
     if (e != cudaSuccess) {
@@ -269,6 +272,14 @@ void release(sarbp_server *S, Job *j) {
     if (j->lane >= 0) j->lane = -1;
 }
 
+// Range-compression batch that the job's next step needs (the one holding its
+// last pulse): the job joins steps as soon as that batch is complete, while
+// later batches are still being compressed.
+cudaEvent_t next_step_chunk(const sarbp_server *S, const Job *j) {
+    const int p1 = std::min(j->desc.np, j->next_pulse + j->pps);
+    return j->chunk_done[(size_t)(p1 - 1) / S->spec_rows];
+}
+
 // Device time of step `par` once it has completed (caller holds S->mu).
 void fold_step(sarbp_server *S, int par) {
     if (!S->step_pending[par] || cudaEventQuery(S->step_ev[par]) != cudaSuccess) return;
@@ -305,11 +316,12 @@ void worker_main(sarbp_server *S) {
             }
         }
         for (Job *j : S->active)
-            if (j->state == JobState::Loading && cudaEventQuery(j->ready_ev) == cudaSuccess) {
-                j->state = JobState::Active;
+            if (!j->admit_counted && cudaEventQuery(j->ready_ev) == cudaSuccess) {
+                if (j->state == JobState::Loading) j->state = JobState::Active;
                 float ms = 0.f;
                 if (cudaEventElapsedTime(&ms, j->admit_ev, j->ready_ev) == cudaSuccess) S->st.admit_device_s += ms * 1e-3;
                 cudaGetLastError();
+                j->admit_counted = true;
             }
         fold_step(S, 0);
         fold_step(S, 1);
@@ -353,7 +365,9 @@ void worker_main(sarbp_server *S) {
         // 3. one step over every admitted job that still has pulses
         std::vector<Job *> step;
         for (Job *j : S->active)
-            if (j->state == JobState::Active) step.push_back(j);
+            if (j->state == JobState::Active ||
+                (j->state == JobState::Loading && cudaEventQuery(next_step_chunk(S, j)) == cudaSuccess))
+                step.push_back(j);
         if (!step.empty()) {
             // at most two steps in flight
             const int par = S->step_parity;
@@ -448,7 +462,7 @@ void worker_main(sarbp_server *S) {
                 break;
             }
         if (oldest) {
-            cudaEvent_t ev = oldest->state == JobState::Loading ? oldest->ready_ev : oldest->done_ev;
+            cudaEvent_t ev = oldest->state == JobState::Loading ? next_step_chunk(S, oldest) : oldest->done_ev;
             lk.unlock();
             cudaEventSynchronize(ev);
             lk.lock();
@@ -540,6 +554,7 @@ sarbp_status sarbp_server_destroy(sarbp_server *S) {
         if (j->done_ev) cudaEventDestroy(j->done_ev);
         if (j->ready_ev) cudaEventDestroy(j->ready_ev);
         if (j->admit_ev) cudaEventDestroy(j->admit_ev);
+        for (cudaEvent_t e : j->chunk_done) cudaEventDestroy(e);
         if (j->h_err) cudaFreeHost(j->h_err);
         delete j;
     }
@@ -634,13 +649,22 @@ sarbp_status sarbp_server_submit(sarbp_server *S, const sarbp_job *job, uint64_t
         return SARBP_ERR_BUDGET;
     }
     cudaSetDevice(S->cfg.device);
-    if (cudaEventCreateWithFlags(&j->done_ev, cudaEventDisableTiming) != cudaSuccess ||
+    bool ev_ok = true;
+    j->chunk_done.assign((d.np + S->spec_rows - 1) / S->spec_rows, nullptr);
+    for (cudaEvent_t &e : j->chunk_done)
+        if (ev_ok && cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) {
+            ev_ok = false;
+            e = nullptr;
+        }
+    j->chunk_done.erase(std::remove(j->chunk_done.begin(), j->chunk_done.end(), nullptr), j->chunk_done.end());
+    if (!ev_ok || cudaEventCreateWithFlags(&j->done_ev, cudaEventDisableTiming) != cudaSuccess ||
         cudaEventCreate(&j->ready_ev) != cudaSuccess || cudaEventCreate(&j->admit_ev) != cudaSuccess ||
         cudaMallocHost(&j->h_err, sizeof(unsigned)) != cudaSuccess) {
         cudaGetLastError();
         if (j->done_ev) cudaEventDestroy(j->done_ev);
         if (j->ready_ev) cudaEventDestroy(j->ready_ev);
         if (j->admit_ev) cudaEventDestroy(j->admit_ev);
+        for (cudaEvent_t e : j->chunk_done) cudaEventDestroy(e);
         delete j;
         return SARBP_ERR_CUDA;
     }
@@ -652,6 +676,7 @@ sarbp_status sarbp_server_submit(sarbp_server *S, const sarbp_job *job, uint64_t
             cudaEventDestroy(j->done_ev);
             cudaEventDestroy(j->ready_ev);
             cudaEventDestroy(j->admit_ev);
+            for (cudaEvent_t e : j->chunk_done) cudaEventDestroy(e);
             cudaFreeHost(j->h_err);
             delete j;
             return SARBP_ERR_CANCELLED;
@@ -709,6 +734,7 @@ sarbp_status sarbp_server_wait(sarbp_server *S, uint64_t ticket, int32_t timeout
     if (j->done_ev) cudaEventDestroy(j->done_ev);
     if (j->ready_ev) cudaEventDestroy(j->ready_ev);
     if (j->admit_ev) cudaEventDestroy(j->admit_ev);
+    for (cudaEvent_t e : j->chunk_done) cudaEventDestroy(e);
     if (j->h_err) cudaFreeHost(j->h_err);
     delete j;
     return st;
