@@ -451,6 +451,12 @@ sarbp_status sarbp_server_wait(sarbp_server *srv, uint64_t ticket, int32_t timeo
 /* Cancels a queued job (SARBP_ERR_NOT_READY if it was already admitted). */
 sarbp_status sarbp_server_cancel(sarbp_server *srv, uint64_t ticket);
 sarbp_status sarbp_server_get_stats(sarbp_server *srv, sarbp_server_stats *out);
+/* Test switch of a server, not for production use (no reference counterpart):
+ * SARBP_SERVER_DEBUG_FAIL_ADMIT_TICKET = t (> 0) refuses the device allocation
+ * of ticket t's admission on the host, as a full device would, so that job
+ * fails with SARBP_ERR_OUT_OF_MEMORY and the others proceed; 0 clears it. */
+enum { SARBP_SERVER_DEBUG_FAIL_ADMIT_TICKET = 1 };
+sarbp_status sarbp_server_debug_set(sarbp_server *srv, int32_t key, int64_t value);
 
 /* ------------------------------------------------- reference-layout shim -- */
 

@@ -139,7 +139,7 @@ struct sarbp_server {
     sarbp_server_stats st{};
     Clock::time_point busy_since;
     bool busy = false;
-    uint64_t fail_admit_ticket = 0;       // SARBP_SERVE_FAIL_ADMIT: host-side fault injection (tests)
+    uint64_t fail_admit_ticket = 0;       // sarbp_server_debug_set: host-side fault injection (tests)
 };
 
 namespace {
@@ -496,7 +496,6 @@ sarbp_status sarbp_server_create(sarbp_server **out, const sarbp_server_config *
     sarbp_server *S = new sarbp_server();
     S->cfg = *cfg;
     if (S->cfg.pulses_per_step == 0) S->cfg.pulses_per_step = 512;
-    if (const char *f = std::getenv("SARBP_SERVE_FAIL_ADMIT")) S->fail_admit_ticket = std::strtoull(f, nullptr, 10);
     S->sms = prop.multiProcessorCount;
     bool ok = cudaStreamCreateWithFlags(&S->s0, cudaStreamNonBlocking) == cudaSuccess &&
               cudaStreamCreateWithFlags(&S->sa, cudaStreamNonBlocking) == cudaSuccess &&
@@ -753,6 +752,19 @@ sarbp_status sarbp_server_cancel(sarbp_server *S, uint64_t ticket) {
     S->st.cancelled++;
     S->cv_done.notify_all();
     return SARBP_OK;
+}
+
+sarbp_status sarbp_server_debug_set(sarbp_server *S, int32_t key, int64_t value) {
+    if (!S) return SARBP_ERR_INVALID_ARGUMENT;
+    std::lock_guard<std::mutex> lk(S->mu);
+    switch (key) {
+        case SARBP_SERVER_DEBUG_FAIL_ADMIT_TICKET:
+            if (value < 0) return SARBP_ERR_INVALID_ARGUMENT;
+            S->fail_admit_ticket = (uint64_t)value;
+            return SARBP_OK;
+        default:
+            return SARBP_ERR_INVALID_ARGUMENT;
+    }
 }
 
 sarbp_status sarbp_server_get_stats(sarbp_server *S, sarbp_server_stats *out) {

@@ -219,6 +219,7 @@ SIGNATURES = {
                           ctypes.c_int),
     "sarbp_server_cancel": ([ctypes.c_void_p, ctypes.c_uint64], ctypes.c_int),
     "sarbp_server_get_stats": ([ctypes.c_void_p, ctypes.POINTER(ServerStats)], ctypes.c_int),
+    "sarbp_server_debug_set": ([ctypes.c_void_p, ctypes.c_int32, ctypes.c_int64], ctypes.c_int),
     "sarbp_launch_back_projection": ([ctypes.c_void_p, ctypes.c_void_p, ctypes.POINTER(RefParams),
                                       ctypes.c_int32, ctypes.c_int32], ctypes.c_int),
     "sarbp_launch_generate_echo": ([ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
@@ -239,6 +240,7 @@ DEBUG_BP_CHECKED = 3
 DEBUG_WAIT_LIMIT_NS = 4
 DEBUG_WAIT_FAULT_CHUNK = 5
 DEBUG_DEVICE_FLAGS = 6
+SERVER_DEBUG_FAIL_ADMIT_TICKET = 1
 
 _lib = None
 
@@ -631,6 +633,12 @@ class Server:
             return st, s, None
         _, _, image = self._keep.pop(ticket, (None, None, None))
         return st, s, image
+
+    def debug_set(self, key: int, value: int):
+        """Test switch of this server (sarbp_server_debug_set)."""
+        st = self.lib.sarbp_server_debug_set(self.h, int(key), int(value))
+        if st != OK:
+            raise SarbpError(st, "server debug_set")
 
     def stats(self) -> ServerStats:
         s = ServerStats()

@@ -168,13 +168,14 @@ def test_malformed_requests_rejected_at_submit(jobs):
         assert srv.stats().submitted == 1
 
 
-def test_injected_admission_failure(jobs, monkeypatch):
+def test_injected_admission_failure(jobs):
     """A refused device allocation at admission (injected on the host for
-    ticket 2) fails that job with SARBP_ERR_OUT_OF_MEMORY; the jobs before and
-    after it complete with their one-shot images."""
-    monkeypatch.setenv("SARBP_SERVE_FAIL_ADMIT", "2")
+    ticket 2 through sarbp_server_debug_set) fails that job with
+    SARBP_ERR_OUT_OF_MEMORY; the jobs before and after it complete with their
+    one-shot images."""
     s0, e0, ref0 = jobs[4]
     with sarbp.Server(0, max_jobs=4, hbm_budget_bytes=4 << 30) as srv:
+        srv.debug_set(sarbp.SERVER_DEBUG_FAIL_ADMIT_TICKET, 2)
         t = [submit(srv, s0, e0) for _ in range(3)]
         assert t[1] == 2
         res = [srv.wait(x, 120000) for x in t]
