@@ -690,7 +690,11 @@ __global__ void __launch_bounds__(kThreads, SARBP_BP_MINBLOCKS)
         const bool ok =
             mbar_wait_bounded(smem_addr(&S.bar[stage]), (c / kStages) & 1, TESTF ? P.wait_ns : kDefaultWaitNs);
         if (!ok) { failed = true; }
-        if (__syncthreads_or(failed)) { failed = true; break; }
+        // One block barrier per chunk, after the conversion: each thread has seen
+        // its own wait complete, the chunk's parameters were published by the
+        // previous chunk's barrier, and a thread whose wait ran out converts
+        // in-bounds shared memory only before the barrier's vote ends the loop
+        // (config 2 53.04 -> 52.64 ms against a barrier on each side, same bits).
         // trimmed to the pairs the tile reads for complex16 rows (warp per pulse:
         // config 5 892 -> 864 ms); the flat complex64 pass measured slower with
         // the per-element test (config 2 1296 -> 1283 Gupd/s), and complex64 rows
@@ -699,7 +703,7 @@ __global__ void __launch_bounds__(kThreads, SARBP_BP_MINBLOCKS)
         convert<MODE, STORE,
                 !CHECKED && STORE == SARBP_STORE_C32H && (MODE == SARBP_MODE_SPLIT || MODE == SARBP_MODE_FP16STORE)>(
             S, stage, sbuf, count, win, win_magic, chunk);
-        __syncthreads();
+        if (__syncthreads_or(failed)) { failed = true; break; }
         if constexpr (ADJ) {  // every warp has finished chunk c-1: combine its pulse sums
             if (c > 0) flush_projection(P, S, (c - 1) & 1, pc0 - chunk, chunk);
         }
