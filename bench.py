@@ -627,9 +627,57 @@ def serve_requests(ctx, n_req, seed=4):
     return reqs
 
 
-def serve_sweep(reqs, rates, jobs, schedules):
+def serve_one_shot(reqs, reps=3):
+    """Each request imaged alone through the one-shot calls with its echo
+    already in HBM: device times (CUDA events on the launching stream, best of
+    `reps` after one warm-up) of its range compression and its back-projection,
+    the same kernels and plans the server runs.  Returns (updates, rc_ms, bp_ms)
+    per request."""
+    import torch
+    from sar_cambrianaccelerationcard_gb300 import sarbp
+    ctx = sarbp.Context(0)
+    stream = torch.cuda.Stream()
+    sptr = sarbp.ctypes.c_void_p(stream.cuda_stream)
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+    out = []
+    for sc, host, _ in reqs:
+        r, g, lay = sarbp.scene_args(sc)
+        echo = host.cuda()
+        apc = torch.from_numpy(sc.apc).cuda()
+        rc = torch.empty((sc.np_, lay.nbins * 2), dtype=torch.float32, device="cuda")
+        img = torch.empty((g.ny, g.nx * 2), dtype=torch.float32, device="cuda")
+        view = sarbp.RcView()
+        view.data, view.scale = rc.data_ptr(), None
+        view.storage, view.np, view.nbins = sarbp.STORE_C64, sc.np_, lay.nbins
+        view.t0_bins, view.bin_rate = lay.t0_bins, lay.bin_rate
+        best_rc = best_bp = float("inf")
+        for k in range(reps + 1):
+            ev[0].record(stream)
+            ctx.check(ctx.lib.sarbp_range_compress(ctx.h, sarbp.ctypes.byref(r), echo.data_ptr(), sc.np_, sc.ns,
+                                                   sarbp.STORE_C64, rc.data_ptr(), None, sptr), "rc")
+            ev[1].record(stream)
+            ctx.check(ctx.lib.sarbp_backproject(ctx.h, sarbp.ctypes.byref(r), sarbp.ctypes.byref(view),
+                                                apc.data_ptr(), sarbp.ctypes.byref(g), sarbp.MODE_SPLIT,
+                                                img.data_ptr(), 0, sptr), "bp")
+            ev[2].record(stream)
+            stream.synchronize()
+            if k:
+                best_rc = min(best_rc, ev[0].elapsed_time(ev[1]))
+                best_bp = min(best_bp, ev[1].elapsed_time(ev[2]))
+        out.append((float(sc.np_) * g.nx * g.ny, best_rc, best_bp))
+        del echo, apc, rc, img
+    ctx.close()
+    torch.cuda.empty_cache()
+    return out
+
+
+def serve_sweep(reqs, rates, jobs, schedules, one_shot=None):
     """Poisson arrivals of the requests at each rate against one sarbp server
-    per (schedule, rate); latency is submit entry -> image in host memory."""
+    per (schedule, rate); latency is submit entry -> image in host memory.
+    With one_shot (serve_one_shot's figures) each run also reports the rates
+    the same job draws reach imaged one at a time: back-projection alone (the
+    reference for the steps' back-projection) and range compression plus
+    back-projection (the reference for busy-time throughput)."""
     import threading
     from sar_cambrianaccelerationcard_gb300 import sarbp
     # rate-major, the schedules' order rotated per rate, so that a slow drift over
@@ -688,6 +736,12 @@ def serve_sweep(reqs, rates, jobs, schedules):
                     "bp_in_steps_gpix_pulse_s": stats.updates / max(stats.step_device_s, 1e-9) / 1e9,
                     "peak_active": stats.peak_active, "graph_launches": stats.graph_launches,
                     "peak_gb": stats.peak_bytes / 2**30, "clocks": clk})
+        if one_shot is not None:
+            u = sum(one_shot[i][0] for i in order)
+            t_bp = sum(one_shot[i][2] for i in order) * 1e-3
+            t_rc = sum(one_shot[i][1] for i in order) * 1e-3
+            out[-1]["one_shot_same_jobs"] = {"bp_gpix_pulse_s": u / t_bp / 1e9,
+                                             "rc_bp_gpix_pulse_s": u / (t_bp + t_rc) / 1e9}
     return out
 
 
@@ -714,7 +768,8 @@ def serve_measure(rates=(20.0, 40.0), jobs=30, n_req=12, step_updates=(1 << 31,)
     reqs = serve_requests(ctx, n_req)
     ctx.close()
     torch.cuda.empty_cache()
-    sweep = serve_sweep(reqs, list(rates), jobs, schedule_names(step_updates))
+    one_shot = serve_one_shot(reqs)
+    sweep = serve_sweep(reqs, list(rates), jobs, schedule_names(step_updates), one_shot)
     del reqs
     return {"metric": "serving p50/p99 latency (ms) and aggregate Gpix*pulse/s", "mode": "split",
             "workload": SERVE_WORKLOAD + f"; {n_req} distinct requests drawn at random, {jobs} jobs per rate",
@@ -733,7 +788,8 @@ def run_serve(args):
     ctx.close()
     torch.cuda.empty_cache()
     schedules = schedule_names(int(x) for x in args.step_updates.split(","))
-    out = serve_sweep(reqs, [float(r) for r in args.rates.split(",")], args.jobs, schedules)
+    one_shot = serve_one_shot(reqs)
+    out = serve_sweep(reqs, [float(r) for r in args.rates.split(",")], args.jobs, schedules, one_shot)
     line = {"metric": "serving p50/p99 latency and aggregate Gpix*pulse/s", "mode": "split",
             "workload": SERVE_WORKLOAD + "; 24 distinct requests drawn at random",
             "server": {"max_jobs": 16, "hbm_budget_gb": 96, "graphs": True,
