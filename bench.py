@@ -81,7 +81,7 @@ def parse():
                     help="CEOS raw-data decode of the reference scene's size (3072 lines x 2048 cells)")
     ap.add_argument("--rates", default="10,20,30,40", help="arrival rates (jobs/s) for --serve")
     ap.add_argument("--jobs", type=int, default=60, help="jobs per rate for --serve")
-    ap.add_argument("--step-updates", default="2147483648,0",
+    ap.add_argument("--step-updates", default="4294967296,0",
                     help="--serve schedules: comma list of step_updates (0: fixed 512 pulses per step)")
     return ap.parse_args()
 
@@ -530,6 +530,42 @@ def run_ours(args):
             img_fp16 = img_d.cpu().numpy().view(np.complex64)
         del h16, sc16
 
+    # --- the plain FP64 GPU mode (the comparator of the >= 5x target) against the
+    # split mode on the same 1024^2 centre tile x all pulses of the same data
+    fp64cmp = None
+    if not args.no_extras and args.mode == "split" and args.size == "full":
+        side = 1024
+        x0, y0 = g.nx // 2 - side // 2, g.ny // 2 - side // 2
+        gs = sub_grid(g, x0, y0, side, side)
+        tile_img = torch.empty((side, 2 * side), dtype=torch.float32, device="cuda")
+
+        def bp_tile(m):
+            ctx.check(ctx.lib.sarbp_backproject(ctx.h, sarbp.ctypes.byref(r), sarbp.ctypes.byref(view),
+                                                apc_d.data_ptr(), sarbp.ctypes.byref(gs), m, tile_img.data_ptr(),
+                                                0, sptr), "bp tile")
+
+        tev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+        tms = {}
+        for m, reps in ((sarbp.MODE_FP64, 2), (sarbp.MODE_SPLIT, 10)):
+            bp_tile(m)  # warm-up
+            stream.synchronize()
+            tev[0].record(stream)
+            for _ in range(reps):
+                bp_tile(m)
+            tev[1].record(stream)
+            stream.synchronize()
+            tms[m] = tev[0].elapsed_time(tev[1]) / reps
+        ctx.synchronize()
+        upd = float(scene.np_) * side * side
+        r64 = upd / (tms[sarbp.MODE_FP64] * 1e-3) / 1e9
+        rsp = upd / (tms[sarbp.MODE_SPLIT] * 1e-3) / 1e9
+        fp64cmp = {"tile": [x0, y0, side, side], "unit": "Gpix*pulse/s",
+                   "fp64_gpu": {"value": r64, "ms": tms[sarbp.MODE_FP64]},
+                   "split": {"value": rsp, "ms": tms[sarbp.MODE_SPLIT]},
+                   "split_over_fp64": rsp / r64,
+                   "fp16store_over_fp64": (fp16["value"] / r64) if fp16 else None}
+        del tile_img
+
     # --- accuracy against the FP64 CPU oracle (BPA_SAR.m:177-197 restated):
     # the oracle's own range compression of its own echo, back-projected over
     # the 512^2 centre tile and over patches around the brightest isolated
@@ -584,6 +620,7 @@ def run_ours(args):
             "rc_ms": rc_ms,
             "accuracy": acc,
             "fp16store": fp16,
+            "fp64_comparator": fp64cmp,
             **extras,
             "e2e": e2e,
             "roofline": roofline,
@@ -758,7 +795,7 @@ def schedule_names(step_updates):
     return out
 
 
-def serve_measure(rates=(20.0, 40.0), jobs=30, n_req=12, step_updates=(1 << 31,)):
+def serve_measure(rates=(20.0, 40.0), jobs=30, n_req=12, step_updates=(1 << 32,)):
     """The serving key of the default run: a bounded sweep (n_req distinct
     requests drawn at random, `jobs` per rate, one schedule)."""
     import torch
