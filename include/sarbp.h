@@ -35,7 +35,9 @@
 extern "C" {
 #endif
 
-#define SARBP_ABI_VERSION 1
+/* Raised when a struct a caller allocates or an entry point changes (2: the
+ * serving stats' step and admission device times, the debug switches). */
+#define SARBP_ABI_VERSION 2
 
 typedef enum sarbp_status {
     SARBP_OK = 0,
@@ -503,7 +505,7 @@ sarbp_status sarbp_launch_generate_echo(sarbp_complex64 *Srnm, const float *Ptar
 /* ------------------------------------------------------------ measurement -- */
 
 /* Issue-rate microbenchmarks on the context's device: FP32 FMA lanes/s and
- * MUFU (sin/cos) lanes/s, plus the SM clock (Hz) seen during the run.  The
+ * MUFU (sin/cos) lanes/s over all its SMs, and the SM count.  The
  * back-projection roofline is built from these (the kernel is FP32/MUFU issue
  * bound, not HBM or tensor bound). */
 sarbp_status sarbp_probe_issue_rates(sarbp_ctx *ctx, double *fp32_lanes_per_s,

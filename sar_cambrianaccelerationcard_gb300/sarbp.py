@@ -242,11 +242,14 @@ DEBUG_WAIT_FAULT_CHUNK = 5
 DEBUG_DEVICE_FLAGS = 6
 SERVER_DEBUG_FAIL_ADMIT_TICKET = 1
 
+ABI_VERSION = 2  # SARBP_ABI_VERSION of the include/sarbp.h these bindings follow
+
 _lib = None
 
 
 def load(path: str = LIB_PATH):
-    """Load libsarbp.so; raises if it has not been built."""
+    """Load libsarbp.so; raises if it has not been built or was built from
+    another ABI version than these bindings."""
     global _lib
     if _lib is None:
         if not os.path.exists(path):
@@ -257,6 +260,9 @@ def load(path: str = LIB_PATH):
             f = getattr(L, name)
             f.argtypes = args
             f.restype = res
+        if L.sarbp_abi_version() != ABI_VERSION:
+            raise RuntimeError(f"{path} has ABI version {L.sarbp_abi_version()}, these bindings {ABI_VERSION}: "
+                               "rebuild the library")
         _lib = L
     return _lib
 

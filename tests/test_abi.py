@@ -76,7 +76,10 @@ int main(void) {
 
 
 def test_abi_version_and_status_strings(lib):
-    assert lib.sarbp_abi_version() == 1
+    from sar_cambrianaccelerationcard_gb300 import sarbp
+    header = open(HEADER).read()
+    version = int(re.search(r"#define SARBP_ABI_VERSION (\d+)", header).group(1))
+    assert lib.sarbp_abi_version() == version == sarbp.ABI_VERSION
     assert lib.sarbp_status_string(0) == b"ok"
     assert lib.sarbp_status_string(2) == b"unsupported"
     assert lib.sarbp_status_string(999) == b"unknown status"
