@@ -129,7 +129,7 @@ class ClockSampler:
             self.proc = None
             return
         # return once nvidia-smi has written its first sample: its start-up
-        # (driver queries) then falls before the timed region, not inside it
+        # (NVML queries) then falls before the timed region, not inside it
         t0 = time.time()
         while time.time() - t0 < 5.0 and self.proc.poll() is None:
             if os.path.getsize(self.path) > 0:

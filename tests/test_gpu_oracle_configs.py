@@ -12,7 +12,7 @@ workloads, reduced so the oracle finishes in seconds (BPA_SAR.m:80-111,
     sub-apertures of 256 pulses x 2 x 2 image tiles as the full-size run is.
 
 Both sides take the oracle's FP64 echo (cast to complex64 for the GPU).
-Tolerances (the spec accuracy target):
+Tolerances (the accuracy target of the split and FP16-storage modes):
   relative L2 <= -60 dB; point targets: peak position within 0.05 pixel,
   PSLR and ISLR within 0.1 dB of the oracle's (range and azimuth cuts).
 Plain FP32 BP is the accuracy comparator: it must focus every target, and
