@@ -165,3 +165,33 @@ def test_coarse_pixels_inside_and_outside_the_split_envelope(contexts, orc, spac
     err = metrics.rel_l2_db(sarbp.image_scene(plain, s, e64, sarbp.MODE_FP64), ref)
     print(s.name, f"ns {s.ns} split refused, fp64 {err:.1f} dB")
     assert err <= TOL_DB["fp64"]
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("step_updates", [0, 1 << 24])
+def test_served_random_geometries_vs_oracle(contexts, orc, step_updates):
+    """Six of the random geometries served together in one mix (the server
+    plans each job at submit and advances it in per-step pulse slices: 128
+    pulses, or about 2^24 pixel*pulse updates per job and step): every image
+    within -60 dB of the oracle and within -100 dB of the same job's one-shot
+    image (only the sub-aperture summation order differs)."""
+    plain, _ = contexts
+    cases = []
+    for seed in range(6):
+        s = random_scene(seed)
+        e64 = orc.echo(s).astype(np.complex64)
+        cases.append((s, e64, orc.image(s, e64.astype(np.complex128)),
+                      sarbp.image_scene(plain, s, e64, sarbp.MODE_SPLIT)))
+    with sarbp.Server(0, max_jobs=6, hbm_budget_bytes=8 << 30, pulses_per_step=128,
+                      step_updates=step_updates) as srv:
+        tickets = []
+        for s, e64, _, _ in cases:
+            r, g, _ = sarbp.scene_args(s)
+            tickets.append(srv.submit(r, g, e64, s.apc, sarbp.MODE_SPLIT))
+        results = [srv.wait(t, 120000) for t in tickets]
+        assert srv.stats().peak_active >= 2
+    for (s, _, ref, one_shot), (st, stats, img) in zip(cases, results):
+        assert st == sarbp.OK, s.name
+        err, vs_one = metrics.rel_l2_db(img, ref), metrics.rel_l2_db(img, one_shot)
+        print(s.name, f"steps {stats.steps} served vs oracle {err:.1f} dB, vs one-shot {vs_one:.1f} dB")
+        assert err <= -60.0 and vs_one <= -100.0, (s.name, err, vs_one)
