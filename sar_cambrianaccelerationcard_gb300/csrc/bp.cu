@@ -830,7 +830,7 @@ cudaError_t launch_variant(const BpPlan &p, cudaStream_t s, int tiles, int tiles
     if (CHUNK && p.chunk != CHUNK) return cudaErrorInvalidValue;
     auto k = bp_kernel<MODE, STORE, NTERMS, CHECKED, PIX, ADJ, CHUNK, TESTF>;
     const size_t smem = bp_smem_bytes(STORE, p.win, p.chunk);
-    cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaError_t e = allow_dynamic_smem(reinterpret_cast<const void *>(k));
     if (e != cudaSuccess) return e;
     if (t_occupancy) return cudaOccupancyMaxActiveBlocksPerMultiprocessor(t_occupancy, k, kThreads, smem);
     dim3 grid(tiles, p.segments);

@@ -10,11 +10,36 @@
 #include <cstdlib>
 #include <complex>
 #include <cstring>
+#include <mutex>
+#include <set>
 #include <string>
 #include <thread>
 #include <vector>
 
 #include "sarbp_internal.h"
+
+namespace sarbp {
+
+cudaError_t allow_dynamic_smem(const void *kernel) {
+    static std::mutex m;
+    static std::set<std::pair<const void *, int>> done;
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    std::lock_guard<std::mutex> lk(m);
+    if (done.count({kernel, dev})) return cudaSuccess;
+    cudaFuncAttributes fa;
+    int optin = 0;
+    e = cudaFuncGetAttributes(&fa, kernel);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 optin - (int)fa.sharedSizeBytes);
+    if (e == cudaSuccess) done.insert({kernel, dev});
+    return e;
+}
+
+}  // namespace sarbp
 
 namespace sarbp {
 

@@ -307,7 +307,7 @@ cudaError_t fwd_n(const RcPlan &p, const float2 *echo, const float2 *filt, const
     constexpr int T = threads_for<N>();
     const size_t smem = sizeof(float2) * N + kTabSmem;
     auto k = rc_forward_kernel<N, T>;
-    cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaError_t e = allow_dynamic_smem(reinterpret_cast<const void *>(k));
     if (e != cudaSuccess || t_prepare) return e;
     k<<<p.np, T, smem, s>>>(p.ns, p.L, echo, filt, etab, spec, scale);
     return cudaGetLastError();
@@ -321,12 +321,12 @@ cudaError_t inv_n(const RcPlan &p, const float2 *spec, const float2 *etab, const
     cudaError_t e;
     if (p.storage == SARBP_STORE_C64) {
         auto k = rc_inverse_kernel<N, T, SARBP_STORE_C64>;
-        e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        e = allow_dynamic_smem(reinterpret_cast<const void *>(k));
         if (e != cudaSuccess || t_prepare) return e;
         k<<<p.np * p.L, T, smem, s>>>(p.ns, p.L, p.nbins, spec, etab, scale, out);
     } else {
         auto k = rc_inverse_kernel<N, T, SARBP_STORE_C32H>;
-        e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        e = allow_dynamic_smem(reinterpret_cast<const void *>(k));
         if (e != cudaSuccess || t_prepare) return e;
         k<<<p.np * p.L, T, smem, s>>>(p.ns, p.L, p.nbins, spec, etab, scale, out);
     }
@@ -339,7 +339,7 @@ cudaError_t fwd2(const RcPlan &p, const float2 *echo, const float2 *filt, const 
     constexpr int T = threads_for_half<M>();
     const size_t smem = sizeof(float2) * M + kTabSmem;
     auto k = rc_forward2_kernel<M, T>;
-    cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaError_t e = allow_dynamic_smem(reinterpret_cast<const void *>(k));
     if (e != cudaSuccess || t_prepare) return e;
     k<<<2 * p.np, T, smem, s>>>(p.ns, p.L, echo, filt, etab, spec, bound2);
     return cudaGetLastError();
@@ -353,12 +353,12 @@ cudaError_t inv2(const RcPlan &p, const float2 *spec, const float2 *etab, const 
     cudaError_t e;
     if (p.storage == SARBP_STORE_C64) {
         auto k = rc_inverse2_kernel<M, T, SARBP_STORE_C64>;
-        e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        e = allow_dynamic_smem(reinterpret_cast<const void *>(k));
         if (e != cudaSuccess || t_prepare) return e;
         k<<<2 * p.np * p.L, T, smem, s>>>(p.ns, p.L, p.nbins, spec, etab, bound2, scale, out);
     } else {
         auto k = rc_inverse2_kernel<M, T, SARBP_STORE_C32H>;
-        e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        e = allow_dynamic_smem(reinterpret_cast<const void *>(k));
         if (e != cudaSuccess || t_prepare) return e;
         k<<<2 * p.np * p.L, T, smem, s>>>(p.ns, p.L, p.nbins, spec, etab, bound2, scale, out);
     }

@@ -41,6 +41,14 @@ struct Tuning {
 constexpr unsigned kFaultBytes = 16;
 constexpr unsigned long long kDefaultWaitNs = 2000000000ull;
 
+// Raises the kernel's dynamic shared-memory limit on the current device to the
+// device's opt-in maximum (less the kernel's static shared memory), once per
+// (kernel, device).  Launches then need no attribute call of their own (a host
+// cost on every launch otherwise), and threads launching the same kernel with
+// different sizes cannot lower each other's limit between its setting and
+// their launch.  Thread-safe (plan.cpp).
+cudaError_t allow_dynamic_smem(const void *kernel);
+
 // SMs of the current device, queried once per device: grid-stride launches
 // size their grids as a multiple of it.
 inline int current_sms() {

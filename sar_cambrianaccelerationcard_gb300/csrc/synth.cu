@@ -149,8 +149,7 @@ cudaError_t launch_echo_synth(const double *apc, int np, int ns, const sarbp_tar
     if (np <= 0 || ns <= 0) return cudaSuccess;
     if (nt < 0 || nt > kMaxTargets) return cudaErrorInvalidValue;
     const size_t smem = sizeof(TgtPre) * (size_t)(nt > 0 ? nt : 1);
-    cudaError_t e = cudaFuncSetAttribute(echo_synth_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)(sizeof(TgtPre) * kMaxTargets));
+    cudaError_t e = allow_dynamic_smem(reinterpret_cast<const void *>(echo_synth_kernel));
     if (e != cudaSuccess) return e;
     echo_synth_kernel<<<np, kSynthThreads, smem, s>>>(apc, ns, tg, nt, t_rec0, fs, kr, tp, tc, fc, c, echo,
                                                    power_acc);

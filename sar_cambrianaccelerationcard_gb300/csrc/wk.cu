@@ -222,7 +222,7 @@ cudaError_t cols_n(const DftPlan &p, const float2 *in, float2 *out, int ncols, f
     constexpr int C = SARBP_WK_COLS, T = SARBP_WK_COL_THREADS;
     const size_t smem = sizeof(float2) * (size_t)C * (N + kColPad) + kTabSmem;
     auto k = dft_cols_kernel<N, T, INV, C>;
-    cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaError_t e = allow_dynamic_smem(reinterpret_cast<const void *>(k));
     if (e != cudaSuccess) return e;
     k<<<(ncols + C - 1) / C, T, smem, s>>>(in, out, ncols, scale, p.etab);
     return cudaGetLastError();
@@ -234,7 +234,7 @@ cudaError_t pow2_n(const DftPlan &p, float2 *data, int rows, long long ld, float
     constexpr int T = dft_threads<N>();
     const size_t smem = sizeof(float2) * N + kTabSmem;
     auto k = dft_pow2_kernel<N, T, INV>;
-    cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaError_t e = allow_dynamic_smem(reinterpret_cast<const void *>(k));
     if (e != cudaSuccess) return e;
     k<<<rows, T, smem, s>>>(data, ld, scale, p.etab, io);
     return cudaGetLastError();
@@ -246,7 +246,7 @@ cudaError_t blue_m(const DftPlan &p, float2 *data, int rows, long long ld, float
     constexpr int T = dft_threads<M>();
     const size_t smem = sizeof(float2) * M + kTabSmem;
     auto k = dft_bluestein_kernel<M, T, INV>;
-    cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaError_t e = allow_dynamic_smem(reinterpret_cast<const void *>(k));
     if (e != cudaSuccess) return e;
     k<<<rows, T, smem, s>>>(data, ld, p.n, scale, p.etab, p.chirp, INV ? p.kinv : p.kfwd, io);
     return cudaGetLastError();
@@ -484,7 +484,7 @@ cudaError_t launch_wk_stolt_ff(const float2 *in, float2 *out, int NA, int NR, co
                                const float2 *col_ip, const float2 *row_q, double a4r, double nr_over_fr, int taps,
                                cudaStream_t s) {
     const size_t smem = wk_stolt_smem(NR);
-    cudaError_t e = cudaFuncSetAttribute(wk_stolt_ff_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaError_t e = allow_dynamic_smem(reinterpret_cast<const void *>(wk_stolt_ff_kernel));
     if (e != cudaSuccess) return e;
     const double a2 = 0.5 * a4r;
     const float a2h = (float)a2, a2l = (float)(a2 - (double)a2h);
@@ -497,7 +497,7 @@ cudaError_t launch_wk_stolt(const float2 *in, float2 *out, int NA, int NR, const
                             const double *col_fr, const double *row_q, double a4r, double f0, double inv_gap, int taps,
                             cudaStream_t s) {
     const size_t smem = wk_stolt_smem(NR);
-    cudaError_t e = cudaFuncSetAttribute(wk_stolt_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaError_t e = allow_dynamic_smem(reinterpret_cast<const void *>(wk_stolt_kernel));
     if (e != cudaSuccess) return e;
     wk_stolt_kernel<<<NA, kStoltThreads, smem, s>>>(in, out, NR, col_f2, col_ph, col_fr, row_q, a4r, f0, inv_gap, taps);
     return cudaGetLastError();
