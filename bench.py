@@ -820,12 +820,29 @@ def serve_measure(rates=(20.0, 40.0), jobs=30, n_req=12, step_updates=(1 << 32,)
     ctx.close()
     torch.cuda.empty_cache()
     one_shot = serve_one_shot(reqs)
+    h2d = pinned_h2d_gbs()
     sweep = serve_sweep(reqs, list(rates), jobs, schedule_names(step_updates), one_shot)
     del reqs
     return {"metric": "serving p50/p99 latency (ms) and aggregate Gpix*pulse/s", "mode": "split",
             "workload": SERVE_WORKLOAD + f"; {n_req} distinct requests drawn at random, {jobs} jobs per rate",
             "server": {"max_jobs": 16, "hbm_budget_gb": 96, "graphs": True}, "sweep": sweep,
-            "seconds": time.perf_counter() - t0}
+            "pinned_h2d_gbs": h2d, "seconds": time.perf_counter() - t0}
+
+
+def pinned_h2d_gbs(nbytes=256 << 20, reps=10):
+    """This host's pinned host-to-device copy rate (the path every served echo
+    takes), one 256 MiB copy at a time after three warm-up copies."""
+    import torch
+    x = torch.empty(nbytes, dtype=torch.uint8, pin_memory=True)
+    d = torch.empty(nbytes, dtype=torch.uint8, device="cuda")
+    for _ in range(3):
+        d.copy_(x, non_blocking=True)
+    torch.cuda.synchronize()
+    t = time.perf_counter()
+    for _ in range(reps):
+        d.copy_(x, non_blocking=True)
+    torch.cuda.synchronize()
+    return reps * nbytes / (time.perf_counter() - t) / 1e9
 
 
 def run_serve(args):
