@@ -54,7 +54,9 @@ __device__ __forceinline__ float block_sum(float v, float *red) {
     return t;  // valid in thread 0
 }
 
-template <int N, int T>
+// SCALE: also the per-pulse bound sum_k |Y[k]| and the FP16 storage scale
+// from it (complex16 rows only).
+template <int N, int T, bool SCALE>
 __global__ void __launch_bounds__(T, (fft_min_blocks<N, T>())) rc_forward_kernel(int ns, int L, const float2 *__restrict__ echo,
                                                        const float2 *__restrict__ filt,
                                                        const float2 *__restrict__ etab,
@@ -81,10 +83,11 @@ __global__ void __launch_bounds__(T, (fft_min_blocks<N, T>())) rc_forward_kernel
     fft_io<N, T, false>(sm, E, v, [&](int k, float2 x) {
         const float2 y = cmul(x, __ldg(&filt[k]));
         out[k] = y;
-        acc += sqrtf(fmaf(y.x, y.x, y.y * y.y));
+        if constexpr (SCALE) acc += sqrtf(fmaf(y.x, y.x, y.y * y.y));
     });
+    if constexpr (!SCALE) return;
     const float bound = block_sum<T>(acc, red);
-    if (threadIdx.x == 0 && scale) {
+    if (threadIdx.x == 0) {
         // power-of-two scale so that stored FP16 magnitudes stay <= 2^14
         float sc = 1.f;
         if (bound > 0.f && isfinite(bound)) sc = exp2f(ceilf(log2f(bound) - 14.f));
@@ -306,7 +309,8 @@ cudaError_t fwd_n(const RcPlan &p, const float2 *echo, const float2 *filt, const
                   float2 *spec, float *scale, cudaStream_t s) {
     constexpr int T = threads_for<N>();
     const size_t smem = sizeof(float2) * N + kTabSmem;
-    auto k = rc_forward_kernel<N, T>;
+    // the FP16 scale only for complex16 rows (a scale array is ignored otherwise)
+    auto k = p.storage == SARBP_STORE_C32H ? rc_forward_kernel<N, T, true> : rc_forward_kernel<N, T, false>;
     cudaError_t e = allow_dynamic_smem(reinterpret_cast<const void *>(k));
     if (e != cudaSuccess || t_prepare) return e;
     k<<<p.np, T, smem, s>>>(p.ns, p.L, echo, filt, etab, spec, scale);
