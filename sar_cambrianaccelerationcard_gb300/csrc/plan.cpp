@@ -99,9 +99,13 @@ void bp_extremes_host(const double *apc, int np, const sarbp_grid &g, BpExtremes
     ext_axes(g, &lux, &luy);
     double P[kLattice * kLattice][3];
     for (int k = 0; k < kLattice * kLattice; ++k) ext_lattice(g, k / kLattice, k % kLattice, P[k]);
-    auto run = [&](int p0, int p1, ExtAcc &acc, unsigned &bad) {
+    // each thread accumulates in its own stack copy and stores it once: the
+    // threads' slots of `acc` share cache lines, and updating them per point
+    // cost 2-4x in false sharing (4096 pulses on 4 threads: 3.2 against 0.9 ms)
+    auto run = [&](int p0, int p1, ExtAcc &out, unsigned &bad_out) {
+        ExtAcc acc;
         ext_acc_init(acc);
-        bad = 0;
+        unsigned bad = 0;
         for (int i = p0; i < p1; ++i) {
             const double *a = apc + 3 * (size_t)i;
             if (!std::isfinite(a[0]) || !std::isfinite(a[1]) || !std::isfinite(a[2])) {
@@ -110,6 +114,8 @@ void bp_extremes_host(const double *apc, int np, const sarbp_grid &g, BpExtremes
             }
             for (int k = 0; k < kLattice * kLattice; ++k) ext_acc_point(acc, g, lux, luy, P[k], a);
         }
+        out = acc;
+        bad_out = bad;
     };
     const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
     const int nt = (int)std::min<long long>(std::min<unsigned>(hw, 8u), std::max(1, np / 1024));
