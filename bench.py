@@ -473,7 +473,7 @@ def run_ours(args):
     roofline_rc = {"bound": "hbm", "achieved": rc_bytes / (rc_ms * 1e-3) / 1e9 if rc_ms else None, "peak": hbm,
                    "unit": "GB/s", "frac": (rc_bytes / (rc_ms * 1e-3) / 1e9 / hbm) if (rc_ms and hbm) else None,
                    "traffic": MEASURED_TRAFFIC.get((args.size, args.mode), {}).get("rc"),
-                   "kernel": "rc_forward_kernel<16384,512> + rc_inverse_kernel<16384,512,0>", "ms": rc_ms}
+                   "kernel": "rc_forward_kernel<16384,512,false> + rc_inverse_kernel<16384,512,0>", "ms": rc_ms}
     if rc_ms and l2.get("rc"):
         bw = l2["rc"] / (rc_ms * 1e-3) / 1e9
         roofline_rc["l2"] = {"achieved": bw, "peak": L2_PEAK_GBS, "unit": "GB/s", "frac": bw / L2_PEAK_GBS,
