@@ -217,7 +217,7 @@ typedef struct sarbp_bp_plan_info {
     int32_t segments;        /* pulse segments the launch is split into */
     int32_t ctas_per_sm;     /* resident CTAs per SM of the chosen kernel */
     int32_t pulse_chunk;     /* pulses staged per chunk (16, 8 or 4: two CTAs per SM where it can) */
-    int32_t reserved;
+    int32_t linear_phase;    /* 1: the linear-term phase form (SPLIT / FP16STORE, large tiles) */
     uint64_t smem_bytes;     /* dynamic shared memory per CTA */
     double rmin, rmax;       /* nearest and farthest range, lattice x pulses (m) */
     double cos_x, cos_y;     /* largest |cosine| between line of sight and grid axis x, y */
@@ -538,14 +538,19 @@ int64_t sarbp_kernel_launches(const sarbp_ctx *ctx);
  *                               then lets every copy in flight land before it exits
  *   SARBP_DEBUG_DEVICE_FLAGS    (get only) device check bits of the last call
  *                               that reported any: 1 wait ran out, 2 index clamped,
- *                               8 staging window, 16 a copy did not land in the drain */
+ *                               8 staging window, 16 a copy did not land in the drain
+ *   SARBP_DEBUG_BP_LINEAR_PHASE  SPLIT / FP16STORE back-projection phase form:
+ *                               1 linear-term form, -1 series form, 0 the planner's
+ *                               choice (linear-term for tiles whose half-diagonal
+ *                               exceeds 12 m) */
 enum {
     SARBP_DEBUG_BP_CHUNK = 1,
     SARBP_DEBUG_BP_SEGMENTS = 2,
     SARBP_DEBUG_BP_CHECKED = 3,
     SARBP_DEBUG_WAIT_LIMIT_NS = 4,
     SARBP_DEBUG_WAIT_FAULT_CHUNK = 5,
-    SARBP_DEBUG_DEVICE_FLAGS = 6
+    SARBP_DEBUG_DEVICE_FLAGS = 6,
+    SARBP_DEBUG_BP_LINEAR_PHASE = 7
 };
 sarbp_status sarbp_debug_set(sarbp_ctx *ctx, int32_t key, int64_t value);
 sarbp_status sarbp_debug_get(sarbp_ctx *ctx, int32_t key, int64_t *value);

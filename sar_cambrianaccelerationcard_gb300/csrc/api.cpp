@@ -883,6 +883,7 @@ sarbp_status sarbp_bp_plan(sarbp_ctx *ctx, const sarbp_radar *radar, const sarbp
     out->segments = p.segments;
     out->ctas_per_sm = occ;
     out->pulse_chunk = p.chunk;
+    out->linear_phase = p.lin;
     out->smem_bytes = sarbp::bp_smem_bytes(p.storage, p.win, p.chunk);
     out->rmin = ex.rmin;
     out->rmax = ex.rmax;
@@ -1722,6 +1723,10 @@ sarbp_status sarbp_debug_set(sarbp_ctx *ctx, int32_t key, int64_t value) {
         case SARBP_DEBUG_WAIT_FAULT_CHUNK:
             t.wait_fault_chunk = value < 0 ? -1 : (int)std::min<int64_t>(value, 1 << 30);
             return SARBP_OK;
+        case SARBP_DEBUG_BP_LINEAR_PHASE:
+            if (value < -1 || value > 1) return fail(ctx, SARBP_ERR_INVALID_ARGUMENT, "linear phase must be -1, 0 or 1");
+            t.linear_phase = (int)value;
+            return SARBP_OK;
         default:
             return fail(ctx, SARBP_ERR_INVALID_ARGUMENT, "unknown debug key %d", (int)key);
     }
@@ -1737,6 +1742,7 @@ sarbp_status sarbp_debug_get(sarbp_ctx *ctx, int32_t key, int64_t *value) {
         case SARBP_DEBUG_WAIT_LIMIT_NS: *value = t.wait_ns; return SARBP_OK;
         case SARBP_DEBUG_WAIT_FAULT_CHUNK: *value = t.wait_fault_chunk; return SARBP_OK;
         case SARBP_DEBUG_DEVICE_FLAGS: *value = ctx->last_device_flags; return SARBP_OK;
+        case SARBP_DEBUG_BP_LINEAR_PHASE: *value = t.linear_phase; return SARBP_OK;
         default: return fail(ctx, SARBP_ERR_INVALID_ARGUMENT, "unknown debug key %d", (int)key);
     }
 }

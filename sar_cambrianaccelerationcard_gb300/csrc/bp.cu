@@ -40,6 +40,8 @@
 #include "ffloat.cuh"
 #include "tma.cuh"
 
+#include <cstddef>
+
 namespace sarbp {
 namespace {
 
@@ -85,6 +87,13 @@ struct __align__(16) Prm {
     float scale;   // FP16 storage scale
     int need;      // (M, d) pairs [0, need) any pixel of the tile reads (the rest are not converted)
 };
+
+// Linear-term split (LIN) kernels: the phase increments per pixel step,
+// (PX, PX, PY, PY), in the 16 bytes of the FP64-only ax, ay (offset 64,
+// 16-byte aligned), so the record keeps its size.
+__device__ __forceinline__ float4 &prm_k4(Prm &q) { return *reinterpret_cast<float4 *>(&q.ax); }
+__device__ __forceinline__ const float4 &prm_k4(const Prm &q) { return *reinterpret_cast<const float4 *>(&q.ax); }
+static_assert(offsetof(Prm, ax) % 16 == 0 && offsetof(Prm, az) - offsetof(Prm, ax) == 16, "k4 slot");
 
 __device__ __forceinline__ float4 lds128(unsigned addr) {
     float4 v;
@@ -203,7 +212,7 @@ __device__ __noinline__ void drain_after_timeout(const BpPlan &P, uint64_t *bars
 // one chunk.  Every warp arrives once on the stage's barrier.  `fault` (tests
 // only) arms warp 0's arrival with kFaultBytes that no copy delivers, so the
 // phase cannot complete and the consumers' bounded wait runs out.
-template <int MODE, int STORE, int PIX>
+template <int MODE, int STORE, int PIX, bool LIN = false>
 __device__ __forceinline__ void produce(const BpPlan &P, const Smem &S, int stage, int p0, int count,
                                         const TileGeo &T, bool fault) {
     constexpr int kTileY = 8 * PIX;
@@ -259,12 +268,34 @@ __device__ __forceinline__ void produce(const BpPlan &P, const Smem &S, int stag
                 const float c1 = 0.5f * iR, c2 = -0.125f * iR * i2, c3 = 0.0625f * iR * i2 * i2;
                 const float c4 = -0.0390625f * iR * i2 * i2 * i2;
                 const float bb = ((bT.h - (float)ws) + bT.l) - 0.5f - (float)cen;
-                q.k0 = make_float4(c1, c1, c2, c2);
-                q.k1 = make_float4(c3, c3, c4, c4);
-                q.k2 = make_float4(bb, bb, phT, phT);
-                q.k3 = make_float4(A, A, B, B);
+                if constexpr (LIN) {
+                    // the series in m = n / (2 R_T): dR = m + m^2 (d2 + m (d3 + m d4)), and
+                    // the phase's linear part from the increments per pixel step, half of
+                    // 4 pi / lambda (u.w) / R_T reduced modulo 2 pi in FP64 (the pixel
+                    // offsets are half-integers, 2 xc and 2 yc integers)
+                    const float d2 = -0.5f * iR, d3 = 0.5f * i2, d4 = -0.625f * i2 * iR;
+                    const double ax = __ldg(&P.apc[3 * p]), ay = __ldg(&P.apc[3 * p + 1]),
+                                 az = __ldg(&P.apc[3 * p + 2]);
+                    const double wx = T.pcx - ax, wy = T.pcy - ay, wz = T.pcz - az;
+                    const double kh = CUDART_PI * 2.0 * P.fc / P.c / sqrt(fma(wx, wx, fma(wy, wy, wz * wz)));
+                    const double px = kh * (P.g.ux[0] * wx + P.g.ux[1] * wy + P.g.ux[2] * wz);
+                    const double py = kh * (P.g.uy[0] * wx + P.g.uy[1] * wy + P.g.uy[2] * wz);
+                    const float pxr = (float)(px - 2.0 * CUDART_PI * rint(px * (0.5 / CUDART_PI)));
+                    const float pyr = (float)(py - 2.0 * CUDART_PI * rint(py * (0.5 / CUDART_PI)));
+                    q.k0 = make_float4(c1, c1, d2, d2);
+                    q.k1 = make_float4(d3, d3, d4, d4);
+                    q.k2 = make_float4(bb, bb, phT, phT);
+                    q.k3 = make_float4(A * c1, A * c1, B * c1, B * c1);
+                    prm_k4(q) = make_float4(pxr, pxr, pyr, pyr);
+                } else {
+                    q.k0 = make_float4(c1, c1, c2, c2);
+                    q.k1 = make_float4(c3, c3, c4, c4);
+                    q.k2 = make_float4(bb, bb, phT, phT);
+                    q.k3 = make_float4(A, A, B, B);
+                }
             } else {  // inert pulse: every pixel reads the centre bin of an all-zero window
                 q.k0 = q.k1 = q.k2 = q.k3 = make_float4(0.f, 0.f, 0.f, 0.f);
+                if constexpr (LIN) prm_k4(q) = make_float4(0.f, 0.f, 0.f, 0.f);
             }
         } else {
             const double ax = __ldg(&P.apc[3 * p]), ay = __ldg(&P.apc[3 * p + 1]), az = __ldg(&P.apc[3 * p + 2]);
@@ -508,10 +539,13 @@ __device__ __forceinline__ void project_chunk(const Smem &S, int stage, int coun
 // TESTF: the waits take their limit from P.wait_ns and P.fault_chunk arms one
 // chunk's barrier so that its wait runs out (tests of the timeout path, through
 // sarbp_debug_set); production variants wait 2 s and carry no injector.
-template <int MODE, int STORE, int NTERMS, bool CHECKED, int PIX, bool ADJ = false, int CHUNK = 0, bool TESTF = false>
+template <int MODE, int STORE, int NTERMS, bool CHECKED, int PIX, bool ADJ = false, int CHUNK = 0, bool TESTF = false,
+          bool LIN = false>
 __global__ void __launch_bounds__(kThreads, SARBP_BP_MINBLOCKS)
     bp_kernel(const __grid_constant__ BpPlan P, int tiles_y, int pulses_per_seg, float qq_max) {
     static_assert(!ADJ || MODE == SARBP_MODE_SPLIT || MODE == SARBP_MODE_FP16STORE, "projection: split arithmetic");
+    static_assert(!LIN || (!ADJ && (MODE == SARBP_MODE_SPLIT || MODE == SARBP_MODE_FP16STORE)),
+                  "linear-term phase: split back-projection only");
     constexpr int kPix = PIX;  // pixels per thread, all in one column
     constexpr int kTileY = 8 * PIX;
     extern __shared__ __align__(128) unsigned char smem_raw[];
@@ -604,16 +638,18 @@ __global__ void __launch_bounds__(kThreads, SARBP_BP_MINBLOCKS)
 
     const f2 XC2 = pk2(xc, xc);
     const f2 BPM2 = pk2(bpm, bpm), KH2 = pk2(kph_hi, kph_hi), KL2 = pk2(kph_lo, kph_lo);
-    f2 YC2[kPix / 2], QQ2[kPix / 2], TH2[ADJ ? kPix / 2 : 1];
+    f2 YC2[kPix / 2], QQ2[kPix / 2], TH2[ADJ ? kPix / 2 : 1], Y2C2[LIN ? kPix / 2 : 1];
 #pragma unroll
     for (int h = 0; h < kPix / 2; ++h) {
         YC2[h] = pk2(yc[2 * h], yc[2 * h + 1]);
         QQ2[h] = pk2(qq[2 * h], qq[2 * h + 1]);
         if constexpr (ADJ) TH2[h] = pk2(wth[2 * h], wth[2 * h + 1]);
+        if constexpr (LIN) Y2C2[h] = pk2(2.f * yc[2 * h], 2.f * yc[2 * h + 1]);
     }
+    const f2 X2C2 = pk2(2.f * xc, 2.f * xc);
 
     if (nchunks > 0)
-        produce<MODE, STORE, PIX>(P, S, 0, p_begin, min(chunk, p_end - p_begin), T, TESTF && P.fault_chunk == 0);
+        produce<MODE, STORE, PIX, LIN>(P, S, 0, p_begin, min(chunk, p_end - p_begin), T, TESTF && P.fault_chunk == 0);
 
     bool failed = false;
     bool clamped = false;
@@ -626,7 +662,7 @@ __global__ void __launch_bounds__(kThreads, SARBP_BP_MINBLOCKS)
         const int count = min(chunk, p_end - pc0);
         if (c + 1 < nchunks) {
             const int pn = pc0 + chunk;
-            produce<MODE, STORE, PIX>(P, S, (c + 1) % kStages, pn, min(chunk, p_end - pn), T,
+            produce<MODE, STORE, PIX, LIN>(P, S, (c + 1) % kStages, pn, min(chunk, p_end - pn), T,
                                       TESTF && P.fault_chunk == c + 1);
         }
         const bool ok =
@@ -655,6 +691,65 @@ __global__ void __launch_bounds__(kThreads, SARBP_BP_MINBLOCKS)
         if constexpr (ADJ) {
             project_chunk<NTERMS, kPix>(S, stage, count, win, sbase, cen, XC2, YC2, QQ2, BPM2, KH2, KL2, TH2, wm,
                                   reinterpret_cast<float *>(S.red + ((c & 1) * kWarps + warp) * kChunk));
+        } else if (LIN && (MODE == SARBP_MODE_SPLIT || MODE == SARBP_MODE_FP16STORE)) {
+            // linear-term form (large tiles): m = n / (2 R_T) centred offset, bin from
+            // dR = m + m^2 poly(m), phase from the increments per pixel step (reduced
+            // modulo 2 pi per pulse) plus 4 pi / lambda times the nonlinear remainder
+            // qq c1 + m^2 poly(m), so no FP32 quantity of the size of the tile's
+            // extent enters the phase
+            f2 MP = pk2(kMagic + (float)cen, kMagic + (float)cen);
+            const f2 WIN2 = pk2((float)win, (float)win);
+#pragma unroll kPulseUnroll
+            for (int pl = 0; pl < count; ++pl) {
+                const Prm &q = S.prm[stage * kChunk + pl];
+                f2 C1, D2, D3, D4, BT, PHT, AP, BP, PX, PY;
+                lds2x2(&q.k0, C1, D2);
+                lds2x2(&q.k1, D3, D4);
+                lds2x2(&q.k2, BT, PHT);
+                lds2x2(&q.k3, AP, BP);
+                lds2x2(&prm_k4(q), PX, PY);
+                const f2 XAP = fmul2(XC2, AP);
+                const f2 PHX = ffma2(X2C2, PX, PHT);
+#pragma unroll
+                for (int h = 0; h < kPix / 2; ++h) {
+                    const f2 qc = fmul2(QQ2[h], C1);
+                    const f2 m = ffma2(YC2[h], BP, fadd2(XAP, qc));
+                    const f2 m2 = fmul2(m, m);
+                    const f2 poly = NTERMS == 4 ? ffma2(m, ffma2(m, D4, D3), D2) : ffma2(m, D3, D2);
+                    const f2 dR = ffma2(m2, poly, m);
+                    f2 b2 = ffma2(dR, BPM2, BT);  // bin positions relative to the window middle
+                    const f2 nl = ffma2(m2, poly, qc);
+                    const f2 ph2 = ffma2(nl, KH2, ffma2(Y2C2[h], PY, PHX));
+                    float bb[2], ph[2];
+                    upk2(b2, bb[0], bb[1]);
+                    upk2(ph2, ph[0], ph[1]);
+                    if (CHECKED) {
+                        const float needf = (float)(q.need - 2) - cenf;
+#pragma unroll
+                        for (int u = 0; u < 2; ++u) {
+                            const float bc = fminf(fmaxf(bb[u], -cenf), wmax - cenf);
+                            clamped |= !(bc == bb[u]) || bb[u] > needf;
+                            bb[u] = bc;
+                        }
+                        b2 = pk2(bb[0], bb[1]);
+                    }
+                    const f2 t2 = fadd2(b2, MP);
+                    float tt[2];
+                    upk2(t2, tt[0], tt[1]);
+#pragma unroll
+                    for (int u = 0; u < 2; ++u) {
+                        const int j = 2 * h + u;
+                        const float4 v = lds128((__float_as_uint(tt[u]) << 4) + sbase);
+                        const float sr = fmaf(bb[u], v.z, v.x);
+                        const float si = fmaf(bb[u], v.w, v.y);
+                        float sn, cs;
+                        __sincosf(ph[u], &sn, &cs);
+                        acc_r[j] = fmaf(sr, cs, fmaf(-si, sn, acc_r[j]));
+                        acc_i[j] = fmaf(sr, sn, fmaf(si, cs, acc_i[j]));
+                    }
+                }
+                MP = fadd2(MP, WIN2);
+            }
         } else if (MODE == SARBP_MODE_SPLIT || MODE == SARBP_MODE_FP16STORE) {
             // geometry, bin and phase for pixel pairs (2j, 2j+1) in packed FP32x2;
             // interpolation and the complex accumulate per pixel
@@ -825,10 +920,11 @@ __global__ void reduce_segments_kernel(const float2 *__restrict__ partial, int s
 // resident CTAs per SM there instead of launching it.
 thread_local int *t_occupancy = nullptr;
 
-template <int MODE, int STORE, int NTERMS, bool CHECKED, int PIX, bool ADJ = false, int CHUNK = 0, bool TESTF = false>
+template <int MODE, int STORE, int NTERMS, bool CHECKED, int PIX, bool ADJ = false, int CHUNK = 0, bool TESTF = false,
+          bool LIN = false>
 cudaError_t launch_variant(const BpPlan &p, cudaStream_t s, int tiles, int tiles_y, int pps, float qq_max) {
     if (CHUNK && p.chunk != CHUNK) return cudaErrorInvalidValue;
-    auto k = bp_kernel<MODE, STORE, NTERMS, CHECKED, PIX, ADJ, CHUNK, TESTF>;
+    auto k = bp_kernel<MODE, STORE, NTERMS, CHECKED, PIX, ADJ, CHUNK, TESTF, LIN>;
     const size_t smem = bp_smem_bytes(STORE, p.win, p.chunk);
     cudaError_t e = allow_dynamic_smem(reinterpret_cast<const void *>(k));
     if (e != cudaSuccess) return e;
@@ -840,6 +936,13 @@ cudaError_t launch_variant(const BpPlan &p, cudaStream_t s, int tiles, int tiles
 
 template <int MODE, int STORE, int PIX>
 cudaError_t launch_split(const BpPlan &p, cudaStream_t s, int tiles, int tiles_y, int pps, float qq_max) {
+    if (p.lin) {  // large tiles: the linear-term phase (runtime pulse chunk)
+        if (p.checked)
+            return p.nterms == 3 ? launch_variant<MODE, STORE, 3, true, PIX, false, 0, false, true>(p, s, tiles, tiles_y, pps, qq_max)
+                                 : launch_variant<MODE, STORE, 4, true, PIX, false, 0, false, true>(p, s, tiles, tiles_y, pps, qq_max);
+        return p.nterms == 3 ? launch_variant<MODE, STORE, 3, false, PIX, false, 0, false, true>(p, s, tiles, tiles_y, pps, qq_max)
+                             : launch_variant<MODE, STORE, 4, false, PIX, false, 0, false, true>(p, s, tiles, tiles_y, pps, qq_max);
+    }
     if (p.checked)
         return p.nterms == 3 ? launch_variant<MODE, STORE, 3, true, PIX>(p, s, tiles, tiles_y, pps, qq_max)
                              : launch_variant<MODE, STORE, 4, true, PIX>(p, s, tiles, tiles_y, pps, qq_max);

@@ -196,6 +196,7 @@ bool plan_bp(int sms, const sarbp_radar &r, const sarbp_rc_view &rc, const BpExt
     // falls as R_T grows, so the remainder is largest at the nearest tile centre
     // (rmin_tile); x1.1 covers the terms past the first omitted one (|e| < 0.09).
     constexpr double kSeriesTol = 5e-7;  // 1.1e-4 rad of C-band phase at the tile corners
+    constexpr double kLinearPhaseHalfDiag = 12.0;  // m: tiles beyond it take the linear-term phase
     why = "no tile size fits";
     bool chosen = false;
 #ifdef SARBP_BP_FORCE_PIX
@@ -236,6 +237,12 @@ bool plan_bp(int sms, const sarbp_radar &r, const sarbp_rc_view &rc, const BpExt
         p.win = win;
         p.chunk = chunk;
         p.nterms = (1.1 * rt * 0.0390625 * e * e * e * e < kSeriesTol) ? 3 : 4;
+        // phase form: the series form's FP32 differential range rounds to 2^-24 of
+        // n ~ 2 R_T d, a phase error growing with the tile's extent d (about
+        // -82 dB below 12 m of half-diagonal, -67 to -74 dB above); the
+        // linear-term form keeps it near -100 dB for ~10% more time
+        const int force = tune ? tune->linear_phase : 0;
+        p.lin = split && (force > 0 || (force == 0 && tile_diag > kLinearPhaseHalfDiag));
         chosen = true;
         break;
     }

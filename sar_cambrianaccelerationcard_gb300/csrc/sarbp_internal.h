@@ -34,6 +34,7 @@ struct Tuning {
     int bp_segments = 0;           // pulse segments (1..64); 0: planner
     int checked = 0;               // 1: clamped, self-reporting back-projection kernels
     long long wait_ns = 0;         // limit of the staging waits; 0: 2 s
+    int linear_phase = 0;          // 1 / -1: force the linear-term / series phase form; 0: planner
     int wait_fault_chunk = -1;     // >= 0: that chunk's staging barrier of every CTA is armed with
                                    // kFaultBytes more than its copies deliver (the wait runs out); the
                                    // drain then delivers them, as a late copy would
@@ -127,6 +128,7 @@ struct BpPlan {
     int accumulate;
     int win;                 // staged bins per (tile, pulse), multiple of 4
     int nterms;              // polynomial terms for the differential range (3 or 4)
+    int lin;                 // 1: linear-term phase (SPLIT / FP16STORE back-projection, large tiles)
     int checked;             // 1: clamp every interpolation index and report clamps
     int pix;                 // pixels per thread (8, 4 or 2): tiles of 32 x (8 pix) pixels
     int chunk;               // pulses per staged chunk (16, 8 or 4)

@@ -106,7 +106,7 @@ class RcView(ctypes.Structure):
 class BpPlanInfo(ctypes.Structure):
     _fields_ = [("tile_x", ctypes.c_int32), ("tile_y", ctypes.c_int32), ("window", ctypes.c_int32),
                 ("series_terms", ctypes.c_int32), ("segments", ctypes.c_int32), ("ctas_per_sm", ctypes.c_int32),
-                ("pulse_chunk", ctypes.c_int32), ("reserved", ctypes.c_int32), ("smem_bytes", ctypes.c_uint64), ("rmin", ctypes.c_double), ("rmax", ctypes.c_double),
+                ("pulse_chunk", ctypes.c_int32), ("linear_phase", ctypes.c_int32), ("smem_bytes", ctypes.c_uint64), ("rmin", ctypes.c_double), ("rmax", ctypes.c_double),
                 ("cos_x", ctypes.c_double), ("cos_y", ctypes.c_double)]
 
 
@@ -240,6 +240,7 @@ DEBUG_BP_CHECKED = 3
 DEBUG_WAIT_LIMIT_NS = 4
 DEBUG_WAIT_FAULT_CHUNK = 5
 DEBUG_DEVICE_FLAGS = 6
+DEBUG_BP_LINEAR_PHASE = 7
 SERVER_DEBUG_FAIL_ADMIT_TICKET = 1
 
 ABI_VERSION = 2  # SARBP_ABI_VERSION of the include/sarbp.h these bindings follow

@@ -257,3 +257,55 @@ def test_weighted_projection_on_random_geometries(contexts, orc, seed):
     print(s.name, f"projection vs oracle {err:.1f} dB, adjoint mismatch {abs(lhs - out.sum()) / abs(lhs):.1e}")
     assert err <= -60.0
     assert abs(lhs - out.sum()) <= 1e-3 * abs(lhs)
+
+
+def _plan(ctx, s, mode=sarbp.MODE_SPLIT):
+    r, g, lay = sarbp.scene_args(s)
+    v = sarbp.RcView()
+    v.data, v.scale, v.storage, v.np, v.nbins = None, None, sarbp.STORE_C64, s.np_, lay.nbins
+    v.t0_bins, v.bin_rate = lay.t0_bins, lay.bin_rate
+    return ctx.bp_plan(r, v, s.apc, g, mode)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("seed", [3, 5, 11])
+def test_linear_phase_form_on_large_tiles(orc, seed):
+    """Tiles with half-diagonals beyond 12 m (0.61-1.46 m pixels): the series
+    form's FP32 differential range costs phase accuracy in proportion to the
+    tile's extent; the linear-term form (phase increments per pixel step
+    reduced modulo 2 pi per pulse, FP32 only for the nonlinear remainder) does
+    not.  The planner picks it there; forced either way, both stay within the
+    -60 dB target and the linear-term form is at least 10 dB closer to the
+    oracle."""
+    s = random_scene(seed)
+    e64 = orc.echo(s).astype(np.complex64)
+    ref = orc.image(s, e64.astype(np.complex128))
+    errs, forms = {}, {}
+    for form in (-1, 1, 0):
+        with sarbp.Context(0) as ctx:
+            ctx.debug_set(sarbp.DEBUG_BP_LINEAR_PHASE, form)
+            forms[form] = _plan(ctx, s).linear_phase
+            errs[form] = metrics.rel_l2_db(sarbp.image_scene(ctx, s, e64, sarbp.MODE_SPLIT), ref)
+    print(s.name, "series", f"{errs[-1]:.1f}", "linear-term", f"{errs[1]:.1f}", "planner", f"{errs[0]:.1f} dB")
+    assert forms == {-1: 0, 1: 1, 0: 1}
+    assert errs[-1] <= -60.0 and errs[1] <= -60.0
+    assert errs[1] <= errs[-1] - 10.0
+    assert errs[0] == errs[1]
+
+
+@pytest.mark.gpu
+def test_linear_phase_form_on_config2_tiles(orc):
+    """Config 2's geometry (0.25 m pixels, 8.8 m half-diagonal tiles) keeps the
+    series form; forced to the linear-term form it is at least as accurate."""
+    s = scenes.config2(np_=512, n_img=256)
+    s.targets = scenes.isolated_targets(s.grid, seed=21)
+    e64 = orc.echo(s).astype(np.complex64)
+    ref = orc.image(s, e64.astype(np.complex128))
+    errs = {}
+    for form in (0, 1):
+        with sarbp.Context(0) as ctx:
+            ctx.debug_set(sarbp.DEBUG_BP_LINEAR_PHASE, form)
+            assert _plan(ctx, s).linear_phase == form
+            errs[form] = metrics.rel_l2_db(sarbp.image_scene(ctx, s, e64, sarbp.MODE_SPLIT), ref)
+    print("config-2 geometry: series", f"{errs[0]:.1f}", "linear-term", f"{errs[1]:.1f} dB")
+    assert errs[0] <= -75.0 and errs[1] <= errs[0] + 1.0

@@ -94,11 +94,13 @@ def test_projection_wait_runs_out(case):
 def test_debug_switches_validate_and_read_back():
     with sarbp.Context(0) as ctx:
         for key, bad in ((sarbp.DEBUG_BP_CHUNK, 5), (sarbp.DEBUG_BP_SEGMENTS, 65), (sarbp.DEBUG_WAIT_LIMIT_NS, -1),
-                         (99, 0)):
+                         (sarbp.DEBUG_BP_LINEAR_PHASE, 2), (99, 0)):
             with pytest.raises(sarbp.SarbpError) as e:
                 ctx.debug_set(key, bad)
             assert e.value.status == sarbp.ERR_INVALID_ARGUMENT
         ctx.debug_set(sarbp.DEBUG_BP_CHUNK, 8)
         assert ctx.debug_get(sarbp.DEBUG_BP_CHUNK) == 8
         assert ctx.debug_get(sarbp.DEBUG_WAIT_FAULT_CHUNK) == -1
+        ctx.debug_set(sarbp.DEBUG_BP_LINEAR_PHASE, -1)
+        assert ctx.debug_get(sarbp.DEBUG_BP_LINEAR_PHASE) == -1
         assert ctx.debug_get(sarbp.DEBUG_DEVICE_FLAGS) == 0
