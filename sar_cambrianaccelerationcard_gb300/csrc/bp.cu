@@ -271,17 +271,18 @@ __device__ __forceinline__ void produce(const BpPlan &P, const Smem &S, int stag
                 if constexpr (LIN) {
                     // the series in m = n / (2 R_T): dR = m + m^2 (d2 + m (d3 + m d4)), and
                     // the phase's linear part from the increments per pixel step, half of
-                    // 4 pi / lambda (u.w) / R_T reduced modulo 2 pi in FP64 (the pixel
-                    // offsets are half-integers, 2 xc and 2 yc integers)
+                    // 4 pi / lambda (u.w) / R_T reduced modulo 2 pi (the pixel offsets are
+                    // half-integers, 2 xc and 2 yc integers), in float-float:
+                    // u.w = a1 / 2 + xT g11 + yT g12 (x), a2 / 2 + xT g12 + yT g22 (y),
+                    // 1 / R_T from iR and one Newton correction
                     const float d2 = -0.5f * iR, d3 = 0.5f * i2, d4 = -0.625f * i2 * iR;
-                    const double ax = __ldg(&P.apc[3 * p]), ay = __ldg(&P.apc[3 * p + 1]),
-                                 az = __ldg(&P.apc[3 * p + 2]);
-                    const double wx = T.pcx - ax, wy = T.pcy - ay, wz = T.pcz - az;
-                    const double kh = CUDART_PI * 2.0 * P.fc / P.c / sqrt(fma(wx, wx, fma(wy, wy, wz * wz)));
-                    const double px = kh * (P.g.ux[0] * wx + P.g.ux[1] * wy + P.g.ux[2] * wz);
-                    const double py = kh * (P.g.uy[0] * wx + P.g.uy[1] * wy + P.g.uy[2] * wz);
-                    const float pxr = (float)(px - 2.0 * CUDART_PI * rint(px * (0.5 / CUDART_PI)));
-                    const float pyr = (float)(py - 2.0 * CUDART_PI * rint(py * (0.5 / CUDART_PI)));
+                    const ff g11 = {P.gf11, P.gf11l}, g12 = {P.gf12, P.gf12l}, g22 = {P.gf22, P.gf22l};
+                    const ff uxw = ff_add(ff{0.5f * a1.h, 0.5f * a1.l}, ff_add(ff_mul_f(g11, T.xT), ff_mul_f(g12, T.yT)));
+                    const ff uyw = ff_add(ff{0.5f * a2.h, 0.5f * a2.l}, ff_add(ff_mul_f(g12, T.xT), ff_mul_f(g22, T.yT)));
+                    const ff invR = quick_two_sum(iR, iR * (fmaf(-r, iR, 1.f) - corr * iR));
+                    const ff kh = {0.5f * P.kp_h, 0.5f * P.kp_l};  // 2 pi fc / c
+                    const float pxr = ff_mod_2pi(ff_mul(ff_mul(kh, uxw), invR));
+                    const float pyr = ff_mod_2pi(ff_mul(ff_mul(kh, uyw), invR));
                     q.k0 = make_float4(c1, c1, d2, d2);
                     q.k1 = make_float4(d3, d3, d4, d4);
                     q.k2 = make_float4(bb, bb, phT, phT);

@@ -36,5 +36,13 @@ __device__ __forceinline__ ff ff_mul(ff a, ff b) {
     return quick_two_sum(p, e + fmaf(a.h, b.l, a.l * b.h));
 }
 
+// v modulo 2 pi, in [-pi, pi], rounded to float (2 pi as a float pair).
+__device__ __forceinline__ float ff_mod_2pi(ff v) {
+    const ff twopi = {6.28318548202514648f, -1.7484555314695172e-07f};
+    const float n = rintf(v.h * 0.159154943091895336f);
+    const ff r = ff_add(v, ff_mul_f(twopi, -n));
+    return r.h + r.l;
+}
+
 }  // namespace
 }  // namespace sarbp

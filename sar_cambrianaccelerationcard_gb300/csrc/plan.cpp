@@ -178,9 +178,9 @@ bool plan_bp(int sms, const sarbp_radar &r, const sarbp_rc_view &rc, const BpExt
     split2(rc.t0_bins * rc.bin_rate, &p.tb_h, &p.tb_l);
     split2(2.0 * r.fc / r.c, &p.kc_h, &p.kc_l);
     split2(4.0 * 3.141592653589793 * r.fc / r.c, &p.kp_h, &p.kp_l);
-    p.gf11 = (float)p.g.g11;
-    p.gf12 = (float)p.g.g12;
-    p.gf22 = (float)p.g.g22;
+    split2(p.g.g11, &p.gf11, &p.gf11l);
+    split2(p.g.g12, &p.gf12, &p.gf12l);
+    split2(p.g.g22, &p.gf22, &p.gf22l);
 
     const double lux = std::sqrt(p.g.g11), luy = std::sqrt(p.g.g22);
     double cx = ex.cx, sy = ex.sy;

@@ -122,6 +122,7 @@ struct BpPlan {
     // FP64 division or conversion
     float kp_h, kp_l;
     float gf11, gf12, gf22;
+    float gf11l, gf12l, gf22l;     // their float-float low parts (linear-term phase increments)
     float2 *image;           // [ny][nx] final image
     float2 *partial;         // [segments][ny][nx] scratch when segments > 1
     int segments;            // pulse segments (1: write image directly)
