@@ -68,10 +68,12 @@ typedef enum sarbp_mode {
  * (1.1e-4 rad at C band).  When even 32 x 16 does not, the call returns
  * SARBP_ERR_UNSUPPORTED ("tiles too large for the differential-range series"):
  * pixel spacings above about 1.4 m at 2 km slant range, 2.9 m at 5 km, 5 m at
- * 10 km.  SARBP_MODE_FP64 images any geometry.  Their error against an FP64
- * image grows with the tile's extent along the line of sight (FP32 rounding of
- * the differential range): about -82 dB with 0.25-0.4 m pixels, -67 to -74 dB
- * with 0.45-2 m pixels. */
+ * 10 km.  SARBP_MODE_FP64 images any geometry.  Tiles up to 12 m of
+ * half-diagonal use the series form of the phase (about -82 dB against an FP64
+ * image); larger ones the linear-term form (per-pixel-step phase increments
+ * reduced modulo 2 pi per pulse, FP32 only for the nonlinear remainder: -89 to
+ * -113 dB on 0.45-2 m pixels, about 12% more time); sarbp_bp_plan reports the
+ * form (linear_phase). */
 
 /* Storage of range-compressed data. */
 typedef enum sarbp_storage {
