@@ -65,10 +65,13 @@ typedef enum sarbp_mode {
 } sarbp_mode;
 /* SPLIT and FP16STORE image with tiles of 32 x 64, 32 x 32 or 32 x 16 pixels,
  * the tallest whose differential-range series remainder stays below 5e-7 m
- * (1.1e-4 rad at C band).  When even 32 x 16 does not, the call returns
- * SARBP_ERR_UNSUPPORTED ("tiles too large for the differential-range series"):
- * pixel spacings above about 1.4 m at 2 km slant range, 2.9 m at 5 km, 5 m at
- * 10 km.  SARBP_MODE_FP64 images any geometry.  Tiles up to 12 m of
+ * (1.1e-4 rad at C band) and whose staging window fits shared memory.  When
+ * even 32 x 16 does not, the call returns SARBP_ERR_UNSUPPORTED with the bound
+ * that failed: for grids at 45 degrees to the track, pixel spacings above about
+ * 1.4 m at 2 km slant range or 2.9 m at 5 km (the series bound, which
+ * SARBP_MODE_FP64 does not have), 5 m at 10 km (the staging-window bound,
+ * common to every mode: the smallest tile spans more range bins than a
+ * 4-pulse chunk stages in 227 KB).  Tiles up to 12 m of
  * half-diagonal use the series form of the phase (about -82 dB against an FP64
  * image); larger ones the linear-term form (per-pixel-step phase increments
  * reduced modulo 2 pi per pulse, FP32 only for the nonlinear remainder: -89 to
