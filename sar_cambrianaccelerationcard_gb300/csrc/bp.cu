@@ -937,10 +937,13 @@ cudaError_t launch_variant(const BpPlan &p, cudaStream_t s, int tiles, int tiles
 
 template <int MODE, int STORE, int PIX>
 cudaError_t launch_split(const BpPlan &p, cudaStream_t s, int tiles, int tiles_y, int pps, float qq_max) {
-    if (p.lin) {  // large tiles: the linear-term phase (runtime pulse chunk)
+    if (p.lin) {  // large tiles: the linear-term phase
         if (p.checked)
             return p.nterms == 3 ? launch_variant<MODE, STORE, 3, true, PIX, false, 0, false, true>(p, s, tiles, tiles_y, pps, qq_max)
                                  : launch_variant<MODE, STORE, 4, true, PIX, false, 0, false, true>(p, s, tiles, tiles_y, pps, qq_max);
+        if (p.chunk == kChunk)
+            return p.nterms == 3 ? launch_variant<MODE, STORE, 3, false, PIX, false, kChunk, false, true>(p, s, tiles, tiles_y, pps, qq_max)
+                                 : launch_variant<MODE, STORE, 4, false, PIX, false, kChunk, false, true>(p, s, tiles, tiles_y, pps, qq_max);
         return p.nterms == 3 ? launch_variant<MODE, STORE, 3, false, PIX, false, 0, false, true>(p, s, tiles, tiles_y, pps, qq_max)
                              : launch_variant<MODE, STORE, 4, false, PIX, false, 0, false, true>(p, s, tiles, tiles_y, pps, qq_max);
     }

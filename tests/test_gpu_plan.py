@@ -163,11 +163,13 @@ def test_wide_windows_keep_two_ctas(ctx, case, storage, chunk):
     assert info.ctas_per_sm == 2
 
 
+@pytest.mark.parametrize("form", [-1, 1], ids=["series", "linear"])
 @pytest.mark.parametrize("storage", [sarbp.STORE_C64, sarbp.STORE_C32H])
-def test_chunk_size_does_not_change_results(ctx, storage):
+def test_chunk_size_does_not_change_results(ctx, storage, form):
     """Pixels accumulate pulses in the same order whatever the staging chunk, so
-    16-, 8- and 4-pulse chunks give the same bits (back-projection and the
-    weighted projection; 300 pulses: ragged last chunks)."""
+    16-, 8- and 4-pulse chunks give the same bits (back-projection in both phase
+    forms, 16-pulse chunks compiled in; the weighted projection; 300 pulses:
+    ragged last chunks)."""
     s = scenes.config1(np_=300, ns=1024, n_img=96)
     r, g, lay = sarbp.scene_args(s)
     echo = sarbp.synthesize(ctx, s)
@@ -177,13 +179,16 @@ def test_chunk_size_does_not_change_results(ctx, storage):
     w = (np.random.default_rng(4).standard_normal((g.ny, g.nx)) + 0j).astype(np.complex64)
     imgs, projs = {}, {}
     try:
+        ctx.debug_set(sarbp.DEBUG_BP_LINEAR_PHASE, form)
         for c in ("16", "8", "4"):
             ctx.debug_set(sarbp.DEBUG_BP_CHUNK, int(c))
-            assert ctx.bp_plan(r, view(s, storage), s.apc, g, mode).pulse_chunk == int(c)
+            info = ctx.bp_plan(r, view(s, storage), s.apc, g, mode)
+            assert info.pulse_chunk == int(c) and info.linear_phase == (1 if form > 0 else 0)
             imgs[c] = ctx.backproject(r, data, s.apc, g, mode, lay.t0_bins, lay.bin_rate, scale=scale)
             projs[c] = ctx.project_weighted(r, data, s.apc, g, mode, lay.t0_bins, lay.bin_rate, w, scale=scale)
     finally:
         ctx.debug_set(sarbp.DEBUG_BP_CHUNK, 0)
+        ctx.debug_set(sarbp.DEBUG_BP_LINEAR_PHASE, 0)
     for c in ("8", "4"):
         assert np.array_equal(imgs[c], imgs["16"])
         assert np.array_equal(projs[c], projs["16"])
