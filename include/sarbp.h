@@ -254,8 +254,9 @@ sarbp_status sarbp_backproject_ex(sarbp_ctx *ctx, const sarbp_radar *radar,
  * out[p] = sum over pixels of conj(weight[pixel]) * S_p(bin) exp(j phase_p),
  * the pulse's back-projected term with corrections.  With weight = |I|^2 I this
  * is the per-pulse gradient of the image sharpness sum |I|^4:
- * d/d dphase[p] = -4 Im(out[p]).  SPLIT or FP16STORE arithmetic (mode), sums
- * over tiles in FP64 in a fixed order.  weight [ny][nx] complex64 (host or
+ * d/d dphase[p] = -4 Im(out[p]).  SPLIT or FP16STORE arithmetic (mode) in the
+ * phase form the back-projection takes for the grid, sums over tiles in FP64
+ * in a fixed order.  weight [ny][nx] complex64 (host or
  * device); out [np] complex128 as (re, im) pairs (host or device). */
 sarbp_status sarbp_project_weighted(sarbp_ctx *ctx, const sarbp_radar *radar,
                                     const sarbp_rc_view *rc, const double *apc,
@@ -544,10 +545,10 @@ int64_t sarbp_kernel_launches(const sarbp_ctx *ctx);
  *   SARBP_DEBUG_DEVICE_FLAGS    (get only) device check bits of the last call
  *                               that reported any: 1 wait ran out, 2 index clamped,
  *                               8 staging window, 16 a copy did not land in the drain
- *   SARBP_DEBUG_BP_LINEAR_PHASE  SPLIT / FP16STORE back-projection phase form:
- *                               1 linear-term form, -1 series form, 0 the planner's
- *                               choice (linear-term for tiles whose half-diagonal
- *                               exceeds 12 m) */
+ *   SARBP_DEBUG_BP_LINEAR_PHASE  SPLIT / FP16STORE phase form of back-projection
+ *                               and weighted projection: 1 linear-term form, -1
+ *                               series form, 0 the planner's choice (linear-term
+ *                               for tiles whose half-diagonal exceeds 12 m) */
 enum {
     SARBP_DEBUG_BP_CHUNK = 1,
     SARBP_DEBUG_BP_SEGMENTS = 2,

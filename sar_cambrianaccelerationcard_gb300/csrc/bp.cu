@@ -466,11 +466,13 @@ __device__ __forceinline__ void flush_projection(const BpPlan &P, const Smem &S,
 // Pulses go in pairs through one shared butterfly: the xor-16 step splits the
 // pair's two pulses between the half-warps and the xor-8 step splits re / im,
 // so a pair costs 6 shuffles instead of 20 for two separate 32-lane sums.
-template <int NTERMS, int PIX>
+// LIN: the linear-term phase (as the back-projection's LIN loop), the weight's
+// phase added to it the same way.
+template <int NTERMS, int PIX, bool LIN>
 __device__ __forceinline__ void project_chunk(const Smem &S, int stage, int count, int win, unsigned sbase, int cen,
                                               f2 XC2, const f2 (&YC2)[PIX / 2], const f2 (&QQ2)[PIX / 2], f2 BPM2,
                                               f2 KH2, f2 KL2, const f2 (&TH2)[PIX / 2], const float (&wm)[PIX],
-                                              float *red) {
+                                              f2 X2C2, const f2 (&Y2C2)[LIN ? PIX / 2 : 1], float *red) {
     const int lane = threadIdx.x & 31;
     const bool hi16 = (lane & 16) != 0, hi8 = (lane & 8) != 0;
     f2 MP = pk2(kMagic + (float)cen, kMagic + (float)cen);
@@ -482,24 +484,41 @@ __device__ __forceinline__ void project_chunk(const Smem &S, int stage, int coun
         for (int u2 = 0; u2 < 2; ++u2) {
             if (u2 == 1 && pl + 1 >= count) break;  // odd tail: pulse-uniform
             const Prm &q = S.prm[stage * kChunk + pl + u2];
-            f2 C1, C2, C3, C4, BT, PHT, AA, BB;
+            // k0..k3 (and k4 for LIN) as the producer wrote them: (C1, C2 | D2),
+            // (C3 | D3, C4 | D4), (BT, PHT), (A | A c1, B | B c1), (PX, PY)
+            f2 C1, C2, C3, C4, BT, PHT, AA, BB, PX, PY;
             lds2x2(&q.k0, C1, C2);
             lds2x2(&q.k1, C3, C4);
             lds2x2(&q.k2, BT, PHT);
             lds2x2(&q.k3, AA, BB);
+            f2 PHX = PHT;
+            if constexpr (LIN) {
+                lds2x2(&prm_k4(q), PX, PY);
+                PHX = ffma2(X2C2, PX, PHT);
+            }
             const f2 XA = fmul2(XC2, AA);
 #pragma unroll
             for (int h = 0; h < PIX / 2; ++h) {
-                const f2 n = ffma2(YC2[h], BB, fadd2(XA, QQ2[h]));
-                f2 poly = NTERMS == 4 ? ffma2(n, ffma2(n, C4, C3), C2) : ffma2(n, C3, C2);
-                poly = ffma2(n, poly, C1);
-                const f2 dR = fmul2(n, poly);
-                const f2 b2 = ffma2(dR, BPM2, BT);
+                f2 b2, ph2;
+                if constexpr (LIN) {
+                    const f2 qc = fmul2(QQ2[h], C1);
+                    const f2 m = ffma2(YC2[h], BB, fadd2(XA, qc));
+                    const f2 m2 = fmul2(m, m);
+                    const f2 poly = NTERMS == 4 ? ffma2(m, ffma2(m, C4, C3), C2) : ffma2(m, C3, C2);
+                    b2 = ffma2(ffma2(m2, poly, m), BPM2, BT);
+                    ph2 = fadd2(ffma2(ffma2(m2, poly, qc), KH2, ffma2(Y2C2[h], PY, PHX)), TH2[h]);
+                } else {
+                    const f2 n = ffma2(YC2[h], BB, fadd2(XA, QQ2[h]));
+                    f2 poly = NTERMS == 4 ? ffma2(n, ffma2(n, C4, C3), C2) : ffma2(n, C3, C2);
+                    poly = ffma2(n, poly, C1);
+                    const f2 dR = fmul2(n, poly);
+                    b2 = ffma2(dR, BPM2, BT);
 #if SARBP_BP_PHASE_COMPENSATED
-                const f2 ph2 = fadd2(ffma2(dR, KL2, ffma2(dR, KH2, PHT)), TH2[h]);
+                    ph2 = fadd2(ffma2(dR, KL2, ffma2(dR, KH2, PHT)), TH2[h]);
 #else
-                const f2 ph2 = fadd2(ffma2(dR, KH2, PHT), TH2[h]);
+                    ph2 = fadd2(ffma2(dR, KH2, PHT), TH2[h]);
 #endif
+                }
                 float bb[2], ph[2], tt[2];
                 upk2(b2, bb[0], bb[1]);
                 upk2(ph2, ph[0], ph[1]);
@@ -545,8 +564,8 @@ template <int MODE, int STORE, int NTERMS, bool CHECKED, int PIX, bool ADJ = fal
 __global__ void __launch_bounds__(kThreads, SARBP_BP_MINBLOCKS)
     bp_kernel(const __grid_constant__ BpPlan P, int tiles_y, int pulses_per_seg, float qq_max) {
     static_assert(!ADJ || MODE == SARBP_MODE_SPLIT || MODE == SARBP_MODE_FP16STORE, "projection: split arithmetic");
-    static_assert(!LIN || (!ADJ && (MODE == SARBP_MODE_SPLIT || MODE == SARBP_MODE_FP16STORE)),
-                  "linear-term phase: split back-projection only");
+    static_assert(!LIN || MODE == SARBP_MODE_SPLIT || MODE == SARBP_MODE_FP16STORE,
+                  "linear-term phase: split arithmetic only");
     constexpr int kPix = PIX;  // pixels per thread, all in one column
     constexpr int kTileY = 8 * PIX;
     extern __shared__ __align__(128) unsigned char smem_raw[];
@@ -690,8 +709,8 @@ __global__ void __launch_bounds__(kThreads, SARBP_BP_MINBLOCKS)
         const float4 *stg = S.staged + (size_t)sbuf * chunk * win;
         const unsigned sbase = smem_addr(stg) - kMagicBitsShift4;
         if constexpr (ADJ) {
-            project_chunk<NTERMS, kPix>(S, stage, count, win, sbase, cen, XC2, YC2, QQ2, BPM2, KH2, KL2, TH2, wm,
-                                  reinterpret_cast<float *>(S.red + ((c & 1) * kWarps + warp) * kChunk));
+            project_chunk<NTERMS, kPix, LIN>(S, stage, count, win, sbase, cen, XC2, YC2, QQ2, BPM2, KH2, KL2, TH2, wm,
+                                             X2C2, Y2C2, reinterpret_cast<float *>(S.red + ((c & 1) * kWarps + warp) * kChunk));
         } else if (LIN && (MODE == SARBP_MODE_SPLIT || MODE == SARBP_MODE_FP16STORE)) {
             // linear-term form (large tiles): m = n / (2 R_T) centred offset, bin from
             // dR = m + m^2 poly(m), phase from the increments per pixel step (reduced
@@ -1040,6 +1059,16 @@ __global__ void __launch_bounds__(32 * kProjWarps)
 
 template <int STORE, int PIX>
 cudaError_t launch_proj_pix(const BpPlan &p, cudaStream_t s, int tiles, int tiles_y, int pps, float qq_max) {
+    if (p.lin) {  // large tiles: the linear-term phase
+        if constexpr (PIX == 8) {
+            if (p.chunk == kChunk)
+                return p.nterms == 3
+                           ? launch_variant<SARBP_MODE_SPLIT, STORE, 3, false, PIX, true, kChunk, false, true>(p, s, tiles, tiles_y, pps, qq_max)
+                           : launch_variant<SARBP_MODE_SPLIT, STORE, 4, false, PIX, true, kChunk, false, true>(p, s, tiles, tiles_y, pps, qq_max);
+        }
+        return p.nterms == 3 ? launch_variant<SARBP_MODE_SPLIT, STORE, 3, false, PIX, true, 0, false, true>(p, s, tiles, tiles_y, pps, qq_max)
+                             : launch_variant<SARBP_MODE_SPLIT, STORE, 4, false, PIX, true, 0, false, true>(p, s, tiles, tiles_y, pps, qq_max);
+    }
     if constexpr (PIX == 8) {  // the usual tile: pulse chunk fixed at compile time
         if (p.chunk == kChunk)
             return p.nterms == 3

@@ -167,9 +167,9 @@ def test_wide_windows_keep_two_ctas(ctx, case, storage, chunk):
 @pytest.mark.parametrize("storage", [sarbp.STORE_C64, sarbp.STORE_C32H])
 def test_chunk_size_does_not_change_results(ctx, storage, form):
     """Pixels accumulate pulses in the same order whatever the staging chunk, so
-    16-, 8- and 4-pulse chunks give the same bits (back-projection in both phase
-    forms, 16-pulse chunks compiled in; the weighted projection; 300 pulses:
-    ragged last chunks)."""
+    16-, 8- and 4-pulse chunks give the same bits (back-projection and the
+    weighted projection, in both phase forms, 16-pulse chunks compiled in; 300
+    pulses: ragged last chunks)."""
     s = scenes.config1(np_=300, ns=1024, n_img=96)
     r, g, lay = sarbp.scene_args(s)
     echo = sarbp.synthesize(ctx, s)

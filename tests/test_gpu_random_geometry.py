@@ -294,6 +294,42 @@ def test_linear_phase_form_on_large_tiles(orc, seed):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("seed", [3, 5, 11])
+def test_linear_phase_form_in_the_projection(orc, seed):
+    """The weighted projection takes the planner's phase form too: on tiles
+    beyond 12 m the linear-term form is closer to the oracle's projection than
+    the series form (GB300: -95 to -106 dB against -64 to -72 dB), both stay
+    within -60 dB, and the adjoint identity with the back-projection of the
+    same form holds to 1e-5 (the series form's, with its larger phase error, to
+    1e-3)."""
+    s = random_scene(seed)
+    rng = np.random.default_rng(2900 + seed)
+    e64 = orc.echo(s).astype(np.complex64)
+    rc = orc.range_compress(s, e64.astype(np.complex128)).astype(np.complex64)
+    r, g, lay = sarbp.scene_args(s)
+    w = (rng.standard_normal((g.ny, g.nx)) + 1j * rng.standard_normal((g.ny, g.nx))).astype(np.complex64)
+    zeros = np.zeros(s.np_)
+    ref = orc.project_weighted(s, rc, w, zeros, zeros)
+    errs, adj, forms = {}, {}, {}
+    for form in (-1, 1, 0):
+        with sarbp.Context(0) as ctx:
+            ctx.debug_set(sarbp.DEBUG_BP_LINEAR_PHASE, form)
+            forms[form] = _plan(ctx, s).linear_phase
+            out = ctx.project_weighted(r, rc, s.apc, g, sarbp.MODE_SPLIT, lay.t0_bins, lay.bin_rate, w)
+            img = ctx.backproject(r, rc, s.apc, g, sarbp.MODE_SPLIT, lay.t0_bins, lay.bin_rate)
+        errs[form] = metrics.rel_l2_db(out, ref)
+        lhs = np.vdot(w.astype(np.complex128), img.astype(np.complex128))
+        adj[form] = abs(lhs - out.sum()) / abs(lhs)
+    print(s.name, "projection vs oracle: series", f"{errs[-1]:.1f}", "linear-term", f"{errs[1]:.1f}",
+          "planner", f"{errs[0]:.1f} dB; adjoint mismatch", f"{adj[-1]:.1e} / {adj[1]:.1e}")
+    assert forms == {-1: 0, 1: 1, 0: 1}
+    assert errs[-1] <= -60.0 and errs[1] <= -60.0
+    assert errs[1] <= errs[-1] - 20.0
+    assert errs[0] == errs[1]
+    assert adj[-1] <= 1e-3 and adj[1] <= 1e-5
+
+
+@pytest.mark.gpu
 def test_linear_phase_form_on_config2_tiles(orc):
     """Config 2's geometry (0.25 m pixels, 8.8 m half-diagonal tiles) keeps the
     series form; forced to the linear-term form it is at least as accurate."""
